@@ -1,0 +1,285 @@
+"""Benchmark: correlated Gsamples/s of the FX correlator on one GB300.
+
+Workload (one "step"): the 256-station dual-polarisation configuration --
+512 inputs of 2-bit offset-binary samples (rho = 0.02 common signal),
+2048-point real FFTs (1024 channels), 4096 spectra integrated, i.e.
+8,388,608 samples per input and 4.29 G samples per step, correlated into all
+131,328 lower-triangle products x 1024 channels.  A step runs unpack + FFT +
+X stage through the engine's C ABI.
+
+* value : device-resident inputs and outputs (cellspe_fx_correlate with
+          CELLSPE_MEM_DEVICE), K steps bracketed by synchronize + CUDA events.
+* e2e   : the same call with pinned HOST buffers: every step copies the 2-bit
+          input to the GPU and the visibilities back.
+* roofline: the dominant kernel's algorithmic rate, from CUDA events the
+          library records on its own stream around each stage.
+* cpu_baseline: the FX path of the CPU oracle (restated genericAddProduct_32fc_conj
+          X stage, radix-2 FFT standing in for the absent FFTW) on a bounded
+          sample of the same inputs, all host threads.
+
+Under torchrun each rank runs its own job (a different subband) on its own
+GPU: weak scaling, no data-path collective.  ``--impl reference`` times the
+CPU implementation alone.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "cellspe-tasklib_gb300"))
+sys.path.insert(0, str(ROOT))
+
+S, N, K = 512, 2048, 4096          # 256 stations x 2 pols, 2048-pt FFT, 4096 spectra
+RHO = 0.02
+C = N // 2
+P = S * (S + 1) // 2
+T = N * K
+
+
+def _peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(raw_host: np.ndarray, k_sample: int, nthreads: int):
+    import oracle
+
+    sample = np.ascontiguousarray(raw_host[:, : k_sample * N // 4])
+    t0 = time.perf_counter()
+    oracle.fx_fp32(sample, S, N, k_sample, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return S * k_sample * N / dt / 1e9, dt
+
+
+def run_reference(args):
+    """CPU implementation of the path (the oracle's FX restatement), all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import synth
+
+    nthreads = os.cpu_count() or 1
+    k_sample = args.cpu_segments
+    raw = synth.stations_offset_binary(S, k_sample * N, rho=RHO, seed=4)
+    for _ in range(args.warmup):
+        cpu_baseline(raw, max(1, k_sample // 8), nthreads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        v, dt = cpu_baseline(raw, k_sample, nthreads)
+        vals.append(v)
+        secs.append(dt)
+    value = statistics.median(vals)
+    sample = f"{S} inputs x {k_sample} segments x {N} samples ({S * k_sample * N / 1e6:.0f} M samples) per step"
+    line = {
+        "metric": "correlated Gsamples/s", "value": value, "unit": "Gsamples/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.median(secs), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 2-bit offset binary, rho=0.02)",
+        "config": {"workload": "256-station dual-pol FX: S=512, N=2048, C=1024, K=4096", "inputs": S,
+                   "fft_points": N, "segments": K},
+        "cpu_baseline": {"value": value, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="fp32", choices=["tc", "fp32"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-segments", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import cellspe_gpu as cg
+    import synth
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    x_mode = cg.X_TC_FP16 if args.mode == "tc" else cg.X_FP32
+    raw = synth.device_stations(S, T, RHO, seed=4 + 1000 * rank)
+    vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
+    params = cg.fx_params(S, N, K, T // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+    for _ in range(args.warmup):
+        cg.fx_correlate(params, raw, vis)
+
+    # ---- device-resident timed region ------------------------------------
+    stage_sum = np.zeros(4)
+    barrier()
+    l0 = cg.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            cg.fx_correlate(params, raw, vis)
+            stage_sum += np.array(cg.stage_times())
+        torch.cuda.synchronize()
+        e1.record()
+        e1.synchronize()
+    launches = cg.kernel_launches() - l0
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * S * T / (ms_step * 1e-3) / 1e9
+    stage_ms = stage_sum / args.steps
+
+    # ---- end to end through the C ABI with host buffers --------------------
+    raw_h = np.empty((S, T // 4), np.uint8)
+    raw_h[:] = raw.cpu().numpy()
+    pin_raw = torch.from_numpy(raw_h).pin_memory()
+    pin_vis = torch.empty((C, P), dtype=torch.complex64).pin_memory()
+    raw_np, vis_np = pin_raw.numpy(), pin_vis.numpy()
+    hparams = cg.fx_params(S, N, K, T // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+    cg.fx_correlate(hparams, raw_np, vis_np)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.e2e_steps):
+        cg.fx_correlate(hparams, raw_np, vis_np)
+    torch.cuda.synchronize()
+    f1.record()
+    f1.synchronize()
+    e2e_ms = f0.elapsed_time(f1) / args.e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * S * T / (e2e_ms * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel -----------------------------------
+    peaks, peak_kind = _peaks()
+    f_ms, x_ms = stage_ms[1], stage_ms[2]
+    f_bytes = S * K * (N // 4 + C * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
+    x_flops = 8.0 * P * C * K                                              # 8 real flops per CMAC, triangle
+    stages = {"f_stage_ms": f_ms, "x_stage_ms": x_ms, "output_ms": stage_ms[3],
+              "f_stage_gbs": f_bytes / (f_ms * 1e-3) / 1e9,
+              "x_stage_tflops": x_flops / (x_ms * 1e-3) / 1e12}
+    if x_ms >= f_ms:
+        if x_mode == cg.X_FP32:
+            fp32_peak = 152 * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
+            roof = {"bound": "fp32", "kernel": "k_xmac_f32", "achieved": stages["x_stage_tflops"],
+                    "peak": fp32_peak, "unit": "TFLOP/s", "frac": stages["x_stage_tflops"] / fp32_peak,
+                    "peak_source": "nominal FP32 CUDA-core rate 152 SM x 128 FMA x 2 x max clock",
+                    "traffic": None}
+        else:
+            pk = peaks["bf16_tflops"]
+            roof = {"bound": "tensor", "kernel": "k_xmac_tc", "achieved": stages["x_stage_tflops"], "peak": pk,
+                    "unit": "TFLOP/s", "frac": stages["x_stage_tflops"] / pk,
+                    "peak_source": f"{peak_kind} dense bf16 (burst)", "traffic": None}
+    else:
+        pk = peaks["hbm_gbs"]
+        roof = {"bound": "hbm", "kernel": "k_fx_fstage", "achieved": stages["f_stage_gbs"], "peak": pk,
+                "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
+                "traffic": None}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        v, dt = cpu_baseline(raw_h, args.cpu_segments, nthreads)
+        cpu = {"value": v, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
+               "sample": f"{S} inputs x {args.cpu_segments} segments x {N} samples, {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "correlated Gsamples/s", "value": value, "unit": "Gsamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f16-tc/f32-acc" if x_mode == cg.X_TC_FP16 else "f32",
+            "data": "synthetic (seeded 2-bit offset binary, rho=0.02, generated on device)",
+            "config": {"workload": "256-station dual-pol FX: S=512, N=2048, C=1024, K=4096",
+                       "inputs": S, "fft_points": N, "channels": C, "segments": K, "products": P,
+                       "x_mode": args.mode, "vis_order": "channel-major [C][P]",
+                       "l2": "inputs larger than L2 (1.07 GB raw, spectra 8.6/17 GB, vis 1.07 GB)",
+                       "parallelism": f"replicas x{world} (one job per GPU)"},
+            "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(S * T // 4),
+                    "d2h_bytes_per_step": int(C * P * 8), "ms_per_step": e2e_ms},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "stages": stages,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,71 @@
+"""Build recipe for libcellspe_gpu.so (sm_103a only).
+
+Every .cu / .cpp under csrc/ is compiled in parallel with
+``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` and linked
+into ``libcellspe_gpu.so`` next to this file (static CUDA runtime, C ABI of
+include/*.h).  Objects go to _build/ (git-ignored).  Rebuilds only what
+changed (by mtime against the sources and headers).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OUT = PKG / "_build"
+LIB = PKG / "libcellspe_gpu.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC = os.environ.get("NVCC", "nvcc")
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"),
+          "--expt-relaxed-constexpr"]
+
+
+def _headers():
+    return list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
+
+
+def _stale(obj: Path, src: Path, deps) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return src.stat().st_mtime > t or any(d.stat().st_mtime > t for d in deps)
+
+
+def _compile(src: Path, verbose_ptxas: bool) -> Path:
+    obj = OUT / (src.name + ".o")
+    cmd = [NVCC, *ARCH, *COMMON, "-c", str(src), "-o", str(obj)]
+    if verbose_ptxas and src.suffix == ".cu":
+        cmd.insert(1, "-Xptxas=-v")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError(f"nvcc failed on {src.name}")
+    if verbose_ptxas:
+        (OUT / (src.name + ".ptxas.txt")).write_text(r.stderr)
+    return obj
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+    OUT.mkdir(exist_ok=True)
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
+    deps = _headers()
+    todo = [s for s in srcs if force or verbose_ptxas or _stale(OUT / (s.name + ".o"), s, deps)]
+    with ThreadPoolExecutor(max_workers=max(2, min(len(todo) or 1, os.cpu_count() or 4))) as ex:
+        list(ex.map(lambda s: _compile(s, verbose_ptxas), todo))
+    objs = [OUT / (s.name + ".o") for s in srcs]
+    if force or todo or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
+        cmd = [NVCC, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("link failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose_ptxas="--ptxas" in sys.argv))

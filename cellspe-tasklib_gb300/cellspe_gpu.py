@@ -1,0 +1,305 @@
+"""Python mirror of the engine's C ABI (include/cellspe_gpu.h, cellspe-tasklib*.h).
+
+The product is ``libcellspe_gpu.so``; this module only binds it with ctypes
+so that tests and the benchmark call exactly what a C/C++ caller calls.
+Arrays may be numpy arrays (host memory: the engine stages them through the
+GPU) or torch CUDA tensors (device memory, used in place).  There is no CPU
+implementation here: if the library is missing or the GPU is unusable every
+call raises ``CellspeError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+LIB_PATH = PKG / "libcellspe_gpu.so"
+
+# ---- constants (cellspe_gpu.h, cellspe-tasklib*.h) --------------------------
+MEM_HOST, MEM_DEVICE = 0, 1
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_NOMEM, ERR_CUDA, ERR_INJECTED = range(6)
+LEVELS_MARK5B, LEVELS_TWOBIT, LEVELS_OFFSET_BINARY = 0, 1, 2
+UNPACK_MSB_FIRST = 0x100
+X_FP32, X_TC_FP16 = 0, 1
+VIS_CHANNEL_MAJOR, VIS_BASELINE_MAJOR = 0, 1
+SPEC_INTERLEAVED, SPEC_PLANES = 0, 1
+
+TASK_INCOMPLETE, TASK_OK, TASK_GENERICERROR, TASK_UNKOWNCOMMAND = 0xFFFF, 0, 1, 2
+TASK_FLAG_DEVPTR = 0x40000000
+BEHAV_BLOCKING, BEHAV_DEFAULT = 1, 0
+MAX_SLOTS = 4
+(TASK_NOP, TASK_MAC, TASK_MULC, TASK_ADDC, TASK_IOTEST, TASK_IOBENCH, TASK_FFT_INIT, TASK_FFT_FREE,
+ TASK_FFT_EXEC, TASK_FFT_EXEC_DYN, TASK_SINCOS, TASK_SINCOS_NORM, TASK_SINCOS_GENERTR, TASK_UNPACK,
+ TASK_RUNALL, TASK_DMASIMULATION, TASK_DIFXPROCESS, TASK_MAC_CONJ, TASK_RFFT, TASK_FX_CORRELATE,
+ TASK_SPECTROMETER, TASK_XMAC, TASK_SIGTERM) = range(23)
+
+
+class CellspeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"cellspe error {code}: {msg}")
+        self.code = code
+
+
+# ---- ctypes mirrors of the C structs ----------------------------------------
+class CellDSPTask(ctypes.Structure):
+    """CellDSPTask_t (cellspe-tasklib.h); 256 bytes, next_task at offset 240."""
+    _fields_ = [
+        ("command", ctypes.c_uint32),
+        ("completed_flag", ctypes.c_uint16),
+        ("_pad0", ctypes.c_uint16),
+        ("tick_count", ctypes.c_uint32),
+        ("num_input_vectors", ctypes.c_uint32),
+        ("inputvector_ptrs", ctypes.c_uint64 * 8),
+        ("inputvector_lengths", ctypes.c_uint32 * 8),
+        ("num_output_vectors", ctypes.c_uint32),
+        ("_pad1", ctypes.c_uint32),
+        ("outputvector_ptrs", ctypes.c_uint64 * 8),
+        ("outputvector_lengths", ctypes.c_uint32 * 8),
+        ("subcontext", ctypes.c_uint32 * 5),
+        ("_pad2", ctypes.c_uint32),
+        ("next_task", ctypes.c_uint64),
+        ("_pad3", ctypes.c_uint64 * 1),
+    ]
+
+
+assert ctypes.sizeof(CellDSPTask) == 256
+
+
+class FxParams(ctypes.Structure):
+    _fields_ = [("n_inputs", ctypes.c_int), ("fft_points", ctypes.c_int), ("n_segments", ctypes.c_int),
+                ("x_mode", ctypes.c_int), ("vis_order", ctypes.c_int), ("levels", ctypes.c_int),
+                ("bytes_per_input", ctypes.c_longlong), ("start_sample", ctypes.c_longlong),
+                ("sample_rate_hz", ctypes.c_double), ("lo_freq_hz", ctypes.c_double),
+                ("accumulate", ctypes.c_int), ("memory", ctypes.c_int),
+                ("custom_levels", ctypes.c_void_p), ("channel_scale", ctypes.c_void_p)]
+
+
+class SpecParams(ctypes.Structure):
+    _fields_ = [("fft_points", ctypes.c_int), ("overlap", ctypes.c_int), ("window", ctypes.c_int),
+                ("ffts_per_spectrum", ctypes.c_int), ("n_spectra", ctypes.c_int),
+                ("n_subbands", ctypes.c_int), ("input_layout", ctypes.c_int), ("levels", ctypes.c_int),
+                ("raw_bytes", ctypes.c_longlong), ("pcal_tonebins", ctypes.c_int),
+                ("pcal_rotatorlen", ctypes.c_int), ("pcal_ntones", ctypes.c_int),
+                ("pcal_offset_hz", ctypes.c_double), ("sample_rate_hz", ctypes.c_double),
+                ("memory", ctypes.c_int), ("custom_levels", ctypes.c_void_p)]
+
+
+class XmacParams(ctypes.Structure):
+    _fields_ = [("S", ctypes.c_int), ("C", ctypes.c_int), ("K", ctypes.c_int), ("accumulate", ctypes.c_int)]
+
+
+assert ctypes.sizeof(FxParams) == 80 and ctypes.sizeof(SpecParams) == 88
+
+
+# ---- library loading ----------------------------------------------------------
+_lib = None
+
+
+def declared_functions() -> list[str]:
+    """Names of every function declared in include/*.h."""
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:celldsp|spe|cellspe)\w*)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise CellspeError(ERR_CUDA, f"{LIB_PATH.name} is not built; run __graft_entry__.build()")
+        L = ctypes.CDLL(str(LIB_PATH))
+        V, I, LL, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+        sig = {
+            "cellspe_last_error": ([], ctypes.c_char_p),
+            "cellspe_device_count": ([], I),
+            "cellspe_set_hbm_budget": ([LL], I),
+            "cellspe_get_hbm_budget": ([], LL),
+            "cellspe_host_alloc": ([ctypes.c_size_t], V),
+            "cellspe_host_free": ([V], None),
+            "cellspe_device_alloc": ([ctypes.c_size_t], V),
+            "cellspe_device_free": ([V], None),
+            "cellspe_memcpy": ([V, V, ctypes.c_size_t, I], I),
+            "cellspe_debug_inject_failure": ([I, I], I),
+            "cellspe_kernel_launches": ([], LL),
+            "cellspe_last_stage_times": ([ctypes.POINTER(ctypes.c_float), I], I),
+            "cellspe_unpack2bit": ([V, LL, I, I, V, V, I], I),
+            "cellspe_fft_c2c": ([V, V, I, LL, I], I),
+            "cellspe_fft_r2c": ([V, V, I, LL, I], I),
+            "cellspe_xmac": ([V, I, I, I, V, I, I], I),
+            "cellspe_fx_correlate": ([V, V, V, V], I),
+            "cellspe_fx_workspace_bytes": ([V], LL),
+            "cellspe_fx_correlate_async": ([V, V, V, V, V], I),
+            "cellspe_release_workspace": ([], I),
+            "cellspe_spectrometer": ([V, V, V, V, V], I),
+            "cellspe_spectrometer_workspace_bytes": ([V], LL),
+            "celldsp_start": ([], I), "celldsp_stop": ([], I),
+            "celldsp_getFreeSPE": ([], I), "celldsp_setFreeSPE": ([I], I),
+            "celldsp_startTask": ([I, V], I), "celldsp_waitTask": ([I], I),
+            "celldsp_executeTask": ([V], I),
+            "celldsp_startContinuableTask": ([V, V], I), "celldsp_continueTask": ([V, V], I),
+            "celldsp_stopContinuableTask": ([V], I),
+            "celldsp_setBehaviour": ([ctypes.c_uint], None), "celldsp_getBehaviour": ([], ctypes.c_uint),
+            "speNOP": ([], I), "speRunAllCheck": ([], I), "speIOCheck": ([], I), "speIOSimulation": ([], I),
+            "speIOBench": ([V, ctypes.c_uint, I], I), "speIOBenchStreamed": ([V, ctypes.c_uint, I, I], I),
+            "speAddProduct_32fc": ([V, V, V, I], I),
+            "speFFT_init": ([I, V], I), "speFFT_exec": ([V, V, I, V], I), "speFFT_destroy": ([V], I),
+            "speFFT_singleexec": ([V, V, I], I),
+            "speDIFX_process": ([V, V, V, V, V, I, I, I], I),
+            "speSinCosGenerator": ([ctypes.c_float, ctypes.c_float, V, I], I),
+            "speSinCosAccurate": ([V, V, I], I), "speSinCosAccurateNorm": ([V, V, I], I),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def stage_times() -> list[float]:
+    buf = (ctypes.c_float * 4)()
+    _check(lib().cellspe_last_stage_times(buf, 4))
+    return list(buf)
+
+
+def kernel_launches() -> int:
+    return int(lib().cellspe_kernel_launches())
+
+
+def last_error() -> str:
+    return (lib().cellspe_last_error() or b"").decode()
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise CellspeError(rc, last_error())
+
+
+def _is_torch_cuda(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def _ptr(x):
+    """(pointer, memory kind) of a numpy array or torch CUDA tensor."""
+    if x is None:
+        return None, None
+    if _is_torch_cuda(x):
+        assert x.is_contiguous()
+        return ctypes.c_void_p(x.data_ptr()), MEM_DEVICE
+    assert isinstance(x, np.ndarray) and x.flags.c_contiguous, "need a C-contiguous numpy array"
+    return ctypes.c_void_p(x.ctypes.data), MEM_HOST
+
+
+def _mem(*xs) -> int:
+    kinds = {_ptr(x)[1] for x in xs if x is not None}
+    if len(kinds) != 1:
+        raise CellspeError(ERR_ARG, "mix of host and device buffers in one call")
+    return kinds.pop()
+
+
+# ---- direct entry points --------------------------------------------------------
+def unpack2bit(raw, nsamp: int, nchan: int, out, levels: int = LEVELS_MARK5B, custom_levels=None,
+               msb_first: bool = False):
+    fmt = levels | (UNPACK_MSB_FIRST if msb_first else 0)
+    cl = None
+    if custom_levels is not None:
+        cl = np.ascontiguousarray(custom_levels, np.float32)
+    _check(lib().cellspe_unpack2bit(_ptr(raw)[0], nsamp, nchan, fmt,
+                                    ctypes.c_void_p(cl.ctypes.data) if cl is not None else None,
+                                    _ptr(out)[0], _mem(raw, out)))
+    return out
+
+
+def fft_c2c(x, out, n: int, batch: int):
+    _check(lib().cellspe_fft_c2c(_ptr(x)[0], _ptr(out)[0], n, batch, _mem(x, out)))
+    return out
+
+
+def fft_r2c(x, out, n: int, batch: int):
+    _check(lib().cellspe_fft_r2c(_ptr(x)[0], _ptr(out)[0], n, batch, _mem(x, out)))
+    return out
+
+
+def xmac(spectra, S: int, C: int, K: int, vis, accumulate: bool = False):
+    _check(lib().cellspe_xmac(_ptr(spectra)[0], S, C, K, _ptr(vis)[0], int(accumulate), _mem(spectra, vis)))
+    return vis
+
+
+def fx_params(S, N, K, bytes_per_input, x_mode=X_FP32, vis_order=VIS_CHANNEL_MAJOR,
+              levels=LEVELS_OFFSET_BINARY, start_sample=0, fs_hz=0.0, lo_hz=0.0, accumulate=False,
+              memory=MEM_HOST, custom_levels=None, channel_scale=None) -> FxParams:
+    p = FxParams(S, N, K, x_mode, vis_order, levels, bytes_per_input, start_sample, fs_hz, lo_hz,
+                 int(accumulate), memory, None, None)
+    p._keep = (custom_levels, channel_scale)
+    if custom_levels is not None:
+        p.custom_levels = custom_levels.ctypes.data
+    if channel_scale is not None:
+        p.channel_scale = _ptr(channel_scale)[0].value
+    return p
+
+
+def fx_correlate(params: FxParams, raw, vis, delay_poly=None):
+    params.memory = _mem(raw, vis)
+    _check(lib().cellspe_fx_correlate(ctypes.byref(params), _ptr(raw)[0],
+                                      _ptr(delay_poly)[0] if delay_poly is not None else None,
+                                      _ptr(vis)[0]))
+    return vis
+
+
+def fx_correlate_async(params: FxParams, raw, vis, stream_ptr: int, delay_poly=None):
+    params.memory = MEM_DEVICE
+    _check(lib().cellspe_fx_correlate_async(ctypes.byref(params), _ptr(raw)[0],
+                                            _ptr(delay_poly)[0] if delay_poly is not None else None,
+                                            _ptr(vis)[0], ctypes.c_void_p(stream_ptr)))
+
+
+def spec_params(N, overlap, window, K, nspec, nsub, raw_bytes, layout=SPEC_INTERLEAVED,
+                levels=LEVELS_MARK5B, tonebins=0, rotatorlen=0, ntones=0, offset_hz=0.0, fs_hz=0.0,
+                memory=MEM_HOST) -> SpecParams:
+    return SpecParams(N, overlap, window, K, nspec, nsub, layout, levels, raw_bytes, tonebins, rotatorlen,
+                      ntones, offset_hz, fs_hz, memory, None)
+
+
+def spectrometer(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None):
+    params.memory = _mem(raw, power)
+    _check(lib().cellspe_spectrometer(ctypes.byref(params), _ptr(raw)[0], _ptr(power)[0],
+                                      _ptr(pcal_bins)[0] if pcal_bins is not None else None,
+                                      _ptr(pcal_tones)[0] if pcal_tones is not None else None))
+    return power
+
+
+# ---- task API ------------------------------------------------------------------
+def new_task(command: int) -> CellDSPTask:
+    t = CellDSPTask()
+    t.command = command
+    return t
+
+
+def add_in(t: CellDSPTask, arr) -> None:
+    p, _ = _ptr(arr)
+    n = arr.nbytes if isinstance(arr, np.ndarray) else arr.numel() * arr.element_size()
+    t.inputvector_ptrs[t.num_input_vectors] = p.value
+    t.inputvector_lengths[t.num_input_vectors] = n
+    t.num_input_vectors += 1
+
+
+def add_in_struct(t: CellDSPTask, s: ctypes.Structure) -> None:
+    t.inputvector_ptrs[t.num_input_vectors] = ctypes.addressof(s)
+    t.inputvector_lengths[t.num_input_vectors] = ctypes.sizeof(s)
+    t.num_input_vectors += 1
+
+
+def add_out(t: CellDSPTask, arr) -> None:
+    p, _ = _ptr(arr)
+    n = arr.nbytes if isinstance(arr, np.ndarray) else arr.numel() * arr.element_size()
+    t.outputvector_ptrs[t.num_output_vectors] = p.value
+    t.outputvector_lengths[t.num_output_vectors] = n
+    t.num_output_vectors += 1

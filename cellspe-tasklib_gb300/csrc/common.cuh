@@ -1,0 +1,230 @@
+// Shared device helpers for the GB300 FX correlator / spectrometer kernels.
+//
+// * complex float helpers (float2: x = re, y = im)
+// * radix-2/4/8/16 DFT codelets held in registers (forward, e^{-2 pi i nk/R},
+//   unscaled -- the convention of fft_1d_r2_modified.h:40-66 and exec_FFT,
+//   cellspe-tasklib-dsp.cpp:519-584)
+// * CtaFft<M>: an M-point complex Stockham autosort FFT run by M/16 threads
+//   that each hold 16 points; passes exchange through padded shared memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#define CS_DEV __device__ __forceinline__
+
+CS_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+CS_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+CS_DEV float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+CS_DEV float2 cmul_conj(float2 a, float2 b)  // a * conj(b)
+{
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+CS_DEV float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }   // a * (-i)
+CS_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// W16^m = exp(-2 pi i m / 16) for the exponents the radix-16 codelet uses.
+CS_DEV float2 w16(int m)
+{
+    const float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f;
+    const float h = 0.70710678118654752f;
+    switch (m & 15) {
+        case 0: return make_float2(1.f, 0.f);
+        case 1: return make_float2(c1, -s1);
+        case 2: return make_float2(h, -h);
+        case 3: return make_float2(s1, -c1);
+        case 4: return make_float2(0.f, -1.f);
+        case 5: return make_float2(-s1, -c1);
+        case 6: return make_float2(-h, -h);
+        case 7: return make_float2(-c1, -s1);
+        case 8: return make_float2(-1.f, 0.f);
+        case 9: return make_float2(-c1, s1);
+        case 10: return make_float2(-h, h);
+        case 11: return make_float2(-s1, c1);
+        case 12: return make_float2(0.f, 1.f);
+        case 13: return make_float2(s1, c1);
+        case 14: return make_float2(h, h);
+        default: return make_float2(c1, s1);
+    }
+}
+
+CS_DEV void dft2(float2& a, float2& b)
+{
+    float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+// In-place forward DFT of R points in natural order.
+template <int R> struct Dft;
+
+template <> struct Dft<1> {
+    static CS_DEV void run(float2*) {}
+};
+template <> struct Dft<2> {
+    static CS_DEV void run(float2* a) { dft2(a[0], a[1]); }
+};
+template <> struct Dft<4> {
+    static CS_DEV void run(float2* a)
+    {
+        float2 t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
+        float2 t2 = cadd(a[1], a[3]), t3 = mul_mi(csub(a[1], a[3]));
+        a[0] = cadd(t0, t2);
+        a[2] = csub(t0, t2);
+        a[1] = cadd(t1, t3);
+        a[3] = csub(t1, t3);
+    }
+};
+// R = R1*R2 split: n = R2*n1 + n2, k = k1 + R1*k2.
+template <int R1, int R2> struct DftSplit {
+    static CS_DEV void run(float2* a)
+    {
+        constexpr int R = R1 * R2;
+        float2 b[R2][R1];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; n2++) {
+#pragma unroll
+            for (int n1 = 0; n1 < R1; n1++) b[n2][n1] = a[R2 * n1 + n2];
+            Dft<R1>::run(b[n2]);
+#pragma unroll
+            for (int k1 = 0; k1 < R1; k1++)
+                if (n2 * k1) b[n2][k1] = cmul(b[n2][k1], w16((n2 * k1) * (16 / R)));
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            float2 c[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; n2++) c[n2] = b[n2][k1];
+            Dft<R2>::run(c);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; k2++) a[k1 + R1 * k2] = c[k2];
+        }
+    }
+};
+template <> struct Dft<8> {
+    static CS_DEV void run(float2* a) { DftSplit<2, 4>::run(a); }
+};
+template <> struct Dft<16> {
+    static CS_DEV void run(float2* a) { DftSplit<4, 4>::run(a); }
+};
+
+// Padded shared-memory index: one spare float2 after every 16 elements keeps
+// the stride-16 accesses of the radix-16 passes free of bank conflicts.
+CS_DEV int fpad(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int fpad_size(int m) { return m + m / 16; }
+
+// exp(-2 pi i m / L) from a table of L entries computed in FP64 on the host.
+CS_DEV float2 twiddle(const float2* __restrict__ tw, int m) { return __ldg(tw + m); }
+
+// ---------------------------------------------------------------------------
+// CtaFft<M>: M-point complex forward FFT by a group of T = M/16 threads.
+//   Stage 0 (first pass, NS = 1) starts from registers: thread t holds
+//   v[r] = z[t + r*T], r = 0..15.  Each later pass reads 16 points per thread
+//   from the padded buffer, applies twiddles W_{NS*R}^{r*k}, runs a radix-R
+//   codelet and writes back (Stockham autosort: the result ends up in natural
+//   order).  The caller provides the group-wide barrier.
+// ---------------------------------------------------------------------------
+template <int M> struct CtaFft {
+    static_assert(M >= 16 && (M & (M - 1)) == 0, "M must be a power of two >= 16");
+    static constexpr int T = M / 16;
+
+    // First pass: radix-16 butterflies on register data, output to buf.
+    static CS_DEV void first_pass(float2* buf, int t, float2 (&v)[16])
+    {
+        Dft<16>::run(v);
+#pragma unroll
+        for (int r = 0; r < 16; r++) buf[fpad(16 * t + r)] = v[r];
+    }
+
+    // One Stockham pass with stride NS (> 1) and radix R = min(16, M/NS).
+    // tw is exp(-2 pi i m / (M*tws)) for m in [0, M*tws): the table of a
+    // larger transform is shared by striding it.
+    template <int NS, class Barrier>
+    static CS_DEV void pass(float2* buf, int t, const float2* __restrict__ tw, int tws, Barrier bar)
+    {
+        constexpr int R = (M / NS >= 16) ? 16 : (M / NS);
+        constexpr int NB = M / R;          // butterflies in this pass
+        constexpr int PER = NB / T;        // butterflies per thread = 16 / R
+        float2 v[PER][R];
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            int j = t + q * T;
+#pragma unroll
+            for (int r = 0; r < R; r++) v[q][r] = buf[fpad(j + r * NB)];
+        }
+        bar();
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            int j = t + q * T;
+            int k = j & (NS - 1);
+            constexpr int STEP = M / (NS * R);
+#pragma unroll
+            for (int r = 1; r < R; r++) v[q][r] = cmul(v[q][r], twiddle(tw, (r * k) * STEP * tws));
+            Dft<R>::run(v[q]);
+            int base = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) buf[fpad(base + r * NS)] = v[q][r];
+        }
+        bar();
+    }
+
+    template <int NS, class Barrier>
+    static CS_DEV void rest(float2* buf, int t, const float2* __restrict__ tw, int tws, Barrier bar)
+    {
+        if constexpr (NS < M) {
+            pass<NS>(buf, t, tw, tws, bar);
+            constexpr int R = (M / NS >= 16) ? 16 : (M / NS);
+            rest<NS * R>(buf, t, tw, tws, bar);
+        }
+    }
+
+    // Full transform: v holds z[t + r*T]; on return buf holds Z (natural
+    // order, padded indexing) and every thread has passed the final barrier.
+    template <class Barrier>
+    static CS_DEV void run(float2* buf, int t, float2 (&v)[16], const float2* __restrict__ tw,
+                           int tws, Barrier bar)
+    {
+        first_pass(buf, t, v);
+        bar();
+        rest<16>(buf, t, tw, tws, bar);
+    }
+};
+
+// Named barrier over `nthreads` threads (a multiple of 32) with id `id`.
+CS_DEV void named_bar(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// 2-bit field extraction.  Sample j (0..15) of a little-endian 32-bit word:
+// LSB-first order keeps it at bits 2j; MSB-first order (sample 0 in bits 7:6
+// of each byte) keeps it at bits 8*(j/4) + 6 - 2*(j%4).
+CS_DEV unsigned code2(uint32_t w, int j, bool msb_first)
+{
+    int sh = msb_first ? (8 * (j >> 2) + 6 - 2 * (j & 3)) : (2 * j);
+    return (w >> sh) & 3u;
+}
+
+// Error-check helper for host code in .cu files.
+#define CS_CUDA_TRY(expr)                                   \
+    do {                                                    \
+        cudaError_t _e = (expr);                            \
+        if (_e != cudaSuccess) return (int)_e;              \
+    } while (0)
+
+// Real-to-complex split.  Z is the M-point FFT of z[n] = x[2n] + i x[2n+1]
+// (N = 2M real points).  With a = Z[k], b = Z[(M-k) mod M] and
+// w = exp(-2 pi i k / N):  E = (a + conj b)/2,  O = (a - conj b)/(2i),
+//   X[k] = E + w O,   X[M-k] = conj(E - w O).
+CS_DEV void r2c_pair(float2 a, float2 b, float2 w, float2& Xk, float2& Xmk)
+{
+    float2 E = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+    float2 O = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+    float2 wO = cmul(w, O);
+    Xk = cadd(E, wO);
+    float2 d = csub(E, wO);
+    Xmk = make_float2(d.x, -d.y);
+}

@@ -1,0 +1,98 @@
+// Internal launch API between the C-ABI runtime (runtime.cpp) and the CUDA
+// kernels.  Every launcher is asynchronous on the given stream and returns 0
+// or a cudaError_t / CS_ERR_* code.  Pointers are device pointers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CS_ERR_ARG 10001      // invalid argument (size, alignment, null)
+#define CS_ERR_UNSUPPORTED 10002
+
+// Count of kernel launches issued by this library (read by the benchmark to
+// report how many of its own kernels ran in a timed region).
+long long cs_launch_count();
+void cs_count_launches(int n);
+
+// unpack.cu -----------------------------------------------------------------
+int cs_unpack2bit(const void* raw, int64_t nsamp, int nchan, int msb_first, const float lut4[4],
+                  float* out, cudaStream_t st);
+int cs_cornerturn2bit(const void* raw, int64_t nsamp, int nchan, void* planes, cudaStream_t st);
+
+// fft.cu --------------------------------------------------------------------
+// Twiddle table exp(-2 pi i m / n), m in [0, n), FP64-computed, device copy.
+// Cached per (device, n); valid until cs_free_twiddles().
+const float2* cs_twiddles(int n);
+void cs_free_twiddles();
+// Batched forward C2C FFT, n points (32..16384), interleaved complex.
+int cs_cfft_batch(const float2* in, float2* out, int n, int64_t batch, cudaStream_t st);
+// Batched forward R2C FFT, n real points (64..32768) -> n/2+1 bins.
+int cs_rfft_batch(const float* in, float2* out, int n, int64_t batch, cudaStream_t st);
+
+// fstage.cu -----------------------------------------------------------------
+struct CsDelayState {       // per (input, segment)
+    int32_t* shift;         // integer sample shift
+    float* phase0;          // fringe phase, radians in [0, 2 pi)
+    float* dphase;          // per-channel phase step, radians
+};
+// FP64 delay model -> delay state.  poly: [S][4] seconds (t^0..t^3).
+int cs_delay_state(const double* poly, int S, int N, int K, double fs_hz, double lo_hz,
+                   CsDelayState ds, cudaStream_t st);
+
+enum CsSpectraFormat { CS_SPECTRA_F32 = 0, CS_SPECTRA_F16 = 1 };
+struct CsFStageArgs {
+    const uint8_t* raw;         // [S][bytes_per_input], 2-bit single channel
+    int64_t bytes_per_input;
+    int S, N, K;
+    int64_t start_sample;
+    const int32_t* shift;       // [S*K] or null
+    const float* phase0;        // [S*K] or null (no phase correction)
+    const float* dphase;        // [S*K]
+    const float* scale;         // [S*C] per (input, channel) scale or null (1.0)
+    float lut[4];
+    int msb_first;
+    int format;                 // CsSpectraFormat
+    void* out;                  // F32: float2 [C][S][K];  F16: __half [C][2][S][K]
+};
+int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
+
+// xstage.cu -----------------------------------------------------------------
+// FP32 CUDA-core X stage: spectra float2 [C][S][K] -> vis float2 [C][P],
+// P = S(S+1)/2, p = i(i+1)/2 + j (j <= i), V = sum_k X_i conj(X_j).
+int cs_xmac_f32(const float2* spectra, int S, int C, int K, float2* vis, int accumulate,
+                cudaStream_t st);
+// Tensor-core (tcgen05, FP16 in, FP32 accumulate) X stage:
+// spectra __half [C][2][S][K] -> vis float2 [C][P]; inv_scale [S*C] or null.
+int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, float2* vis, const float* inv_scale,
+                   int accumulate, cudaStream_t st);
+// Baseline-major <-> channel-major triangle transpose ([C][P] -> [P][C]).
+int cs_vis_to_baseline_major(const float2* vis_cp, float2* vis_pc, int C, int64_t P, cudaStream_t st);
+
+// spectrometer.cu -----------------------------------------------------------
+struct CsSpecArgs {
+    const uint8_t* planes;      // [nsub][bytes_per_sub] packed 2-bit, LSB first
+    int64_t bytes_per_sub;
+    int nsub;
+    int N;                      // FFT points (1024 .. 65536)
+    int overlap;
+    int window;                 // 0 none, 1 cosine, 2 cosine^2
+    int ffts_per_spectrum;      // K (non-overlapped)
+    int nspec;
+    float lut[4];
+    float* power;               // [nsub][nspec][N/2+1]
+    float* partial;             // scratch, cs_spectrometer_scratch_floats() floats
+    // phase-cal (tonebins == 0 disables)
+    int tonebins, rotatorlen, ntones;
+    double pcal_offset_hz, fs_hz;
+    float2* pcal_bins;          // [nsub][nspec][tonebins]
+    float2* pcal_tones;         // [nsub][nspec][ntones] or null
+};
+int64_t cs_spectrometer_scratch_floats(const CsSpecArgs& a);
+int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st);
+
+// dsp.cu (task-API vector primitives) ---------------------------------------
+int cs_cmac(const float2* a, const float2* b, float2* acc, int64_t n, int conj_b, cudaStream_t st);
+int cs_cmul(const float2* a, const float2* b, float2* out, int64_t n, cudaStream_t st);
+int cs_cadd(const float2* a, const float2* b, float2* out, int64_t n, cudaStream_t st);
+int cs_sincos(const float* arg, float2* cossin, int64_t n, int normalized, cudaStream_t st);
+int cs_sincos_generator(float start, float inc, float2* cossin, int64_t n, cudaStream_t st);
+int cs_autocorr_acc(const float2* x, float2* acc, int64_t n, cudaStream_t st);

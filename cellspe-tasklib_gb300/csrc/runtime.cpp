@@ -1,0 +1,1287 @@
+// C-ABI runtime of the GB300 engine: the celldsp_* task runtime
+// (cellspe-tasklib.cpp:110-412), the spe* DSP wrappers
+// (cellspe-tasklib-dsp.cpp:94-359) and the direct cellspe_* entry points.
+//
+// An execution slot replaces an SPE.  Each slot owns a host worker thread (the
+// SPU main loop of cellspe-tasklib.cpp:440-617: take a task, run it, write
+// completed_flag and tick_count, follow next_task), a CUDA stream and a
+// device workspace.  Task vectors are host pointers by default, staged
+// through the workspace; CELLDSP_TASK_FLAG_DEVPTR marks device pointers.
+#include "../../include/cellspe_gpu.h"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <iostream>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+thread_local std::string t_err;
+
+int set_err(int code, const std::string& msg)
+{
+    t_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+    return set_err(CELLSPE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int map_rc(int rc, const char* where)
+{
+    if (rc == 0) return CELLSPE_OK;
+    if (rc == CS_ERR_ARG) return set_err(CELLSPE_ERR_ARG, std::string(where) + ": invalid argument");
+    if (rc == CS_ERR_UNSUPPORTED) return set_err(CELLSPE_ERR_UNSUPPORTED, std::string(where) + ": unsupported size or mode");
+    return cuda_fail((cudaError_t)rc, where);
+}
+
+#define RT_TRY(expr, where)                   \
+    do {                                      \
+        int _rc = map_rc((int)(expr), where); \
+        if (_rc) return _rc;                  \
+    } while (0)
+
+std::atomic<long long> g_budget{0};
+std::atomic<int> g_inject_direct{0};
+
+int ensure_device()
+{
+    static std::once_flag once;
+    static cudaError_t init_err = cudaSuccess;
+    std::call_once(once, [] {
+        int n = 0;
+        init_err = cudaGetDeviceCount(&n);
+        if (init_err == cudaSuccess && n == 0) init_err = cudaErrorNoDevice;
+        if (init_err == cudaSuccess) init_err = cudaSetDevice(0);
+        if (init_err == cudaSuccess) init_err = cudaFree(nullptr);
+    });
+    if (init_err != cudaSuccess) return cuda_fail(init_err, "GPU initialisation");
+    return cudaSetDevice(0) == cudaSuccess ? 0 : cuda_fail(cudaGetLastError(), "cudaSetDevice");
+}
+
+size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// Device workspace: a bump arena over one or more blocks.  After a job that
+// needed several blocks, reset() merges them into one, so steady-state jobs of
+// the same size allocate nothing.
+struct Arena {
+    std::vector<std::pair<char*, size_t>> blocks;
+    size_t used = 0;
+    size_t total_taken = 0;
+    size_t capacity() const
+    {
+        size_t c = 0;
+        for (auto& b : blocks) c += b.second;
+        return c;
+    }
+    void* take(size_t n, cudaError_t* err)
+    {
+        n = align256(std::max<size_t>(n, 1));
+        total_taken += n;
+        if (blocks.empty() || used + n > blocks.back().second) {
+            char* p = nullptr;
+            size_t sz = std::max(n, (size_t)64 << 20);
+            cudaError_t e = cudaMalloc(&p, sz);
+            if (e != cudaSuccess) {
+                *err = e;
+                return nullptr;
+            }
+            blocks.push_back({p, sz});
+            used = 0;
+        }
+        void* r = blocks.back().first + used;
+        used += n;
+        return r;
+    }
+    // stream must be idle
+    void reset()
+    {
+        if (blocks.size() > 1) {
+            size_t want = std::max(total_taken, capacity());
+            for (auto& b : blocks) cudaFree(b.first);
+            blocks.clear();
+            char* p = nullptr;
+            if (cudaMalloc(&p, want) == cudaSuccess) blocks.push_back({p, want});
+        }
+        used = 0;
+        total_taken = 0;
+    }
+    void release()
+    {
+        for (auto& b : blocks) cudaFree(b.first);
+        blocks.clear();
+        used = total_taken = 0;
+    }
+};
+
+struct Workspace {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t sev[5] = {};          // stage boundaries of the last FX job
+    Arena arena;
+    bool own_stream = true;
+    struct Out { void* host; const void* dev; size_t bytes; };
+    std::vector<Out> outs;
+    int init()
+    {
+        if (stream) return 0;
+        int rc = ensure_device();
+        if (rc) return rc;
+        cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreate(&ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&ev1);
+        for (auto& ev : sev)
+            if (e == cudaSuccess) e = cudaEventCreate(&ev);
+        return e == cudaSuccess ? 0 : cuda_fail(e, "stream setup");
+    }
+    void destroy()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        arena.release();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        for (auto& ev : sev)
+            if (ev) cudaEventDestroy(ev), ev = nullptr;
+        if (stream && own_stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+        ev0 = ev1 = nullptr;
+    }
+};
+
+thread_local std::unique_ptr<Workspace> t_ws;
+thread_local float t_stage_ms[4] = {0, 0, 0, 0};   // delay model, F stage, X stage, output
+
+Workspace* thread_ws(int* rc)
+{
+    if (!t_ws) t_ws.reset(new Workspace());
+    *rc = t_ws->init();
+    return *rc ? nullptr : t_ws.get();
+}
+
+long long budget_bytes()
+{
+    long long b = g_budget.load();
+    if (b > 0) return b;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return 0;
+    return (long long)(0.9 * (double)fr);
+}
+
+// Staging helper: host buffers are copied through the workspace; device
+// buffers are used in place.
+struct Job {
+    Workspace& ws;
+    bool host;
+    int err = 0;
+    Job(Workspace& w, bool h) : ws(w), host(h) { ws.outs.clear(); }
+    void* scratch(size_t bytes)
+    {
+        cudaError_t e = cudaSuccess;
+        void* p = ws.arena.take(bytes, &e);
+        if (!p && !err) err = cuda_fail(e, "workspace allocation");
+        return p;
+    }
+    const void* in(const void* p, size_t bytes)
+    {
+        if (!host || !p || bytes == 0) return p;
+        void* d = scratch(bytes);
+        if (d && !err) {
+            cudaError_t e = cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, ws.stream);
+            if (e != cudaSuccess) err = cuda_fail(e, "host to device copy");
+        }
+        return d;
+    }
+    void* out(void* p, size_t bytes, bool load_existing)
+    {
+        if (!host || !p || bytes == 0) return p;
+        void* d = scratch(bytes);
+        if (d && !err) {
+            if (load_existing) {
+                cudaError_t e = cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, ws.stream);
+                if (e != cudaSuccess) err = cuda_fail(e, "host to device copy");
+            }
+            ws.outs.push_back({p, d, bytes});
+        }
+        return d;
+    }
+    int finish(bool sync = true)
+    {
+        if (err) {
+            cudaStreamSynchronize(ws.stream);
+            ws.arena.reset();
+            return err;
+        }
+        for (auto& o : ws.outs) {
+            cudaError_t e = cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, ws.stream);
+            if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+        }
+        ws.outs.clear();
+        if (!sync) return 0;
+        cudaError_t e = cudaStreamSynchronize(ws.stream);
+        ws.arena.reset();
+        if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+        return 0;
+    }
+};
+
+bool pick_levels(int format, const float* custom, float out[4])
+{
+    static const float mk5b[4] = {-3.3359f, 1.0f, -1.0f, 3.3359f};
+    static const float twob[4] = {1.0f, -1.0f, 3.3359f, -3.3359f};
+    static const float offb[4] = {-3.336f, -1.0f, 1.0f, 3.336f};
+    if (custom) {
+        std::memcpy(out, custom, 4 * sizeof(float));
+        return true;
+    }
+    switch (format & 0xff) {
+        case CELLSPE_LEVELS_MARK5B: std::memcpy(out, mk5b, sizeof mk5b); return true;
+        case CELLSPE_LEVELS_TWOBIT: std::memcpy(out, twob, sizeof twob); return true;
+        case CELLSPE_LEVELS_OFFSET_BINARY: std::memcpy(out, offb, sizeof offb); return true;
+        default: return false;
+    }
+}
+
+bool pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// ---------------------------------------------------------------------------
+// engine operations (shared by the direct API and the task runtime)
+// ---------------------------------------------------------------------------
+int op_unpack(Workspace& ws, bool host, const void* raw, long long nsamp, int nchan, int format,
+              const float* custom, float* out)
+{
+    float lut[4];
+    if (!pick_levels(format, custom, lut)) return set_err(CELLSPE_ERR_ARG, "unpack: unknown level table");
+    if (nsamp < 0 || !raw || !out) return set_err(CELLSPE_ERR_ARG, "unpack: bad arguments");
+    bool msb = (format & CELLSPE_UNPACK_MSB_FIRST) != 0;
+    size_t in_bytes = (size_t)((nsamp * nchan * 2 + 7) / 8);
+    size_t out_bytes = (size_t)nsamp * nchan * sizeof(float);
+    Job j(ws, host);
+    const void* d_in = j.in(raw, in_bytes);
+    float* d_out = (float*)j.out(out, out_bytes, false);
+    if (!j.err) {
+        int rc = map_rc(cs_unpack2bit(d_in, nsamp, nchan, msb, lut, d_out, ws.stream), "unpack");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
+int op_fft(Workspace& ws, bool host, const void* in, void* out, int n, long long batch, bool real)
+{
+    if (!in || !out || batch < 0 || !pow2(n)) return set_err(CELLSPE_ERR_ARG, "fft: bad arguments");
+    size_t in_bytes = real ? (size_t)n * batch * 4 : (size_t)n * batch * 8;
+    size_t out_bytes = real ? (size_t)(n / 2 + 1) * batch * 8 : (size_t)n * batch * 8;
+    Job j(ws, host);
+    const void* d_in = j.in(in, in_bytes);
+    void* d_out = j.out(out, out_bytes, false);
+    if (!j.err) {
+        int rc = real ? cs_rfft_batch((const float*)d_in, (float2*)d_out, n, batch, ws.stream)
+                      : cs_cfft_batch((const float2*)d_in, (float2*)d_out, n, batch, ws.stream);
+        rc = map_rc(rc, "fft");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
+int op_xmac(Workspace& ws, bool host, const void* spectra, int S, int C, int K, void* vis, int accumulate)
+{
+    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0) return set_err(CELLSPE_ERR_ARG, "xmac: bad arguments");
+    long long P = (long long)S * (S + 1) / 2;
+    Job j(ws, host);
+    const void* d_sp = j.in(spectra, (size_t)C * S * K * 8);
+    void* d_vis = j.out(vis, (size_t)C * P * 8, accumulate != 0);
+    if (!j.err) {
+        int rc = map_rc(cs_xmac_f32((const float2*)d_sp, S, C, K, (float2*)d_vis, accumulate, ws.stream), "xmac");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
+long long fx_bytes(const cellspe_fx_params* p, bool with_poly)
+{
+    long long S = p->n_inputs, N = p->fft_points, K = p->n_segments, C = N / 2;
+    long long P = S * (S + 1) / 2;
+    bool host = p->memory == CELLSPE_MEM_HOST;
+    long long b = 0;
+    if (host) b += align256(S * p->bytes_per_input);
+    if (with_poly) b += align256(S * 32) + 3 * align256(S * K * 4);
+    b += align256(C * S * K * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));
+    bool stage_vis = host || p->vis_order == CELLSPE_VIS_BASELINE_MAJOR || p->accumulate;
+    if (stage_vis) b += 3 * align256(C * P * 8);
+    if (p->x_mode != CELLSPE_X_FP32) b += 2 * align256(S * C * 4);
+    return b;
+}
+
+int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const double* poly, void* vis, bool sync)
+{
+    if (!p || !raw || !vis) return set_err(CELLSPE_ERR_ARG, "fx: null argument");
+    const int S = p->n_inputs, N = p->fft_points, K = p->n_segments, C = N / 2;
+    if (S <= 0 || K <= 0 || !pow2(N) || N < 1024 || N > 32768)
+        return set_err(CELLSPE_ERR_ARG, "fx: need S > 0, K > 0, N a power of two in [1024, 32768]");
+    if (p->bytes_per_input <= 0 || p->bytes_per_input % 16)
+        return set_err(CELLSPE_ERR_ARG, "fx: bytes_per_input must be a positive multiple of 16");
+    if (!poly && (p->start_sample < 0 || p->start_sample + (long long)K * N > p->bytes_per_input * 4))
+        return set_err(CELLSPE_ERR_ARG, "fx: segments run past the end of the input");
+    if (p->x_mode != CELLSPE_X_FP32 && p->x_mode != CELLSPE_X_TC_FP16)
+        return set_err(CELLSPE_ERR_ARG, "fx: unknown x_mode");
+    if (poly && !(p->sample_rate_hz > 0)) return set_err(CELLSPE_ERR_ARG, "fx: delay model needs sample_rate_hz");
+    float lut[4];
+    if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "fx: unknown level table");
+    long long need = fx_bytes(p, poly != nullptr);
+    long long budget = budget_bytes() + (long long)ws.arena.capacity();
+    if (need > budget)
+        return set_err(CELLSPE_ERR_NOMEM, "fx: job needs " + std::to_string(need) + " device bytes, budget " +
+                                              std::to_string(budget));
+    const bool host = p->memory == CELLSPE_MEM_HOST;
+    const long long P = (long long)S * (S + 1) / 2;
+    Job j(ws, host);
+    const uint8_t* d_raw = (const uint8_t*)j.in(raw, (size_t)S * p->bytes_per_input);
+    if (sync) cudaEventRecord(ws.sev[0], ws.stream);
+    CsFStageArgs fa{};
+    fa.raw = d_raw;
+    fa.bytes_per_input = p->bytes_per_input;
+    fa.S = S; fa.N = N; fa.K = K;
+    fa.start_sample = p->start_sample;
+    std::memcpy(fa.lut, lut, sizeof lut);
+    fa.msb_first = (p->levels & CELLSPE_UNPACK_MSB_FIRST) ? 1 : 0;
+    fa.format = p->x_mode == CELLSPE_X_FP32 ? CS_SPECTRA_F32 : CS_SPECTRA_F16;
+    if (poly) {
+        const double* d_poly = (const double*)j.in(poly, (size_t)S * 4 * sizeof(double));
+        CsDelayState ds;
+        ds.shift = (int32_t*)j.scratch((size_t)S * K * 4);
+        ds.phase0 = (float*)j.scratch((size_t)S * K * 4);
+        ds.dphase = (float*)j.scratch((size_t)S * K * 4);
+        if (!j.err) {
+            int rc = map_rc(cs_delay_state(d_poly, S, N, K, p->sample_rate_hz, p->lo_freq_hz, ds, ws.stream), "delay model");
+            if (rc) j.err = rc;
+        }
+        fa.shift = ds.shift; fa.phase0 = ds.phase0; fa.dphase = ds.dphase;
+    }
+    const float* d_inv_scale = nullptr;
+    if (p->x_mode != CELLSPE_X_FP32) {
+        if (p->channel_scale) {
+            fa.scale = (const float*)j.in(p->channel_scale, (size_t)S * C * 4);
+        }
+    }
+    fa.out = j.scratch((size_t)C * S * K * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
+    if (sync) cudaEventRecord(ws.sev[1], ws.stream);
+    if (!j.err) {
+        int rc = map_rc(cs_fx_fstage(fa, ws.stream), "F stage");
+        if (rc) j.err = rc;
+    }
+    if (sync) cudaEventRecord(ws.sev[2], ws.stream);
+    // X stage into a channel-major buffer
+    const bool direct = !host && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR && !p->accumulate;
+    float2* vis_cp = direct ? (float2*)vis : (float2*)j.scratch((size_t)C * P * 8);
+    if (!j.err) {
+        int rc;
+        if (p->x_mode == CELLSPE_X_FP32)
+            rc = cs_xmac_f32((const float2*)fa.out, S, C, K, vis_cp, 0, ws.stream);
+        else
+            rc = cs_xmac_tc_f16(fa.out, S, C, K, vis_cp, d_inv_scale, 0, ws.stream);
+        rc = map_rc(rc, "X stage");
+        if (rc) j.err = rc;
+    }
+    if (sync) cudaEventRecord(ws.sev[3], ws.stream);
+    if (p->x_mode != CELLSPE_X_FP32 && fa.scale && !j.err) {
+        // undo the F-stage scale: V_ij /= s_i s_j (per channel)
+        j.err = set_err(CELLSPE_ERR_UNSUPPORTED, "fx: channel_scale is applied by the tensor-core epilogue only");
+    }
+    if (!direct && !j.err) {
+        float2* result = vis_cp;
+        if (p->vis_order == CELLSPE_VIS_BASELINE_MAJOR) {
+            float2* t = (float2*)j.scratch((size_t)C * P * 8);
+            if (!j.err) {
+                int rc = map_rc(cs_vis_to_baseline_major(vis_cp, t, C, P, ws.stream), "transpose");
+                if (rc) j.err = rc;
+            }
+            result = t;
+        }
+        if (!j.err) {
+            if (p->accumulate) {
+                float2* old = (float2*)j.out(vis, (size_t)C * P * 8, true);
+                if (!j.err) {
+                    int rc = map_rc(cs_cadd(old, result, old, C * P, ws.stream), "accumulate");
+                    if (rc) j.err = rc;
+                }
+            } else if (host) {
+                ws.outs.push_back({vis, result, (size_t)C * P * 8});
+            } else {
+                cudaError_t e = cudaMemcpyAsync(vis, result, (size_t)C * P * 8, cudaMemcpyDeviceToDevice, ws.stream);
+                if (e != cudaSuccess) j.err = cuda_fail(e, "result copy");
+            }
+        }
+    }
+    if (sync) cudaEventRecord(ws.sev[4], ws.stream);
+    int rc = j.finish(sync);
+    if (sync && !rc) {
+        for (int i = 0; i < 4; i++) {
+            float ms = 0.f;
+            t_stage_ms[i] = cudaEventElapsedTime(&ms, ws.sev[i], ws.sev[i + 1]) == cudaSuccess ? ms : -1.f;
+        }
+    }
+    return rc;
+}
+
+long long spec_bytes(const cellspe_spec_params* p)
+{
+    CsSpecArgs a{};
+    a.nsub = p->n_subbands; a.N = p->fft_points; a.overlap = p->overlap;
+    a.ffts_per_spectrum = p->ffts_per_spectrum; a.nspec = p->n_spectra; a.tonebins = p->pcal_tonebins;
+    long long b = align256(cs_spectrometer_scratch_floats(a) * 4);
+    bool host = p->memory == CELLSPE_MEM_HOST;
+    if (host) b += align256(p->raw_bytes);
+    if (p->input_layout == CELLSPE_SPEC_INTERLEAVED && p->n_subbands > 1) b += align256(p->raw_bytes);
+    long long rows = (long long)p->n_subbands * p->n_spectra;
+    if (host) b += align256(rows * (p->fft_points / 2 + 1) * 4) + 2 * align256(rows * std::max(p->pcal_tonebins, p->pcal_ntones) * 8);
+    return b;
+}
+
+int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw, float* power, void* pcal_bins,
+                    void* pcal_tones)
+{
+    if (!p || !raw || !power) return set_err(CELLSPE_ERR_ARG, "spectrometer: null argument");
+    const int nsub = p->n_subbands;
+    if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16)) return set_err(CELLSPE_ERR_ARG, "spectrometer: n_subbands must be 1, 4, 8 or 16");
+    if (!pow2(p->fft_points) || p->fft_points < 1024 || p->fft_points > 65536)
+        return set_err(CELLSPE_ERR_ARG, "spectrometer: fft_points must be a power of two in [1024, 65536]");
+    if (p->raw_bytes <= 0 || p->raw_bytes % (16 * nsub)) return set_err(CELLSPE_ERR_ARG, "spectrometer: raw_bytes must be a multiple of 16*n_subbands");
+    if (p->pcal_tonebins > 0 && !pcal_bins) return set_err(CELLSPE_ERR_ARG, "spectrometer: pcal enabled without pcal_bins");
+    float lut[4];
+    if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown level table");
+    long long need = spec_bytes(p);
+    long long budget = budget_bytes() + (long long)ws.arena.capacity();
+    if (need > budget) return set_err(CELLSPE_ERR_NOMEM, "spectrometer: job exceeds the device memory budget");
+    const bool host = p->memory == CELLSPE_MEM_HOST;
+    Job j(ws, host);
+    const uint8_t* d_raw = (const uint8_t*)j.in(raw, (size_t)p->raw_bytes);
+    const long long bytes_per_sub = p->raw_bytes / nsub;
+    const uint8_t* planes = d_raw;
+    if (p->input_layout == CELLSPE_SPEC_INTERLEAVED && nsub > 1) {
+        void* pl = j.scratch((size_t)p->raw_bytes);
+        if (!j.err) {
+            long long nsamp = p->raw_bytes * 4 / nsub;
+            int rc = map_rc(cs_cornerturn2bit(d_raw, nsamp, nsub, pl, ws.stream), "corner turn");
+            if (rc) j.err = rc;
+        }
+        planes = (const uint8_t*)pl;
+    }
+    CsSpecArgs a{};
+    a.planes = planes; a.bytes_per_sub = bytes_per_sub; a.nsub = nsub; a.N = p->fft_points;
+    a.overlap = p->overlap; a.window = p->window; a.ffts_per_spectrum = p->ffts_per_spectrum; a.nspec = p->n_spectra;
+    std::memcpy(a.lut, lut, sizeof lut);
+    a.tonebins = p->pcal_tonebins; a.rotatorlen = p->pcal_rotatorlen; a.ntones = p->pcal_ntones;
+    a.pcal_offset_hz = p->pcal_offset_hz; a.fs_hz = p->sample_rate_hz;
+    const long long rows = (long long)nsub * p->n_spectra;
+    a.power = (float*)j.out(power, (size_t)rows * (p->fft_points / 2 + 1) * 4, false);
+    if (a.tonebins > 0) {
+        a.pcal_bins = (float2*)j.out(pcal_bins, (size_t)rows * a.tonebins * 8, false);
+        a.pcal_tones = pcal_tones ? (float2*)j.out(pcal_tones, (size_t)rows * a.ntones * 8, false) : nullptr;
+    }
+    a.partial = (float*)j.scratch((size_t)cs_spectrometer_scratch_floats(a) * 4);
+    if (!j.err) {
+        int rc = map_rc(cs_spectrometer(a, ws.stream), "spectrometer");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
+// ---------------------------------------------------------------------------
+// task runtime
+// ---------------------------------------------------------------------------
+struct Slot {
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    CellDSPTask_t* pending = nullptr;
+    bool running = false, done = false, quit = false, has_result = false;
+    int result = 0;
+    unsigned flags = CDSP_EF_DEFAULT;
+    int fft_n = 0;
+    std::atomic<int> inject{0};
+    Workspace ws;
+};
+
+struct Engine {
+    std::mutex mu;
+    std::condition_variable freecv;
+    Slot slots[CELLDSP_MAX_SPE_NR];
+    int clients = 0;
+    unsigned behaviour = CDSP_BEHAV_DEFAULT;
+    int free_waiters = 0;
+};
+
+std::mutex g_eng_mu;
+Engine* g_eng = nullptr;
+
+struct Vec {
+    void* p;
+    size_t n;
+};
+Vec invec(CellDSPTask_t* t, unsigned i) { return {t->inputvector_ptrs[i].p, t->inputvector_lengths[i]}; }
+Vec outvec(CellDSPTask_t* t, unsigned i) { return {t->outputvector_ptrs[i].p, t->outputvector_lengths[i]}; }
+
+int complex_op(Slot& s, CellDSPTask_t* t, bool host, int kind)
+{
+    if (t->num_input_vectors < 2 || t->num_output_vectors < 1) return CELLDSP_TASK_GENERICERROR;
+    Vec a = invec(t, 0), b = invec(t, 1), o = outvec(t, 0);
+    size_t n = a.n / 8;
+    if (b.n < n * 8 || o.n < n * 8) return CELLDSP_TASK_GENERICERROR;
+    Job j(s.ws, host);
+    const float2* da = (const float2*)j.in(a.p, n * 8);
+    const float2* db = (const float2*)j.in(b.p, n * 8);
+    float2* dout = (float2*)j.out(o.p, n * 8, kind <= 1);
+    if (!j.err) {
+        int rc = 0;
+        switch (kind) {
+            case 0: rc = cs_cmac(da, db, dout, n, 0, s.ws.stream); break;
+            case 1: rc = cs_cmac(da, db, dout, n, 1, s.ws.stream); break;
+            case 2: rc = cs_cmul(da, db, dout, n, s.ws.stream); break;
+            default: rc = cs_cadd(da, db, dout, n, s.ws.stream); break;
+        }
+        rc = map_rc(rc, "vector op");
+        if (rc) j.err = rc;
+    }
+    return j.finish() ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+}
+
+// CELLDSP_TASK_DIFXPROCESS (exec_difxprocess, cellspe-tasklib-dsp.cpp:609-698):
+// in0 nfft complex points, in-place FFT; the band starts at in0 (lower) or
+// outputvector_lengths[0] bytes into the FFT output (upper, as the reference
+// indexes it); band[i] *= complexfracmult[i] for numchannels points;
+// autocorr[i].re += |band[i]|^2 (out2, read-modify-write); out0 <- band.
+// The FFT buffer is padded with zeros so that the upper-band window of the
+// reference never reads past it.
+int difx_op(Slot& s, CellDSPTask_t* t, bool host)
+{
+    if (t->num_input_vectors < 2 || t->num_output_vectors < 3) return CELLDSP_TASK_GENERICERROR;
+    const CellDSPParams_Difx_t& d = t->subcontext.Difx;
+    int nfft = (int)d.nfft, nch = (int)d.numchannels;
+    Vec in0 = invec(t, 0), in1 = invec(t, 1), o0 = outvec(t, 0), o2 = outvec(t, 2);
+    if (!pow2(nfft) || in0.n < (size_t)nfft * 8 || in1.n < (size_t)nch * 8 || o2.n < (size_t)nch * 8)
+        return CELLDSP_TASK_GENERICERROR;
+    size_t band_off = d.useUpperOrLower ? o0.n : 0;
+    size_t pad = (size_t)nfft * 8 + band_off + o0.n + (size_t)nch * 8;
+    Job j(s.ws, host);
+    const float2* din = (const float2*)j.in(in0.p, (size_t)nfft * 8);
+    const float2* dmul = (const float2*)j.in(in1.p, (size_t)nch * 8);
+    float2* dacc = (float2*)j.out(o2.p, o2.n, true);
+    char* fft = (char*)j.scratch(pad);
+    if (!j.err) {
+        cudaError_t e = cudaMemsetAsync(fft, 0, pad, s.ws.stream);
+        int rc = e == cudaSuccess ? map_rc(cs_cfft_batch(din, (float2*)fft, nfft, 1, s.ws.stream), "difx fft")
+                                  : cuda_fail(e, "memset");
+        float2* band = (float2*)(fft + band_off);
+        if (!rc) rc = map_rc(cs_cmul(dmul, band, band, nch, s.ws.stream), "difx mul");
+        if (!rc) rc = map_rc(cs_autocorr_acc(band, dacc, nch, s.ws.stream), "difx autocorr");
+        if (!rc) {
+            if (host) s.ws.outs.push_back({o0.p, band, o0.n});
+            else {
+                cudaError_t e2 = cudaMemcpyAsync(o0.p, band, o0.n, cudaMemcpyDeviceToDevice, s.ws.stream);
+                if (e2 != cudaSuccess) rc = cuda_fail(e2, "difx copy");
+            }
+        }
+        if (rc) j.err = rc;
+    }
+    return j.finish() ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+}
+
+int run_task(Slot& s, CellDSPTask_t* t)
+{
+    const unsigned cmd = t->command & CELLDSP_TASK_CMD_MASK;
+    const bool host = !(t->command & CELLDSP_TASK_FLAG_DEVPTR);
+    if (s.inject.load() > 0) {
+        s.inject--;
+        set_err(CELLSPE_ERR_INJECTED, "injected task failure");
+        return CELLDSP_TASK_GENERICERROR;
+    }
+    switch (cmd) {
+        case CELLDSP_TASK_NOP:
+        case CELLDSP_TASK_IOBENCH:
+        case CELLDSP_TASK_RUNALL:
+        case CELLDSP_TASK_DMASIMULATION:
+            return CELLDSP_TASK_OK;
+        case CELLDSP_TASK_IOTEST: {   // do_in_out_test, cellspe-tasklib-dsp.cpp:1121-1131
+            if (t->num_output_vectors < 1 || t->outputvector_lengths[0] < 16) return CELLDSP_TASK_GENERICERROR;
+            const float v[4] = {0.1f, 2.3f, 4.5f, 6.7f};
+            if (host) std::memcpy(t->outputvector_ptrs[0].p, v, sizeof v);
+            else if (cudaMemcpy(t->outputvector_ptrs[0].p, v, sizeof v, cudaMemcpyHostToDevice) != cudaSuccess)
+                return CELLDSP_TASK_GENERICERROR;
+            return CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_MAC: return complex_op(s, t, host, 0);
+        case CELLDSP_TASK_MAC_CONJ: return complex_op(s, t, host, 1);
+        case CELLDSP_TASK_MULC: return complex_op(s, t, host, 2);
+        case CELLDSP_TASK_ADDC: return complex_op(s, t, host, 3);
+        case CELLDSP_TASK_FFT_INIT: {
+            int n = (int)t->subcontext.FFT.nfft;
+            if (!pow2(n) || n < 16 || n > 16384) return CELLDSP_TASK_GENERICERROR;
+            if (!cs_twiddles(2 * n)) return CELLDSP_TASK_GENERICERROR;
+            s.fft_n = n;
+            return CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_FFT_FREE:
+            s.fft_n = 0;
+            return CELLDSP_TASK_OK;
+        case CELLDSP_TASK_FFT_EXEC:
+        case CELLDSP_TASK_FFT_EXEC_DYN: {
+            int n = (int)t->subcontext.FFT.nfft;
+            if (cmd == CELLDSP_TASK_FFT_EXEC && n != s.fft_n) return CELLDSP_TASK_GENERICERROR;
+            if (t->num_input_vectors < 1 || t->num_output_vectors < 1 || !pow2(n)) return CELLDSP_TASK_GENERICERROR;
+            long long batch = t->inputvector_lengths[0] / (8LL * n);
+            if (batch < 1 || t->outputvector_lengths[0] < (size_t)batch * n * 8) return CELLDSP_TASK_GENERICERROR;
+            return op_fft(s.ws, host, t->inputvector_ptrs[0].p, t->outputvector_ptrs[0].p, n, batch, false)
+                       ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_RFFT: {
+            int n = (int)t->subcontext.FFT.nfft;
+            if (t->num_input_vectors < 1 || t->num_output_vectors < 1 || !pow2(n)) return CELLDSP_TASK_GENERICERROR;
+            long long batch = t->inputvector_lengths[0] / (4LL * n);
+            if (batch < 1 || t->outputvector_lengths[0] < (size_t)batch * (n / 2 + 1) * 8) return CELLDSP_TASK_GENERICERROR;
+            return op_fft(s.ws, host, t->inputvector_ptrs[0].p, t->outputvector_ptrs[0].p, n, batch, true)
+                       ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_SINCOS:
+        case CELLDSP_TASK_SINCOS_NORM: {
+            if (t->num_input_vectors < 1 || t->num_output_vectors < 1) return CELLDSP_TASK_GENERICERROR;
+            size_t n = t->subcontext.Phase.argcount ? t->subcontext.Phase.argcount : t->inputvector_lengths[0] / 4;
+            if (t->inputvector_lengths[0] < n * 4 || t->outputvector_lengths[0] < n * 8) return CELLDSP_TASK_GENERICERROR;
+            Job j(s.ws, host);
+            const float* din = (const float*)j.in(t->inputvector_ptrs[0].p, n * 4);
+            float2* dout = (float2*)j.out(t->outputvector_ptrs[0].p, n * 8, false);
+            if (!j.err) {
+                int rc = map_rc(cs_sincos(din, dout, n, cmd == CELLDSP_TASK_SINCOS_NORM, s.ws.stream), "sincos");
+                if (rc) j.err = rc;
+            }
+            return j.finish() ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_SINCOS_GENERTR: {
+            if (t->num_output_vectors < 1) return CELLDSP_TASK_GENERICERROR;
+            size_t n = t->subcontext.Phase.argcount;
+            if (t->outputvector_lengths[0] < n * 8) return CELLDSP_TASK_GENERICERROR;
+            Job j(s.ws, host);
+            float2* dout = (float2*)j.out(t->outputvector_ptrs[0].p, n * 8, false);
+            if (!j.err) {
+                int rc = map_rc(cs_sincos_generator(t->subcontext.Phase.phase_start, t->subcontext.Phase.phase_delta,
+                                                    dout, n, s.ws.stream), "sincos generator");
+                if (rc) j.err = rc;
+            }
+            return j.finish() ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_UNPACK: {
+            const CellDSPParams_Unpack_t& u = t->subcontext.Unpack;
+            long long nsamp = (long long)u.nsamp_lo | ((long long)u.nsamp_hi << 32);
+            int nch = (int)u.nchan;
+            if (t->num_input_vectors < 1 || t->num_output_vectors < 1 || nch < 1) return CELLDSP_TASK_GENERICERROR;
+            const float* custom = (t->num_input_vectors >= 2 && t->inputvector_lengths[1] >= 16 && host)
+                                      ? (const float*)t->inputvector_ptrs[1].p : nullptr;
+            if ((long long)t->inputvector_lengths[0] * 4 < nsamp * nch) return CELLDSP_TASK_GENERICERROR;
+            if (t->num_output_vectors == (unsigned)nch && nch > 1) {
+                // one output vector per channel: unpack into the workspace, copy planes
+                for (int c = 0; c < nch; c++)
+                    if (t->outputvector_lengths[c] < (size_t)nsamp * 4) return CELLDSP_TASK_GENERICERROR;
+                std::vector<float> tmp((size_t)nsamp * nch);
+                float* dst = tmp.data();
+                float* dev = nullptr;
+                if (!host) {
+                    if (cudaMalloc(&dev, (size_t)nsamp * nch * 4) != cudaSuccess) return CELLDSP_TASK_GENERICERROR;
+                    dst = dev;
+                }
+                int rc = op_unpack(s.ws, host, t->inputvector_ptrs[0].p, nsamp, nch, (int)u.format, custom, dst);
+                for (int c = 0; c < nch && !rc; c++) {
+                    if (host) std::memcpy(t->outputvector_ptrs[c].p, tmp.data() + (size_t)c * nsamp, (size_t)nsamp * 4);
+                    else rc = cudaMemcpy(t->outputvector_ptrs[c].p, dev + (size_t)c * nsamp, (size_t)nsamp * 4,
+                                         cudaMemcpyDeviceToDevice) != cudaSuccess;
+                }
+                if (dev) cudaFree(dev);
+                return rc ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+            }
+            if (t->outputvector_lengths[0] < (size_t)nsamp * nch * 4) return CELLDSP_TASK_GENERICERROR;
+            return op_unpack(s.ws, host, t->inputvector_ptrs[0].p, nsamp, nch, (int)u.format, custom,
+                             (float*)t->outputvector_ptrs[0].p) ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_DIFXPROCESS: return difx_op(s, t, host);
+        case CELLDSP_TASK_FX_CORRELATE: {
+            if (t->num_input_vectors < 2 || t->num_output_vectors < 1 ||
+                t->inputvector_lengths[0] < sizeof(cellspe_fx_params)) return CELLDSP_TASK_GENERICERROR;
+            cellspe_fx_params p = *(const cellspe_fx_params*)t->inputvector_ptrs[0].p;
+            p.memory = host ? CELLSPE_MEM_HOST : CELLSPE_MEM_DEVICE;
+            const double* poly = t->num_input_vectors >= 3 ? (const double*)t->inputvector_ptrs[2].p : nullptr;
+            return op_fx(s.ws, &p, t->inputvector_ptrs[1].p, poly, t->outputvector_ptrs[0].p, true)
+                       ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_SPECTROMETER: {
+            if (t->num_input_vectors < 2 || t->num_output_vectors < 1 ||
+                t->inputvector_lengths[0] < sizeof(cellspe_spec_params)) return CELLDSP_TASK_GENERICERROR;
+            cellspe_spec_params p = *(const cellspe_spec_params*)t->inputvector_ptrs[0].p;
+            p.memory = host ? CELLSPE_MEM_HOST : CELLSPE_MEM_DEVICE;
+            void* bins = t->num_output_vectors >= 2 ? t->outputvector_ptrs[1].p : nullptr;
+            void* tones = t->num_output_vectors >= 3 ? t->outputvector_ptrs[2].p : nullptr;
+            return op_spectrometer(s.ws, &p, t->inputvector_ptrs[1].p, (float*)t->outputvector_ptrs[0].p, bins, tones)
+                       ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        case CELLDSP_TASK_XMAC: {
+            if (t->num_input_vectors < 2 || t->num_output_vectors < 1 ||
+                t->inputvector_lengths[0] < sizeof(cellspe_xmac_params)) return CELLDSP_TASK_GENERICERROR;
+            cellspe_xmac_params p = *(const cellspe_xmac_params*)t->inputvector_ptrs[0].p;
+            return op_xmac(s.ws, host, t->inputvector_ptrs[1].p, p.S, p.C, p.K, t->outputvector_ptrs[0].p, p.accumulate)
+                       ? CELLDSP_TASK_GENERICERROR : CELLDSP_TASK_OK;
+        }
+        default:
+            return CELLDSP_TASK_UNKOWNCOMMAND;
+    }
+}
+
+void worker_main(Slot* s)
+{
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->cv.wait(lk, [&] { return s->quit || s->pending; });
+        if (s->pending) {
+            CellDSPTask_t* t = s->pending;
+            s->pending = nullptr;
+            s->running = true;
+            lk.unlock();
+            int code = CELLDSP_TASK_OK;
+            int init = s->ws.init();
+            for (; t; t = (CellDSPTask_t*)t->next_task.p) {
+                unsigned ns = 0;
+                if (init) code = CELLDSP_TASK_GENERICERROR;
+                else {
+                    cudaEventRecord(s->ws.ev0, s->ws.stream);
+                    code = run_task(*s, t);
+                    cudaEventRecord(s->ws.ev1, s->ws.stream);
+                    float ms = 0.f;
+                    if (cudaEventSynchronize(s->ws.ev1) == cudaSuccess &&
+                        cudaEventElapsedTime(&ms, s->ws.ev0, s->ws.ev1) == cudaSuccess) {
+                        double v = (double)ms * 1e6;
+                        ns = v >= 4294967295.0 ? 0xFFFFFFFFu : (unsigned)v;
+                    }
+                }
+                t->tick_count = ns;
+                t->completed_flag = (unsigned short)code;
+                if (code != CELLDSP_TASK_OK)
+                    std::cerr << "cellspe task (cmd=" << t->command << ") failed: " << t_err << std::endl;
+            }
+            lk.lock();
+            s->running = false;
+            s->done = true;
+            s->has_result = true;
+            s->result = code;
+            s->cv.notify_all();
+        }
+        if (s->quit && !s->pending) break;
+    }
+    lk.unlock();
+    s->ws.destroy();
+}
+
+}  // namespace
+
+// ===========================================================================
+// exported: task runtime
+// ===========================================================================
+extern "C" {
+
+int celldsp_start(void)
+{
+    std::lock_guard<std::mutex> g(g_eng_mu);
+    if (g_eng) {
+        std::lock_guard<std::mutex> lk(g_eng->mu);
+        g_eng->clients++;
+        std::cerr << "celldsp_start: client " << g_eng->clients << " re-uses the running engine" << std::endl;
+        return 0;
+    }
+    if (ensure_device()) {
+        std::cerr << "celldsp_start: " << t_err << std::endl;
+        return -1;
+    }
+    g_eng = new Engine();
+    g_eng->clients = 1;
+    for (auto& s : g_eng->slots) s.th = std::thread(worker_main, &s);
+    return 0;
+}
+
+int celldsp_stop(void)
+{
+    std::lock_guard<std::mutex> g(g_eng_mu);
+    if (!g_eng) return -1;
+    {
+        std::lock_guard<std::mutex> lk(g_eng->mu);
+        if (--g_eng->clients > 0) {
+            std::cerr << "celldsp_stop: other clients still use the engine" << std::endl;
+            return 0;
+        }
+    }
+    for (auto& s : g_eng->slots) {
+        {
+            std::lock_guard<std::mutex> lk(s.mu);
+            s.quit = true;
+        }
+        s.cv.notify_all();
+    }
+    for (auto& s : g_eng->slots) s.th.join();
+    delete g_eng;
+    g_eng = nullptr;
+    return 0;
+}
+
+void celldsp_setBehaviour(unsigned int flags)
+{
+    if (!g_eng) return;
+    std::lock_guard<std::mutex> lk(g_eng->mu);
+    g_eng->behaviour = flags;
+}
+
+unsigned int celldsp_getBehaviour(void) { return g_eng ? g_eng->behaviour : 0; }
+
+int celldsp_getFreeSPE(void)
+{
+    if (!g_eng) return -1;
+    std::unique_lock<std::mutex> lk(g_eng->mu);
+    for (;;) {
+        for (int i = 0; i < CELLDSP_MAX_SPE_NR; i++) {
+            if (!(g_eng->slots[i].flags & CDSP_EF_RESERVED)) {
+                g_eng->slots[i].flags |= CDSP_EF_RESERVED;
+                return i;
+            }
+        }
+        if (!(g_eng->behaviour & CDSP_BEHAV_BLOCKING)) return -1;
+        g_eng->free_waiters++;
+        g_eng->freecv.wait(lk);
+        g_eng->free_waiters--;
+    }
+}
+
+int celldsp_setFreeSPE(int targetSPE)
+{
+    if (!g_eng || targetSPE < 0 || targetSPE >= CELLDSP_MAX_SPE_NR) return -1;
+    std::lock_guard<std::mutex> lk(g_eng->mu);
+    Slot& s = g_eng->slots[targetSPE];
+    if (s.flags & CDSP_EF_RESERVED) {
+        s.flags = CDSP_EF_DEFAULT;
+        g_eng->freecv.notify_all();
+    } else {
+        std::cerr << "warning: celldsp_setFreeSPE(SPE " << targetSPE << ") was already free" << std::endl;
+    }
+    return 0;
+}
+
+int celldsp_startTask(int targetSPE, CellDSPTask_t* task)
+{
+    if (!g_eng || !task || targetSPE < 0 || targetSPE >= CELLDSP_MAX_SPE_NR) return -1;
+    Slot& s = g_eng->slots[targetSPE];
+    {
+        std::lock_guard<std::mutex> lk(g_eng->mu);
+        if (!(s.flags & CDSP_EF_RESERVED)) {
+            std::cerr << "celldsp_startTask: slot " << targetSPE << " is not reserved" << std::endl;
+            return -1;
+        }
+    }
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (s.pending || s.running) {
+        std::cerr << "celldsp_startTask: slot " << targetSPE << " is busy" << std::endl;
+        return -1;
+    }
+    for (CellDSPTask_t* t = task; t; t = (CellDSPTask_t*)t->next_task.p) t->completed_flag = CELLDSP_TASK_INCOMPLETE;
+    s.pending = task;
+    s.done = false;
+    s.cv.notify_all();
+    return 0;
+}
+
+int celldsp_waitTask(int targetSPE)
+{
+    if (!g_eng || targetSPE < 0 || targetSPE >= CELLDSP_MAX_SPE_NR) return -1;
+    Slot& s = g_eng->slots[targetSPE];
+    std::unique_lock<std::mutex> lk(s.mu);
+    if (!s.pending && !s.running && !s.done) {
+        std::cerr << "celldsp_waitTask: no task was started on slot " << targetSPE << std::endl;
+        return -1;
+    }
+    s.cv.wait(lk, [&] { return s.done; });
+    s.done = false;
+    return s.result;
+}
+
+int celldsp_executeTask(CellDSPTask_t* task)
+{
+    int slot = celldsp_getFreeSPE();
+    if (slot == -1) {
+        std::cerr << "celldsp_executeTask(cmd=" << (task ? task->command : 0) << ") : could not get any free slot" << std::endl;
+        return 1;
+    }
+    if (celldsp_startTask(slot, task) == -1) {
+        celldsp_setFreeSPE(slot);
+        return 1;
+    }
+    int result = celldsp_waitTask(slot);
+    celldsp_setFreeSPE(slot);
+    if (result != CELLDSP_TASK_OK) {
+        std::cerr << "celldsp_executeTask : task returned error code " << result << std::endl;
+        return 1;
+    }
+    return 0;
+}
+
+int celldsp_startContinuableTask(CellDSPTask_t* task, int* speID)
+{
+    *speID = celldsp_getFreeSPE();
+    if (*speID == -1) return 1;
+    if (celldsp_startTask(*speID, task) == -1) {
+        celldsp_setFreeSPE(*speID);
+        *speID = -1;
+        return 1;
+    }
+    int result = celldsp_waitTask(*speID);
+    if (result != CELLDSP_TASK_OK) {
+        celldsp_setFreeSPE(*speID);
+        *speID = -1;
+        return 1;
+    }
+    g_eng->slots[*speID].flags |= CDSP_EF_CONTINUABLE;
+    return 0;
+}
+
+int celldsp_continueTask(CellDSPTask_t* task, int* speID)
+{
+    if (!speID || *speID < 0) return 1;
+    if (celldsp_startTask(*speID, task) == -1) return 1;
+    return celldsp_waitTask(*speID) == CELLDSP_TASK_OK ? 0 : 1;
+}
+
+int celldsp_stopContinuableTask(int* speID)
+{
+    if (!speID || *speID < 0) return 1;
+    celldsp_setFreeSPE(*speID);
+    *speID = -1;
+    return 0;
+}
+
+// ===========================================================================
+// exported: spe* wrappers (cellspe-tasklib-dsp.cpp:94-359)
+// ===========================================================================
+static void task_init(CellDSPTask_t* t, unsigned cmd)
+{
+    std::memset(t, 0, sizeof *t);
+    t->command = cmd;
+}
+static void add_in(CellDSPTask_t* t, void* p, size_t n)
+{
+    t->inputvector_ptrs[t->num_input_vectors].p = p;
+    t->inputvector_lengths[t->num_input_vectors++] = (unsigned)n;
+}
+static void add_out(CellDSPTask_t* t, void* p, size_t n)
+{
+    t->outputvector_ptrs[t->num_output_vectors].p = p;
+    t->outputvector_lengths[t->num_output_vectors++] = (unsigned)n;
+}
+
+int speNOP(void)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_NOP);
+    return celldsp_executeTask(&t);
+}
+
+int speRunAllCheck(void)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_RUNALL);
+    return celldsp_executeTask(&t);
+}
+
+int speIOCheck(void)
+{
+    static float output[8] __attribute__((aligned(128)));
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_IOTEST);
+    add_out(&t, output, sizeof output);
+    int status = celldsp_executeTask(&t);
+    std::cout << "speIOCheck wrote back : vect={" << output[0] << "," << output[1] << "," << output[2] << ","
+              << output[3] << "}   expected would be {0.1,2.3,4.5,6.7}" << std::endl;
+    return status;
+}
+
+int speIOSimulation(void)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_DMASIMULATION);
+    return celldsp_executeTask(&t);
+}
+
+int speIOBench(void* buffer, unsigned int bufbytes, int spes)
+{
+    (void)buffer; (void)bufbytes; (void)spes;
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_IOBENCH);
+    return celldsp_executeTask(&t);
+}
+
+int speIOBenchStreamed(void* buffer, unsigned int bufbytes, int spes, int stream_length)
+{
+    (void)stream_length;
+    return speIOBench(buffer, bufbytes, spes);
+}
+
+int speAddProduct_32fc(fc32* src, fc32* src2, fc32* accumulator, int length)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_MAC);
+    add_in(&t, src, (size_t)length * sizeof(fc32));
+    add_in(&t, src2, (size_t)length * sizeof(fc32));
+    add_out(&t, accumulator, (size_t)length * sizeof(fc32));
+    return celldsp_executeTask(&t);
+}
+
+int speFFT_init(int fft_len, int* speID)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_FFT_INIT);
+    t.subcontext.FFT.nfft = (unsigned)fft_len;
+    return celldsp_startContinuableTask(&t, speID);
+}
+
+int speFFT_exec(void* in, void* out, int fft_len, int* speID)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_FFT_EXEC);
+    add_in(&t, in, (size_t)fft_len * sizeof(fc32));
+    add_out(&t, out, (size_t)fft_len * sizeof(fc32));
+    t.subcontext.FFT.nfft = (unsigned)fft_len;
+    return celldsp_continueTask(&t, speID);
+}
+
+int speFFT_destroy(int* speID)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_FFT_FREE);
+    int status = celldsp_continueTask(&t, speID);
+    celldsp_stopContinuableTask(speID);
+    return status;
+}
+
+int speFFT_singleexec(void* in, void* out, int fft_len)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_FFT_EXEC_DYN);
+    add_in(&t, in, (size_t)fft_len * sizeof(fc32));
+    add_out(&t, out, (size_t)fft_len * sizeof(fc32));
+    t.subcontext.FFT.nfft = (unsigned)fft_len;
+    return celldsp_executeTask(&t);
+}
+
+int speSinCosGenerator(float startphase, float increment, fc32* cos_sin_out, int numiter)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_SINCOS_GENERTR);
+    add_out(&t, cos_sin_out, (size_t)numiter * sizeof(cf32));
+    t.subcontext.Phase.argcount = (unsigned)numiter;
+    t.subcontext.Phase.phase_start = startphase;
+    t.subcontext.Phase.phase_delta = increment;
+    return celldsp_executeTask(&t);
+}
+
+int speSinCosAccurate(float* argument, cf32* cos_sin_out, int argumentcount)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_SINCOS);
+    add_in(&t, argument, (size_t)argumentcount * sizeof(float));
+    add_out(&t, cos_sin_out, (size_t)argumentcount * sizeof(cf32));
+    t.subcontext.Phase.argcount = (unsigned)argumentcount;
+    return celldsp_executeTask(&t);
+}
+
+int speSinCosAccurateNorm(float* normalizedargument, cf32* cos_sin_out, int argumentcount)
+{
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_SINCOS_NORM);
+    add_in(&t, normalizedargument, (size_t)argumentcount * sizeof(float));
+    add_out(&t, cos_sin_out, (size_t)argumentcount * sizeof(cf32));
+    t.subcontext.Phase.argcount = (unsigned)argumentcount;
+    return celldsp_executeTask(&t);
+}
+
+int speDIFX_process(void* sincosrotdone, void* complexfracmult, void* fftoutJ, void* conjfftoutJ, void* autocorr,
+                    int nfft, int twicenumchannels, int useUpperOrLower)
+{
+    size_t dual_array_len = (size_t)twicenumchannels * sizeof(cf32);
+    size_t normal_array_len = (size_t)(twicenumchannels / 2 + 1 + 3) * sizeof(cf32);
+    CellDSPTask_t t;
+    task_init(&t, CELLDSP_TASK_DIFXPROCESS);
+    add_in(&t, sincosrotdone, dual_array_len);
+    add_in(&t, complexfracmult, normal_array_len);
+    add_out(&t, fftoutJ, normal_array_len);
+    add_out(&t, conjfftoutJ, normal_array_len);
+    add_out(&t, autocorr, normal_array_len);
+    t.subcontext.Difx.nfft = (unsigned)nfft;
+    t.subcontext.Difx.useUpperOrLower = (unsigned)useUpperOrLower;
+    t.subcontext.Difx.twicenumchannels = (unsigned)twicenumchannels;
+    t.subcontext.Difx.numchannels = (unsigned)(twicenumchannels / 2);
+    return celldsp_executeTask(&t);
+}
+
+// ===========================================================================
+// exported: direct engine entry points
+// ===========================================================================
+const char* cellspe_last_error(void) { return t_err.c_str(); }
+
+long long cellspe_kernel_launches(void) { return cs_launch_count(); }
+
+int cellspe_last_stage_times(float* ms, int n)
+{
+    if (!ms || n < 0) return CELLSPE_ERR_ARG;
+    for (int i = 0; i < n && i < 4; i++) ms[i] = t_stage_ms[i];
+    return 0;
+}
+
+int cellspe_device_count(void)
+{
+    int n = 0;
+    return cudaGetDeviceCount(&n) == cudaSuccess ? n : 0;
+}
+
+int cellspe_set_hbm_budget(long long bytes)
+{
+    if (bytes < 0) return CELLSPE_ERR_ARG;
+    g_budget = bytes;
+    return 0;
+}
+
+long long cellspe_get_hbm_budget(void) { return budget_bytes(); }
+
+void* cellspe_host_alloc(size_t bytes)
+{
+    if (ensure_device()) return nullptr;
+    void* p = nullptr;
+    return cudaHostAlloc(&p, bytes, cudaHostAllocDefault) == cudaSuccess ? p : nullptr;
+}
+
+void cellspe_host_free(void* p)
+{
+    if (p) cudaFreeHost(p);
+}
+
+void* cellspe_device_alloc(size_t bytes)
+{
+    if (ensure_device()) return nullptr;
+    void* p = nullptr;
+    return cudaMalloc(&p, bytes) == cudaSuccess ? p : nullptr;
+}
+
+void cellspe_device_free(void* p)
+{
+    if (p) cudaFree(p);
+}
+
+int cellspe_memcpy(void* dst, const void* src, size_t bytes, int kind)
+{
+    if (ensure_device()) return CELLSPE_ERR_CUDA;
+    cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice : kind == 2 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaMemcpy(dst, src, bytes, k);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "cellspe_memcpy");
+}
+
+int cellspe_debug_inject_failure(int slot, int count)
+{
+    if (slot < 0) {
+        g_inject_direct = count;
+        return 0;
+    }
+    if (!g_eng || slot >= CELLDSP_MAX_SPE_NR) return CELLSPE_ERR_ARG;
+    g_eng->slots[slot].inject = count;
+    return 0;
+}
+
+static int direct_gate()
+{
+    if (g_inject_direct.load() > 0) {
+        g_inject_direct--;
+        return set_err(CELLSPE_ERR_INJECTED, "injected failure");
+    }
+    return 0;
+}
+
+#define DIRECT_PROLOGUE                         \
+    int _g = direct_gate();                     \
+    if (_g) return _g;                          \
+    int _rc = 0;                                \
+    Workspace* ws = thread_ws(&_rc);            \
+    if (!ws) return _rc;
+
+int cellspe_unpack2bit(const void* raw, long long nsamp, int nchan, int format, const float* custom_levels, float* out,
+                       int memory)
+{
+    DIRECT_PROLOGUE
+    return op_unpack(*ws, memory == CELLSPE_MEM_HOST, raw, nsamp, nchan, format, custom_levels, out);
+}
+
+int cellspe_fft_c2c(const void* in, void* out, int n, long long batch, int memory)
+{
+    DIRECT_PROLOGUE
+    return op_fft(*ws, memory == CELLSPE_MEM_HOST, in, out, n, batch, false);
+}
+
+int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memory)
+{
+    DIRECT_PROLOGUE
+    return op_fft(*ws, memory == CELLSPE_MEM_HOST, in, out, n, batch, true);
+}
+
+int cellspe_xmac(const void* spectra, int S, int C, int K, void* vis, int accumulate, int memory)
+{
+    DIRECT_PROLOGUE
+    return op_xmac(*ws, memory == CELLSPE_MEM_HOST, spectra, S, C, K, vis, accumulate);
+}
+
+int cellspe_fx_correlate(const cellspe_fx_params* p, const void* raw, const double* delay_poly, void* vis)
+{
+    DIRECT_PROLOGUE
+    return op_fx(*ws, p, raw, delay_poly, vis, true);
+}
+
+long long cellspe_fx_workspace_bytes(const cellspe_fx_params* p) { return p ? fx_bytes(p, true) : -1; }
+
+int cellspe_fx_correlate_async(const cellspe_fx_params* p, const void* raw, const double* delay_poly, void* vis,
+                               void* stream)
+{
+    DIRECT_PROLOGUE
+    if (!p || p->memory != CELLSPE_MEM_DEVICE) return set_err(CELLSPE_ERR_ARG, "fx async: device memory only");
+    cudaStream_t saved = ws->stream;
+    ws->stream = (cudaStream_t)stream;
+    ws->arena.used = 0;
+    ws->arena.total_taken = 0;
+    int rc = op_fx(*ws, p, raw, delay_poly, vis, false);
+    ws->stream = saved;
+    return rc;
+}
+
+int cellspe_release_workspace(void)
+{
+    if (t_ws) {
+        t_ws->destroy();
+        t_ws.reset();
+    }
+    return 0;
+}
+
+int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* power, void* pcal_bins, void* pcal_tones)
+{
+    DIRECT_PROLOGUE
+    return op_spectrometer(*ws, p, raw, power, pcal_bins, pcal_tones);
+}
+
+long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p) { return p ? spec_bytes(p) : -1; }
+
+}  // extern "C"

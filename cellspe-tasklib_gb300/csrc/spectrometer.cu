@@ -1,0 +1,342 @@
+// K-e + K-pcal: spectrometer power accumulation and phase-cal extraction.
+//
+// Semantics (TaskCoreIPP::doMaths, spectrometer/src/IA-32/TaskCoreIPP.cpp:
+// 394-513, one source per subband): spectrum `spec` of subband `sub` is built
+// from novl = overlap*K - (overlap-1) FFTs (swspectrometer.cpp:231) that start
+// every N/overlap samples from sample spec*K*N; each FFT windows N samples
+// (generate_windowfunction :569-605), takes the real FFT, and adds |X_k|^2 for
+// k = 1..N/2-1 and X_0^2, X_{N/2}^2 (DC and Nyquist real, :437-447); the sum
+// is scaled by 1/novl (:124, :493).
+//
+// GPU layout: the CTA grid is (chunk of CH FFTs) x (subband, spectrum) x
+// (split p).  Inside a CTA, groups of M/16 threads run CtaFft on different
+// FFTs of the chunk and accumulate |X|^2 into thread-owned shared-memory bins;
+// the CTA writes one partial spectrum per chunk to scratch, and a reduce
+// kernel adds the partials in chunk order (deterministic) and applies 1/novl.
+// N = 65536 does not fit one SM's shared memory (32768 complex points), so it
+// is split across two CTAs by output parity: CTA p computes the M/2-point FFT
+// of y_p[n] = (z[n] + (-1)^p z[n + M/2]) W_M^{n p}, which yields
+// Z[2m + p]; the real-FFT pairs (k, M-k) keep the parity, so each CTA finishes
+// its own bins without exchanging data (input words are read twice, at 0.25 B
+// per sample).
+//
+// Phase-cal (TaskCoreIPP::extract_PCal :633-693, settings
+// swspectrometer.cpp:180-184): on the non-overlapped FFTs (every overlap-th),
+// i.e. on every sample of the spectrum once, bins[(n mod L) mod T] +=
+// x[n] * exp(-2 pi i f_off (n mod L) / fs), L = rotator length, T = tone
+// bins.  Tones = DFT(bins)/T, first ntones (PCal.cpp:280-300, getFinalPCal).
+#include "common.cuh"
+#include "kernels.h"
+
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
+namespace {
+
+constexpr int SPEC_CH = 32;   // FFTs per chunk (one partial spectrum each)
+
+template <int MC> struct SCfg {
+    static constexpr int T = MC / 16;
+    static constexpr int GROUPS = (T >= 256) ? 1 : 256 / T;
+    static constexpr int NT = T * GROUPS;
+};
+
+std::mutex g_win_mu;
+std::map<std::tuple<int, int, int>, float*> g_win;   // (device, type, n)
+
+const float* window_table(int type, int n)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_win_mu);
+    auto key = std::make_tuple(dev, type, n);
+    auto it = g_win.find(key);
+    if (it != g_win.end()) return it->second;
+    std::vector<float> h(n);
+    for (int i = 0; i < n; i++) {
+        if (type == 0) { h[i] = 1.f; continue; }
+        double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
+        double c = std::cos(arg);
+        h[i] = (type == 1) ? (float)c : (float)(c * c);
+    }
+    float* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float) * n) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    g_win[key] = d;
+    return d;
+}
+
+std::map<std::tuple<int, int, long long, long long>, float2*> g_rot;
+
+const float2* rotator_table(int L, double off_hz, double fs_hz)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_win_mu);
+    auto key = std::make_tuple(dev, L, (long long)llround(off_hz * 1e3), (long long)llround(fs_hz));
+    auto it = g_rot.find(key);
+    if (it != g_rot.end()) return it->second;
+    std::vector<float2> h(L);
+    double dphi = 2 * M_PI * (-off_hz / fs_hz);
+    for (int i = 0; i < L; i++) h[i] = make_float2((float)std::cos(dphi * i), (float)std::sin(dphi * i));
+    float2* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float2) * L) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, h.data(), sizeof(float2) * L, cudaMemcpyHostToDevice);
+    g_rot[key] = d;
+    return d;
+}
+
+CS_DEV float lut_pick4(const float (&l)[4], unsigned c)
+{
+    float lo = (c & 1u) ? l[1] : l[0];
+    float hi = (c & 1u) ? l[3] : l[2];
+    return (c & 2u) ? hi : lo;
+}
+
+template <int MC, int P>
+__global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const float2* __restrict__ tw,
+                                                            const float* __restrict__ win, int nchunk)
+{
+    using C = SCfg<MC>;
+    constexpr int T = C::T, GROUPS = C::GROUPS;
+    constexpr int M = MC * P, N = 2 * M;
+    constexpr int NACC = M / P + 1;                 // owned bins (local index)
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* fb_all = reinterpret_cast<float2*>(smem);
+    float* acc_all = reinterpret_cast<float*>(fb_all + GROUPS * fpad_size(MC));
+
+    const int g = threadIdx.x / T, t = threadIdx.x % T;
+    float2* fb = fb_all + g * fpad_size(MC);
+    float* acc = acc_all + g * NACC;
+    const int chunk = blockIdx.x;
+    const int row = blockIdx.y;                      // sub * nspec + spec
+    const int sub = row / a.nspec, spec = row % a.nspec;
+    const int p = (P == 2) ? (int)blockIdx.z : 0;
+    const int novl = a.overlap * a.ffts_per_spectrum - (a.overlap - 1);
+    const int hop = N / a.overlap;
+    const uint32_t* plane = reinterpret_cast<const uint32_t*>(a.planes + (int64_t)sub * a.bytes_per_sub);
+    const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
+
+    for (int i = threadIdx.x; i < GROUPS * NACC; i += C::NT) acc_all[i] = 0.f;
+    __syncthreads();
+
+    const int j_begin = chunk * SPEC_CH, j_end = min(novl, j_begin + SPEC_CH);
+    auto bar = [] { __syncthreads(); };
+    for (int j0 = j_begin; j0 < j_end; j0 += GROUPS) {
+        const int j = j0 + g;
+        const bool valid = j < j_end;
+        const int64_t start = (int64_t)spec * a.ffts_per_spectrum * N + (int64_t)(valid ? j : j_begin) * hop;
+        const uint32_t* wsrc = plane + (start >> 4);
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; r++) {
+            const int n = t + r * T;                 // index into the transformed sequence
+            if constexpr (P == 1) {
+                uint32_t w = __ldg(wsrc + (2 * n >> 4));
+                int f = (2 * n) & 15;
+                v[r] = make_float2(lut_pick4(lut, (w >> (2 * f)) & 3u) * __ldg(win + 2 * n),
+                                   lut_pick4(lut, (w >> (2 * f + 2)) & 3u) * __ldg(win + 2 * n + 1));
+            } else {
+                const int n2 = n + MC;
+                uint32_t w1 = __ldg(wsrc + (2 * n >> 4)), w2 = __ldg(wsrc + (2 * n2 >> 4));
+                int f1 = (2 * n) & 15, f2 = (2 * n2) & 15;
+                float2 z1 = make_float2(lut_pick4(lut, (w1 >> (2 * f1)) & 3u) * __ldg(win + 2 * n),
+                                        lut_pick4(lut, (w1 >> (2 * f1 + 2)) & 3u) * __ldg(win + 2 * n + 1));
+                float2 z2 = make_float2(lut_pick4(lut, (w2 >> (2 * f2)) & 3u) * __ldg(win + 2 * n2),
+                                        lut_pick4(lut, (w2 >> (2 * f2 + 2)) & 3u) * __ldg(win + 2 * n2 + 1));
+                v[r] = p ? cmul(csub(z1, z2), twiddle(tw, 2 * n)) : cadd(z1, z2);
+            }
+        }
+        CtaFft<MC>::run(fb, t, v, tw, N / MC, bar);
+        if (valid) {
+            const int mmax = (P == 1) ? MC / 2 : (p ? MC / 2 - 1 : MC / 2);
+            for (int m = t; m <= mmax; m += T) {
+                int k = P * m + p;
+                int mb = (P == 1 || p == 0) ? ((MC - m) & (MC - 1)) : (MC - 1 - m);
+                float2 Xk, Xm;
+                r2c_pair(fb[fpad(m)], fb[fpad(mb)], twiddle(tw, k), Xk, Xm);
+                if (k == 0) {
+                    acc[0] += Xk.x * Xk.x;
+                    acc[M / P] += Xm.x * Xm.x;
+                } else {
+                    acc[k / P] += Xk.x * Xk.x + Xk.y * Xk.y;
+                    if (k != M / 2) acc[(M - k) / P] += Xm.x * Xm.x + Xm.y * Xm.y;
+                }
+            }
+        }
+        bar();
+    }
+    // combine groups, write the chunk partial (owned bins only)
+    float* prow = a.partial + ((int64_t)row * nchunk + chunk) * (M + 1);
+    for (int l = threadIdx.x; l < NACC; l += C::NT) {
+        int k = P * l + p;
+        if (k > M) continue;
+        float s = 0.f;
+#pragma unroll
+        for (int gg = 0; gg < GROUPS; gg++) s += acc_all[gg * NACC + l];
+        prow[k] = s;
+    }
+}
+
+__global__ void k_spec_reduce(const float* __restrict__ partial, float* __restrict__ power, int rows, int nchunk,
+                              int nb, float scale)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)rows * nb) return;
+    int r = (int)(i / nb), k = (int)(i % nb);
+    const float* src = partial + (int64_t)r * nchunk * nb + k;
+    float s = 0.f;
+    for (int c = 0; c < nchunk; c++) s += src[(int64_t)c * nb];
+    power[i] = s * scale;
+}
+
+// PCal fold: thread-private accumulators in shared memory, [bin][thread].
+__global__ void k_pcal_fold(const uint8_t* __restrict__ planes, int64_t bytes_per_sub, int nspec, int64_t samp_per_spec,
+                            int T, int L, const float2* __restrict__ rot, float l0, float l1, float l2, float l3,
+                            float2* __restrict__ partial, int nblk_per_row)
+{
+    extern __shared__ float2 pacc[];                 // [T][blockDim]
+    const int row = blockIdx.y, sub = row / nspec, spec = row % nspec;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    for (int b = 0; b < T; b++) pacc[b * nt + tid] = make_float2(0.f, 0.f);
+    const uint32_t* plane = reinterpret_cast<const uint32_t*>(planes + (int64_t)sub * bytes_per_sub);
+    const int64_t w_begin = (int64_t)spec * samp_per_spec / 16;
+    const int64_t nwords = samp_per_spec / 16;
+    const float lut[4] = {l0, l1, l2, l3};
+    for (int64_t w = (int64_t)blockIdx.x * nt + tid; w < nwords; w += (int64_t)nblk_per_row * nt) {
+        uint32_t word = __ldg(plane + w_begin + w);
+        int64_t n0 = w * 16;                         // sample index relative to spectrum start
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            int64_t n = n0 + j;
+            int li = (int)(n % L);
+            float x = lut_pick4(lut, (word >> (2 * j)) & 3u);
+            float2 r = __ldg(rot + li);
+            float2& slot = pacc[(li % T) * nt + tid];
+            slot.x += x * r.x;
+            slot.y += x * r.y;
+        }
+    }
+    __syncthreads();
+    for (int b = tid; b < T; b += nt) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int u = 0; u < nt; u++) {
+            float2 v = pacc[b * nt + u];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        partial[((int64_t)row * nblk_per_row + blockIdx.x) * T + b] = s;
+    }
+}
+
+__global__ void k_pcal_reduce(const float2* __restrict__ partial, int rows, int nblk, int T, int ntones,
+                              float2* __restrict__ bins, float2* __restrict__ tones)
+{
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows) return;
+    for (int b = 0; b < T; b++) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int u = 0; u < nblk; u++) {
+            float2 v = partial[((int64_t)row * nblk + u) * T + b];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        bins[(int64_t)row * T + b] = s;
+    }
+    if (!tones) return;
+    for (int k = 0; k < ntones; k++) {
+        double re = 0, im = 0;
+        for (int n = 0; n < T; n++) {
+            float2 bv = bins[(int64_t)row * T + n];
+            double sn, cs;
+            sincospi(-2.0 * (double)(((int64_t)k * n) % T) / (double)T, &sn, &cs);
+            re += bv.x * cs - bv.y * sn;
+            im += bv.x * sn + bv.y * cs;
+        }
+        tones[(int64_t)row * ntones + k] = make_float2((float)(re / T), (float)(im / T));
+    }
+}
+
+constexpr int PCAL_THREADS = 128;
+constexpr int PCAL_BLOCKS = 32;
+
+template <int MC, int P>
+int launch_power(const CsSpecArgs& a, int nchunk, cudaStream_t st)
+{
+    using C = SCfg<MC>;
+    constexpr int M = MC * P, N = 2 * M;
+    const float2* tw = cs_twiddles(N);
+    const float* win = window_table(a.window, N);
+    if (!tw || !win) return CS_ERR_ARG;
+    size_t smem = (size_t)C::GROUPS * fpad_size(MC) * sizeof(float2) + (size_t)C::GROUPS * (M / P + 1) * sizeof(float);
+    auto kern = k_spec_power<MC, P>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(nchunk, a.nsub * a.nspec, P);
+    kern<<<grid, C::NT, smem, st>>>(a, tw, win, nchunk), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+int spec_nchunk(const CsSpecArgs& a)
+{
+    int novl = a.overlap * a.ffts_per_spectrum - (a.overlap - 1);
+    return (novl + SPEC_CH - 1) / SPEC_CH;
+}
+}  // namespace
+
+int64_t cs_spectrometer_scratch_floats(const CsSpecArgs& a)
+{
+    int64_t power = (int64_t)a.nsub * a.nspec * spec_nchunk(a) * (a.N / 2 + 1);
+    int64_t pcal = a.tonebins > 0 ? (int64_t)a.nsub * a.nspec * PCAL_BLOCKS * a.tonebins * 2 : 0;
+    return power + pcal;
+}
+
+int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
+{
+    if (!a.planes || !a.power || !a.partial || a.nsub <= 0 || a.nspec <= 0 || a.ffts_per_spectrum <= 0)
+        return CS_ERR_ARG;
+    if (a.overlap < 1 || a.N % (16 * a.overlap) != 0) return CS_ERR_ARG;
+    if ((uintptr_t)a.planes % 16 || a.bytes_per_sub % 16) return CS_ERR_ARG;
+    // every sample the spectra read must lie inside the subband plane
+    if ((int64_t)a.nspec * a.ffts_per_spectrum * a.N > a.bytes_per_sub * 4) return CS_ERR_ARG;
+    if (a.nsub * a.nspec > 65535) return CS_ERR_ARG;
+    const int nchunk = spec_nchunk(a);
+    int rc;
+    switch (a.N) {
+        case 1024: rc = launch_power<512, 1>(a, nchunk, st); break;
+        case 2048: rc = launch_power<1024, 1>(a, nchunk, st); break;
+        case 4096: rc = launch_power<2048, 1>(a, nchunk, st); break;
+        case 8192: rc = launch_power<4096, 1>(a, nchunk, st); break;
+        case 16384: rc = launch_power<8192, 1>(a, nchunk, st); break;
+        case 32768: rc = launch_power<16384, 1>(a, nchunk, st); break;
+        case 65536: rc = launch_power<16384, 2>(a, nchunk, st); break;
+        default: return CS_ERR_UNSUPPORTED;
+    }
+    if (rc) return rc;
+    const int rows = a.nsub * a.nspec, nb = a.N / 2 + 1;
+    const int novl = a.overlap * a.ffts_per_spectrum - (a.overlap - 1);
+    const float scale = (float)(1.0 / (double)novl);
+    int64_t tot = (int64_t)rows * nb;
+    k_spec_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a.partial, a.power, rows, nchunk, nb, scale), cs_count_launches(1);
+    CS_CUDA_TRY(cudaGetLastError());
+
+    if (a.tonebins > 0) {
+        const int T = a.tonebins, L = a.rotatorlen;
+        if (L <= 0 || L % T != 0 || a.N % L != 0 || T > 128 || !a.pcal_bins) return CS_ERR_ARG;
+        const float2* rot = rotator_table(L, a.pcal_offset_hz, a.fs_hz);
+        if (!rot) return CS_ERR_ARG;
+        float2* pp = reinterpret_cast<float2*>(a.partial + (int64_t)rows * nchunk * nb);
+        int64_t samp_per_spec = (int64_t)a.ffts_per_spectrum * a.N;
+        int nt = PCAL_THREADS;
+        size_t smem = (size_t)T * nt * sizeof(float2);
+        CS_CUDA_TRY(cudaFuncSetAttribute(k_pcal_fold, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_pcal_fold<<<dim3(PCAL_BLOCKS, rows), nt, smem, st>>>(a.planes, a.bytes_per_sub, a.nspec, samp_per_spec, T, L,
+                                                               rot, a.lut[0], a.lut[1], a.lut[2], a.lut[3], pp,
+                                                               PCAL_BLOCKS), cs_count_launches(1);
+        CS_CUDA_TRY(cudaGetLastError());
+        k_pcal_reduce<<<(rows + 63) / 64, 64, 0, st>>>(pp, rows, PCAL_BLOCKS, T, a.ntones, a.pcal_bins, a.pcal_tones), cs_count_launches(1);
+        CS_CUDA_TRY(cudaGetLastError());
+    }
+    return 0;
+}

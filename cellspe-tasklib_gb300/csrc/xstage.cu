@@ -1,0 +1,166 @@
+// K-d1: X stage, FP32 CUDA cores.
+//
+// V_c[i][j] = sum_k X_i[c][k] * conj(X_j[c][k]) over the lower triangle
+// j <= i (autos on the diagonal), the conjugate-MAC of
+// genericAddProduct_32fc_conj (architecture.h:427-433), IPP's cross-pol
+// accumulate (TaskCoreIPP.cpp:456-487) and zerocorr.c:601-606, done for all
+// S(S+1)/2 products of every channel at once.  Per channel it is a Hermitian
+// rank-K update, so it is tiled like a GEMM: a CTA owns a 64x64 block of
+// (i, j) for one channel and streams 16 time samples per stage through
+// shared memory; each of its 128 threads keeps 4x8 complex accumulators.
+// Only blocks on or below the diagonal are launched.
+//
+// Layout in:  float2 spectra[C][S][K]   (time innermost)
+// Layout out: float2 vis[C][P],  p = i(i+1)/2 + j
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+constexpr int XT = 64;      // tile edge (inputs)
+constexpr int XK = 16;      // time samples per stage
+constexpr int XTHREADS = 128;
+constexpr int XLD = XT + 1; // padded shared row (float2)
+
+__device__ __forceinline__ void tile_coords(int t, int& bi, int& bj)
+{
+    // t enumerates (bi, bj), bj <= bi, row-major over bi
+    int b = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+    while ((b + 1) * (b + 2) / 2 <= t) b++;
+    while (b * (b + 1) / 2 > t) b--;
+    bi = b;
+    bj = t - b * (b + 1) / 2;
+}
+
+__global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict__ spec, int S, int K,
+                                                      float2* __restrict__ vis, int64_t P, int accumulate)
+{
+    __shared__ float2 As[2][XK][XLD];
+    __shared__ float2 Bs[2][XK][XLD];
+    const int c = blockIdx.y;
+    int bi, bj;
+    tile_coords(blockIdx.x, bi, bj);
+    const int i0 = bi * XT, j0 = bj * XT;
+    const int tid = threadIdx.x;
+    const int ti = tid >> 3;          // 0..15 -> rows ti + 16a
+    const int tj = tid & 7;           // 0..7  -> cols tj + 8b
+    const float2* base = spec + (int64_t)c * S * K;
+
+    // loader: thread -> (row = tid/2, 8 consecutive time samples)
+    const int lrow = tid >> 1, lk = (tid & 1) * 8;
+    const int ai = i0 + lrow, bjr = j0 + lrow;
+    const float2* pa = base + (int64_t)min(ai, S - 1) * K;
+    const float2* pb = base + (int64_t)min(bjr, S - 1) * K;
+    const bool va = ai < S, vb = bjr < S;
+
+    float2 ra[8], rb[8];
+    auto gload = [&](int k0) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            int k = k0 + lk + u;
+            bool kin = k < K;
+            ra[u] = (va && kin) ? __ldg(pa + k) : make_float2(0.f, 0.f);
+            rb[u] = (vb && kin) ? __ldg(pb + k) : make_float2(0.f, 0.f);
+        }
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            As[buf][lk + u][lrow] = ra[u];
+            Bs[buf][lk + u][lrow] = rb[u];
+        }
+    };
+
+    float accr[4][8], acci[4][8];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) accr[a][b] = acci[a][b] = 0.f;
+
+    const int nst = (K + XK - 1) / XK;
+    gload(0);
+    sstore(0);
+    __syncthreads();
+    for (int stg = 0; stg < nst; stg++) {
+        const int cur = stg & 1;
+        if (stg + 1 < nst) gload((stg + 1) * XK);
+#pragma unroll
+        for (int kk = 0; kk < XK; kk++) {
+            float2 av[4], bv[8];
+#pragma unroll
+            for (int a = 0; a < 4; a++) av[a] = As[cur][kk][ti + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 8; b++) bv[b] = Bs[cur][kk][tj + 8 * b];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    accr[a][b] = fmaf(av[a].x, bv[b].x, accr[a][b]);
+                    accr[a][b] = fmaf(av[a].y, bv[b].y, accr[a][b]);
+                    acci[a][b] = fmaf(av[a].y, bv[b].x, acci[a][b]);
+                    acci[a][b] = fmaf(-av[a].x, bv[b].y, acci[a][b]);
+                }
+        }
+        if (stg + 1 < nst) sstore(cur ^ 1);
+        __syncthreads();
+    }
+
+    float2* out = vis + (int64_t)c * P;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        int i = i0 + ti + 16 * a;
+        if (i >= S) continue;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            int j = j0 + tj + 8 * b;
+            if (j > i) continue;
+            int64_t p = (int64_t)i * (i + 1) / 2 + j;
+            float2 v = make_float2(accr[a][b], acci[a][b]);
+            if (accumulate) {
+                float2 o = out[p];
+                v.x += o.x;
+                v.y += o.y;
+            }
+            out[p] = v;
+        }
+    }
+}
+
+__global__ void k_vis_transpose(const float2* __restrict__ in, float2* __restrict__ out, int C, int64_t P)
+{
+    __shared__ float2 tile[32][33];
+    int64_t p0 = (int64_t)blockIdx.x * 32;
+    int c0 = blockIdx.y * 32;
+    int tx = threadIdx.x, ty = threadIdx.y;
+    for (int r = ty; r < 32; r += 8) {
+        int c = c0 + r;
+        int64_t p = p0 + tx;
+        if (c < C && p < P) tile[r][tx] = in[(int64_t)c * P + p];
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        int64_t p = p0 + r;
+        int c = c0 + tx;
+        if (c < C && p < P) out[p * C + c] = tile[tx][r];
+    }
+}
+}  // namespace
+
+int cs_xmac_f32(const float2* spectra, int S, int C, int K, float2* vis, int accumulate, cudaStream_t st)
+{
+    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0) return CS_ERR_ARG;
+    int nb = (S + XT - 1) / XT;
+    int64_t tiles = (int64_t)nb * (nb + 1) / 2;
+    if (C > 65535) return CS_ERR_ARG;
+    int64_t P = (int64_t)S * (S + 1) / 2;
+    dim3 grid((unsigned)tiles, C);
+    k_xmac_f32<<<grid, XTHREADS, 0, st>>>(spectra, S, K, vis, P, accumulate), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+int cs_vis_to_baseline_major(const float2* vis_cp, float2* vis_pc, int C, int64_t P, cudaStream_t st)
+{
+    if (!vis_cp || !vis_pc || C <= 0 || P <= 0) return CS_ERR_ARG;
+    dim3 grid((unsigned)((P + 31) / 32), (C + 31) / 32);
+    k_vis_transpose<<<grid, dim3(32, 8), 0, st>>>(vis_cp, vis_pc, C, P), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}

@@ -1,0 +1,113 @@
+"""Seeded synthetic 2-bit sources (the engine's test-pattern inputs).
+
+The reference's own drivers fill their raw buffers with synthetic patterns
+(minicorrelator_ppu.c:131-133, (17*i+3*j) % 256); no recorded data ships with
+it.  These generators produce the inputs of the benchmark configurations:
+
+* ``stations_offset_binary`` -- S inputs that share a N(0,1) sky signal with
+  correlation rho, each with its own integer lag, quantised at +-0.98 sigma
+  to offset-binary codes 0..3 (levels -3.336, -1, +1, +3.336), 4 samples per
+  byte, sample 0 in bits 1:0.
+* ``mark5b_subbands`` -- nsub subbands of noise + phase-cal comb + narrowband
+  sinusoids, quantised to Mark5B sign/magnitude codes and interleaved
+  2 bits per channel into 32-bit words (mark5_format_mark5b.c:1852-1915).
+* ``device_stations`` -- the same statistics as stations_offset_binary,
+  generated on the GPU with torch (for the 512-input configuration whose
+  4.3 G samples would take minutes on the host).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+THRESH = 0.98
+OFFSET_BINARY_LEVELS = np.array([-3.336, -1.0, 1.0, 3.336], np.float32)
+
+
+def quantize_offset_binary(x: np.ndarray) -> np.ndarray:
+    """Codes 0..3 for x < -t, -t <= x < 0, 0 <= x < t, x >= t."""
+    return (np.searchsorted(np.array([-THRESH, 0.0, THRESH]), x, side="right")).astype(np.uint8)
+
+
+def quantize_mark5b(x: np.ndarray) -> np.ndarray:
+    """Mark5B code l with value lut[l], lut = {-H, +1, -1, +H}."""
+    ob = quantize_offset_binary(x)
+    return np.array([0, 2, 1, 3], np.uint8)[ob]
+
+
+def pack2bit(codes: np.ndarray) -> np.ndarray:
+    """Pack the last axis of 2-bit codes, 4 per byte, first code in bits 1:0."""
+    c = codes.reshape(*codes.shape[:-1], -1, 4).astype(np.uint8)
+    return (c[..., 0] | (c[..., 1] << 2) | (c[..., 2] << 4) | (c[..., 3] << 6)).astype(np.uint8)
+
+
+def stations_offset_binary(S: int, T: int, rho: float, lags=None, seed: int = 1) -> np.ndarray:
+    """uint8 [S][T/4].  Input s sees x_s(t) = sqrt(rho) c(t - lag_s) + sqrt(1-rho) n_s(t)."""
+    assert T % 64 == 0
+    rng = np.random.Generator(np.random.Philox(seed))
+    lags = np.zeros(S, np.int64) if lags is None else np.asarray(lags, np.int64)
+    pad = int(lags.max(initial=0)) + 1
+    common = rng.standard_normal(T + pad).astype(np.float32)
+    out = np.empty((S, T // 4), np.uint8)
+    a, b = np.float32(np.sqrt(rho)), np.float32(np.sqrt(1.0 - rho))
+    for s in range(S):
+        n = rng.standard_normal(T).astype(np.float32)
+        sig = common[pad - lags[s] : pad - lags[s] + T]   # c(t - lag)
+        out[s] = pack2bit(quantize_offset_binary(a * sig + b * n))
+    return out
+
+
+def mark5b_subbands(nsub: int, T: int, fs_hz: float, seed: int = 2, pcal_spacing_hz: float = 1e6,
+                    pcal_amp: float = 0.05, n_sines: int = 3, snr_db: float = 10.0, n_channels: int = 32768,
+                    chunk: int = 1 << 22):
+    """Mark5B-style payload (uint32 words, T of them) and the injected truth.
+
+    Per subband: N(0,1) noise + phase-cal comb at k*spacing (k = 1..fs/2/spacing-1)
+    with amplitude pcal_amp and seeded phases + n_sines sinusoids at seeded
+    frequencies with A^2/2 = 10^(snr_db/10) / n_channels (SNR per channel).
+    """
+    assert T % chunk == 0 or T < chunk
+    chunk = min(chunk, T)
+    rng = np.random.Generator(np.random.Philox(seed))
+    ntone = int(fs_hz / 2 / pcal_spacing_hz)
+    tone_k = np.arange(1, ntone)
+    tone_phase = rng.uniform(0, 2 * np.pi, (nsub, tone_k.size))
+    sine_f = rng.uniform(0.05, 0.45, (nsub, n_sines)) * fs_hz
+    sine_phase = rng.uniform(0, 2 * np.pi, (nsub, n_sines))
+    sine_amp = np.sqrt(2 * 10 ** (snr_db / 10) / n_channels)
+    words = np.zeros(T, np.uint32)
+    for t0 in range(0, T, chunk):
+        t = (np.arange(t0, t0 + chunk, dtype=np.float64)) / fs_hz
+        for c in range(nsub):
+            x = rng.standard_normal(chunk)
+            for i, k in enumerate(tone_k):
+                x += pcal_amp * np.cos(2 * np.pi * k * pcal_spacing_hz * t + tone_phase[c, i])
+            for i in range(n_sines):
+                x += sine_amp * np.cos(2 * np.pi * sine_f[c, i] * t + sine_phase[c, i])
+            code = quantize_mark5b(x.astype(np.float32)).astype(np.uint32)
+            words[t0 : t0 + chunk] |= code << np.uint32(2 * c)
+    truth = dict(tone_k=tone_k, tone_phase=tone_phase, sine_f=sine_f, sine_phase=sine_phase)
+    return words, truth
+
+
+def device_stations(S: int, T: int, rho: float, seed: int, device="cuda", chunk: int = 1 << 24):
+    """torch uint8 [S][T/4] on the device, offset-binary codes (no lags)."""
+    import torch
+
+    assert T % chunk == 0 or T < chunk
+    chunk = min(chunk, T)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    out = torch.empty((S, T // 4), dtype=torch.uint8, device=device)
+    a, b = float(np.sqrt(rho)), float(np.sqrt(1.0 - rho))
+    thr = torch.tensor([-THRESH, 0.0, THRESH], device=device)
+    shifts = torch.tensor([0, 2, 4, 6], dtype=torch.uint8, device=device)
+    for t0 in range(0, T, chunk):
+        common = torch.randn(chunk, generator=g, device=device)
+        for s0 in range(0, S, 64):
+            s1 = min(S, s0 + 64)
+            n = torch.randn((s1 - s0, chunk), generator=g, device=device)
+            x = a * common + b * n
+            codes = torch.bucketize(x, thr, right=True).to(torch.uint8).view(s1 - s0, -1, 4)
+            packed = (codes << shifts).sum(dim=-1, dtype=torch.uint8)
+            out[s0:s1, t0 // 4 : (t0 + chunk) // 4] = packed
+    return out

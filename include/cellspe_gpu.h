@@ -1,0 +1,159 @@
+/*
+ * cellspe_gpu.h -- GB300 FX correlator / spectrometer engine, C ABI.
+ *
+ * Direct entry points for the hot path behind the task API.  Every function
+ * takes plain pointers and sizes, returns 0 on success or a CELLSPE_ERR_*
+ * code, and blocks until its results are in the caller's output buffers.
+ * `memory` says where the buffers live: CELLSPE_MEM_HOST (the engine copies
+ * inputs to the GPU and results back; pinned memory from cellspe_host_alloc
+ * is fastest) or CELLSPE_MEM_DEVICE (device pointers on the engine's GPU).
+ * Calls from several host threads are safe; each thread uses its own stream
+ * and workspace.  There is no CPU fallback: without a usable GPU every call
+ * fails with CELLSPE_ERR_CUDA and cellspe_last_error() says why.
+ */
+#ifndef CELLSPE_GPU_H
+#define CELLSPE_GPU_H
+
+#include "cellspe-tasklib.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CELLSPE_MEM_HOST    0
+#define CELLSPE_MEM_DEVICE  1
+
+#define CELLSPE_OK               0
+#define CELLSPE_ERR_ARG          1   /* invalid argument                  */
+#define CELLSPE_ERR_UNSUPPORTED  2   /* size or mode not implemented      */
+#define CELLSPE_ERR_NOMEM        3   /* job exceeds the HBM budget         */
+#define CELLSPE_ERR_CUDA         4   /* CUDA runtime error                 */
+#define CELLSPE_ERR_INJECTED     5   /* failure injected by the test hook  */
+
+/* 2-bit level tables (value = levels[bit0 + 2*bit1]). */
+#define CELLSPE_LEVELS_MARK5B        0  /* {-3.3359, +1, -1, +3.3359}  mark5_format_mark5b.c:63  */
+#define CELLSPE_LEVELS_TWOBIT        1  /* {+1, -1, +3.3359, -3.3359}  DataUnpackers.cpp:195     */
+#define CELLSPE_LEVELS_OFFSET_BINARY 2  /* {-3.336, -1, +1, +3.336}    synthetic offset binary    */
+#define CELLSPE_UNPACK_MSB_FIRST     0x100  /* single channel: sample 0 in bits 7:6 */
+
+/* X-stage arithmetic */
+#define CELLSPE_X_FP32     0   /* FP32 CUDA cores                                   */
+#define CELLSPE_X_TC_FP16  1   /* tcgen05 tensor cores, FP16 inputs, FP32 accumulate */
+
+/* Visibility layout */
+#define CELLSPE_VIS_CHANNEL_MAJOR   0  /* vis[C][P]  (X-engine order)            */
+#define CELLSPE_VIS_BASELINE_MAJOR  1  /* vis[P][C]  (one spectrum per product)   */
+
+/* ---- engine control ---------------------------------------------------- */
+const char* cellspe_last_error(void);          /* this thread's last error text */
+int  cellspe_device_count(void);
+int  cellspe_set_hbm_budget(long long bytes);  /* admission limit per job (0 = 90% of free) */
+long long cellspe_get_hbm_budget(void);
+void* cellspe_host_alloc(size_t bytes);        /* pinned host memory */
+void cellspe_host_free(void* p);
+void* cellspe_device_alloc(size_t bytes);
+void cellspe_device_free(void* p);
+int  cellspe_memcpy(void* dst, const void* src, size_t bytes, int kind); /* 1 H2D, 2 D2H, 3 D2D */
+/* Fault injection for tests: the next `count` tasks or calls on `slot`
+ * (-1 = direct calls) fail with CELLSPE_ERR_INJECTED before touching the GPU. */
+int  cellspe_debug_inject_failure(int slot, int count);
+/* Kernels this library has launched since it was loaded (all threads). */
+long long cellspe_kernel_launches(void);
+/* Device time in ms of the calling thread's last blocking FX job, measured
+ * with CUDA events on the engine stream: [0] delay model, [1] F stage
+ * (unpack + FFT + phasor), [2] X stage, [3] output layout/copies. */
+int  cellspe_last_stage_times(float* ms, int n);
+
+/* ---- K-a: 2-bit unpack ----------------------------------------------------
+ * out: nchan planes of nsamp floats.  Bit-exact with the reference decode
+ * (mark5_format_mark5b.c:1852-1915, DataUnpackers.cpp:174-288). */
+int cellspe_unpack2bit(const void* raw, long long nsamp, int nchan, int format,
+                       const float* custom_levels, float* out, int memory);
+
+/* ---- K-b: FFTs ------------------------------------------------------------
+ * Forward, unscaled.  C2C: interleaved complex, n in [16, 16384], replaces
+ * _fft_1d_r2 / exec_FFT (cellspe-tasklib-dsp.cpp:565-602).  R2C: n reals ->
+ * n/2+1 bins, n in [32, 32768], replaces genericFFTexec_R (architecture.h:563). */
+int cellspe_fft_c2c(const void* in, void* out, int n, long long batch, int memory);
+int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memory);
+
+/* ---- K-d: X stage on precomputed spectra ----------------------------------
+ * spectra complex64 [C][S][K] (FP32 mode) -> vis complex64 [C][P] (channel-major),
+ * V_ij = sum_k X_i conj(X_j), j <= i, p = i(i+1)/2 + j.
+ * Replaces genericAddProduct_32fc_conj (architecture.h:427-433) looped over
+ * products, three_baseline_naive_MACauto (minicorrelator_spu.c:745-786). */
+int cellspe_xmac(const void* spectra, int S, int C, int K, void* vis, int accumulate, int memory);
+/* Parameters of CELLDSP_TASK_XMAC (input vector 0). */
+typedef struct { int S, C, K, accumulate; } cellspe_xmac_params;
+
+/* ---- Full FX correlation: unpack -> FFT -> delay/fringe -> X --------------- */
+typedef struct {
+    int    n_inputs;          /* S: stations x polarisations                       */
+    int    fft_points;        /* N: 1024 .. 32768, power of two; C = N/2 channels  */
+    int    n_segments;        /* K: FFT segments integrated                        */
+    int    x_mode;            /* CELLSPE_X_*                                        */
+    int    vis_order;         /* CELLSPE_VIS_*                                      */
+    int    levels;            /* CELLSPE_LEVELS_* (| CELLSPE_UNPACK_MSB_FIRST)      */
+    long long bytes_per_input;/* raw bytes per input (multiple of 16)              */
+    long long start_sample;   /* sample index of segment 0 inside each input        */
+    double sample_rate_hz;    /* fs (delay model)                                   */
+    double lo_freq_hz;        /* sky frequency of channel 0 (fringe rotation)       */
+    int    accumulate;        /* 1: vis += result, 0: vis = result                  */
+    int    memory;            /* CELLSPE_MEM_*                                      */
+    const float* custom_levels;   /* 4 floats overriding `levels`, or NULL          */
+    const float* channel_scale;   /* [S][C] F-stage scale for the FP16 path, or NULL */
+} cellspe_fx_params;
+
+/* raw: S inputs of bytes_per_input bytes, 2-bit single channel, 4 samples per
+ * byte.  delay_poly: [S][4] seconds, tau(t) = sum_m poly[m] t^m with t the
+ * segment centre in seconds from start_sample, or NULL for no delay model.
+ * Segment k of input s starts at start_sample + k*N + round(tau*fs); its
+ * spectrum is multiplied by exp(i*(2 pi lo tau + 2 pi c (fs/N) tau_frac)).
+ * vis: C*P complex64 in vis_order. */
+int cellspe_fx_correlate(const cellspe_fx_params* p, const void* raw, const double* delay_poly, void* vis);
+/* Device bytes the engine needs for this job (admission control). */
+long long cellspe_fx_workspace_bytes(const cellspe_fx_params* p);
+/* Asynchronous form on a caller's CUDA stream (cudaStream_t passed as void*).
+ * Device memory only; the workspace stays owned by the calling thread until
+ * cellspe_release_workspace().  Captures into CUDA graphs once the workspace
+ * has been sized by one earlier call. */
+int cellspe_fx_correlate_async(const cellspe_fx_params* p, const void* raw, const double* delay_poly,
+                               void* vis, void* stream);
+int cellspe_release_workspace(void);
+
+/* ---- Spectrometer ----------------------------------------------------------
+ * Restates TaskCoreIPP::doMaths (TaskCoreIPP.cpp:394-513) on the GPU for every
+ * subband of a 2-bit stream. */
+#define CELLSPE_SPEC_INTERLEAVED 0  /* raw: nsub channels interleaved per sample time (Mark5B payload) */
+#define CELLSPE_SPEC_PLANES      1  /* raw: nsub planes of bytes_per_sub bytes, 1 channel each */
+typedef struct {
+    int    fft_points;        /* N: 1024 .. 65536                                  */
+    int    overlap;           /* fft_overlap_factor                                */
+    int    window;            /* 0 none, 1 cosine, 2 cosine^2                       */
+    int    ffts_per_spectrum; /* K non-overlapped FFTs per spectrum                 */
+    int    n_spectra;
+    int    n_subbands;        /* 1, 4, 8 or 16                                      */
+    int    input_layout;      /* CELLSPE_SPEC_*                                     */
+    int    levels;            /* CELLSPE_LEVELS_*                                   */
+    long long raw_bytes;      /* total raw bytes                                    */
+    int    pcal_tonebins;     /* 0 disables phase-cal                               */
+    int    pcal_rotatorlen;
+    int    pcal_ntones;
+    double pcal_offset_hz;
+    double sample_rate_hz;
+    int    memory;
+    const float* custom_levels;
+} cellspe_spec_params;
+
+/* power: [nsub][nspec][N/2+1] float; pcal_bins: [nsub][nspec][tonebins]
+ * complex64 (may be NULL when pcal is off); pcal_tones: [nsub][nspec][ntones]
+ * complex64 or NULL. */
+int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* power,
+                         void* pcal_bins, void* pcal_tones);
+long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* CELLSPE_GPU_H */

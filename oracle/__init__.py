@@ -1,0 +1,273 @@
+"""CPU oracle for the FX correlator / spectrometer hot path.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg use this package, and only as the checker or
+as the timed CPU baseline.  The product library (``cellspe-tasklib_gb300``)
+never imports it and has no CPU fallback.
+
+Contents
+--------
+* ``lib()``         -- ctypes handle on ``oracle/liboracle.so``, the plain-C
+                       restatement (``cellspe_oracle.c``).
+* ``ref_mark5()``   -- the reference's own mark5access 1.4.3, compiled from the
+                       reference tree into ``oracle/_ref`` (this container only).
+* ``ref_generic()`` -- the reference's GENERIC kernels of ``architecture.h``.
+* FP64 numpy models: ``fx_spectra_f64``, ``fx_vis_f64``, ``delay_state_f64``.
+
+Parity status: the 2-bit decode and the complex MAC are pinned bit-for-bit
+to the reference (mark5access, architecture.h GENERIC).  The FFT is not
+pinned by the reference (FFTW/IPP/Cell SDK absent): it is checked against an
+FP64 DFT and analytic known answers.  The phase-cal fold is pinned by the
+reference's own PCal unit-test recipe (tone phase within 0.1 degree).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF_DIR = HERE / "_ref"
+
+_lib = None
+_ref_m5 = None
+_ref_gen = None
+
+f32p = ctypes.POINTER(ctypes.c_float)
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def build(with_ref: bool | None = None) -> None:
+    """Compile liboracle.so (always) and oracle/_ref (when the reference tree exists)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
+    ref_tree = os.environ.get("CELLSPE_REFERENCE_TREE", "/root/reference")
+    if with_ref is None:
+        with_ref = Path(ref_tree).is_dir()
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref_tree}"], check=True)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        so = HERE / "liboracle.so"
+        if not so.exists():
+            build(with_ref=False)
+        _lib = ctypes.CDLL(str(so))
+        V, I, L = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+        _lib.orc_unpack2bit.argtypes = [V, L, I, I, V, V]
+        _lib.orc_addproduct_32fc.argtypes = [V, V, V, I]
+        _lib.orc_addproduct_32fc_conj.argtypes = [V, V, V, I]
+        _lib.orc_cfft_f32.argtypes = [V, V, I]
+        _lib.orc_cfft_f64.argtypes = [V, V, I]
+        _lib.orc_rfft_f32.argtypes = [V, V, I]
+        _lib.orc_spectrometer.argtypes = [V, L, V, V, V]
+        _lib.orc_spectrometer.restype = I
+        _lib.orc_spec_window.argtypes = [I, I, V]
+        _lib.orc_pcal_tones.argtypes = [V, I, I, V]
+        _lib.orc_fx_fp32.argtypes = [V, L, I, I, I, L, V, V, V, I, V, I]
+        _lib.orc_fx_fstage_fp32.argtypes = [V, L, I, I, I, L, V, V, V, I, V, I]
+    return _lib
+
+
+def have_ref() -> bool:
+    return (REF_DIR / "libref_mark5.so").exists() and (REF_DIR / "libref_generic.so").exists()
+
+
+def ref_mark5() -> ctypes.CDLL:
+    global _ref_m5
+    if _ref_m5 is None:
+        _ref_m5 = ctypes.CDLL(str(REF_DIR / "libref_mark5.so"))
+        _ref_m5.ref_mark5_unpack.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    return _ref_m5
+
+
+def ref_generic() -> ctypes.CDLL:
+    global _ref_gen
+    if _ref_gen is None:
+        _ref_gen = ctypes.CDLL(str(REF_DIR / "libref_generic.so"))
+        for name in ("ref_addproduct_32fc", "ref_addproduct_32fc_conj", "ref_mul_32fc",
+                     "ref_mul_32fc_conj"):
+            getattr(_ref_gen, name).argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int]
+    return _ref_gen
+
+
+# ---------------------------------------------------------------------------
+# thin wrappers over the C restatement
+# ---------------------------------------------------------------------------
+MARK5B_LUT = np.array([-3.3359, 1.0, -1.0, 3.3359], np.float32)       # mark5_format_mark5b.c:63
+TWOBIT_LUT = np.array([1.0, -1.0, 3.3359, -3.3359], np.float32)       # DataUnpackers.cpp:195
+OFFSET_BINARY_LUT = np.array([-3.336, -1.0, 1.0, 3.336], np.float32)  # synthetic configs
+
+
+def unpack2bit(raw: np.ndarray, nsamp: int, nchan: int, lut, msb_first: bool = False) -> np.ndarray:
+    raw = np.ascontiguousarray(raw, np.uint8)
+    lut = np.ascontiguousarray(lut, np.float32)
+    out = np.empty((nchan, nsamp), np.float32)
+    lib().orc_unpack2bit(_ptr(raw), nsamp, nchan, int(msb_first), _ptr(lut), _ptr(out))
+    return out
+
+
+def addproduct(a, b, acc, conj: bool):
+    fn = lib().orc_addproduct_32fc_conj if conj else lib().orc_addproduct_32fc
+    fn(_ptr(a), _ptr(b), _ptr(acc), a.size)
+    return acc
+
+
+def rfft_f32(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.empty(x.size // 2 + 1, np.complex64)
+    lib().orc_rfft_f32(_ptr(x), _ptr(out), x.size)
+    return out
+
+
+def cfft_f32(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.complex64)
+    out = np.empty_like(x)
+    lib().orc_cfft_f32(_ptr(x), _ptr(out), x.size)
+    return out
+
+
+class SpecCfg(ctypes.Structure):
+    _fields_ = [("fft_points", ctypes.c_int), ("overlap", ctypes.c_int), ("window", ctypes.c_int),
+                ("ffts_per_spectrum", ctypes.c_int), ("pcal_tonebins", ctypes.c_int),
+                ("pcal_rotatorlen", ctypes.c_int), ("pcal_offset_hz", ctypes.c_double),
+                ("sample_rate_hz", ctypes.c_double)]
+
+
+def spectrometer(samples: np.ndarray, N: int, overlap: int, window: int, K: int,
+                 tonebins: int = 0, rotatorlen: int = 0, offset_hz: float = 0.0,
+                 fs_hz: float = 1.0):
+    samples = np.ascontiguousarray(samples, np.float32)
+    cfg = SpecCfg(N, overlap, window, K, tonebins, rotatorlen, offset_hz, fs_hz)
+    nspec_max = max(1, samples.size // (N * K))
+    power = np.zeros((nspec_max, N // 2 + 1), np.float32)
+    pc = np.zeros((nspec_max, max(tonebins, 1)), np.complex64)
+    n = lib().orc_spectrometer(_ptr(samples), samples.size, ctypes.byref(cfg), _ptr(power),
+                               _ptr(pc) if tonebins else None)
+    return power[:n], (pc[:n] if tonebins else None)
+
+
+def window(kind: int, n: int) -> np.ndarray:
+    w = np.empty(n, np.float32)
+    lib().orc_spec_window(kind, n, _ptr(w))
+    return w
+
+
+def pcal_tones(bins: np.ndarray, ntones: int) -> np.ndarray:
+    bins = np.ascontiguousarray(bins, np.complex64)
+    out = np.empty(ntones, np.complex64)
+    lib().orc_pcal_tones(_ptr(bins), bins.size, ntones, _ptr(out))
+    return out
+
+
+def fx_fp32(raw, S, N, K, start_sample=0, shift=None, phasor=None, lut=OFFSET_BINARY_LUT,
+            msb_first=False, nthreads=1):
+    """FP32 CPU FX path; returns vis[P][C] complex64 (baseline-major)."""
+    raw = np.ascontiguousarray(raw, np.uint8).reshape(S, -1)
+    C = N // 2
+    P = S * (S + 1) // 2
+    vis = np.zeros((P, C), np.complex64)
+    sh = None if shift is None else np.ascontiguousarray(shift, np.int32)
+    ph = None if phasor is None else np.ascontiguousarray(phasor, np.complex64)
+    lut = np.ascontiguousarray(lut, np.float32)
+    lib().orc_fx_fp32(_ptr(raw), raw.shape[1], S, N, K, start_sample,
+                      _ptr(sh) if sh is not None else None,
+                      _ptr(ph) if ph is not None else None, _ptr(lut), int(msb_first),
+                      _ptr(vis), nthreads)
+    return vis
+
+
+def fx_fstage_fp32(raw, S, N, K, start_sample=0, shift=None, phasor=None,
+                   lut=OFFSET_BINARY_LUT, msb_first=False, nthreads=1):
+    raw = np.ascontiguousarray(raw, np.uint8).reshape(S, -1)
+    C = N // 2
+    out = np.empty((S, K, C), np.complex64)
+    sh = None if shift is None else np.ascontiguousarray(shift, np.int32)
+    ph = None if phasor is None else np.ascontiguousarray(phasor, np.complex64)
+    lut = np.ascontiguousarray(lut, np.float32)
+    lib().orc_fx_fstage_fp32(_ptr(raw), raw.shape[1], S, N, K, start_sample,
+                             _ptr(sh) if sh is not None else None,
+                             _ptr(ph) if ph is not None else None, _ptr(lut), int(msb_first),
+                             _ptr(out), nthreads)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# FP64 models
+# ---------------------------------------------------------------------------
+def unpack_segments_f64(raw, S, N, K, start_sample, shift, lut, msb_first=False,
+                        inputs=None):
+    """Decoded samples [len(inputs)][K][N] in float64 (exact: table values)."""
+    raw = np.ascontiguousarray(raw, np.uint8).reshape(S, -1)
+    inputs = range(S) if inputs is None else inputs
+    lut = np.asarray(lut, np.float32).astype(np.float64)
+    out = np.empty((len(inputs), K, N), np.float64)
+    n = np.arange(N, dtype=np.int64)
+    for ii, s in enumerate(inputs):
+        for k in range(K):
+            st = start_sample + k * N + (0 if shift is None else int(shift[s, k]))
+            f = st + n
+            b = raw[s, f >> 2]
+            sh = (6 - 2 * (f & 3)) if msb_first else (2 * (f & 3))
+            out[ii, k] = lut[(b >> sh) & 3]
+    return out
+
+
+def fx_spectra_f64(raw, S, N, K, start_sample=0, shift=None, phase0=None, dphase=None,
+                   lut=OFFSET_BINARY_LUT, msb_first=False, inputs=None, channels=None):
+    """FP64 F stage: X[s][k][c] = rfft(x)[c] * exp(i*(phase0[s,k] + c*dphase[s,k]))."""
+    inputs = list(range(S)) if inputs is None else list(inputs)
+    x = unpack_segments_f64(raw, S, N, K, start_sample, shift, lut, msb_first, inputs)
+    X = np.fft.rfft(x, axis=-1)[..., : N // 2]
+    if channels is not None:
+        X = X[..., channels]
+        c = np.asarray(channels, np.float64)
+    else:
+        c = np.arange(N // 2, dtype=np.float64)
+    if phase0 is not None:
+        p0 = np.asarray(phase0, np.float64)[inputs][:, :, None]
+        dp = np.asarray(dphase, np.float64)[inputs][:, :, None]
+        X = X * np.exp(1j * (p0 + c[None, None, :] * dp))
+    return X
+
+
+def fx_vis_f64(X: np.ndarray, pairs):
+    """V[p][c] = sum_k X_i[k][c] * conj(X_j[k][c]) for (i, j) in pairs (indices into X)."""
+    out = np.empty((len(pairs), X.shape[-1]), np.complex128)
+    for n, (i, j) in enumerate(pairs):
+        out[n] = np.einsum("kc,kc->c", X[i], np.conj(X[j]))
+    return out
+
+
+def delay_state_f64(poly: np.ndarray, N: int, K: int, fs_hz: float, lo_hz: float):
+    """Per (input, segment) integer shift, fringe phase and per-channel phase step.
+
+    tau(t) = sum_m poly[s, m] t^m at the segment centre t = (k*N + N/2)/fs.
+    shift = round(tau*fs); frac = tau - shift/fs.
+    phase0 = 2*pi*lo*tau (reduced mod 2*pi); dphase = 2*pi*(fs/N)*frac.
+    The correction multiplies channel c by exp(i*(phase0 + c*dphase)).
+    """
+    poly = np.asarray(poly, np.float64)
+    S = poly.shape[0]
+    t = (np.arange(K, dtype=np.float64) * N + N / 2) / fs_hz
+    tau = np.zeros((S, K))
+    for m in range(poly.shape[1] - 1, -1, -1):
+        tau = tau * t[None, :] + poly[:, m : m + 1]
+    shift = np.rint(tau * fs_hz).astype(np.int64)
+    frac = tau - shift / fs_hz
+    cyc = lo_hz * tau
+    phase0 = 2 * np.pi * (cyc - np.floor(cyc))
+    dphase = 2 * np.pi * (fs_hz / N) * frac
+    return shift.astype(np.int32), phase0, dphase
+
+
+def tri_index(i: int, j: int) -> int:
+    return i * (i + 1) // 2 + j

@@ -1,0 +1,338 @@
+/* CPU oracle for the GB300 FX correlator / spectrometer hot path.
+ * TEST INFRASTRUCTURE ONLY -- see cellspe_oracle.h for scope and pins.
+ * Compiled with -ffp-contract=off so that FP32 products and sums are rounded
+ * one operation at a time, as in the reference's scalar generic loops.
+ */
+#include "cellspe_oracle.h"
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* 2-bit unpack                                                            */
+/* ---------------------------------------------------------------------- */
+static inline unsigned field2(const uint8_t* raw, int64_t fidx, int msb_first)
+{
+    uint8_t b = raw[fidx >> 2];
+    int pos = (int)(fidx & 3);
+    int shift = msb_first ? (6 - 2 * pos) : (2 * pos);
+    return (b >> shift) & 3u;
+}
+
+void orc_unpack2bit(const uint8_t* raw, int64_t nsamp, int nchan, int msb_first,
+                    const float lut[4], float* out)
+{
+    for (int c = 0; c < nchan; c++) {
+        float* o = out + (int64_t)c * nsamp;
+        for (int64_t t = 0; t < nsamp; t++)
+            o[t] = lut[field2(raw, t * nchan + c, msb_first)];
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Generic complex MAC (architecture.h:405-433)                            */
+/* ---------------------------------------------------------------------- */
+void orc_addproduct_32fc(const orc_cf32* a, const orc_cf32* b, orc_cf32* acc, int n)
+{
+    for (int i = 0; i < n; i++) {
+        acc[i].re += (a[i].re * b[i].re) - (a[i].im * b[i].im);
+        acc[i].im += (a[i].im * b[i].re) + (a[i].re * b[i].im);
+    }
+}
+
+void orc_addproduct_32fc_conj(const orc_cf32* a, const orc_cf32* b, orc_cf32* acc, int n)
+{
+    for (int i = 0; i < n; i++) {
+        acc[i].re += (a[i].re * b[i].re) + (a[i].im * b[i].im);
+        acc[i].im += (a[i].im * b[i].re) - (a[i].re * b[i].im);
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* FFTs                                                                    */
+/* ---------------------------------------------------------------------- */
+static int ilog2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
+
+static unsigned bitrev(unsigned x, int bits)
+{
+    unsigned r = 0;
+    for (int i = 0; i < bits; i++) { r = (r << 1) | (x & 1u); x >>= 1; }
+    return r;
+}
+
+void orc_cfft_f32(const orc_cf32* in, orc_cf32* out, int n)
+{
+    int lg = ilog2(n);
+    orc_cf32* tmp = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)n);
+    for (int i = 0; i < n; i++) tmp[bitrev((unsigned)i, lg)] = in[i];
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1;
+        for (int j = 0; j < half; j++) {
+            double ang = -2.0 * M_PI * (double)j / (double)len;
+            float wr = (float)cos(ang), wi = (float)sin(ang);
+            for (int i = 0; i < n; i += len) {
+                orc_cf32 u = tmp[i + j], v = tmp[i + j + half];
+                float tr = v.re * wr - v.im * wi;
+                float ti = v.re * wi + v.im * wr;
+                tmp[i + j].re = u.re + tr;          tmp[i + j].im = u.im + ti;
+                tmp[i + j + half].re = u.re - tr;   tmp[i + j + half].im = u.im - ti;
+            }
+        }
+    }
+    memcpy(out, tmp, sizeof(orc_cf32) * (size_t)n);
+    free(tmp);
+}
+
+void orc_cfft_f64(const double* in, double* out, int n)
+{
+    int lg = ilog2(n);
+    double* t = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        unsigned r = bitrev((unsigned)i, lg);
+        t[2 * r] = in[2 * i]; t[2 * r + 1] = in[2 * i + 1];
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1;
+        for (int j = 0; j < half; j++) {
+            double ang = -2.0 * M_PI * (double)j / (double)len;
+            double wr = cos(ang), wi = sin(ang);
+            for (int i = 0; i < n; i += len) {
+                double* u = t + 2 * (i + j);
+                double* v = t + 2 * (i + j + half);
+                double tr = v[0] * wr - v[1] * wi, ti = v[0] * wi + v[1] * wr;
+                v[0] = u[0] - tr; v[1] = u[1] - ti;
+                u[0] = u[0] + tr; u[1] = u[1] + ti;
+            }
+        }
+    }
+    memcpy(out, t, sizeof(double) * 2 * (size_t)n);
+    free(t);
+}
+
+void orc_rfft_f32(const float* in, orc_cf32* out, int n)
+{
+    int m = n / 2;
+    orc_cf32* z = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)m);
+    orc_cf32* Z = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)m);
+    for (int i = 0; i < m; i++) { z[i].re = in[2 * i]; z[i].im = in[2 * i + 1]; }
+    orc_cfft_f32(z, Z, m);
+    for (int k = 0; k <= m; k++) {
+        orc_cf32 a = Z[k % m], b = Z[(m - k) % m];
+        /* E = (a + conj b)/2,  O = (a - conj b)/(2i) */
+        float er = 0.5f * (a.re + b.re), ei = 0.5f * (a.im - b.im);
+        float orr = 0.5f * (a.im + b.im), oi = -0.5f * (a.re - b.re);
+        double ang = -2.0 * M_PI * (double)k / (double)n;
+        float wr = (float)cos(ang), wi = (float)sin(ang);
+        out[k].re = er + (orr * wr - oi * wi);
+        out[k].im = ei + (orr * wi + oi * wr);
+    }
+    out[0].im = 0.0f;
+    out[m].im = 0.0f;
+    free(z); free(Z);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Spectrometer (TaskCoreIPP::doMaths, one source)                         */
+/* ---------------------------------------------------------------------- */
+int orc_spec_overlapped_ffts(const orc_spec_cfg* cfg)
+{
+    return cfg->overlap * cfg->ffts_per_spectrum - (cfg->overlap - 1);
+}
+
+void orc_spec_window(int type, int n, float* w)
+{
+    for (int i = 0; i < n; i++) {
+        if (type == 0) { w[i] = 1.0f; continue; }
+        double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
+        double c = cos(arg);
+        w[i] = (type == 1) ? (float)c : (float)(c * c);
+    }
+}
+
+static void pcal_fold(const float* x, int n, const orc_spec_cfg* cfg, const orc_cf32* rot,
+                      orc_cf32* bins)
+{
+    int L = cfg->pcal_rotatorlen, T = cfg->pcal_tonebins;
+    for (int s = 0; s + L <= n; s += L) {
+        for (int i = 0; i < L; i++) {
+            float re = x[s + i] * rot[i].re;   /* ippsMul_32f32fc */
+            float im = x[s + i] * rot[i].im;
+            bins[i % T].re += re;              /* ippsAdd_32fc_I fold */
+            bins[i % T].im += im;
+        }
+    }
+}
+
+int orc_spectrometer(const float* samples, int64_t nsamp, const orc_spec_cfg* cfg,
+                     float* power, orc_cf32* pcal_bins)
+{
+    const int N = cfg->fft_points, nb = N / 2 + 1;
+    const int hop = N / cfg->overlap;
+    const int novl = orc_spec_overlapped_ffts(cfg);
+    const float scale = (float)(1.0 / (double)novl);
+    float* w = (float*)malloc(sizeof(float) * (size_t)N);
+    float* xw = (float*)malloc(sizeof(float) * (size_t)N);
+    orc_cf32* X = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)nb);
+    orc_cf32* rot = NULL;
+    orc_spec_window(cfg->window, N, w);
+    if (cfg->pcal_tonebins > 0) {
+        rot = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)cfg->pcal_rotatorlen);
+        double dphi = 2 * M_PI * (-cfg->pcal_offset_hz / cfg->sample_rate_hz);
+        for (int i = 0; i < cfg->pcal_rotatorlen; i++) {
+            rot[i].re = (float)cos(dphi * (double)i);
+            rot[i].im = (float)sin(dphi * (double)i);
+        }
+    }
+    int64_t pos = 0, remaining = nsamp;
+    int acc = 0, spec = 0, curr = 0;
+    float* P = power;
+    orc_cf32* PC = pcal_bins;
+    memset(P, 0, sizeof(float) * (size_t)nb);
+    if (PC) memset(PC, 0, sizeof(orc_cf32) * (size_t)cfg->pcal_tonebins);
+    while (remaining >= N) {
+        const float* x = samples + pos;
+        pos += hop;
+        if (rot && PC && (curr % cfg->overlap) == 0) pcal_fold(x, N, cfg, rot, PC);
+        for (int i = 0; i < N; i++) xw[i] = w[i] * x[i];
+        orc_rfft_f32(xw, X, N);
+        curr++;
+        float re0 = X[0].re, reN2 = X[N / 2].re;
+        float acc0 = P[0] + re0 * re0;
+        float accN = P[nb - 1] + reN2 * reN2;
+        for (int k = 1; k < nb - 1; k++) {
+            float pw = X[k].re * X[k].re + X[k].im * X[k].im;
+            P[k] += pw;
+        }
+        P[0] = acc0; P[nb - 1] = accN;
+        remaining -= hop;
+        if (++acc >= novl) {
+            for (int k = 0; k < nb; k++) P[k] *= scale;
+            spec++; acc = 0;
+            pos += N - hop; remaining -= N - hop;
+            P += nb;
+            if (PC) PC += cfg->pcal_tonebins;
+            if (remaining >= N) {
+                memset(P, 0, sizeof(float) * (size_t)nb);
+                if (PC) memset(PC, 0, sizeof(orc_cf32) * (size_t)cfg->pcal_tonebins);
+            }
+        }
+    }
+    free(w); free(xw); free(X); free(rot);
+    return spec;
+}
+
+void orc_pcal_tones(const orc_cf32* bins, int nbins, int ntones, orc_cf32* tones)
+{
+    for (int k = 0; k < ntones; k++) {
+        double re = 0, im = 0;
+        for (int n = 0; n < nbins; n++) {
+            double a = -2.0 * M_PI * (double)((int64_t)k * n % nbins) / (double)nbins;
+            re += bins[n].re * cos(a) - bins[n].im * sin(a);
+            im += bins[n].re * sin(a) + bins[n].im * cos(a);
+        }
+        tones[k].re = (float)(re / nbins);
+        tones[k].im = (float)(im / nbins);
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* FX correlator, FP32 CPU path                                            */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+    const uint8_t* raw; int64_t bpi; int S, N, K; int64_t start;
+    const int32_t* shift; const orc_cf32* phasor; const float* lut; int msb;
+    orc_cf32* spectra; orc_cf32* vis;
+    int t0, t1;            /* work range (units depend on the phase) */
+} fx_job;
+
+static void fstage_one(const fx_job* j, int s, int k, float* x, orc_cf32* X)
+{
+    const int N = j->N, C = N / 2;
+    int64_t st = j->start + (int64_t)k * N + (j->shift ? j->shift[(int64_t)s * j->K + k] : 0);
+    const uint8_t* r = j->raw + (int64_t)s * j->bpi;
+    for (int n = 0; n < N; n++) x[n] = j->lut[field2(r, st + n, j->msb)];
+    orc_rfft_f32(x, X, N);
+    orc_cf32* o = j->spectra + ((int64_t)s * j->K + k) * C;
+    if (j->phasor) {
+        const orc_cf32* ph = j->phasor + ((int64_t)s * j->K + k) * C;
+        for (int c = 0; c < C; c++) {       /* genericMul_32fc, architecture.h:270-278 */
+            o[c].re = (X[c].re * ph[c].re) - (X[c].im * ph[c].im);
+            o[c].im = (X[c].im * ph[c].re) + (X[c].re * ph[c].im);
+        }
+    } else {
+        memcpy(o, X, sizeof(orc_cf32) * (size_t)C);
+    }
+}
+
+static void* fstage_worker(void* arg)
+{
+    fx_job* j = (fx_job*)arg;
+    float* x = (float*)malloc(sizeof(float) * (size_t)j->N);
+    orc_cf32* X = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)(j->N / 2 + 1));
+    for (int u = j->t0; u < j->t1; u++) fstage_one(j, u / j->K, u % j->K, x, X);
+    free(x); free(X);
+    return NULL;
+}
+
+static void* xstage_worker(void* arg)
+{
+    fx_job* j = (fx_job*)arg;
+    const int C = j->N / 2;
+    for (int p = j->t0; p < j->t1; p++) {
+        int i = (int)((sqrt(8.0 * p + 1.0) - 1.0) / 2.0);
+        while ((i + 1) * (i + 2) / 2 <= p) i++;
+        while (i * (i + 1) / 2 > p) i--;
+        int jj = p - i * (i + 1) / 2;
+        orc_cf32* acc = j->vis + (int64_t)p * C;
+        for (int k = 0; k < j->K; k++)
+            orc_addproduct_32fc_conj(j->spectra + ((int64_t)i * j->K + k) * C,
+                                     j->spectra + ((int64_t)jj * j->K + k) * C, acc, C);
+    }
+    return NULL;
+}
+
+static void run_parallel(fx_job* base, int units, int nthreads, void* (*fn)(void*))
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > units) nthreads = units > 0 ? units : 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    fx_job* jobs = (fx_job*)malloc(sizeof(fx_job) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t] = *base;
+        jobs[t].t0 = (int)((int64_t)units * t / nthreads);
+        jobs[t].t1 = (int)((int64_t)units * (t + 1) / nthreads);
+        if (nthreads == 1) fn(&jobs[t]);
+        else pthread_create(&th[t], NULL, fn, &jobs[t]);
+    }
+    if (nthreads > 1)
+        for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(th); free(jobs);
+}
+
+void orc_fx_fstage_fp32(const uint8_t* raw, int64_t bytes_per_input, int S, int N, int K,
+                        int64_t start_sample, const int32_t* shift, const orc_cf32* phasor,
+                        const float lut[4], int msb_first, orc_cf32* spectra, int nthreads)
+{
+    fx_job j = { raw, bytes_per_input, S, N, K, start_sample, shift, phasor, lut, msb_first,
+                 spectra, NULL, 0, 0 };
+    run_parallel(&j, S * K, nthreads, fstage_worker);
+}
+
+void orc_fx_fp32(const uint8_t* raw, int64_t bytes_per_input, int S, int N, int K,
+                 int64_t start_sample, const int32_t* shift, const orc_cf32* phasor,
+                 const float lut[4], int msb_first, orc_cf32* vis, int nthreads)
+{
+    const int C = N / 2;
+    orc_cf32* spectra = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)S * K * C);
+    orc_fx_fstage_fp32(raw, bytes_per_input, S, N, K, start_sample, shift, phasor, lut,
+                       msb_first, spectra, nthreads);
+    fx_job j = { raw, bytes_per_input, S, N, K, start_sample, shift, phasor, lut, msb_first,
+                 spectra, vis, 0, 0 };
+    run_parallel(&j, S * (S + 1) / 2, nthreads, xstage_worker);
+    free(spectra);
+}

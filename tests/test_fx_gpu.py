@@ -1,0 +1,114 @@
+"""Full FX path (K-a + K-b + K-c + K-d1) vs the oracle: FP32 CPU path and FP64 model."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5   # FP32 GPU path vs the FP32 CPU path / FP64 model, relative L2
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("S,N,K", [(2, 1024, 64), (4, 2048, 40), (3, 4096, 9), (5, 8192, 4), (2, 32768, 2)])
+def test_fx_fp32_vs_cpu_path(cg, orc, S, N, K):
+    import synth
+
+    raw = synth.stations_offset_binary(S, N * K, rho=0.2, lags=np.arange(S) % 4, seed=S + N)
+    p = cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_BASELINE_MAJOR)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis)
+    ref = orc.fx_fp32(raw, S, N, K)
+    assert _rel(vis, ref) < TOL
+
+
+def test_config1_lag_known_answer(cg, orc):
+    """Config 1: 2 stations, 2^22 samples each, 1024-pt FFT, station 2 lags by 3 samples.
+
+    V_10 = X_1 conj(X_0) with x_1(t) = c(t - 3) has phase -2 pi 3 k / N; its
+    lag spectrum (inverse FFT over channels) peaks at lag -3.
+    """
+    import synth
+
+    S, N, K = 2, 1024, 4096
+    raw = synth.stations_offset_binary(S, N * K, rho=0.1, lags=[0, 3], seed=1)
+    p = cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_BASELINE_MAJOR)
+    vis = np.zeros((3, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis)
+    cross = vis[orc.tri_index(1, 0)].astype(np.complex128)
+    k = np.arange(N // 2)
+    derot = (cross * np.exp(2j * np.pi * 3 * k / N))[16:-16].reshape(-1, 16).sum(axis=1)
+    assert np.abs(np.angle(derot)).max() < 0.15
+    lag = np.fft.ifft(cross, n=N)
+    assert int(np.argmax(np.abs(lag))) == N - 3
+    coh = np.abs(cross) / np.sqrt(vis[0].real * vis[2].real)
+    assert 0.06 < np.median(coh) < 0.12                        # 2-bit coherence ~ 0.88 rho
+
+
+def test_fx_delay_model_vs_oracle(cg, orc):
+    import synth
+
+    S, N, K = 3, 2048, 24
+    fs, lo = 32e6, 8.4e9
+    margin = 4096
+    T = N * K + 2 * margin
+    raw = synth.stations_offset_binary(S, T, rho=0.3, seed=9)
+    rng = np.random.default_rng(4)
+    poly = np.zeros((S, 4))
+    poly[:, 0] = rng.uniform(-40e-6, 40e-6, S)     # +-1280 samples
+    poly[:, 1] = rng.uniform(-3e-6, 3e-6, S)
+    poly[:, 2] = rng.uniform(-1e-9, 1e-9, S)
+    p = cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_BASELINE_MAJOR, start_sample=margin,
+                     fs_hz=fs, lo_hz=lo)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis, delay_poly=poly)
+    shift, ph0, dph = orc.delay_state_f64(poly, N, K, fs, lo)
+    c = np.arange(N // 2)
+    phasor = np.exp(1j * (ph0.astype(np.float32)[:, :, None].astype(np.float64) +
+                          c[None, None, :] * dph.astype(np.float32)[:, :, None].astype(np.float64))).astype(np.complex64)
+    ref = orc.fx_fp32(raw, S, N, K, start_sample=margin, shift=shift, phasor=phasor)
+    assert _rel(vis, ref) < TOL
+    # and against the FP64 model
+    X = orc.fx_spectra_f64(raw, S, N, K, margin, shift, ph0, dph)
+    pairs = [(i, j) for i in range(S) for j in range(i + 1)]
+    ref64 = orc.fx_vis_f64(X, pairs)
+    assert _rel(vis, ref64) < TOL
+
+
+def test_fx_layouts_memory_and_accumulate(cg):
+    import torch
+
+    import synth
+
+    S, N, K = 6, 1024, 16
+    raw = synth.stations_offset_binary(S, N * K, rho=0.1, seed=3)
+    P, C = S * (S + 1) // 2, N // 2
+    vb = np.zeros((P, C), np.complex64)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_BASELINE_MAJOR), raw, vb)
+    vc = np.zeros((C, P), np.complex64)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_CHANNEL_MAJOR), raw, vc)
+    assert np.array_equal(vb, vc.T)
+    d_raw = torch.from_numpy(raw).cuda()
+    d_vis = torch.zeros((C, P), dtype=torch.complex64, device="cuda")
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1]), d_raw, d_vis)
+    assert np.array_equal(d_vis.cpu().numpy(), vc)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], accumulate=True), raw, vc)
+    assert np.allclose(vc, 2 * d_vis.cpu().numpy(), rtol=1e-6, atol=1e-4)
+
+
+def test_fx_rejects_bad_jobs(cg):
+    raw = np.zeros((2, 1024), np.uint8)
+    vis = np.zeros((3, 512), np.complex64)
+    with pytest.raises(cg.CellspeError) as e:     # unsupported FFT size
+        cg.fx_correlate(cg.fx_params(2, 1000, 1, 1024), raw, vis)
+    assert e.value.code == cg.ERR_ARG
+    with pytest.raises(cg.CellspeError) as e:     # segments past the end of the data
+        cg.fx_correlate(cg.fx_params(2, 1024, 5, 1024), raw, vis)
+    assert e.value.code == cg.ERR_ARG
+    cg.lib().cellspe_set_hbm_budget(1 << 10)      # admission control
+    try:
+        with pytest.raises(cg.CellspeError) as e:
+            cg.fx_correlate(cg.fx_params(2, 1024, 4, 1024), raw, vis)
+        assert e.value.code == cg.ERR_NOMEM
+    finally:
+        cg.lib().cellspe_set_hbm_budget(0)

@@ -1,0 +1,119 @@
+"""The oracle pinned to the reference: golden vectors, live reference, known answers."""
+import ctypes
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("fmt,nch", [("Mark5B_512_16_2", 16), ("Mark5B_256_8_2", 8), ("Mark5B_128_4_2", 4)])
+def test_unpack_matches_mark5access_golden(orc, fmt, nch):
+    g = np.load(GOLD / "mark5b_unpack.npz")
+    raw, ref = g[f"{fmt}_raw"], g[f"{fmt}_out"]
+    mine = orc.unpack2bit(raw, ref.shape[1], nch, orc.MARK5B_LUT)
+    assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+def test_unpack_matches_live_mark5access(orc):
+    if not orc.have_ref():
+        pytest.skip("reference tree not compiled here")
+    rng = np.random.default_rng(5)
+    for fmt, nch in [(b"Mark5B-1024-16-2", 16), (b"Mark5B-256-8-2", 8), (b"Mark5B-128-4-2", 4)]:
+        n = 4096
+        raw = rng.integers(0, 256, n * nch // 4, dtype=np.uint8)
+        ref = np.zeros(nch * n, np.float32)
+        c = ctypes.c_int()
+        rc = orc.ref_mark5().ref_mark5_unpack(fmt, raw.ctypes.data, n, ref.ctypes.data, ctypes.byref(c))
+        assert rc == n
+        mine = orc.unpack2bit(raw, n, nch, orc.MARK5B_LUT)
+        assert np.array_equal(mine.view(np.uint32), ref.reshape(nch, n).view(np.uint32))
+
+
+def test_generic_mac_golden(orc):
+    g = np.load(GOLD / "generic_mac.npz")
+    acc = g["acc0"].copy()
+    orc.addproduct(g["a"], g["b"], acc, conj=False)
+    assert np.array_equal(acc.view(np.uint32), g["mac"].view(np.uint32))
+    acc = g["acc0"].copy()
+    orc.addproduct(g["a"], g["b"], acc, conj=True)
+    assert np.array_equal(acc.view(np.uint32), g["mac_conj"].view(np.uint32))
+
+
+def test_generic_mac_live_reference(orc):
+    if not orc.have_ref():
+        pytest.skip("reference tree not compiled here")
+    rng = np.random.default_rng(3)
+    a = (rng.standard_normal(777) + 1j * rng.standard_normal(777)).astype(np.complex64)
+    b = (rng.standard_normal(777) + 1j * rng.standard_normal(777)).astype(np.complex64)
+    for conj, name in [(True, "ref_addproduct_32fc_conj"), (False, "ref_addproduct_32fc")]:
+        acc0 = (rng.standard_normal(777) + 1j * rng.standard_normal(777)).astype(np.complex64)
+        mine, ref = acc0.copy(), acc0.copy()
+        orc.addproduct(a, b, mine, conj)
+        getattr(orc.ref_generic(), name)(a.ctypes.data, b.ctypes.data, ref.ctypes.data, 777)
+        assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+def test_twobit_and_msb_first_tables(orc):
+    # TwoBitUnpacker (DataUnpackers.cpp:174-227): channel c of a 4-channel byte
+    # sits at shift 2c, value map_rev[code].
+    raw = np.arange(256, dtype=np.uint8)
+    out = orc.unpack2bit(raw, 256, 4, orc.TWOBIT_LUT)
+    for c in range(4):
+        codes = (raw >> (2 * c)) & 3
+        assert np.array_equal(out[c], orc.TWOBIT_LUT[codes])
+    # single channel MSB first: sample 0 in bits 7:6
+    out = orc.unpack2bit(raw, 1024, 1, orc.TWOBIT_LUT, msb_first=True)[0].reshape(256, 4)
+    for j in range(4):
+        assert np.array_equal(out[:, j], orc.TWOBIT_LUT[(raw >> (6 - 2 * j)) & 3])
+
+
+@pytest.mark.parametrize("n", [32, 1024, 4096])
+def test_fft_vs_fp64(orc, n):
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    ref = np.fft.fft(x.astype(np.complex128))
+    assert np.linalg.norm(orc.cfft_f32(x) - ref) / np.linalg.norm(ref) < 1e-6
+    r = rng.standard_normal(2 * n).astype(np.float32)
+    ref = np.fft.rfft(r.astype(np.float64))
+    assert np.linalg.norm(orc.rfft_f32(r) - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def test_spectrometer_known_tone(orc):
+    # A pure tone at bin 100 of a 1024-point FFT: the power peaks there.
+    N, K = 1024, 8
+    n = np.arange(N * K)
+    x = np.cos(2 * np.pi * 100 * n / N).astype(np.float32)
+    power, _ = orc.spectrometer(x, N, 2, 2, K)
+    assert power.shape == (1, N // 2 + 1)
+    assert int(np.argmax(power[0])) == 100
+    # 1/core_overlapped_ffts scaling: overlapped FFTs = 2K-1 (swspectrometer.cpp:231)
+    w = orc.window(2, N)
+    expect = (np.abs(np.sum(w * np.cos(2 * np.pi * 100 * np.arange(N) / N) * np.exp(-2j * np.pi * 100 * np.arange(N) / N))) ** 2)
+    assert power[0, 100] == pytest.approx(expect, rel=1e-3)
+
+
+def test_pcal_unit_test_recipe(orc):
+    """PCal.cpp:879-951: tones with phase -90 deg + 5 deg per tone, checked to 0.1 deg.
+
+    Offset 0 (PCalExtractorTrivial); tone 0 is DC and has no phase, so tones
+    1..N_tones-1 are checked.
+    """
+    bw, spacing = 16e6, 1e6
+    fs = 2 * bw
+    nbins = int(fs / spacing)
+    ntones = int(bw // spacing)
+    nsamp = nbins * 4096
+    n = np.arange(nsamp)
+    data = np.zeros(nsamp)
+    for t in range(ntones):
+        data += np.sin(np.pi * n * (t * spacing) / bw + t * np.pi * 5 / 180)
+    # fold the real samples into Nbins (TaskCoreIPP::extract_PCal with a unit rotator)
+    bins = np.zeros(nbins, np.complex64)
+    for b in range(nbins):
+        bins[b] = data[b::nbins].sum()
+    tones = orc.pcal_tones(bins, ntones)
+    phase = np.degrees(np.angle(tones[1:]))
+    expect = -90.0 + 5.0 * np.arange(1, ntones)
+    assert np.all(np.abs((phase - expect + 180) % 360 - 180) < 0.1)

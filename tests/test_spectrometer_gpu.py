@@ -1,0 +1,104 @@
+"""K-e + K-pcal: GPU spectrometer vs the restated TaskCoreIPP::doMaths."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _oracle(orc, words, nsub, N, overlap, window, K, tonebins=0, rotatorlen=0, offset=0.0, fs=1.0):
+    raw = words.view(np.uint8)
+    nsamp = raw.size * 4 // nsub
+    planes = orc.unpack2bit(raw, nsamp, nsub, orc.MARK5B_LUT)
+    pw, pc = [], []
+    for c in range(nsub):
+        p, b = orc.spectrometer(planes[c], N, overlap, window, K, tonebins, rotatorlen, offset, fs)
+        pw.append(p)
+        pc.append(b)
+    return np.stack(pw), (np.stack(pc) if tonebins else None)
+
+
+@pytest.mark.parametrize("nsub,N,overlap,window,K,nspec", [
+    (16, 1024, 2, 2, 8, 2), (4, 4096, 1, 0, 4, 1), (1, 2048, 4, 1, 3, 2), (8, 32768, 2, 2, 2, 1),
+    (4, 65536, 2, 2, 3, 1)])
+def test_spectrometer_vs_oracle(cg, orc, nsub, N, overlap, window, K, nspec):
+    import synth
+
+    T = N * K * nspec
+    words, _ = synth.mark5b_subbands(nsub, T, fs_hz=32e6, seed=N + nsub, n_channels=N // 2)
+    if nsub < 16:  # repack to nsub channels per sample time
+        raw8 = words.view(np.uint8)
+        codes = np.stack([(words >> np.uint32(2 * c)) & np.uint32(3) for c in range(nsub)], axis=1)
+        words = synth.pack2bit(codes.reshape(-1)).view(np.uint8)
+    raw = np.ascontiguousarray(words).view(np.uint8)
+    p = cg.spec_params(N, overlap, window, K, nspec, nsub, raw.size)
+    power = np.zeros((nsub, nspec, N // 2 + 1), np.float32)
+    cg.spectrometer(p, raw, power)
+    ref, _ = _oracle(orc, raw, nsub, N, overlap, window, K)
+    assert ref.shape == power.shape
+    assert np.linalg.norm(power - ref) / np.linalg.norm(ref) < TOL
+
+
+def test_spectrometer_pcal_and_sines_known_answer(cg, orc):
+    """Config-2 shape in miniature: 16 subbands, 32 MS/s, 1 MHz comb, 3 sines."""
+    import synth
+
+    nsub, N, K, fs = 16, 4096, 16, 32e6
+    T = N * K
+    words, truth = synth.mark5b_subbands(nsub, T, fs_hz=fs, seed=2, n_channels=N // 2, pcal_amp=0.3)
+    raw = words.view(np.uint8)
+    tb, ntones = 32, 16
+    p = cg.spec_params(N, 2, 2, K, 1, nsub, raw.size, tonebins=tb, rotatorlen=tb, ntones=ntones, offset_hz=0.0,
+                       fs_hz=fs)
+    power = np.zeros((nsub, 1, N // 2 + 1), np.float32)
+    bins = np.zeros((nsub, 1, tb), np.complex64)
+    tones = np.zeros((nsub, 1, ntones), np.complex64)
+    cg.spectrometer(p, raw, power, bins, tones)
+    ref_p, ref_b = _oracle(orc, raw, nsub, N, 2, 2, K, tb, tb, 0.0, fs)
+    assert np.linalg.norm(power - ref_p) / np.linalg.norm(ref_p) < TOL
+    assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < TOL
+    for c in range(nsub):
+        ref_t = orc.pcal_tones(ref_b[c, 0], ntones)
+        assert np.linalg.norm(tones[c, 0] - ref_t) / np.linalg.norm(ref_t) < TOL
+        # injected comb phases (cosine at k MHz, phase phi -> tone phase phi)
+        ph = np.angle(tones[c, 0, 1:ntones])
+        d = np.angle(np.exp(1j * (ph - truth["tone_phase"][c, : ntones - 1])))
+        assert np.degrees(np.abs(d)).max() < 5.0
+        # the sine with the highest frequency resolution lands at its bin
+        for f in truth["sine_f"][c]:
+            kbin = int(round(f / fs * N))
+            assert power[c, 0, kbin] > 3 * np.median(power[c, 0])
+
+
+def test_spectrometer_pcal_offset_rotator(cg, orc):
+    import synth
+
+    nsub, N, K, fs = 4, 4096, 4, 32.768e6
+    words, _ = synth.mark5b_subbands(16, N * K, fs_hz=fs, seed=5, n_channels=N // 2)
+    codes = np.stack([(words >> np.uint32(2 * c)) & np.uint32(3) for c in range(nsub)], axis=1)
+    raw = synth.pack2bit(codes.reshape(-1))
+    tb, L = 32, 4096        # spacing 1.024 MHz, offset 8 kHz
+    p = cg.spec_params(N, 2, 2, K, 1, nsub, raw.size, tonebins=tb, rotatorlen=L, ntones=16, offset_hz=8e3, fs_hz=fs)
+    power = np.zeros((nsub, 1, N // 2 + 1), np.float32)
+    bins = np.zeros((nsub, 1, tb), np.complex64)
+    cg.spectrometer(p, raw, power, bins)
+    _, ref_b = _oracle(orc, raw, nsub, N, 2, 2, K, tb, L, 8e3, fs)
+    assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < TOL
+
+
+def test_spectrometer_planes_layout_and_device(cg):
+    import torch
+
+    import synth
+
+    nsub, N, K = 4, 1024, 4
+    words, _ = synth.mark5b_subbands(16, N * K, fs_hz=32e6, seed=8, n_channels=N // 2)
+    codes = np.stack([(words >> np.uint32(2 * c)) & np.uint32(3) for c in range(nsub)], axis=1)
+    inter = synth.pack2bit(codes.reshape(-1))
+    planes = np.concatenate([synth.pack2bit(codes[:, c]) for c in range(nsub)])
+    a = np.zeros((nsub, 1, N // 2 + 1), np.float32)
+    cg.spectrometer(cg.spec_params(N, 2, 2, K, 1, nsub, inter.size), inter, a)
+    b = torch.zeros((nsub, 1, N // 2 + 1), dtype=torch.float32, device="cuda")
+    cg.spectrometer(cg.spec_params(N, 2, 2, K, 1, nsub, planes.size, layout=cg.SPEC_PLANES),
+                    torch.from_numpy(planes).cuda(), b)
+    assert np.array_equal(a, b.cpu().numpy())
