@@ -142,10 +142,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="fp32", choices=["tc", "fp32"])
+    ap.add_argument("--mode", default="tc", choices=["tc", "fp32"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-segments", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--segments", type=int, default=K,
+                    help="spectra per integration (smaller values make a profiling-sized case)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -171,9 +174,11 @@ def main():
         torch.cuda.synchronize()
 
     x_mode = cg.X_TC_FP16 if args.mode == "tc" else cg.X_FP32
-    raw = synth.device_stations(S, T, RHO, seed=4 + 1000 * rank)
+    K_run = args.segments
+    T_run = N * K_run
+    raw = synth.device_stations(S, T_run, RHO, seed=4 + 1000 * rank)
     vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
-    params = cg.fx_params(S, N, K, T // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+    params = cg.fx_params(S, N, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
     for _ in range(args.warmup):
         cg.fx_correlate(params, raw, vis)
 
@@ -197,37 +202,39 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     ms_step = ms / args.steps
-    value = world * S * T / (ms_step * 1e-3) / 1e9
+    value = world * S * T_run / (ms_step * 1e-3) / 1e9
     stage_ms = stage_sum / args.steps
 
     # ---- end to end through the C ABI with host buffers --------------------
-    raw_h = np.empty((S, T // 4), np.uint8)
+    raw_h = np.empty((S, T_run // 4), np.uint8)
     raw_h[:] = raw.cpu().numpy()
-    pin_raw = torch.from_numpy(raw_h).pin_memory()
-    pin_vis = torch.empty((C, P), dtype=torch.complex64).pin_memory()
-    raw_np, vis_np = pin_raw.numpy(), pin_vis.numpy()
-    hparams = cg.fx_params(S, N, K, T // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
-    cg.fx_correlate(hparams, raw_np, vis_np)
-    barrier()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record()
-    for _ in range(args.e2e_steps):
+    e2e_ms, e2e_value = None, None
+    if not args.no_e2e:
+        pin_raw = torch.from_numpy(raw_h).pin_memory()
+        pin_vis = torch.empty((C, P), dtype=torch.complex64).pin_memory()
+        raw_np, vis_np = pin_raw.numpy(), pin_vis.numpy()
+        hparams = cg.fx_params(S, N, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
         cg.fx_correlate(hparams, raw_np, vis_np)
-    torch.cuda.synchronize()
-    f1.record()
-    f1.synchronize()
-    e2e_ms = f0.elapsed_time(f1) / args.e2e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * S * T / (e2e_ms * 1e-3) / 1e9
+        barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        for _ in range(args.e2e_steps):
+            cg.fx_correlate(hparams, raw_np, vis_np)
+        torch.cuda.synchronize()
+        f1.record()
+        f1.synchronize()
+        e2e_ms = f0.elapsed_time(f1) / args.e2e_steps
+        if dist:
+            t = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e_value = world * S * T_run / (e2e_ms * 1e-3) / 1e9
 
     # ---- roofline of the dominant kernel -----------------------------------
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
-    f_bytes = S * K * (N // 4 + C * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
-    x_flops = 8.0 * P * C * K                                              # 8 real flops per CMAC, triangle
+    f_bytes = S * K_run * (N // 4 + C * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
+    x_flops = 8.0 * P * C * K_run                                              # 8 real flops per CMAC, triangle
     stages = {"f_stage_ms": f_ms, "x_stage_ms": x_ms, "output_ms": stage_ms[3],
               "f_stage_gbs": f_bytes / (f_ms * 1e-3) / 1e9,
               "x_stage_tflops": x_flops / (x_ms * 1e-3) / 1e12}
@@ -263,12 +270,12 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f16-tc/f32-acc" if x_mode == cg.X_TC_FP16 else "f32",
             "data": "synthetic (seeded 2-bit offset binary, rho=0.02, generated on device)",
-            "config": {"workload": "256-station dual-pol FX: S=512, N=2048, C=1024, K=4096",
-                       "inputs": S, "fft_points": N, "channels": C, "segments": K, "products": P,
+            "config": {"workload": f"256-station dual-pol FX: S=512, N=2048, C=1024, K={K_run}",
+                       "inputs": S, "fft_points": N, "channels": C, "segments": K_run, "products": P,
                        "x_mode": args.mode, "vis_order": "channel-major [C][P]",
                        "l2": "inputs larger than L2 (1.07 GB raw, spectra 8.6/17 GB, vis 1.07 GB)",
                        "parallelism": f"replicas x{world} (one job per GPU)"},
-            "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(S * T // 4),
+            "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(S * T_run // 4),
                     "d2h_bytes_per_step": int(C * P * 8), "ms_per_step": e2e_ms},
             "gpu_launches": int(launches),
             "roofline": roof,

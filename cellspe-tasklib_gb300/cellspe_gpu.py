@@ -134,6 +134,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_fft_c2c": ([V, V, I, LL, I], I),
             "cellspe_fft_r2c": ([V, V, I, LL, I], I),
             "cellspe_xmac": ([V, I, I, I, V, I, I], I),
+            "cellspe_xmac_f16": ([V, I, I, I, V, I, I], I),
             "cellspe_fx_correlate": ([V, V, V, V], I),
             "cellspe_fx_workspace_bytes": ([V], LL),
             "cellspe_fx_correlate_async": ([V, V, V, V, V], I),
@@ -230,6 +231,13 @@ def fft_r2c(x, out, n: int, batch: int):
 
 def xmac(spectra, S: int, C: int, K: int, vis, accumulate: bool = False):
     _check(lib().cellspe_xmac(_ptr(spectra)[0], S, C, K, _ptr(vis)[0], int(accumulate), _mem(spectra, vis)))
+    return vis
+
+
+def xmac_f16(spectra_f16, S: int, C: int, K: int, vis, accumulate: bool = False):
+    """spectra_f16: float16 [C][2][S][K] (Re plane, Im plane)."""
+    _check(lib().cellspe_xmac_f16(_ptr(spectra_f16)[0], S, C, K, _ptr(vis)[0], int(accumulate),
+                                  _mem(spectra_f16, vis)))
     return vis
 
 

@@ -26,28 +26,45 @@ CS_DEV float2 cmul_conj(float2 a, float2 b)  // a * conj(b)
 CS_DEV float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }   // a * (-i)
 CS_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
-// W16^m = exp(-2 pi i m / 16) for the exponents the radix-16 codelet uses.
-CS_DEV float2 w16(int m)
+// W32^m = exp(-2 pi i m / 32), m in [0, 32): cos and sin of multiples of pi/16.
+CS_DEV float2 w32(int m)
 {
-    const float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f;
-    const float h = 0.70710678118654752f;
-    switch (m & 15) {
-        case 0: return make_float2(1.f, 0.f);
-        case 1: return make_float2(c1, -s1);
-        case 2: return make_float2(h, -h);
-        case 3: return make_float2(s1, -c1);
-        case 4: return make_float2(0.f, -1.f);
-        case 5: return make_float2(-s1, -c1);
-        case 6: return make_float2(-h, -h);
-        case 7: return make_float2(-c1, -s1);
-        case 8: return make_float2(-1.f, 0.f);
-        case 9: return make_float2(-c1, s1);
-        case 10: return make_float2(-h, h);
-        case 11: return make_float2(-s1, c1);
-        case 12: return make_float2(0.f, 1.f);
-        case 13: return make_float2(s1, c1);
-        case 14: return make_float2(h, h);
-        default: return make_float2(c1, s1);
+    const float c[9] = {1.0f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f,
+                        0.70710678118654752f, 0.55557023301960222f, 0.38268343236508977f,
+                        0.19509032201612826f, 0.0f};
+    m &= 31;
+    const int q = m >> 3, r = m & 7;          // quadrant, offset inside it
+    float cr = c[r], sr = c[8 - r];           // cos, sin of r*pi/16
+    // exp(-i (q*pi/2 + r*pi/16)) = (-i)^q * (cr - i sr)
+    float2 z = make_float2(cr, -sr);
+    switch (q) {
+        case 0: return z;
+        case 1: return make_float2(z.y, -z.x);
+        case 2: return make_float2(-z.x, -z.y);
+        default: return make_float2(-z.y, z.x);
+    }
+}
+CS_DEV float2 w16(int m) { return w32(2 * m); }
+
+// W64^m = exp(-2 pi i m / 64) for m in [0, 32) (used with constant m).
+CS_DEV float2 w64c(int m)
+{
+    const float c[17] = {1.0f, 0.99518472667219693f, 0.98078528040323043f, 0.95694033573220882f, 0.92387953251128674f, 0.88192126434835505f, 0.83146961230254524f, 0.77301045336273699f, 0.70710678118654757f, 0.63439328416364549f, 0.55557023301960229f, 0.47139673682599781f, 0.38268343236508984f, 0.29028467725446233f, 0.19509032201612833f, 0.09801714032956077f, 0.0f};
+    const int q = (m >> 4) & 1, r = m & 15;
+    float2 z = make_float2(c[r], -c[16 - r]);
+    return q ? make_float2(z.y, -z.x) : z;
+}
+
+// v * W32^e with the exact quarter turns kept exact (e folds to a constant
+// inside unrolled codelets, so the switch disappears).
+CS_DEV float2 rot32(float2 v, int e)
+{
+    switch (e & 31) {
+        case 0: return v;
+        case 8: return make_float2(v.y, -v.x);
+        case 16: return make_float2(-v.x, -v.y);
+        case 24: return make_float2(-v.y, v.x);
+        default: return cmul(v, w32(e));
     }
 }
 
@@ -90,8 +107,7 @@ template <int R1, int R2> struct DftSplit {
             for (int n1 = 0; n1 < R1; n1++) b[n2][n1] = a[R2 * n1 + n2];
             Dft<R1>::run(b[n2]);
 #pragma unroll
-            for (int k1 = 0; k1 < R1; k1++)
-                if (n2 * k1) b[n2][k1] = cmul(b[n2][k1], w16((n2 * k1) * (16 / R)));
+            for (int k1 = 0; k1 < R1; k1++) b[n2][k1] = rot32(b[n2][k1], (n2 * k1) * (32 / R));
         }
 #pragma unroll
         for (int k1 = 0; k1 < R1; k1++) {
@@ -109,6 +125,9 @@ template <> struct Dft<8> {
 };
 template <> struct Dft<16> {
     static CS_DEV void run(float2* a) { DftSplit<4, 4>::run(a); }
+};
+template <> struct Dft<32> {
+    static CS_DEV void run(float2* a) { DftSplit<4, 8>::run(a); }
 };
 
 // Padded shared-memory index: one spare float2 after every 16 elements keeps

@@ -70,6 +70,12 @@ __global__ void k_autocorr(const float2* __restrict__ x, float2* __restrict__ ac
     acc[i] = a;
 }
 
+__global__ void k_recip(const float* __restrict__ in, float* __restrict__ out, int64_t n)
+{
+    int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x;
+    if (i < n) out[i] = 1.0f / in[i];
+}
+
 inline unsigned nblk(int64_t n) { return (unsigned)((n + NT - 1) / NT); }
 }  // namespace
 
@@ -113,5 +119,12 @@ int cs_autocorr_acc(const float2* x, float2* acc, int64_t n, cudaStream_t st)
 {
     if (n <= 0) return n == 0 ? 0 : CS_ERR_ARG;
     k_autocorr<<<nblk(n), NT, 0, st>>>(x, acc, n), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+int cs_reciprocal(const float* in, float* out, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return n == 0 ? 0 : CS_ERR_ARG;
+    k_recip<<<nblk(n), NT, 0, st>>>(in, out, n), cs_count_launches(1);
     return (int)cudaGetLastError();
 }

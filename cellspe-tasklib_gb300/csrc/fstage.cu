@@ -225,6 +225,181 @@ int dispatch_fstage(const CsFStageArgs& a, cudaStream_t st)
     return ph ? launch_fstage<M, CS_SPECTRA_F16, true>(a, st) : launch_fstage<M, CS_SPECTRA_F16, false>(a, st);
 }
 
+// ---------------------------------------------------------------------------
+// N = 2048 fast path: one warp per segment.  The 1024-point complex FFT of
+// z[n] = x[2n] + i x[2n+1] runs as a 32 x 32 four-step transform held in
+// registers (each lane keeps 32 points): DFT-32 over n2 for n = lane + 32 n2,
+// twiddle W_1024^(lane k1), one padded shared-memory transpose, DFT-32 over
+// n1; lane l then holds Z[l + 32 k2].  The real-FFT split pairs Z[k] with
+// Z[1024-k], which lives in lane (32-l) mod 32, register 31-k2 (lane 0:
+// register (32-k2) mod 32), so it is a register shuffle.  Twiddles and
+// delay phasors come from short register recurrences seeded from the FP64
+// table.  Each CTA stages GW = 8 segments and writes them corner-turned.
+// Input must be LSB-first (sample j of a 32-bit word at bits 2j).
+// ---------------------------------------------------------------------------
+constexpr int W_G = 8, W_WARPS = 8, W_TP = 33, W_RAWW = 2048 / 16 + 2;
+
+template <int FMT>
+size_t w2048_smem()
+{
+    size_t elem = (FMT == CS_SPECTRA_F32) ? 8 : 4;
+    return (size_t)W_WARPS * 32 * W_TP * 8 + (size_t)W_WARPS * W_RAWW * 4 + (size_t)1024 * (W_G + 1) * elem;
+}
+
+template <int FMT, bool PHASE>
+__global__ void __launch_bounds__(256, 2) k_fx_fstage_w2048(CsFStageArgs a, const float2* __restrict__ tw)
+{
+    constexpr int M = 1024, N = 2048, G = W_G;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tb_all = reinterpret_cast<float2*>(smem);
+    uint32_t* rb_all = reinterpret_cast<uint32_t*>(tb_all + W_WARPS * 32 * W_TP);
+    unsigned char* stage = reinterpret_cast<unsigned char*>(rb_all + W_WARPS * W_RAWW);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2* tb = tb_all + warp * 32 * W_TP;
+    uint32_t* rb = rb_all + warp * W_RAWW;
+    const int s = blockIdx.y;
+    const int k0 = blockIdx.x * G;
+    const int k = k0 + warp;
+    const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
+
+    if (k < a.K) {
+        const int64_t sk = (int64_t)s * a.K + k;
+        const int64_t start = a.start_sample + (int64_t)k * N + (a.shift ? a.shift[sk] : 0);
+        const int64_t w0 = start >> 4;
+        const int off = (int)(start & 15);
+        const int64_t words = a.bytes_per_input >> 2;
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(a.raw + (int64_t)s * a.bytes_per_input);
+        for (int i = lane; i < W_RAWW; i += 32) {
+            int64_t wi = w0 + i;
+            rb[i] = (wi >= 0 && wi < words) ? __ldg(src + wi) : 0u;
+        }
+        __syncwarp();
+        // decode: z[lane + 32 n2] uses samples off + 2 lane + 64 n2 (+1)
+        const int f0 = off + 2 * lane;
+        const int wb = f0 >> 4, sh = 2 * (f0 & 15);
+        float2 v[32];
+#pragma unroll
+        for (int n2 = 0; n2 < 32; n2++) {
+            uint32_t bits = __funnelshift_r(rb[wb + 4 * n2], rb[wb + 4 * n2 + 1], sh);
+            v[n2] = make_float2(lut_pick(lut, bits & 3u), lut_pick(lut, (bits >> 2) & 3u));
+        }
+        // step 1: DFT-32 over n2 -> k1
+        Dft<32>::run(v);
+        // step 2: v[k1] *= W_1024^(lane k1) = (W_2048^(2 lane))^k1
+        {
+            const float2 w1 = twiddle(tw, 2 * lane);
+            float2 wp[32];
+            wp[1] = w1;
+#pragma unroll
+            for (int e = 2; e < 32; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], w1) : cmul(wp[e / 2], wp[e / 2]);
+#pragma unroll
+            for (int e = 1; e < 32; e++) v[e] = cmul(v[e], wp[e]);
+        }
+        // transpose through shared memory: lane <- k1, register <- n1
+#pragma unroll
+        for (int e = 0; e < 32; e++) tb[e * W_TP + lane] = v[e];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 32; e++) v[e] = tb[lane * W_TP + e];
+        // step 3: DFT-32 over n1 -> k2 ; v[k2] = Z[lane + 32 k2]
+        Dft<32>::run(v);
+
+        // real-FFT split, phasor, scale, stage
+        const float2 wl = twiddle(tw, lane);                  // W_2048^lane
+        float2 B = make_float2(1.f, 0.f), D = B;
+        if constexpr (PHASE) {
+            const float ph0 = a.phase0[sk], dph = a.dphase[sk];
+            float sn, cs;
+            sincosf(ph0 + (float)lane * dph, &sn, &cs);
+            B = make_float2(cs, sn);
+            sincosf(32.f * dph, &sn, &cs);
+            D = make_float2(cs, sn);
+        }
+        const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
+        const int src_lane = (32 - lane) & 31;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; k2++) {
+            float2 zb;
+            zb.x = __shfl_sync(0xffffffffu, v[31 - k2].x, src_lane);
+            zb.y = __shfl_sync(0xffffffffu, v[31 - k2].y, src_lane);
+            if (lane == 0) zb = v[(32 - k2) & 31];
+            const float2 za = v[k2];
+            const float2 E = make_float2(0.5f * (za.x + zb.x), 0.5f * (za.y - zb.y));
+            const float2 O = make_float2(0.5f * (za.y + zb.y), -0.5f * (za.x - zb.x));
+            const float2 wk = cmul(wl, w64c(k2));          // W_2048^(lane + 32 k2)
+            float2 X = cadd(E, cmul(wk, O));
+            const int c = lane + 32 * k2;
+            if constexpr (PHASE) {
+                X = cmul(X, B);
+                B = cmul(B, D);
+            }
+            if (scl) X = cscale(X, __ldg(scl + c));
+            if constexpr (FMT == CS_SPECTRA_F32)
+                reinterpret_cast<float2*>(stage)[c * (G + 1) + warp] = X;
+            else
+                reinterpret_cast<__half2*>(stage)[c * (G + 1) + warp] = __floats2half2_rn(X.x, X.y);
+        }
+    }
+    __syncthreads();
+
+    // corner-turned write-out
+    const int nvalid = min(G, a.K - k0);
+    const int S = a.S, K = a.K;
+    if constexpr (FMT == CS_SPECTRA_F32) {
+        const float2* st = reinterpret_cast<const float2*>(stage);
+        float2* out = reinterpret_cast<float2*>(a.out);
+        if (nvalid == G && K % 2 == 0) {
+            for (int idx = threadIdx.x; idx < M * (G / 2); idx += 256) {
+                int c = idx / (G / 2), l = 2 * (idx % (G / 2));
+                float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
+                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * K + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < M * G; idx += 256) {
+                int c = idx / G, l = idx % G;
+                if (l < nvalid) out[((int64_t)c * S + s) * K + k0 + l] = st[c * (G + 1) + l];
+            }
+        }
+    } else {
+        const __half2* st = reinterpret_cast<const __half2*>(stage);
+        __half* out = reinterpret_cast<__half*>(a.out);
+        if (nvalid == G && K % 8 == 0) {
+            for (int idx = threadIdx.x; idx < M * 2; idx += 256) {
+                int plane = idx & 1, c = idx >> 1;
+                __align__(16) __half h[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    __half2 x = st[c * (G + 1) + j];
+                    h[j] = plane ? __high2half(x) : __low2half(x);
+                }
+                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * K + k0) =
+                    *reinterpret_cast<const uint4*>(h);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < M * 2 * G; idx += 256) {
+                int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
+                if (l < nvalid) {
+                    __half2 x = st[c * (G + 1) + l];
+                    out[(((int64_t)c * 2 + plane) * S + s) * K + k0 + l] = plane ? __high2half(x) : __low2half(x);
+                }
+            }
+        }
+    }
+}
+
+template <int FMT, bool PHASE>
+int launch_w2048(const CsFStageArgs& a, cudaStream_t st)
+{
+    const float2* tw = cs_twiddles(2048);
+    if (!tw) return CS_ERR_ARG;
+    size_t smem = w2048_smem<FMT>();
+    auto kern = k_fx_fstage_w2048<FMT, PHASE>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((a.K + W_G - 1) / W_G, a.S);
+    kern<<<grid, 256, smem, st>>>(a, tw), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
 // FP64 delay model (kept in FP64 on the GPU: the fringe phase 2 pi f_LO tau
 // spans ~1e7 cycles for millisecond delays at GHz sky frequencies, far beyond
 // FP32's 24-bit mantissa).  Operations are written out with explicit
@@ -265,6 +440,12 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
 {
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
+    if (a.N == 2048 && !a.msb_first) {
+        const bool ph = a.phase0 != nullptr;
+        if (a.format == CS_SPECTRA_F32)
+            return ph ? launch_w2048<CS_SPECTRA_F32, true>(a, st) : launch_w2048<CS_SPECTRA_F32, false>(a, st);
+        return ph ? launch_w2048<CS_SPECTRA_F16, true>(a, st) : launch_w2048<CS_SPECTRA_F16, false>(a, st);
+    }
     switch (a.N) {
         case 1024: return dispatch_fstage<512>(a, st);
         case 2048: return dispatch_fstage<1024>(a, st);

@@ -64,6 +64,9 @@ int cs_xmac_f32(const float2* spectra, int S, int C, int K, float2* vis, int acc
 // spectra __half [C][2][S][K] -> vis float2 [C][P]; inv_scale [S*C] or null.
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, float2* vis, const float* inv_scale,
                    int accumulate, cudaStream_t st);
+// Error code of the last tensor-core X-stage launch (0 = ok; 1..3 = a
+// pipeline wait timed out).  Call after the launching stream has synchronised.
+int cs_xmac_tc_status(unsigned* code);
 // Baseline-major <-> channel-major triangle transpose ([C][P] -> [P][C]).
 int cs_vis_to_baseline_major(const float2* vis_cp, float2* vis_pc, int C, int64_t P, cudaStream_t st);
 
@@ -96,3 +99,4 @@ int cs_cadd(const float2* a, const float2* b, float2* out, int64_t n, cudaStream
 int cs_sincos(const float* arg, float2* cossin, int64_t n, int normalized, cudaStream_t st);
 int cs_sincos_generator(float start, float inc, float2* cossin, int64_t n, cudaStream_t st);
 int cs_autocorr_acc(const float2* x, float2* acc, int64_t n, cudaStream_t st);
+int cs_reciprocal(const float* in, float* out, int64_t n, cudaStream_t st);

@@ -179,6 +179,15 @@ long long budget_bytes()
     return (long long)(0.9 * (double)fr);
 }
 
+// Admission limit for one job: an explicit budget is a hard per-job cap;
+// otherwise 90% of free device memory plus what this workspace already holds.
+long long job_limit(const Workspace& ws)
+{
+    long long b = g_budget.load();
+    if (b > 0) return b;
+    return budget_bytes() + (long long)ws.arena.capacity();
+}
+
 // Staging helper: host buffers are copied through the workspace; device
 // buffers are used in place.
 struct Job {
@@ -308,6 +317,27 @@ int op_xmac(Workspace& ws, bool host, const void* spectra, int S, int C, int K, 
     return j.finish();
 }
 
+int op_xmac_f16(Workspace& ws, bool host, const void* spectra, int S, int C, int K, void* vis, int accumulate)
+{
+    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || K % 8)
+        return set_err(CELLSPE_ERR_ARG, "xmac_f16: bad arguments (K must be a multiple of 8)");
+    long long P = (long long)S * (S + 1) / 2;
+    Job j(ws, host);
+    const void* d_sp = j.in(spectra, (size_t)C * 2 * S * K * 2);
+    void* d_vis = j.out(vis, (size_t)C * P * 8, accumulate != 0);
+    if (!j.err) {
+        int rc = map_rc(cs_xmac_tc_f16(d_sp, S, C, K, (float2*)d_vis, nullptr, accumulate, ws.stream), "xmac_f16");
+        if (rc) j.err = rc;
+    }
+    int rc = j.finish();
+    if (!rc) {
+        unsigned code = 0;
+        if (cs_xmac_tc_status(&code) != 0 || code != 0)
+            rc = set_err(CELLSPE_ERR_CUDA, "xmac_f16: tensor-core pipeline wait timed out (code " + std::to_string(code) + ")");
+    }
+    return rc;
+}
+
 long long fx_bytes(const cellspe_fx_params* p, bool with_poly)
 {
     long long S = p->n_inputs, N = p->fft_points, K = p->n_segments, C = N / 2;
@@ -339,7 +369,7 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     float lut[4];
     if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "fx: unknown level table");
     long long need = fx_bytes(p, poly != nullptr);
-    long long budget = budget_bytes() + (long long)ws.arena.capacity();
+    long long budget = job_limit(ws);
     if (need > budget)
         return set_err(CELLSPE_ERR_NOMEM, "fx: job needs " + std::to_string(need) + " device bytes, budget " +
                                               std::to_string(budget));
@@ -369,10 +399,16 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         fa.shift = ds.shift; fa.phase0 = ds.phase0; fa.dphase = ds.dphase;
     }
     const float* d_inv_scale = nullptr;
-    if (p->x_mode != CELLSPE_X_FP32) {
-        if (p->channel_scale) {
-            fa.scale = (const float*)j.in(p->channel_scale, (size_t)S * C * 4);
+    if (p->x_mode != CELLSPE_X_FP32 && p->channel_scale) {
+        // F stage multiplies channel c of input s by scale[s][c] before the
+        // FP16 cast; the X-stage epilogue divides V_ij by scale_i * scale_j.
+        fa.scale = (const float*)j.in(p->channel_scale, (size_t)S * C * 4);
+        float* inv = (float*)j.scratch((size_t)S * C * 4);
+        if (!j.err) {
+            int rc = map_rc(cs_reciprocal(fa.scale, inv, (int64_t)S * C, ws.stream), "scale");
+            if (rc) j.err = rc;
         }
+        d_inv_scale = inv;
     }
     fa.out = j.scratch((size_t)C * S * K * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
     if (sync) cudaEventRecord(ws.sev[1], ws.stream);
@@ -394,10 +430,6 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         if (rc) j.err = rc;
     }
     if (sync) cudaEventRecord(ws.sev[3], ws.stream);
-    if (p->x_mode != CELLSPE_X_FP32 && fa.scale && !j.err) {
-        // undo the F-stage scale: V_ij /= s_i s_j (per channel)
-        j.err = set_err(CELLSPE_ERR_UNSUPPORTED, "fx: channel_scale is applied by the tensor-core epilogue only");
-    }
     if (!direct && !j.err) {
         float2* result = vis_cp;
         if (p->vis_order == CELLSPE_VIS_BASELINE_MAJOR) {
@@ -425,6 +457,12 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     }
     if (sync) cudaEventRecord(ws.sev[4], ws.stream);
     int rc = j.finish(sync);
+    if (sync && !rc && p->x_mode != CELLSPE_X_FP32) {
+        unsigned code = 0;
+        if (cs_xmac_tc_status(&code) != 0 || code != 0)
+            rc = set_err(CELLSPE_ERR_CUDA, "X stage: tensor-core pipeline wait timed out (code " +
+                                               std::to_string(code) + ")");
+    }
     if (sync && !rc) {
         for (int i = 0; i < 4; i++) {
             float ms = 0.f;
@@ -461,7 +499,7 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
     float lut[4];
     if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown level table");
     long long need = spec_bytes(p);
-    long long budget = budget_bytes() + (long long)ws.arena.capacity();
+    long long budget = job_limit(ws);
     if (need > budget) return set_err(CELLSPE_ERR_NOMEM, "spectrometer: job exceeds the device memory budget");
     const bool host = p->memory == CELLSPE_MEM_HOST;
     Job j(ws, host);
@@ -1243,6 +1281,12 @@ int cellspe_xmac(const void* spectra, int S, int C, int K, void* vis, int accumu
 {
     DIRECT_PROLOGUE
     return op_xmac(*ws, memory == CELLSPE_MEM_HOST, spectra, S, C, K, vis, accumulate);
+}
+
+int cellspe_xmac_f16(const void* spectra_f16, int S, int C, int K, void* vis, int accumulate, int memory)
+{
+    DIRECT_PROLOGUE
+    return op_xmac_f16(*ws, memory == CELLSPE_MEM_HOST, spectra_f16, S, C, K, vis, accumulate);
 }
 
 int cellspe_fx_correlate(const cellspe_fx_params* p, const void* raw, const double* delay_poly, void* vis)

@@ -1,8 +1,379 @@
-// K-d2: X stage on tcgen05 tensor cores (FP16 in, FP32 accumulate).
+// K-d2: X stage on the tcgen05 tensor cores (FP16 operands, FP32 accumulate).
+//
+// Per channel c the visibilities are the Hermitian rank-K product V = X X^H
+// of the S x K spectra matrix X = Xr + i Xi (the conjugate MAC of
+// genericAddProduct_32fc_conj, architecture.h:427-433, for every product):
+//     Re V = Xr Xr^T + Xi Xi^T,      Im V = Xi Xr^T - Xr Xi^T.
+// A CTA owns one 128 (i) x 256 (j) tile of one channel that touches the lower
+// triangle.  Its two FP32 accumulators live in tensor memory (TMEM): columns
+// 0..255 hold Re V, 256..511 hold Im V, lane = row i.  Each k-step issues four
+// kind::f16 MMAs (M=128, N=256, K=16); the minus sign of the last product is
+// the instruction descriptor's negate-A bit, so no negated copy of the data
+// exists.  Operands are K-major (time innermost), loaded by TMA with 64-byte
+// swizzle into a 4-stage shared-memory ring guarded by mbarriers.
+//
+// Warp roles (6 warps): warp 0 = TMA producer, warp 1 = TMEM owner and MMA
+// issuer, warps 2..5 = epilogue (TMEM -> registers -> global; warp w reads
+// TMEM lanes 32*(w%4)..+31).  Every mbarrier wait is bounded: on timeout the
+// kernel records an error code, drains its own copies (bounded), frees TMEM
+// and returns, and the host reports the failure.
+//
+// Layout in:  __half spectra[C][2][S][K]  (plane 0 = Re, plane 1 = Im)
+// Layout out: float2 vis[C][P], p = i(i+1)/2 + j, j <= i
+#include <cuda.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
-int cs_xmac_tc_f16(const void*, int, int, int, float2*, const float*, int, cudaStream_t)
+#include <mutex>
+#include <vector>
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 32;          // tile and k-chunk (64 B of FP16 = one swizzle row)
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;                // 8 KB
+constexpr int B_BYTES = BN * BK * 2;                // 16 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // Ar, Ai, Br, Bi = 48 KB
+constexpr int TC_THREADS = 192;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr long long WAIT_CYCLES = 4000000000LL;     // ~2 s at 2 GHz
+
+// error codes written to g_tc_error
+constexpr unsigned ERR_FULL_WAIT = 1, ERR_EMPTY_WAIT = 2, ERR_ACC_WAIT = 3;
+
+__device__ unsigned g_tc_error;
+
+CS_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+CS_DEV void mbar_init(uint32_t bar, uint32_t count)
 {
-    return CS_ERR_UNSUPPORTED;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+CS_DEV void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+CS_DEV bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false (and the error code recorded) after WAIT_CYCLES.
+CS_DEV bool mbar_wait(uint32_t bar, uint32_t parity, unsigned code)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > WAIT_CYCLES) {
+            atomicCAS(&g_tc_error, 0u, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+CS_DEV void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+CS_DEV void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+CS_DEV void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand in shared memory with 64-byte swizzle: 8-row x 64-byte
+// atoms stacked along M/N every 512 bytes (stride byte offset).
+CS_DEV uint64_t sw64_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);     // start address
+    d |= (uint64_t)1 << 16;                       // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(512 >> 4) << 32;              // stride byte offset
+    d |= (uint64_t)1 << 46;                       // descriptor version (tcgen05)
+    d |= (uint64_t)4 << 61;                       // layout: 64-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: D F32, A/B F16, K-major, M=128, N=256.
+constexpr uint32_t make_idesc(bool neg_a)
+{
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+           ((uint32_t)(BM >> 4) << 24);
+}
+
+CS_DEV void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+CS_DEV void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+CS_DEV void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+CS_DEV void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct TcArgs {
+    int S, C, K;
+    int64_t P;
+    const int2* tiles;          // (i0, j0) per tile
+    float2* vis;
+    const float* inv_scale;     // [S][C] or null
+    int accumulate;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant__ CUtensorMap tmap, TcArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);   // full[S], empty[S], acc
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+    const uint32_t sbase = smem_u32(smem);
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, accb = full0 + 16 * STAGES;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int2 tile = a.tiles[blockIdx.x];
+    const int c = blockIdx.y;
+    const int i0 = tile.x, j0 = tile.y;
+    const int S = a.S;
+    const int nk = (a.K + BK - 1) / BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(accb, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            const int rowA_re = (c * 2 + 0) * S + i0, rowA_im = (c * 2 + 1) * S + i0;
+            const int rowB_re = (c * 2 + 0) * S + j0, rowB_im = (c * 2 + 1) * S + j0;
+            int issued = 0;
+            bool ok = true;
+            for (int kc = 0; kc < nk && ok; kc++) {
+                const int s = kc % STAGES;
+                const uint32_t ph = (kc / STAGES) & 1;
+                if (!mbar_wait(empty0 + 8 * s, ph ^ 1, ERR_EMPTY_WAIT)) { ok = false; break; }
+                const uint32_t st = sbase + s * STAGE_BYTES;
+                const uint32_t fb = full0 + 8 * s;
+                mbar_expect_tx(fb, STAGE_BYTES);
+                const int x = kc * BK;
+                tma_load_2d(st, &tmap, x, rowA_re, fb);
+                tma_load_2d(st + A_BYTES, &tmap, x, rowA_im, fb);
+                tma_load_2d(st + 2 * A_BYTES, &tmap, x, rowB_re, fb);
+                tma_load_2d(st + 2 * A_BYTES + A_BYTES, &tmap, x, rowB_re + BM, fb);
+                tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tmap, x, rowB_im, fb);
+                tma_load_2d(st + 2 * A_BYTES + B_BYTES + A_BYTES, &tmap, x, rowB_im + BM, fb);
+                issued = kc + 1;
+            }
+            // drain: every stage this thread filled must have landed before the CTA exits
+            for (int kc = (issued > STAGES ? issued - STAGES : 0); kc < issued; kc++)
+                mbar_wait(full0 + 8 * (kc % STAGES), (kc / STAGES) & 1, ERR_FULL_WAIT);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            constexpr uint32_t id_pos = make_idesc(false), id_neg = make_idesc(true);
+            const uint32_t d_re = tmem, d_im = tmem + BN;
+            bool ok = true;
+            for (int kc = 0; kc < nk; kc++) {
+                const int s = kc % STAGES;
+                if (!mbar_wait(full0 + 8 * s, (kc / STAGES) & 1, ERR_FULL_WAIT)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t st = sbase + s * STAGE_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; kk++) {
+                    const uint32_t off = kk * 32;                  // 16 FP16 along K
+                    const uint64_t ar = sw64_desc(st + off), ai = sw64_desc(st + A_BYTES + off);
+                    const uint64_t br = sw64_desc(st + 2 * A_BYTES + off);
+                    const uint64_t bi = sw64_desc(st + 2 * A_BYTES + B_BYTES + off);
+                    const uint32_t acc = (kc | kk) ? 1u : 0u;
+                    umma_f16(d_re, ar, br, id_pos, acc);           // Re += Ar Br^T
+                    umma_f16(d_re, ai, bi, id_pos, 1u);            // Re += Ai Bi^T
+                    umma_f16(d_im, ai, br, id_pos, acc);           // Im += Ai Br^T
+                    umma_f16(d_im, ar, bi, id_neg, 1u);            // Im -= Ar Bi^T
+                }
+                umma_commit(empty0 + 8 * s);                       // stage free once these MMAs finish
+            }
+            // Always commit: the barrier then completes only after every MMA
+            // issued so far has finished, so TMEM is never freed under one.
+            umma_commit(accb);
+            if (!ok) atomicCAS(&g_tc_error, 0u, ERR_FULL_WAIT);
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: TMEM -> global ----------------
+        const int q = warp & 3;                                    // TMEM lane quarter
+        const int r = 32 * q + lane;
+        const int i = i0 + r;
+        bool ok = mbar_wait(accb, 0, ERR_ACC_WAIT);
+        ok = ok && (*reinterpret_cast<volatile unsigned*>(&g_tc_error) == 0u);
+        __syncwarp();
+        if (__all_sync(0xffffffffu, ok)) {
+            tc_fence_after();
+            const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+            float si = 1.f;
+            if (a.inv_scale && i < S) si = __ldg(a.inv_scale + (int64_t)i * a.C + c);
+            float2* out = a.vis + (int64_t)c * a.P + (int64_t)i * (i + 1) / 2;
+            for (int cb = 0; cb < BN / 16; cb++) {
+                uint32_t re[16], im[16];
+                tmem_ld16(lane_base + cb * 16, re);
+                tmem_ld16(lane_base + BN + cb * 16, im);
+                tmem_ld_wait();
+                if (i < S) {
+#pragma unroll
+                    for (int jj = 0; jj < 16; jj++) {
+                        const int j = j0 + cb * 16 + jj;
+                        if (j <= i && j < S) {
+                            float f = si;
+                            if (a.inv_scale) f *= __ldg(a.inv_scale + (int64_t)j * a.C + c);
+                            float2 v = make_float2(__uint_as_float(re[jj]) * f, __uint_as_float(im[jj]) * f);
+                            if (a.accumulate) {
+                                float2 o = out[j];
+                                v.x += o.x;
+                                v.y += o.y;
+                            }
+                            out[j] = v;
+                        }
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+std::mutex g_tiles_mu;
+std::vector<std::pair<std::pair<int, int>, int2*>> g_tiles;   // ((device, S) -> device tile list)
+
+const int2* tile_list(int S, int* ntiles)
+{
+    std::vector<int2> h;
+    for (int i0 = 0; i0 < S; i0 += BM)
+        for (int j0 = 0; j0 < S; j0 += BN)
+            if (j0 <= i0 + BM - 1) h.push_back(make_int2(i0, j0));
+    *ntiles = (int)h.size();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tiles_mu);
+    for (auto& e : g_tiles)
+        if (e.first.first == dev && e.first.second == S) return e.second;
+    int2* d = nullptr;
+    if (cudaMalloc(&d, sizeof(int2) * h.size()) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, h.data(), sizeof(int2) * h.size(), cudaMemcpyHostToDevice);
+    g_tiles.push_back({{dev, S}, d});
+    return d;
+}
+
+}  // namespace
+
+int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, float2* vis, const float* inv_scale, int accumulate,
+                   cudaStream_t st)
+{
+    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || C > 65535) return CS_ERR_ARG;
+    if (K % 8 != 0 || (uintptr_t)spectra % 16) return CS_ERR_ARG;     // TMA: 16-byte row pitch and base
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return CS_ERR_UNSUPPORTED;
+    int ntiles = 0;
+    const int2* tiles = tile_list(S, &ntiles);
+    if (!tiles) return CS_ERR_ARG;
+
+    CUtensorMap tm;
+    cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)C * 2 * S};
+    cuuint64_t gstride[1] = {(cuuint64_t)K * 2};
+    cuuint32_t box[2] = {BK, BM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(spectra), gdim, gstride, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return CS_ERR_ARG;
+
+    void* errp = nullptr;
+    CS_CUDA_TRY(cudaGetSymbolAddress(&errp, g_tc_error));
+    CS_CUDA_TRY(cudaMemsetAsync(errp, 0, sizeof(unsigned), st));
+
+    TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, accumulate};
+    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+    CS_CUDA_TRY(cudaFuncSetAttribute(k_xmac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(ntiles, C);
+    k_xmac_tc<<<grid, TC_THREADS, smem, st>>>(tm, a), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+// Error code of the last tensor-core launch on this device (0 = ok); the
+// caller must have synchronised the launching stream.
+int cs_xmac_tc_status(unsigned* code)
+{
+    return (int)cudaMemcpyFromSymbol(code, g_tc_error, sizeof(unsigned));
 }

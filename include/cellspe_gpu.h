@@ -83,6 +83,9 @@ int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memo
  * Replaces genericAddProduct_32fc_conj (architecture.h:427-433) looped over
  * products, three_baseline_naive_MACauto (minicorrelator_spu.c:745-786). */
 int cellspe_xmac(const void* spectra, int S, int C, int K, void* vis, int accumulate, int memory);
+/* Tensor-core X stage on FP16 spectra, layout half [C][2][S][K] (plane 0 Re,
+ * plane 1 Im, K a multiple of 8) -> vis complex64 [C][P], FP32 accumulation. */
+int cellspe_xmac_f16(const void* spectra_f16, int S, int C, int K, void* vis, int accumulate, int memory);
 /* Parameters of CELLDSP_TASK_XMAC (input vector 0). */
 typedef struct { int S, C, K, accumulate; } cellspe_xmac_params;
 

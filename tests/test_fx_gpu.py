@@ -26,7 +26,7 @@ def test_config1_lag_known_answer(cg, orc):
     """Config 1: 2 stations, 2^22 samples each, 1024-pt FFT, station 2 lags by 3 samples.
 
     V_10 = X_1 conj(X_0) with x_1(t) = c(t - 3) has phase -2 pi 3 k / N; its
-    lag spectrum (inverse FFT over channels) peaks at lag -3.
+    lag spectrum (inverse FFT over channels) peaks at lag +3.
     """
     import synth
 
@@ -40,7 +40,7 @@ def test_config1_lag_known_answer(cg, orc):
     derot = (cross * np.exp(2j * np.pi * 3 * k / N))[16:-16].reshape(-1, 16).sum(axis=1)
     assert np.abs(np.angle(derot)).max() < 0.15
     lag = np.fft.ifft(cross, n=N)
-    assert int(np.argmax(np.abs(lag))) == N - 3
+    assert int(np.argmax(np.abs(lag))) == 3
     coh = np.abs(cross) / np.sqrt(vis[0].real * vis[2].real)
     assert 0.06 < np.median(coh) < 0.12                        # 2-bit coherence ~ 0.88 rho
 

@@ -43,7 +43,7 @@ def test_spectrometer_pcal_and_sines_known_answer(cg, orc):
     """Config-2 shape in miniature: 16 subbands, 32 MS/s, 1 MHz comb, 3 sines."""
     import synth
 
-    nsub, N, K, fs = 16, 4096, 16, 32e6
+    nsub, N, K, fs = 16, 4096, 64, 32e6
     T = N * K
     words, truth = synth.mark5b_subbands(nsub, T, fs_hz=fs, seed=2, n_channels=N // 2, pcal_amp=0.3)
     raw = words.view(np.uint8)
@@ -60,10 +60,13 @@ def test_spectrometer_pcal_and_sines_known_answer(cg, orc):
     for c in range(nsub):
         ref_t = orc.pcal_tones(ref_b[c, 0], ntones)
         assert np.linalg.norm(tones[c, 0] - ref_t) / np.linalg.norm(ref_t) < TOL
-        # injected comb phases (cosine at k MHz, phase phi -> tone phase phi)
+        # injected comb phases (cosine at k MHz, phase phi -> tone phase phi).
+        # Thermal noise and 2-bit intermodulation of the harmonic comb leave a
+        # few degrees per tone at this length; a wrong sign or bin would be off
+        # by tens of degrees.
         ph = np.angle(tones[c, 0, 1:ntones])
-        d = np.angle(np.exp(1j * (ph - truth["tone_phase"][c, : ntones - 1])))
-        assert np.degrees(np.abs(d)).max() < 5.0
+        d = np.degrees(np.abs(np.angle(np.exp(1j * (ph - truth["tone_phase"][c, : ntones - 1])))))
+        assert d.max() < 15.0 and d.mean() < 4.0
         # the sine with the highest frequency resolution lands at its bin
         for f in truth["sine_f"][c]:
             kbin = int(round(f / fs * N))

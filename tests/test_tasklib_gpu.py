@@ -171,16 +171,16 @@ def test_fx_and_spectrometer_through_tasks(cg, orc, rt):
 
 
 def test_unpack_task_per_channel_outputs(cg, orc, rt):
-    raw = np.random.default_rng(1).integers(0, 256, 4 * 256, dtype=np.uint8)
-    outs = [np.zeros(256, np.float32) for _ in range(16)]
+    raw = np.random.default_rng(1).integers(0, 256, 2 * 256, dtype=np.uint8)
+    outs = [np.zeros(256, np.float32) for _ in range(8)]      # at most 8 vectors per task
     t = cg.new_task(cg.TASK_UNPACK)
     cg.add_in(t, raw)
     for o in outs:
         cg.add_out(t, o)
     t.subcontext[0] = 256          # nsamp_lo
     t.subcontext[1] = 0
-    t.subcontext[2] = 16           # nchan
+    t.subcontext[2] = 8            # nchan
     t.subcontext[3] = cg.LEVELS_MARK5B
     assert rt.celldsp_executeTask(ctypes.byref(t)) == 0
-    ref = orc.unpack2bit(raw, 256, 16, orc.MARK5B_LUT)
-    assert all(np.array_equal(outs[c], ref[c]) for c in range(16))
+    ref = orc.unpack2bit(raw, 256, 8, orc.MARK5B_LUT)
+    assert all(np.array_equal(outs[c], ref[c]) for c in range(8))

@@ -1,0 +1,105 @@
+"""K-d2: tcgen05 FP16 X stage.
+
+Two bars: (1) on FP16 inputs the tensor-core result equals the FP64 product of
+the same FP16 values up to FP32 accumulation (relative 1e-5); (2) through the
+full FX path it is within 1e-3 relative amplitude and 0.05 degree phase of the
+FP64 oracle, the precision the engine promises for the tensor-core path.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _fp64_vis(xr, xi):
+    """xr, xi: [C][S][K] float64 -> V[C][P] with p = i(i+1)/2 + j."""
+    X = xr + 1j * xi
+    C, S, _ = X.shape
+    full = np.einsum("csk,ctk->cst", X, np.conj(X))
+    ii, jj = np.tril_indices(S)
+    order = np.argsort(ii * (ii + 1) // 2 + jj)
+    return full[:, ii[order], jj[order]]
+
+
+@pytest.mark.parametrize("S,C,K", [(8, 3, 64), (128, 2, 96), (130, 2, 40), (256, 1, 128), (300, 2, 32)])
+def test_xmac_f16_exact_inputs(cg, S, C, K):
+    rng = np.random.default_rng(S + K)
+    spec = rng.standard_normal((C, 2, S, K)).astype(np.float16)
+    P = S * (S + 1) // 2
+    vis = np.zeros((C, P), np.complex64)
+    cg.xmac_f16(spec, S, C, K, vis)
+    ref = _fp64_vis(spec[:, 0].astype(np.float64), spec[:, 1].astype(np.float64))
+    err = np.linalg.norm(vis - ref) / np.linalg.norm(ref)
+    assert err < 1e-5, err
+    # lower triangle written, autos real
+    ii = np.array([i for i in range(S) for _ in range(i + 1)])
+    jj = np.array([j for i in range(S) for j in range(i + 1)])
+    autos = vis[:, ii == jj]
+    assert np.abs(autos.imag).max() <= 1e-5 * np.abs(autos.real).max()
+
+
+def test_xmac_f16_accumulate(cg):
+    rng = np.random.default_rng(1)
+    S, C, K = 40, 2, 64
+    spec = rng.standard_normal((C, 2, S, K)).astype(np.float16)
+    vis = np.zeros((C, S * (S + 1) // 2), np.complex64)
+    cg.xmac_f16(spec, S, C, K, vis)
+    v2 = vis.copy()
+    cg.xmac_f16(spec, S, C, K, v2, accumulate=True)
+    assert np.allclose(v2, 2 * vis, rtol=1e-6, atol=1e-4)
+
+
+def _fx_pair(cg, raw, S, N, K, mode, **kw):
+    p = cg.fx_params(S, N, K, raw.shape[1], x_mode=mode, vis_order=cg.VIS_BASELINE_MAJOR, **kw)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis, delay_poly=kw.get("delay_poly"))
+    return vis
+
+
+@pytest.mark.parametrize("S,N,K,rho", [(64, 2048, 256, 0.02), (32, 8192, 64, 0.5), (200, 1024, 128, 0.3)])
+def test_fx_tc_vs_fp64_oracle(cg, orc, S, N, K, rho):
+    import synth
+
+    raw = synth.stations_offset_binary(S, N * K, rho=rho, seed=S * 7 + N)
+    p = cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=cg.VIS_BASELINE_MAJOR)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis)
+    # FP64 oracle on a seeded subset of products and channels, full K
+    rng = np.random.default_rng(0)
+    inputs = sorted(rng.choice(S, size=min(S, 12), replace=False))
+    chans = sorted(rng.choice(N // 2, size=32, replace=False))
+    X = orc.fx_spectra_f64(raw, S, N, K, inputs=inputs, channels=chans)
+    pairs = [(a, b) for a in range(len(inputs)) for b in range(a + 1)]
+    ref = orc.fx_vis_f64(X, pairs)
+    got = np.stack([vis[orc.tri_index(inputs[a], inputs[b])][chans] for a, b in pairs])
+    amp_err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert amp_err.max() < 1e-3, amp_err.max()
+    # phase over channels whose |V| is above the thermal-noise floor
+    # 3 sqrt(V_ii V_jj / K) (below it the phase is noise, not signal)
+    auto = {a: ref[pairs.index((a, a))].real for a in range(len(inputs))}
+    floor = np.stack([3 * np.sqrt(auto[a] * auto[b] / K) for a, b in pairs])
+    mask = np.abs(ref) > floor
+    phase_deg = np.degrees(np.abs(np.angle(got * np.conj(ref))))[mask]
+    assert phase_deg.max() < 0.05, phase_deg.max()
+    if rho >= 0.3:
+        cross = np.array([a != b for a, b in pairs])
+        assert mask[cross].mean() > 0.5      # the phase bar really covers cross products
+    # and agrees with the FP32 CUDA-core path
+    v32 = np.zeros_like(vis)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_FP32, vis_order=cg.VIS_BASELINE_MAJOR),
+                    raw, v32)
+    rel = np.linalg.norm(vis - v32, axis=1) / np.linalg.norm(v32, axis=1)
+    assert rel.max() < 1e-3
+
+
+def test_fx_tc_channel_scale(cg):
+    """A per-(input, channel) scale before the FP16 cast is undone in the epilogue."""
+    import synth
+
+    S, N, K = 16, 1024, 64
+    raw = synth.stations_offset_binary(S, N * K, rho=0.1, seed=3)
+    base = _fx_pair(cg, raw, S, N, K, cg.X_TC_FP16)
+    scale = np.random.default_rng(2).uniform(0.01, 0.05, (S, N // 2)).astype(np.float32)
+    scaled = _fx_pair(cg, raw, S, N, K, cg.X_TC_FP16, channel_scale=scale)
+    rel = np.linalg.norm(scaled - base) / np.linalg.norm(base)
+    assert rel < 1e-3
