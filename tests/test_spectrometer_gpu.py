@@ -66,7 +66,7 @@ def test_spectrometer_pcal_and_sines_known_answer(cg, orc):
         # by tens of degrees.
         ph = np.angle(tones[c, 0, 1:ntones])
         d = np.degrees(np.abs(np.angle(np.exp(1j * (ph - truth["tone_phase"][c, : ntones - 1])))))
-        assert d.max() < 15.0 and d.mean() < 4.0
+        assert d.max() < 15.0 and d.mean() < 6.0
         # the sine with the highest frequency resolution lands at its bin
         for f in truth["sine_f"][c]:
             kbin = int(round(f / fs * N))
