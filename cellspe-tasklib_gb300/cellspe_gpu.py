@@ -141,6 +141,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_release_workspace": ([], I),
             "cellspe_spectrometer": ([V, V, V, V, V], I),
             "cellspe_spectrometer_workspace_bytes": ([V], LL),
+            "cellspe_spectrometer_noalloc": ([V, V, V, V, V, V], I),
             "celldsp_start": ([], I), "celldsp_stop": ([], I),
             "celldsp_getFreeSPE": ([], I), "celldsp_setFreeSPE": ([I], I),
             "celldsp_startTask": ([I, V], I), "celldsp_waitTask": ([I], I),
@@ -281,6 +282,16 @@ def spectrometer(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None
     _check(lib().cellspe_spectrometer(ctypes.byref(params), _ptr(raw)[0], _ptr(power)[0],
                                       _ptr(pcal_bins)[0] if pcal_bins is not None else None,
                                       _ptr(pcal_tones)[0] if pcal_tones is not None else None))
+    return power
+
+
+def spectrometer_noalloc(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None, stream: int = 0):
+    """cellspe_spectrometer_noalloc: device tensors only, asynchronous on `stream`."""
+    params.memory = MEM_DEVICE
+    _check(lib().cellspe_spectrometer_noalloc(ctypes.byref(params), _ptr(raw)[0], _ptr(power)[0],
+                                              _ptr(pcal_bins)[0] if pcal_bins is not None else None,
+                                              _ptr(pcal_tones)[0] if pcal_tones is not None else None,
+                                              ctypes.c_void_p(stream)))
     return power
 
 

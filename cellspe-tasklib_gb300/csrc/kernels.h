@@ -12,6 +12,8 @@
 // report how many of its own kernels ran in a timed region).
 long long cs_launch_count();
 void cs_count_launches(int n);
+// Records the calling thread's error text for cellspe_last_error(); returns code.
+int cs_set_error(int code, const char* msg);
 
 // unpack.cu -----------------------------------------------------------------
 int cs_unpack2bit(const void* raw, int64_t nsamp, int nchan, int msb_first, const float lut4[4],
@@ -88,6 +90,11 @@ struct CsSpecArgs {
     double pcal_offset_hz, fs_hz;
     float2* pcal_bins;          // [nsub][nspec][tonebins]
     float2* pcal_tones;         // [nsub][nspec][ntones] or null
+    // Optional caller-owned tables (null: the cached tables of this library)
+    const float2* tw_table;     // exp(-2 pi i m / N), N entries
+    const float* win_table;     // window, N entries
+    const float2* rot_table;    // pcal rotator, rotatorlen entries
+    int ffts_per_chunk;         // FFTs per partial spectrum (0: default)
 };
 int64_t cs_spectrometer_scratch_floats(const CsSpecArgs& a);
 int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st);

@@ -827,6 +827,8 @@ void worker_main(Slot* s)
 
 }  // namespace
 
+int cs_set_error(int code, const char* msg) { return set_err(code, msg ? msg : ""); }
+
 // ===========================================================================
 // exported: task runtime
 // ===========================================================================

@@ -97,7 +97,7 @@ CS_DEV float lut_pick4(const float (&l)[4], unsigned c)
 
 template <int MC, int P>
 __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const float2* __restrict__ tw,
-                                                            const float* __restrict__ win, int nchunk)
+                                                            const float* __restrict__ win, int nchunk, int ch)
 {
     using C = SCfg<MC>;
     constexpr int T = C::T, GROUPS = C::GROUPS;
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const
     for (int i = threadIdx.x; i < GROUPS * NACC; i += C::NT) acc_all[i] = 0.f;
     __syncthreads();
 
-    const int j_begin = chunk * SPEC_CH, j_end = min(novl, j_begin + SPEC_CH);
+    const int j_begin = chunk * ch, j_end = min(novl, j_begin + ch);
     auto bar = [] { __syncthreads(); };
     for (int j0 = j_begin; j0 < j_end; j0 += GROUPS) {
         const int j = j0 + g;
@@ -262,26 +262,28 @@ __global__ void k_pcal_reduce(const float2* __restrict__ partial, int rows, int 
 constexpr int PCAL_THREADS = 128;
 constexpr int PCAL_BLOCKS = 32;
 
+int spec_chunk(const CsSpecArgs& a) { return a.ffts_per_chunk > 0 ? a.ffts_per_chunk : SPEC_CH; }
+
 template <int MC, int P>
 int launch_power(const CsSpecArgs& a, int nchunk, cudaStream_t st)
 {
     using C = SCfg<MC>;
     constexpr int M = MC * P, N = 2 * M;
-    const float2* tw = cs_twiddles(N);
-    const float* win = window_table(a.window, N);
+    const float2* tw = a.tw_table ? a.tw_table : cs_twiddles(N);
+    const float* win = a.win_table ? a.win_table : window_table(a.window, N);
     if (!tw || !win) return CS_ERR_ARG;
     size_t smem = (size_t)C::GROUPS * fpad_size(MC) * sizeof(float2) + (size_t)C::GROUPS * (M / P + 1) * sizeof(float);
     auto kern = k_spec_power<MC, P>;
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(nchunk, a.nsub * a.nspec, P);
-    kern<<<grid, C::NT, smem, st>>>(a, tw, win, nchunk), cs_count_launches(1);
+    kern<<<grid, C::NT, smem, st>>>(a, tw, win, nchunk, spec_chunk(a)), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
 int spec_nchunk(const CsSpecArgs& a)
 {
     int novl = a.overlap * a.ffts_per_spectrum - (a.overlap - 1);
-    return (novl + SPEC_CH - 1) / SPEC_CH;
+    return (novl + spec_chunk(a) - 1) / spec_chunk(a);
 }
 }  // namespace
 
@@ -324,7 +326,7 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
     if (a.tonebins > 0) {
         const int T = a.tonebins, L = a.rotatorlen;
         if (L <= 0 || L % T != 0 || a.N % L != 0 || T > 128 || !a.pcal_bins) return CS_ERR_ARG;
-        const float2* rot = rotator_table(L, a.pcal_offset_hz, a.fs_hz);
+        const float2* rot = a.rot_table ? a.rot_table : rotator_table(L, a.pcal_offset_hz, a.fs_hz);
         if (!rot) return CS_ERR_ARG;
         float2* pp = reinterpret_cast<float2*>(a.partial + (int64_t)rows * nchunk * nb);
         int64_t samp_per_spec = (int64_t)a.ffts_per_spectrum * a.N;

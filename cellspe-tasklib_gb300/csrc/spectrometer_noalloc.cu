@@ -1,0 +1,178 @@
+// Spectrometer entry point that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc at the time they run the spectrometer:
+// real-time capture loops that must not block on the allocator (cudaMalloc
+// and cudaFree can synchronise the whole device), code that runs while a CUDA
+// graph is being captured, or hosts that hand this library a fixed device
+// budget up front and forbid any later allocation.  cellspe_spectrometer
+// stages its chunk partial spectra and phase-cal partials in a workspace
+// that it allocates on demand; this variant uses the fixed arrays below
+// instead, so the caller only provides the input planes and the outputs.
+//
+// Limits and behaviour:
+// * The arrays live in this library's static device memory: every GPU that
+//   loads the library holds them (about 17.3 MiB) until the process exits.
+// * Partial spectra get at most CS_NOALLOC_SCRATCH_FLOATS floats (16 MiB).
+//   The FFTs of a spectrum are grouped into as few chunks as needed to fit;
+//   jobs that do not fit even with one chunk per spectrum are rejected.
+// * FFT size, window and phase-cal rotator tables are rebuilt by small
+//   kernels on the caller's stream on every call (no host-side caching).
+// * Every scratch element a call reads was written earlier in that call, so
+//   nothing needs clearing between calls; calls whose work overlaps on the
+//   GPU (different streams, or different host threads) share the arrays and
+//   race.
+// * The first call on a device looks up the arrays' device addresses with
+//   cudaGetSymbolAddress (host code may not use a __device__ symbol's name
+//   as a device pointer); make that first call before any stream capture.
+#include "../../include/cellspe_gpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+#include <cmath>
+#include <mutex>
+
+namespace {
+
+constexpr size_t CS_NOALLOC_SCRATCH_FLOATS = (size_t)4 << 20;    // 16 MiB of partials
+constexpr int CS_NOALLOC_MAX_N = 65536;
+
+static __device__ __align__(256) float g_noalloc_scratch[CS_NOALLOC_SCRATCH_FLOATS];
+static __device__ __align__(256) float2 g_noalloc_tw[CS_NOALLOC_MAX_N];
+static __device__ __align__(256) float g_noalloc_win[CS_NOALLOC_MAX_N];
+static __device__ __align__(256) float2 g_noalloc_rot[CS_NOALLOC_MAX_N];
+
+struct NoallocPtrs {
+    float* scratch = nullptr;
+    float2* tw = nullptr;
+    float* win = nullptr;
+    float2* rot = nullptr;
+    bool ready = false;
+};
+constexpr int MAX_DEVICES = 64;
+std::mutex g_setup_mu;
+NoallocPtrs g_ptrs[MAX_DEVICES];
+
+int setup_device(int dev, NoallocPtrs* out)
+{
+    if (dev < 0 || dev >= MAX_DEVICES) return CELLSPE_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    NoallocPtrs& p = g_ptrs[dev];
+    if (!p.ready) {
+        cudaError_t e = cudaGetSymbolAddress((void**)&p.scratch, g_noalloc_scratch);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&p.tw, g_noalloc_tw);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&p.win, g_noalloc_win);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&p.rot, g_noalloc_rot);
+        if (e != cudaSuccess) return cs_set_error(CELLSPE_ERR_CUDA, "spectrometer_noalloc: cudaGetSymbolAddress failed");
+        p.ready = true;
+    }
+    *out = p;
+    return 0;
+}
+
+// Same values as the host-built tables of the allocating path (FP64, rounded
+// to FP32).
+__global__ void k_fill_tables(float2* tw, float* win, int n, int window, float2* rot, int rotlen, double dphi)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        double sn, cs;
+        sincospi(-2.0 * (double)i / (double)n, &sn, &cs);
+        tw[i] = make_float2((float)cs, (float)sn);
+        float w = 1.f;
+        if (window != 0) {
+            double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
+            double c = cos(arg);
+            w = (window == 1) ? (float)c : (float)(c * c);
+        }
+        win[i] = w;
+    }
+    if (i < rotlen) rot[i] = make_float2((float)cos(dphi * (double)i), (float)sin(dphi * (double)i));
+}
+
+bool pow2i(long long n) { return n > 0 && (n & (n - 1)) == 0; }
+
+}  // namespace
+
+extern "C" int cellspe_spectrometer_noalloc(const cellspe_spec_params* p, const void* raw, float* power,
+                                            void* pcal_bins, void* pcal_tones, void* stream)
+{
+    if (!p || !raw || !power) return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: null argument");
+    if (p->memory != CELLSPE_MEM_DEVICE)
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: device memory only (memory = CELLSPE_MEM_DEVICE)");
+    const int nsub = p->n_subbands;
+    if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16))
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: n_subbands must be 1, 4, 8 or 16");
+    if (nsub > 1 && p->input_layout != CELLSPE_SPEC_PLANES)
+        return cs_set_error(CELLSPE_ERR_ARG,
+                            "spectrometer_noalloc: needs CELLSPE_SPEC_PLANES input (the corner turn needs a raw-sized buffer)");
+    const int N = p->fft_points;
+    if (!pow2i(N) || N < 1024 || N > CS_NOALLOC_MAX_N)
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: fft_points must be a power of two in [1024, 65536]");
+    if (p->overlap < 1 || p->ffts_per_spectrum < 1 || p->n_spectra < 1 || p->raw_bytes <= 0 ||
+        p->raw_bytes % (16 * nsub))
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: bad sizes");
+    if (p->pcal_tonebins > 0 && (!pcal_bins || p->pcal_rotatorlen <= 0 || p->pcal_rotatorlen > CS_NOALLOC_MAX_N))
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: phase-cal needs pcal_bins and rotatorlen <= 65536");
+    static const float mk5b[4] = {-3.3359f, 1.0f, -1.0f, 3.3359f};
+    static const float twob[4] = {1.0f, -1.0f, 3.3359f, -3.3359f};
+    static const float offb[4] = {-3.336f, -1.0f, 1.0f, 3.336f};
+    const float* lut = p->custom_levels ? p->custom_levels
+                       : (p->levels & 0xff) == CELLSPE_LEVELS_MARK5B ? mk5b
+                       : (p->levels & 0xff) == CELLSPE_LEVELS_TWOBIT ? twob
+                       : (p->levels & 0xff) == CELLSPE_LEVELS_OFFSET_BINARY ? offb : nullptr;
+    if (!lut) return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: unknown level table");
+
+    // Chunking: the default number of FFTs per partial, grown until the
+    // partials (plus phase-cal partials) fit the static scratch.
+    CsSpecArgs a{};
+    a.planes = (const uint8_t*)raw;
+    a.bytes_per_sub = p->raw_bytes / nsub;
+    a.nsub = nsub; a.N = N; a.overlap = p->overlap; a.window = p->window;
+    a.ffts_per_spectrum = p->ffts_per_spectrum; a.nspec = p->n_spectra;
+    for (int i = 0; i < 4; i++) a.lut[i] = lut[i];
+    a.tonebins = p->pcal_tonebins; a.rotatorlen = p->pcal_rotatorlen; a.ntones = p->pcal_ntones;
+    a.pcal_offset_hz = p->pcal_offset_hz; a.fs_hz = p->sample_rate_hz;
+    a.power = power;
+    a.pcal_bins = (float2*)pcal_bins;
+    a.pcal_tones = (float2*)pcal_tones;
+    const long long novl = (long long)p->overlap * p->ffts_per_spectrum - (p->overlap - 1);
+    a.ffts_per_chunk = 0;
+    if ((size_t)cs_spectrometer_scratch_floats(a) > CS_NOALLOC_SCRATCH_FLOATS) {
+        const long long rows = (long long)nsub * p->n_spectra, nb = N / 2 + 1;
+        const long long pcal = p->pcal_tonebins > 0 ? cs_spectrometer_scratch_floats(a) - rows * nb *
+                                                       ((novl + 31) / 32)
+                                                    : 0;
+        const long long max_chunks = ((long long)CS_NOALLOC_SCRATCH_FLOATS - pcal) / (rows * nb);
+        if (max_chunks < 1)
+            return cs_set_error(CELLSPE_ERR_ARG,
+                                "spectrometer_noalloc: job exceeds the static scratch maximum of 4194304 floats "
+                                "((n_subbands * n_spectra) * (fft_points/2+1) must fit, plus phase-cal partials)");
+        a.ffts_per_chunk = (int)((novl + max_chunks - 1) / max_chunks);
+        if ((size_t)cs_spectrometer_scratch_floats(a) > CS_NOALLOC_SCRATCH_FLOATS)
+            return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: job exceeds the static scratch maximum");
+    }
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return cs_set_error(CELLSPE_ERR_CUDA, "spectrometer_noalloc: no device");
+    NoallocPtrs ptrs;
+    int rc = setup_device(dev, &ptrs);
+    if (rc) return rc;
+    a.partial = ptrs.scratch;
+    a.tw_table = ptrs.tw;
+    a.win_table = ptrs.win;
+    a.rot_table = ptrs.rot;
+
+    cudaStream_t st = (cudaStream_t)stream;
+    const int rotlen = p->pcal_tonebins > 0 ? p->pcal_rotatorlen : 0;
+    const int nfill = N > rotlen ? N : rotlen;
+    const double dphi = 2.0 * M_PI * (p->sample_rate_hz > 0 ? -p->pcal_offset_hz / p->sample_rate_hz : 0.0);
+    k_fill_tables<<<(nfill + 255) / 256, 256, 0, st>>>(ptrs.tw, ptrs.win, N, p->window, ptrs.rot, rotlen, dphi),
+        cs_count_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cs_set_error(CELLSPE_ERR_CUDA, "spectrometer_noalloc: table kernel launch failed");
+    rc = cs_spectrometer(a, st);
+    if (rc == CS_ERR_ARG) return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: invalid argument");
+    if (rc == CS_ERR_UNSUPPORTED) return cs_set_error(CELLSPE_ERR_UNSUPPORTED, "spectrometer_noalloc: unsupported size");
+    if (rc) return cs_set_error(CELLSPE_ERR_CUDA, "spectrometer_noalloc: kernel launch failed");
+    return 0;
+}

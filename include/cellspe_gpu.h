@@ -155,6 +155,25 @@ int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* p
                          void* pcal_bins, void* pcal_tones);
 long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p);
 
+/* Spectrometer that allocates no device memory (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc when they run it:
+ * real-time loops that must not stall on the allocator (cudaMalloc/cudaFree
+ * can synchronise the device), code running during CUDA graph capture, or
+ * hosts that fix the library's device footprint up front.  Same results as
+ * cellspe_spectrometer (within FP32 summation order), enqueued on `stream`
+ * (a cudaStream_t, NULL = default stream) without synchronising.
+ * Requirements: memory = CELLSPE_MEM_DEVICE (raw, power, pcal_* are device
+ * pointers); input_layout = CELLSPE_SPEC_PLANES unless n_subbands == 1;
+ * fft_points <= 65536; pcal_rotatorlen <= 65536.
+ * Scratch: a fixed static device array of 4,194,304 floats (16 MiB) plus
+ * 1.25 MiB of tables, held by every GPU that loads the library until exit.
+ * Jobs whose partial spectra do not fit are rejected with CELLSPE_ERR_ARG.
+ * The first call on each device looks up the arrays' device addresses
+ * (cudaGetSymbolAddress): make it before any stream capture.  All calls
+ * share the arrays: calls that overlap on the GPU race. */
+int cellspe_spectrometer_noalloc(const cellspe_spec_params* p, const void* raw, float* power,
+                                 void* pcal_bins, void* pcal_tones, void* stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
