@@ -103,6 +103,51 @@ def cpu_baseline(raw_host: np.ndarray, k_sample: int, nthreads: int):
     return S * k_sample * N / dt / 1e9, dt
 
 
+def run_serving(cg, torch, seconds: float, rate: float, x_mode: int, seed: int = 5):
+    """Batched streaming service: Poisson arrivals, uneven jobs (S, C, T) as in the
+    serving configuration, device-resident buffers; latency is submit -> done."""
+    rng = np.random.default_rng(seed)
+    s_choices, c_choices = [4, 8, 24, 64, 200], [256, 1024, 4096, 16384]
+    t_arr, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        t_arr.append(t)
+    jobs = [(int(rng.choice(s_choices)), int(rng.choice(c_choices)), 2 ** int(rng.integers(18, 25)),
+             float(rng.uniform(0.01, 0.2))) for _ in t_arr]
+    max_raw = max(S * T // 4 for S, _, T, _ in jobs)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    raw_pool = torch.randint(0, 256, (max_raw,), dtype=torch.uint8, device="cuda", generator=g)
+    svc = cg.Service(max_streams=8)
+    pending, lat, samples = [], [], 0
+    t0 = time.perf_counter()
+    for (S, C, T, _), ta in zip(jobs, t_arr):
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        N = 2 * C
+        raw = raw_pool[: S * T // 4].view(S, T // 4)
+        vis = torch.empty((C, S * (S + 1) // 2), dtype=torch.complex64, device="cuda")
+        p = cg.fx_params(S, N, T // N, T // 4, x_mode=x_mode)
+        pending.append((svc.submit(p, raw, vis), vis))
+        samples += S * T
+        while len(pending) > 64:                      # bounded outstanding outputs
+            jid, _ = pending.pop(0)
+            lat.append(svc.wait(jid))
+    for jid, _ in pending:
+        lat.append(svc.wait(jid))
+    makespan = time.perf_counter() - t0
+    st = svc.stats()
+    svc.close()
+    del raw_pool
+    return {"jobs": len(jobs), "arrival_rate_per_s": rate, "window_s": seconds,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "offered_gsamples_s": samples / seconds / 1e9, "served_gsamples_s": samples / makespan / 1e9,
+            "max_concurrent_jobs": st["max_running"], "failed": st["failed"],
+            "job_mix": "S in {4,8,24,64,200}, C in {256,1024,4096,16384}, T = 2^U, U in [18,24]"}
+
+
 def run_reference(args):
     """CPU implementation of the path (the oracle's FX restatement), all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -147,6 +192,8 @@ def main():
     ap.add_argument("--cpu-segments", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
+                    help="length of the Poisson arrival window of the serving measurement (0 skips it)")
     ap.add_argument("--segments", type=int, default=K,
                     help="spectra per integration (smaller values make a profiling-sized case)")
     args = ap.parse_args()
@@ -256,6 +303,10 @@ def main():
                 "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
                 "traffic": None}
 
+    serving = None
+    if args.serve_seconds > 0:
+        serving = run_serving(cg, torch, args.serve_seconds, 200.0, x_mode)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -281,6 +332,7 @@ def main():
             "roofline": roof,
             "stages": stages,
             "clocks": clk.summary(),
+            "serving": serving,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

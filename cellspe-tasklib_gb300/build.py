@@ -19,6 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = PKG / "libcellspe_gpu.so"
+APPS = sorted((CSRC / "apps").glob("*.cpp"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"),
@@ -64,6 +65,15 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    for src in APPS:                 # entry-point programs linked against the library
+        exe = PKG / src.stem
+        if force or not exe.exists() or exe.stat().st_mtime < max(src.stat().st_mtime, LIB.stat().st_mtime):
+            cmd = ["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                   "-L", str(PKG), "-lcellspe_gpu", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                sys.stderr.write(r.stdout + r.stderr)
+                raise RuntimeError(f"link failed for {src.name}")
     return LIB
 
 

@@ -89,6 +89,16 @@ class SpecParams(ctypes.Structure):
                 ("memory", ctypes.c_int), ("custom_levels", ctypes.c_void_p)]
 
 
+class ServiceConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_streams", ctypes.c_int)]
+
+
+class ServiceStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong), ("queued", ctypes.c_longlong),
+                ("running", ctypes.c_int), ("max_running", ctypes.c_int), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("p99_queue_ms", ctypes.c_double), ("budget_bytes", ctypes.c_longlong)]
+
+
 class XmacParams(ctypes.Structure):
     _fields_ = [("S", ctypes.c_int), ("C", ctypes.c_int), ("K", ctypes.c_int), ("accumulate", ctypes.c_int)]
 
@@ -134,6 +144,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_fft_c2c": ([V, V, I, LL, I], I),
             "cellspe_fft_r2c": ([V, V, I, LL, I], I),
             "cellspe_xmac": ([V, I, I, I, V, I, I], I),
+            "cellspe_vis_lags": ([V, V, LL, I, D, I], I),
             "cellspe_xmac_f16": ([V, I, I, I, V, I, I], I),
             "cellspe_fx_correlate": ([V, V, V, V], I),
             "cellspe_fx_workspace_bytes": ([V], LL),
@@ -142,6 +153,11 @@ def lib() -> ctypes.CDLL:
             "cellspe_spectrometer": ([V, V, V, V, V], I),
             "cellspe_spectrometer_workspace_bytes": ([V], LL),
             "cellspe_spectrometer_noalloc": ([V, V, V, V, V, V], I),
+            "cellspe_service_create": ([V], V),
+            "cellspe_service_submit": ([V, V, V, V, V, ctypes.POINTER(ctypes.c_longlong)], I),
+            "cellspe_service_wait": ([V, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)], I),
+            "cellspe_service_get_stats": ([V, V], I),
+            "cellspe_service_destroy": ([V], None),
             "celldsp_start": ([], I), "celldsp_stop": ([], I),
             "celldsp_getFreeSPE": ([], I), "celldsp_setFreeSPE": ([I], I),
             "celldsp_startTask": ([I, V], I), "celldsp_waitTask": ([I], I),
@@ -235,6 +251,13 @@ def xmac(spectra, S: int, C: int, K: int, vis, accumulate: bool = False):
     return vis
 
 
+def vis_lags(vis, lags, scale: float = 1.0):
+    """vis, lags: complex64 [P][C] (baseline-major)."""
+    P, C = vis.shape[0], vis.shape[-1]
+    _check(lib().cellspe_vis_lags(_ptr(vis)[0], _ptr(lags)[0], P, C, scale, _mem(vis, lags)))
+    return lags
+
+
 def xmac_f16(spectra_f16, S: int, C: int, K: int, vis, accumulate: bool = False):
     """spectra_f16: float16 [C][2][S][K] (Re plane, Im plane)."""
     _check(lib().cellspe_xmac_f16(_ptr(spectra_f16)[0], S, C, K, _ptr(vis)[0], int(accumulate),
@@ -293,6 +316,42 @@ def spectrometer_noalloc(params: SpecParams, raw, power, pcal_bins=None, pcal_to
                                               _ptr(pcal_tones)[0] if pcal_tones is not None else None,
                                               ctypes.c_void_p(stream)))
     return power
+
+
+class Service:
+    """cellspe_service_*: continuous-batching correlation service."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_streams: int = 8):
+        self._h = lib().cellspe_service_create(ctypes.byref(ServiceConfig(hbm_budget_bytes, max_streams)))
+        if not self._h:
+            raise CellspeError(ERR_CUDA, last_error())
+        self._keep = {}
+
+    def submit(self, params: FxParams, raw, vis, delay_poly=None) -> int:
+        params.memory = _mem(raw, vis)
+        jid = ctypes.c_longlong()
+        _check(lib().cellspe_service_submit(self._h, ctypes.byref(params), _ptr(raw)[0],
+                                            _ptr(delay_poly)[0] if delay_poly is not None else None,
+                                            _ptr(vis)[0], ctypes.byref(jid)))
+        self._keep[jid.value] = (params, raw, vis, delay_poly)
+        return jid.value
+
+    def wait(self, job_id: int) -> float:
+        lat = ctypes.c_double()
+        rc = lib().cellspe_service_wait(self._h, job_id, ctypes.byref(lat))
+        self._keep.pop(job_id, None)
+        _check(rc)
+        return lat.value
+
+    def stats(self) -> dict:
+        st = ServiceStats()
+        _check(lib().cellspe_service_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServiceStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().cellspe_service_destroy(self._h)
+            self._h = None
 
 
 # ---- task API ------------------------------------------------------------------

@@ -26,15 +26,17 @@ CS_DEV float2 cmul_conj(float2 a, float2 b)  // a * conj(b)
 CS_DEV float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }   // a * (-i)
 CS_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
-// W32^m = exp(-2 pi i m / 32), m in [0, 32): cos and sin of multiples of pi/16.
+// cos(r pi / 16), r = 0..8 and cos(r pi / 32), r = 0..16 (constant bank:
+// indices are warp-uniform, so reads broadcast).
+static __constant__ float c_cos32[9] = {1.0f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f, 0.70710678118654757f, 0.55557023301960229f, 0.38268343236508984f, 0.19509032201612833f, 0.0f};
+static __constant__ float c_cos64[17] = {1.0f, 0.99518472667219693f, 0.98078528040323043f, 0.95694033573220882f, 0.92387953251128674f, 0.88192126434835505f, 0.83146961230254524f, 0.77301045336273699f, 0.70710678118654757f, 0.63439328416364549f, 0.55557023301960229f, 0.47139673682599781f, 0.38268343236508984f, 0.29028467725446233f, 0.19509032201612833f, 0.09801714032956077f, 0.0f};
+
+// W32^m = exp(-2 pi i m / 32), m in [0, 32).
 CS_DEV float2 w32(int m)
 {
-    const float c[9] = {1.0f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f,
-                        0.70710678118654752f, 0.55557023301960222f, 0.38268343236508977f,
-                        0.19509032201612826f, 0.0f};
     m &= 31;
     const int q = m >> 3, r = m & 7;          // quadrant, offset inside it
-    float cr = c[r], sr = c[8 - r];           // cos, sin of r*pi/16
+    const float cr = c_cos32[r], sr = c_cos32[8 - r];
     // exp(-i (q*pi/2 + r*pi/16)) = (-i)^q * (cr - i sr)
     float2 z = make_float2(cr, -sr);
     switch (q) {
@@ -46,12 +48,11 @@ CS_DEV float2 w32(int m)
 }
 CS_DEV float2 w16(int m) { return w32(2 * m); }
 
-// W64^m = exp(-2 pi i m / 64) for m in [0, 32) (used with constant m).
+// W64^m = exp(-2 pi i m / 64) for m in [0, 32).
 CS_DEV float2 w64c(int m)
 {
-    const float c[17] = {1.0f, 0.99518472667219693f, 0.98078528040323043f, 0.95694033573220882f, 0.92387953251128674f, 0.88192126434835505f, 0.83146961230254524f, 0.77301045336273699f, 0.70710678118654757f, 0.63439328416364549f, 0.55557023301960229f, 0.47139673682599781f, 0.38268343236508984f, 0.29028467725446233f, 0.19509032201612833f, 0.09801714032956077f, 0.0f};
     const int q = (m >> 4) & 1, r = m & 15;
-    float2 z = make_float2(c[r], -c[16 - r]);
+    float2 z = make_float2(c_cos64[r], -c_cos64[16 - r]);
     return q ? make_float2(z.y, -z.x) : z;
 }
 

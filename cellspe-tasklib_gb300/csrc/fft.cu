@@ -71,9 +71,11 @@ template <int M> struct BCfg {
 
 // All groups of a CTA advance in lockstep (whole-CTA barriers); groups past
 // the end of the batch still take part in the barriers but touch no memory.
-template <int M, bool REAL>
+// INV: backward transform e^{+2 pi i nk/M} (complex only), computed as
+// conj(FFT(conj(x))), with the outputs multiplied by `scale`.
+template <int M, bool REAL, bool INV>
 __global__ void __launch_bounds__(BCfg<M>::NT) k_fft_batch(const void* __restrict__ in, float2* __restrict__ out,
-                                                          int64_t batch, const float2* __restrict__ tw)
+                                                          int64_t batch, const float2* __restrict__ tw, float scale)
 {
     using C = BCfg<M>;
     constexpr int T = C::T;
@@ -89,6 +91,7 @@ __global__ void __launch_bounds__(BCfg<M>::NT) k_fft_batch(const void* __restric
         if (!valid) v[r] = make_float2(0.f, 0.f);
         else if (REAL) v[r] = __ldg(reinterpret_cast<const float2*>(in) + b * M + n);  // {x[2n], x[2n+1]}
         else v[r] = __ldg(reinterpret_cast<const float2*>(in) + b * M + n);
+        if (INV) v[r].y = -v[r].y;
     }
     auto bar = [] { __syncthreads(); };
     // REAL: the M-point transform of pairs uses the 2M-point table (stride 2);
@@ -97,7 +100,11 @@ __global__ void __launch_bounds__(BCfg<M>::NT) k_fft_batch(const void* __restric
     if (!valid) return;
     if constexpr (!REAL) {
 #pragma unroll
-        for (int r = 0; r < 16; r++) out[b * M + t + r * T] = fb[fpad(t + r * T)];
+        for (int r = 0; r < 16; r++) {
+            float2 z = fb[fpad(t + r * T)];
+            if (INV) z = make_float2(z.x * scale, -z.y * scale);
+            out[b * M + t + r * T] = z;
+        }
     } else {
         float2* o = out + b * (M + 1);
         for (int kk = t; kk <= M / 2; kk += T) {
@@ -114,35 +121,35 @@ __global__ void __launch_bounds__(BCfg<M>::NT) k_fft_batch(const void* __restric
     }
 }
 
-template <int M, bool REAL>
-int launch_batch(const void* in, float2* out, int64_t batch, cudaStream_t st)
+template <int M, bool REAL, bool INV>
+int launch_batch(const void* in, float2* out, int64_t batch, float scale, cudaStream_t st)
 {
     using C = BCfg<M>;
     const float2* tw = cs_twiddles(2 * M);
     if (!tw) return CS_ERR_ARG;
     size_t smem = (size_t)C::GROUPS * fpad_size(M) * sizeof(float2);
-    auto kern = k_fft_batch<M, REAL>;
+    auto kern = k_fft_batch<M, REAL, INV>;
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int64_t blocks = (batch + C::GROUPS - 1) / C::GROUPS;
-    kern<<<(unsigned)blocks, C::NT, smem, st>>>(in, out, batch, tw), cs_count_launches(1);
+    kern<<<(unsigned)blocks, C::NT, smem, st>>>(in, out, batch, tw, scale), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
-template <bool REAL>
-int dispatch(const void* in, float2* out, int m, int64_t batch, cudaStream_t st)
+template <bool REAL, bool INV>
+int dispatch(const void* in, float2* out, int m, int64_t batch, float scale, cudaStream_t st)
 {
     switch (m) {
-        case 16: return launch_batch<16, REAL>(in, out, batch, st);
-        case 32: return launch_batch<32, REAL>(in, out, batch, st);
-        case 64: return launch_batch<64, REAL>(in, out, batch, st);
-        case 128: return launch_batch<128, REAL>(in, out, batch, st);
-        case 256: return launch_batch<256, REAL>(in, out, batch, st);
-        case 512: return launch_batch<512, REAL>(in, out, batch, st);
-        case 1024: return launch_batch<1024, REAL>(in, out, batch, st);
-        case 2048: return launch_batch<2048, REAL>(in, out, batch, st);
-        case 4096: return launch_batch<4096, REAL>(in, out, batch, st);
-        case 8192: return launch_batch<8192, REAL>(in, out, batch, st);
-        case 16384: return launch_batch<16384, REAL>(in, out, batch, st);
+        case 16: return launch_batch<16, REAL, INV>(in, out, batch, scale, st);
+        case 32: return launch_batch<32, REAL, INV>(in, out, batch, scale, st);
+        case 64: return launch_batch<64, REAL, INV>(in, out, batch, scale, st);
+        case 128: return launch_batch<128, REAL, INV>(in, out, batch, scale, st);
+        case 256: return launch_batch<256, REAL, INV>(in, out, batch, scale, st);
+        case 512: return launch_batch<512, REAL, INV>(in, out, batch, scale, st);
+        case 1024: return launch_batch<1024, REAL, INV>(in, out, batch, scale, st);
+        case 2048: return launch_batch<2048, REAL, INV>(in, out, batch, scale, st);
+        case 4096: return launch_batch<4096, REAL, INV>(in, out, batch, scale, st);
+        case 8192: return launch_batch<8192, REAL, INV>(in, out, batch, scale, st);
+        case 16384: return launch_batch<16384, REAL, INV>(in, out, batch, scale, st);
         default: return CS_ERR_UNSUPPORTED;
     }
 }
@@ -152,7 +159,14 @@ int cs_cfft_batch(const float2* in, float2* out, int n, int64_t batch, cudaStrea
 {
     if (!in || !out || batch < 0) return CS_ERR_ARG;
     if (batch == 0) return 0;
-    return dispatch<false>(in, out, n, batch, st);
+    return dispatch<false, false>(in, out, n, batch, 1.f, st);
+}
+
+int cs_cfft_inverse_batch(const float2* in, float2* out, int n, int64_t batch, float scale, cudaStream_t st)
+{
+    if (!in || !out || batch < 0) return CS_ERR_ARG;
+    if (batch == 0) return 0;
+    return dispatch<false, true>(in, out, n, batch, scale, st);
 }
 
 int cs_rfft_batch(const float* in, float2* out, int n, int64_t batch, cudaStream_t st)
@@ -160,5 +174,5 @@ int cs_rfft_batch(const float* in, float2* out, int n, int64_t batch, cudaStream
     if (!in || !out || batch < 0 || (n & 1)) return CS_ERR_ARG;
     if ((uintptr_t)in % 8) return CS_ERR_ARG;
     if (batch == 0) return 0;
-    return dispatch<true>(in, out, n / 2, batch, st);
+    return dispatch<true, false>(in, out, n / 2, batch, 1.f, st);
 }

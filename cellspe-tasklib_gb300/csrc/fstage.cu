@@ -20,6 +20,10 @@
 #include "common.cuh"
 #include "kernels.h"
 
+#include <algorithm>
+#include <cstdlib>
+#include <mutex>
+
 namespace {
 
 template <int M> struct FCfg {
@@ -27,6 +31,9 @@ template <int M> struct FCfg {
     static constexpr int GROUPS = (T >= 256) ? 1 : 256 / T;
     static constexpr int NT = T * GROUPS;
     static constexpr int RAWW = M / 8 + 2;     // 32-bit raw words staged per segment
+    // groups narrower than a warp cannot use named barriers: the whole CTA
+    // then advances in lockstep on __syncthreads
+    static constexpr bool CTA_BAR = (GROUPS == 1) || (T < 32);
 };
 
 template <int M, int FMT>
@@ -72,7 +79,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
     float2* fb = fbuf_all + g * fpad_size(M);
     uint32_t* rb = rbuf_all + g * Cfg::RAWW;
     auto bar = [&]() {
-        if constexpr (GROUPS == 1) __syncthreads();
+        if constexpr (Cfg::CTA_BAR) __syncthreads();
         else named_bar(1 + g, T);
     };
     const int64_t words = a.bytes_per_input >> 2;
@@ -81,16 +88,18 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
     const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
     constexpr bool DIRECT = (G == 1);
 
-    for (int ls = g; ls < G; ls += GROUPS) {
+    // every group runs the same number of rounds (barriers stay uniform);
+    // segments past K are computed on zeros and not stored
+    for (int ls = g; ls < ((G + GROUPS - 1) / GROUPS) * GROUPS; ls += GROUPS) {
         const int k = k0 + ls;
-        if (k >= a.K) break;                       // uniform over the group
-        const int64_t sk = (int64_t)s * a.K + k;
-        int64_t start = a.start_sample + (int64_t)k * N + (a.shift ? a.shift[sk] : 0);
+        const bool valid = (ls < G) && (k < a.K);
+        const int64_t sk = (int64_t)s * a.K + (valid ? k : 0);
+        int64_t start = a.start_sample + (int64_t)(valid ? k : 0) * N + (a.shift ? a.shift[sk] : 0);
         int64_t w0 = start >> 4;                   // floor for negative starts too
         int off = (int)(start & 15);
         for (int i = t; i < M / 8 + 1; i += T) {
             int64_t wi = w0 + i;
-            rb[i] = (wi >= 0 && wi < words) ? __ldg(src_in + wi) : 0u;
+            rb[i] = (valid && wi >= 0 && wi < words) ? __ldg(src_in + wi) : 0u;
         }
         bar();
         float2 v[16];
@@ -116,6 +125,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
         }
         const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
         auto emit = [&](int c, float2 X) {
+            if (!valid) return;
             if (scl) X = cscale(X, __ldg(scl + c));
             if constexpr (DIRECT) {
                 if constexpr (FMT == CS_SPECTRA_F32) {
@@ -180,14 +190,12 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
                 int l = 8 * (idx % P8);
                 int plane = (idx / P8) & 1;
                 int c = idx / (2 * P8);
-                __align__(16) __half h[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    __half2 x = st[c * (G + 1) + l + j];
-                    h[j] = plane ? __high2half(x) : __low2half(x);
-                }
+                // pick the Re (low) or Im (high) halves of 8 staged half2 words
+                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + l);
+                const uint32_t sel = plane ? 0x7632u : 0x5410u;
                 *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * K + k0 + l) =
-                    *reinterpret_cast<const uint4*>(h);
+                    make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
+                               __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
             }
         } else {
             for (int idx = threadIdx.x; idx < M * 2 * G; idx += Cfg::NT) {
@@ -226,137 +234,197 @@ int dispatch_fstage(const CsFStageArgs& a, cudaStream_t st)
 }
 
 // ---------------------------------------------------------------------------
-// N = 2048 fast path: one warp per segment.  The 1024-point complex FFT of
-// z[n] = x[2n] + i x[2n+1] runs as a 32 x 32 four-step transform held in
-// registers (each lane keeps 32 points): DFT-32 over n2 for n = lane + 32 n2,
-// twiddle W_1024^(lane k1), one padded shared-memory transpose, DFT-32 over
+// N = 2048 fast path: one warp per segment.
+// The 1024-point complex FFT of z[n] = x[2n] + i x[2n+1] runs as a 32 x 32
+// four-step transform held in registers (each lane keeps 32 points): DFT-32
+// over n2 for n = lane + 32 n2, twiddle W_1024^(lane k1) from a shared table,
+// one padded shared-memory transpose (one float plane at a time), DFT-32 over
 // n1; lane l then holds Z[l + 32 k2].  The real-FFT split pairs Z[k] with
 // Z[1024-k], which lives in lane (32-l) mod 32, register 31-k2 (lane 0:
-// register (32-k2) mod 32), so it is a register shuffle.  Twiddles and
-// delay phasors come from short register recurrences seeded from the FP64
-// table.  Each CTA stages GW = 8 segments and writes them corner-turned.
+// register (32-k2) mod 32), so it is a register shuffle.  A CTA of WARPS
+// warps stages W_G = 8 segments of one input and writes them corner-turned;
+// with WARPS = 4 each warp transforms two segments and fetches the raw words
+// of the second with cp.async while it transforms the first.
 // Input must be LSB-first (sample j of a 32-bit word at bits 2j).
 // ---------------------------------------------------------------------------
-constexpr int W_G = 8, W_WARPS = 8, W_TP = 33, W_RAWW = 2048 / 16 + 2;
+constexpr int W_G = 8, W_TP = 33;
+constexpr int W_RAWC = 2048 / 64 + 2;          // 16-byte chunks staged per segment (34 = 136 words)
+constexpr int W_RAWW = 4 * W_RAWC;
 
-template <int FMT>
+template <int FMT, int WARPS>
 size_t w2048_smem()
 {
     size_t elem = (FMT == CS_SPECTRA_F32) ? 8 : 4;
-    return (size_t)W_WARPS * 32 * W_TP * 8 + (size_t)W_WARPS * W_RAWW * 4 + (size_t)1024 * (W_G + 1) * elem;
+    return (size_t)WARPS * 32 * W_TP * 8            // transpose tiles (complex)
+           + (size_t)WARPS * 2 * W_RAWW * 4         // raw double buffers
+           + 16 * 8                                 // pair LUT
+           + (size_t)1024 * (W_G + 1) * elem;       // staging tile
 }
 
-template <int FMT, bool PHASE>
-__global__ void __launch_bounds__(256, 2) k_fx_fstage_w2048(CsFStageArgs a, const float2* __restrict__ tw)
+CS_DEV void cp_async16(uint32_t dst, const void* src, bool valid)
 {
-    constexpr int M = 1024, N = 2048, G = W_G;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+CS_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N_PENDING>
+CS_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N_PENDING) : "memory"); }
+
+template <int FMT, bool PHASE, int WARPS, int ROUNDS>
+__global__ void __launch_bounds__(32 * WARPS, (WARPS == 8) ? 2 : 3) k_fx_fstage_w2048(CsFStageArgs a, const float2* __restrict__ tw)
+{
+    constexpr int M = 1024, N = 2048, G = W_G, NT = 32 * WARPS, PER = G / WARPS;
     extern __shared__ __align__(16) unsigned char smem[];
     float2* tb_all = reinterpret_cast<float2*>(smem);
-    uint32_t* rb_all = reinterpret_cast<uint32_t*>(tb_all + W_WARPS * 32 * W_TP);
-    unsigned char* stage = reinterpret_cast<unsigned char*>(rb_all + W_WARPS * W_RAWW);
+    uint32_t* rb_all = reinterpret_cast<uint32_t*>(tb_all + WARPS * 32 * W_TP);
+    float2* lut16 = reinterpret_cast<float2*>(rb_all + WARPS * 2 * W_RAWW);
+    unsigned char* stage = reinterpret_cast<unsigned char*>(lut16 + 16);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float2* tb = tb_all + warp * 32 * W_TP;
-    uint32_t* rb = rb_all + warp * W_RAWW;
+    uint32_t* rb = rb_all + warp * 2 * W_RAWW;
     const int s = blockIdx.y;
-    const int k0 = blockIdx.x * G;
-    const int k = k0 + warp;
-    const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
+    const int kbase = blockIdx.x * G * ROUNDS;
+    const int64_t chunks = a.bytes_per_input >> 4;
+    const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
 
-    if (k < a.K) {
-        const int64_t sk = (int64_t)s * a.K + k;
-        const int64_t start = a.start_sample + (int64_t)k * N + (a.shift ? a.shift[sk] : 0);
-        const int64_t w0 = start >> 4;
-        const int off = (int)(start & 15);
-        const int64_t words = a.bytes_per_input >> 2;
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(a.raw + (int64_t)s * a.bytes_per_input);
-        for (int i = lane; i < W_RAWW; i += 32) {
-            int64_t wi = w0 + i;
-            rb[i] = (wi >= 0 && wi < words) ? __ldg(src + wi) : 0u;
+    // raw words of this warp's u-th segment (round u / PER, slot u % PER) ->
+    // buffer u & 1 (cp.async, zero fill outside the input); returns the sample
+    // offset inside the staged words
+    auto prefetch = [&](int u) -> int {
+        const int r = u % PER, round = u / PER;
+        const int k = kbase + round * G + warp + WARPS * r;
+        const bool kv = k < a.K;
+        const int64_t start = a.start_sample + (int64_t)k * N + ((a.shift && kv) ? __ldg(a.shift + (int64_t)s * a.K + k) : 0);
+        const int64_t c0 = start >> 6;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rb + (u & 1) * W_RAWW);
+        for (int c = lane; c < W_RAWC; c += 32) {
+            const int64_t ci = c0 + c;
+            const bool ok = kv && ci >= 0 && ci < chunks;
+            cp_async16(dst + 16 * c, ok ? base + 16 * ci : a.raw, ok);
+        }
+        cp_async_commit();
+        return (int)(start & 63);
+    };
+    int off_next = prefetch(0);
+
+    // per-lane twiddle seeds, computed in place (no global loads while the
+    // raw words arrive): W_1024^lane for the four-step twiddles, W_2048^lane / 2
+    // for the real-FFT split
+    if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(a.lut[threadIdx.x & 3], a.lut[threadIdx.x >> 2]);
+    float2 w1, whalf;
+    {
+        float sn, cs;
+        sincospif(-(float)lane / 512.0f, &sn, &cs);
+        w1 = make_float2(cs, sn);
+        sincospif(-(float)lane / 1024.0f, &sn, &cs);
+        whalf = make_float2(0.5f * cs, 0.5f * sn);
+    }
+    __syncthreads();
+    const int src_lane = (32 - lane) & 31;
+
+#pragma unroll 1
+    for (int round = 0; round < ROUNDS; round++) {
+    const int k0 = kbase + round * G;
+#pragma unroll 1
+    for (int r = 0; r < PER; r++) {
+        const int u = round * PER + r;
+        const int ls = warp + WARPS * r;
+        const int k = k0 + ls;
+        const int off = off_next;
+        if (u + 1 < PER * ROUNDS) {
+            off_next = prefetch(u + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncwarp();
-        // decode: z[lane + 32 n2] uses samples off + 2 lane + 64 n2 (+1)
-        const int f0 = off + 2 * lane;
-        const int wb = f0 >> 4, sh = 2 * (f0 & 15);
-        float2 v[32];
+        if (k < a.K) {
+            const int64_t sk = (int64_t)s * a.K + k;
+            const uint32_t* rw = rb + (u & 1) * W_RAWW;
+            const int f0 = off + 2 * lane;
+            const int wb = f0 >> 4, sh = 2 * (f0 & 15);
+            float2 v[32];
 #pragma unroll
-        for (int n2 = 0; n2 < 32; n2++) {
-            uint32_t bits = __funnelshift_r(rb[wb + 4 * n2], rb[wb + 4 * n2 + 1], sh);
-            v[n2] = make_float2(lut_pick(lut, bits & 3u), lut_pick(lut, (bits >> 2) & 3u));
-        }
-        // step 1: DFT-32 over n2 -> k1
-        Dft<32>::run(v);
-        // step 2: v[k1] *= W_1024^(lane k1) = (W_2048^(2 lane))^k1
-        {
-            const float2 w1 = twiddle(tw, 2 * lane);
-            float2 wp[32];
-            wp[1] = w1;
-#pragma unroll
-            for (int e = 2; e < 32; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], w1) : cmul(wp[e / 2], wp[e / 2]);
-#pragma unroll
-            for (int e = 1; e < 32; e++) v[e] = cmul(v[e], wp[e]);
-        }
-        // transpose through shared memory: lane <- k1, register <- n1
-#pragma unroll
-        for (int e = 0; e < 32; e++) tb[e * W_TP + lane] = v[e];
-        __syncwarp();
-#pragma unroll
-        for (int e = 0; e < 32; e++) v[e] = tb[lane * W_TP + e];
-        // step 3: DFT-32 over n1 -> k2 ; v[k2] = Z[lane + 32 k2]
-        Dft<32>::run(v);
-
-        // real-FFT split, phasor, scale, stage
-        const float2 wl = twiddle(tw, lane);                  // W_2048^lane
-        float2 B = make_float2(1.f, 0.f), D = B;
-        if constexpr (PHASE) {
-            const float ph0 = a.phase0[sk], dph = a.dphase[sk];
-            float sn, cs;
-            sincosf(ph0 + (float)lane * dph, &sn, &cs);
-            B = make_float2(cs, sn);
-            sincosf(32.f * dph, &sn, &cs);
-            D = make_float2(cs, sn);
-        }
-        const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
-        const int src_lane = (32 - lane) & 31;
-#pragma unroll
-        for (int k2 = 0; k2 < 32; k2++) {
-            float2 zb;
-            zb.x = __shfl_sync(0xffffffffu, v[31 - k2].x, src_lane);
-            zb.y = __shfl_sync(0xffffffffu, v[31 - k2].y, src_lane);
-            if (lane == 0) zb = v[(32 - k2) & 31];
-            const float2 za = v[k2];
-            const float2 E = make_float2(0.5f * (za.x + zb.x), 0.5f * (za.y - zb.y));
-            const float2 O = make_float2(0.5f * (za.y + zb.y), -0.5f * (za.x - zb.x));
-            const float2 wk = cmul(wl, w64c(k2));          // W_2048^(lane + 32 k2)
-            float2 X = cadd(E, cmul(wk, O));
-            const int c = lane + 32 * k2;
-            if constexpr (PHASE) {
-                X = cmul(X, B);
-                B = cmul(B, D);
+            for (int n2 = 0; n2 < 32; n2++) {
+                const uint32_t bits = __funnelshift_r(rw[wb + 4 * n2], rw[wb + 4 * n2 + 1], sh);
+                v[n2] = lut16[bits & 15u];
             }
-            if (scl) X = cscale(X, __ldg(scl + c));
-            if constexpr (FMT == CS_SPECTRA_F32)
-                reinterpret_cast<float2*>(stage)[c * (G + 1) + warp] = X;
-            else
-                reinterpret_cast<__half2*>(stage)[c * (G + 1) + warp] = __floats2half2_rn(X.x, X.y);
+            Dft<32>::run(v);                                    // over n2 -> k1
+            // v[k1] *= W_1024^(lane k1): powers of w1 by a balanced recurrence
+            // (w^2e = (w^e)^2, w^(2e+1) = w^2e w), applied on the fly
+            {
+                float2 wp[16];
+                wp[1] = w1;
+#pragma unroll
+                for (int e = 2; e < 16; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], w1) : cmul(wp[e / 2], wp[e / 2]);
+#pragma unroll
+                for (int e = 1; e < 16; e++) v[e] = cmul(v[e], wp[e]);
+                const float2 w16p = cmul(wp[8], wp[8]);
+                v[16] = cmul(v[16], w16p);
+#pragma unroll
+                for (int e = 17; e < 32; e++) v[e] = cmul(v[e], cmul(w16p, wp[e - 16]));
+            }
+#pragma unroll
+            for (int e = 0; e < 32; e++) tb[e * W_TP + lane] = v[e];
+            __syncwarp();
+#pragma unroll
+            for (int e = 0; e < 32; e++) v[e] = tb[lane * W_TP + e];
+            __syncwarp();
+            Dft<32>::run(v);                                    // over n1 -> k2: v[k2] = Z[lane + 32 k2]
+
+            float2 B = make_float2(1.f, 0.f), D = B;
+            if constexpr (PHASE) {
+                const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);
+                float sn, cs;
+                sincosf(ph0 + (float)lane * dph, &sn, &cs);
+                B = make_float2(cs, sn);
+                sincosf(32.f * dph, &sn, &cs);
+                D = make_float2(cs, sn);
+            }
+            const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
+#pragma unroll
+            for (int k2 = 0; k2 < 32; k2++) {
+                float2 zb;
+                zb.x = __shfl_sync(0xffffffffu, v[31 - k2].x, src_lane);
+                zb.y = __shfl_sync(0xffffffffu, v[31 - k2].y, src_lane);
+                if (lane == 0) zb = v[(32 - k2) & 31];
+                const float2 za = v[k2];
+                // X = E + W O with E = (a + b*)/2, O = (a - b*)/(2i):
+                // X = s/2 - i (W/2) d,  s = a + b*, d = a - b*
+                const float2 sm = make_float2(za.x + zb.x, za.y - zb.y);
+                const float2 df = make_float2(za.x - zb.x, za.y + zb.y);
+                const float2 t = cmul(cmul(whalf, w64c(k2)), df);
+                float2 X = make_float2(fmaf(0.5f, sm.x, t.y), fmaf(0.5f, sm.y, -t.x));
+                const int c = lane + 32 * k2;
+                if constexpr (PHASE) {
+                    X = cmul(X, B);
+                    B = cmul(B, D);
+                }
+                if (scl) X = cscale(X, __ldg(scl + c));
+                if constexpr (FMT == CS_SPECTRA_F32)
+                    reinterpret_cast<float2*>(stage)[c * (G + 1) + ls] = X;
+                else
+                    reinterpret_cast<__half2*>(stage)[c * (G + 1) + ls] = __floats2half2_rn(X.x, X.y);
+            }
         }
     }
     __syncthreads();
 
-    // corner-turned write-out
-    const int nvalid = min(G, a.K - k0);
+    // corner-turned write-out of the G staged segments
+    const int nvalid = max(0, min(G, a.K - k0));
     const int S = a.S, K = a.K;
     if constexpr (FMT == CS_SPECTRA_F32) {
         const float2* st = reinterpret_cast<const float2*>(stage);
         float2* out = reinterpret_cast<float2*>(a.out);
         if (nvalid == G && K % 2 == 0) {
-            for (int idx = threadIdx.x; idx < M * (G / 2); idx += 256) {
-                int c = idx / (G / 2), l = 2 * (idx % (G / 2));
-                float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
+            for (int idx = threadIdx.x; idx < M * (G / 2); idx += NT) {
+                const int c = idx / (G / 2), l = 2 * (idx % (G / 2));
+                const float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
                 *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * K + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
             }
         } else {
-            for (int idx = threadIdx.x; idx < M * G; idx += 256) {
-                int c = idx / G, l = idx % G;
+            for (int idx = threadIdx.x; idx < M * G; idx += NT) {
+                const int c = idx / G, l = idx % G;
                 if (l < nvalid) out[((int64_t)c * S + s) * K + k0 + l] = st[c * (G + 1) + l];
             }
         }
@@ -364,27 +432,106 @@ __global__ void __launch_bounds__(256, 2) k_fx_fstage_w2048(CsFStageArgs a, cons
         const __half2* st = reinterpret_cast<const __half2*>(stage);
         __half* out = reinterpret_cast<__half*>(a.out);
         if (nvalid == G && K % 8 == 0) {
-            for (int idx = threadIdx.x; idx < M * 2; idx += 256) {
-                int plane = idx & 1, c = idx >> 1;
-                __align__(16) __half h[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    __half2 x = st[c * (G + 1) + j];
-                    h[j] = plane ? __high2half(x) : __low2half(x);
-                }
+            for (int idx = threadIdx.x; idx < M * 2; idx += NT) {
+                const int plane = idx & 1, c = idx >> 1;
+                // pick the Re (low) or Im (high) halves of 8 staged half2 words
+                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1));
+                const uint32_t sel = plane ? 0x7632u : 0x5410u;
                 *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * K + k0) =
-                    *reinterpret_cast<const uint4*>(h);
+                    make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
+                               __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
             }
         } else {
-            for (int idx = threadIdx.x; idx < M * 2 * G; idx += 256) {
-                int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
+            for (int idx = threadIdx.x; idx < M * 2 * G; idx += NT) {
+                const int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
                 if (l < nvalid) {
-                    __half2 x = st[c * (G + 1) + l];
+                    const __half2 x = st[c * (G + 1) + l];
                     out[(((int64_t)c * 2 + plane) * S + s) * K + k0 + l] = plane ? __high2half(x) : __low2half(x);
                 }
             }
         }
     }
+    if (round + 1 < ROUNDS) __syncthreads();     // the staging tile is reused
+    }
+}
+
+template <int FMT, bool PHASE, int WARPS, int ROUNDS>
+int launch_w2048_variant(const CsFStageArgs& a, const float2* tw, cudaStream_t st)
+{
+    size_t smem = w2048_smem<FMT, WARPS>();
+    auto kern = k_fx_fstage_w2048<FMT, PHASE, WARPS, ROUNDS>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((a.K + W_G * ROUNDS - 1) / (W_G * ROUNDS), a.S);
+    kern<<<grid, 32 * WARPS, smem, st>>>(a, tw), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+constexpr int W_NVARIANTS = 3;
+
+template <int FMT, bool PHASE>
+int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cudaStream_t st)
+{
+    switch (choice) {
+        case 2: return launch_w2048_variant<FMT, PHASE, 4, 1>(a, tw, st);
+        case 3: return launch_w2048_variant<FMT, PHASE, 8, 2>(a, tw, st);
+        default: return launch_w2048_variant<FMT, PHASE, 8, 1>(a, tw, st);
+    }
+}
+
+// Schedule choice per (format, phase): 1 = 8 warps, one segment each;
+// 2 = 4 warps, two segments each with the second prefetched; 3 = 8 warps,
+// two rounds of 8 segments per CTA (the second round's raw words prefetched
+// during the first).  Picked once per
+// process by timing both on a 64-input x 64-segment job of zero samples (the
+// FFT's arithmetic does not depend on the values), unless the environment
+// variable CELLSPE_FSTAGE_VARIANT forces 1, 2 or 3.
+int g_w2048_choice[2][2] = {{0, 0}, {0, 0}};
+std::mutex g_w2048_mu;
+
+template <int FMT, bool PHASE>
+int tune_w2048(const float2* tw, cudaStream_t st)
+{
+    const char* env = getenv("CELLSPE_FSTAGE_VARIANT");
+    if (env && env[0] >= '1' && env[0] <= '0' + W_NVARIANTS) return env[0] - '0';
+    const int S = 64, K = 64;
+    const size_t raw_bytes = (size_t)S * K * 2048 / 4;
+    const size_t out_bytes = (size_t)S * K * 1024 * (FMT == CS_SPECTRA_F32 ? 8 : 4);
+    const size_t ph_bytes = PHASE ? (size_t)S * K * 4 : 0;
+    char* buf = nullptr;
+    if (cudaMalloc(&buf, raw_bytes + out_bytes + 2 * ph_bytes) != cudaSuccess) return 1;
+    cudaMemsetAsync(buf, 0, raw_bytes + out_bytes + 2 * ph_bytes, st);
+    CsFStageArgs a{};
+    a.raw = (const uint8_t*)buf;
+    a.bytes_per_input = raw_bytes / S;
+    a.S = S; a.N = 2048; a.K = K;
+    a.phase0 = PHASE ? (const float*)(buf + raw_bytes + out_bytes) : nullptr;
+    a.dphase = PHASE ? (const float*)(buf + raw_bytes + out_bytes + ph_bytes) : nullptr;
+    a.lut[0] = -3.f; a.lut[1] = -1.f; a.lut[2] = 1.f; a.lut[3] = 3.f;
+    a.format = FMT;
+    a.out = buf + raw_bytes;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int choice = 1;
+    for (int v = 1; v <= W_NVARIANTS; v++) {
+        float total = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(e0, st);
+            int rc = launch_w2048_choice<FMT, PHASE>(v, a, tw, st);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rc) ms = 1e30f;
+            if (rep > 0) total += ms;
+        }
+        if (total < best) { best = total; choice = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    return choice;
 }
 
 template <int FMT, bool PHASE>
@@ -392,12 +539,12 @@ int launch_w2048(const CsFStageArgs& a, cudaStream_t st)
 {
     const float2* tw = cs_twiddles(2048);
     if (!tw) return CS_ERR_ARG;
-    size_t smem = w2048_smem<FMT>();
-    auto kern = k_fx_fstage_w2048<FMT, PHASE>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((a.K + W_G - 1) / W_G, a.S);
-    kern<<<grid, 256, smem, st>>>(a, tw), cs_count_launches(1);
-    return (int)cudaGetLastError();
+    int& choice = g_w2048_choice[FMT == CS_SPECTRA_F16][PHASE ? 1 : 0];
+    if (!choice) {
+        std::lock_guard<std::mutex> lk(g_w2048_mu);
+        if (!choice) choice = tune_w2048<FMT, PHASE>(tw, st);
+    }
+    return launch_w2048_choice<FMT, PHASE>(choice, a, tw, st);
 }
 
 // FP64 delay model (kept in FP64 on the GPU: the fringe phase 2 pi f_LO tau
@@ -447,6 +594,7 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
         return ph ? launch_w2048<CS_SPECTRA_F16, true>(a, st) : launch_w2048<CS_SPECTRA_F16, false>(a, st);
     }
     switch (a.N) {
+        case 512: return dispatch_fstage<256>(a, st);
         case 1024: return dispatch_fstage<512>(a, st);
         case 2048: return dispatch_fstage<1024>(a, st);
         case 4096: return dispatch_fstage<2048>(a, st);

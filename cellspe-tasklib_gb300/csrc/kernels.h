@@ -27,6 +27,9 @@ const float2* cs_twiddles(int n);
 void cs_free_twiddles();
 // Batched forward C2C FFT, n points (32..16384), interleaved complex.
 int cs_cfft_batch(const float2* in, float2* out, int n, int64_t batch, cudaStream_t st);
+// Batched backward C2C FFT (e^{+2 pi i nk/n}, FFTW_BACKWARD, unnormalised)
+// with every output multiplied by `scale`.
+int cs_cfft_inverse_batch(const float2* in, float2* out, int n, int64_t batch, float scale, cudaStream_t st);
 // Batched forward R2C FFT, n real points (64..32768) -> n/2+1 bins.
 int cs_rfft_batch(const float* in, float2* out, int n, int64_t batch, cudaStream_t st);
 

@@ -14,6 +14,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <deque>
+#include <unordered_map>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -357,8 +360,8 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
 {
     if (!p || !raw || !vis) return set_err(CELLSPE_ERR_ARG, "fx: null argument");
     const int S = p->n_inputs, N = p->fft_points, K = p->n_segments, C = N / 2;
-    if (S <= 0 || K <= 0 || !pow2(N) || N < 1024 || N > 32768)
-        return set_err(CELLSPE_ERR_ARG, "fx: need S > 0, K > 0, N a power of two in [1024, 32768]");
+    if (S <= 0 || K <= 0 || !pow2(N) || N < 512 || N > 32768)
+        return set_err(CELLSPE_ERR_ARG, "fx: need S > 0, K > 0, N a power of two in [512, 32768]");
     if (p->bytes_per_input <= 0 || p->bytes_per_input % 16)
         return set_err(CELLSPE_ERR_ARG, "fx: bytes_per_input must be a positive multiple of 16");
     if (!poly && (p->start_sample < 0 || p->start_sample + (long long)K * N > p->bytes_per_input * 4))
@@ -533,6 +536,92 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
         if (rc) j.err = rc;
     }
     return j.finish();
+}
+
+
+// ---------------------------------------------------------------------------
+// correlation service: continuous batching over execution streams
+// ---------------------------------------------------------------------------
+struct SvcJob {
+    long long id = 0;
+    cellspe_fx_params p{};
+    const void* raw = nullptr;
+    const double* poly = nullptr;
+    void* vis = nullptr;
+    long long footprint = 0;
+    std::chrono::steady_clock::time_point t_submit, t_start, t_done;
+    int status = 0;
+    bool done = false;
+};
+
+}  // namespace
+
+struct cellspe_service {
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<SvcJob>> queue;
+    std::unordered_map<long long, std::shared_ptr<SvcJob>> jobs;
+    std::vector<std::thread> workers;
+    std::vector<double> latency_ms, queue_ms;
+    long long budget = 0, in_flight = 0, next_id = 1, completed = 0, failed = 0;
+    int running = 0, max_running = 0;
+    bool stop = false;
+};
+
+namespace {
+
+void service_worker(cellspe_service* sv)
+{
+    Workspace ws;
+    int init = ws.init();
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        // admit the oldest job as soon as its device footprint fits next to the
+        // jobs already running (a lone job is always admitted)
+        sv->cv_work.wait(lk, [&] {
+            if (sv->stop) return true;
+            if (sv->queue.empty()) return false;
+            const auto& h = sv->queue.front();
+            return sv->in_flight == 0 || sv->in_flight + h->footprint <= sv->budget;
+        });
+        if (sv->stop && sv->queue.empty()) break;
+        if (sv->stop) break;
+        std::shared_ptr<SvcJob> j = sv->queue.front();
+        sv->queue.pop_front();
+        sv->in_flight += j->footprint;
+        sv->running++;
+        sv->max_running = std::max(sv->max_running, sv->running);
+        lk.unlock();
+        sv->cv_work.notify_all();
+        j->t_start = std::chrono::steady_clock::now();
+        int rc = init ? init : op_fx(ws, &j->p, j->raw, j->poly, j->vis, true);
+        j->t_done = std::chrono::steady_clock::now();
+        lk.lock();
+        sv->in_flight -= j->footprint;
+        sv->running--;
+        j->status = rc;
+        j->done = true;
+        if (rc) sv->failed++;
+        else {
+            sv->completed++;
+            sv->latency_ms.push_back(std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count());
+            sv->queue_ms.push_back(std::chrono::duration<double, std::milli>(j->t_start - j->t_submit).count());
+        }
+        sv->cv_done.notify_all();
+        sv->cv_work.notify_all();
+    }
+    lk.unlock();
+    ws.destroy();
+}
+
+double percentile(std::vector<double> v, double q)
+{
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    double pos = q * (double)(v.size() - 1);
+    size_t i = (size_t)pos;
+    double f = pos - (double)i;
+    return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -1279,6 +1368,23 @@ int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memo
     return op_fft(*ws, memory == CELLSPE_MEM_HOST, in, out, n, batch, true);
 }
 
+int cellspe_vis_lags(const void* vis, void* lags, long long n_products, int n_channels, double scale, int memory)
+{
+    DIRECT_PROLOGUE
+    if (!vis || !lags || n_products <= 0 || !pow2(n_channels) || n_channels < 16 || n_channels > 16384)
+        return set_err(CELLSPE_ERR_ARG, "vis_lags: need products > 0 and n_channels a power of two in [16, 16384]");
+    const bool host = memory == CELLSPE_MEM_HOST;
+    const size_t bytes = (size_t)n_products * n_channels * 8;
+    Job j(*ws, host);
+    const float2* d_in = (const float2*)j.in(vis, bytes);
+    float2* d_out = (float2*)j.out(lags, bytes, false);
+    if (!j.err) {
+        int rc = map_rc(cs_cfft_inverse_batch(d_in, d_out, n_channels, n_products, (float)scale, ws->stream), "vis_lags");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
 int cellspe_xmac(const void* spectra, int S, int C, int K, void* vis, int accumulate, int memory)
 {
     DIRECT_PROLOGUE
@@ -1320,6 +1426,86 @@ int cellspe_release_workspace(void)
         t_ws.reset();
     }
     return 0;
+}
+
+
+// ===========================================================================
+// exported: correlation service
+// ===========================================================================
+cellspe_service* cellspe_service_create(const cellspe_service_config* cfg)
+{
+    if (ensure_device()) return nullptr;
+    auto* sv = new cellspe_service();
+    long long b = (cfg && cfg->hbm_budget_bytes > 0) ? cfg->hbm_budget_bytes : (long long)(0.8 * (double)budget_bytes() / 0.9);
+    sv->budget = b;
+    int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 8;
+    for (int i = 0; i < n; i++) sv->workers.emplace_back(service_worker, sv);
+    return sv;
+}
+
+int cellspe_service_submit(cellspe_service* sv, const cellspe_fx_params* p, const void* raw, const double* delay_poly,
+                           void* vis, long long* job_id)
+{
+    if (!sv || !p || !raw || !vis || !job_id) return set_err(CELLSPE_ERR_ARG, "service_submit: null argument");
+    auto j = std::make_shared<SvcJob>();
+    j->p = *p;
+    j->raw = raw;
+    j->poly = delay_poly;
+    j->vis = vis;
+    j->footprint = fx_bytes(p, delay_poly != nullptr);
+    if (j->footprint > sv->budget)
+        return set_err(CELLSPE_ERR_NOMEM, "service_submit: job footprint exceeds the service HBM budget");
+    j->t_submit = std::chrono::steady_clock::now();
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        j->id = sv->next_id++;
+        sv->jobs[j->id] = j;
+        sv->queue.push_back(j);
+    }
+    sv->cv_work.notify_all();
+    *job_id = j->id;
+    return 0;
+}
+
+int cellspe_service_wait(cellspe_service* sv, long long job_id, double* latency_ms)
+{
+    if (!sv) return set_err(CELLSPE_ERR_ARG, "service_wait: null service");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->jobs.find(job_id);
+    if (it == sv->jobs.end()) return set_err(CELLSPE_ERR_ARG, "service_wait: unknown job id");
+    std::shared_ptr<SvcJob> j = it->second;
+    sv->cv_done.wait(lk, [&] { return j->done; });
+    sv->jobs.erase(job_id);
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count();
+    return j->status;
+}
+
+int cellspe_service_get_stats(cellspe_service* sv, cellspe_service_stats* out)
+{
+    if (!sv || !out) return CELLSPE_ERR_ARG;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    out->completed = sv->completed;
+    out->failed = sv->failed;
+    out->queued = (long long)sv->queue.size();
+    out->running = sv->running;
+    out->max_running = sv->max_running;
+    out->p50_ms = percentile(sv->latency_ms, 0.50);
+    out->p99_ms = percentile(sv->latency_ms, 0.99);
+    out->p99_queue_ms = percentile(sv->queue_ms, 0.99);
+    out->budget_bytes = sv->budget;
+    return 0;
+}
+
+void cellspe_service_destroy(cellspe_service* sv)
+{
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    for (auto& t : sv->workers) t.join();
+    delete sv;
 }
 
 int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* power, void* pcal_bins, void* pcal_tones)

@@ -107,10 +107,10 @@ CS_DEV uint64_t sw64_desc(uint32_t saddr)
     return d;
 }
 
-// kind::f16 instruction descriptor: D F32, A/B F16, K-major, M=128, N=256.
-constexpr uint32_t make_idesc(bool neg_a)
+// kind::f16 instruction descriptor: D F32, A/B F16, K-major, M=128, N=n (16..256, multiple of 16).
+CS_DEV uint32_t make_idesc(bool neg_a, uint32_t n)
 {
-    return (1u << 4) | (0u << 7) | (0u << 10) | ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((neg_a ? 1u : 0u) << 13) | ((n >> 3) << 17) |
            ((uint32_t)(BM >> 4) << 24);
 }
 
@@ -166,6 +166,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     const int i0 = tile.x, j0 = tile.y;
     const int S = a.S;
     const int nk = (a.K + BK - 1) / BK;
+    // columns this tile needs: j < min(j0 + BN, i0 + BM, S), rounded up to 16
+    const int n_need = min(min(j0 + BN, i0 + BM), S) - j0;
+    const uint32_t n_eff = (uint32_t)((n_need + 15) & ~15);
+    const bool half_b = n_eff <= (uint32_t)BM;      // only the first 128 B rows are loaded
+    const uint32_t stage_tx = half_b ? 4 * A_BYTES : STAGE_BYTES;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -200,14 +205,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 if (!mbar_wait(empty0 + 8 * s, ph ^ 1, ERR_EMPTY_WAIT)) { ok = false; break; }
                 const uint32_t st = sbase + s * STAGE_BYTES;
                 const uint32_t fb = full0 + 8 * s;
-                mbar_expect_tx(fb, STAGE_BYTES);
+                mbar_expect_tx(fb, stage_tx);
                 const int x = kc * BK;
                 tma_load_2d(st, &tmap, x, rowA_re, fb);
                 tma_load_2d(st + A_BYTES, &tmap, x, rowA_im, fb);
                 tma_load_2d(st + 2 * A_BYTES, &tmap, x, rowB_re, fb);
-                tma_load_2d(st + 2 * A_BYTES + A_BYTES, &tmap, x, rowB_re + BM, fb);
                 tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tmap, x, rowB_im, fb);
-                tma_load_2d(st + 2 * A_BYTES + B_BYTES + A_BYTES, &tmap, x, rowB_im + BM, fb);
+                if (!half_b) {
+                    tma_load_2d(st + 2 * A_BYTES + A_BYTES, &tmap, x, rowB_re + BM, fb);
+                    tma_load_2d(st + 2 * A_BYTES + B_BYTES + A_BYTES, &tmap, x, rowB_im + BM, fb);
+                }
                 issued = kc + 1;
             }
             // drain: every stage this thread filled must have landed before the CTA exits
@@ -217,7 +224,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t id_pos = make_idesc(false), id_neg = make_idesc(true);
+            const uint32_t id_pos = make_idesc(false, n_eff), id_neg = make_idesc(true, n_eff);
             const uint32_t d_re = tmem, d_im = tmem + BN;
             bool ok = true;
             for (int kc = 0; kc < nk; kc++) {
@@ -255,32 +262,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
         __syncwarp();
         if (__all_sync(0xffffffffu, ok)) {
             tc_fence_after();
+            // Stage each 32-row x 16-column block through shared memory (the
+            // operand ring is free once the accumulators are final) so that a
+            // store instruction writes two 128-byte runs of one output row.
+            float2* stg = reinterpret_cast<float2*>(smem) + (warp - 2) * 32 * 17;
             const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-            float si = 1.f;
-            if (a.inv_scale && i < S) si = __ldg(a.inv_scale + (int64_t)i * a.C + c);
-            float2* out = a.vis + (int64_t)c * a.P + (int64_t)i * (i + 1) / 2;
-            for (int cb = 0; cb < BN / 16; cb++) {
+            const float si = (a.inv_scale && i < S) ? __ldg(a.inv_scale + (int64_t)i * a.C + c) : 1.f;
+            const int ncb = (int)(n_eff / 16);
+            for (int cb = 0; cb < ncb; cb++) {
                 uint32_t re[16], im[16];
                 tmem_ld16(lane_base + cb * 16, re);
                 tmem_ld16(lane_base + BN + cb * 16, im);
                 tmem_ld_wait();
-                if (i < S) {
 #pragma unroll
-                    for (int jj = 0; jj < 16; jj++) {
+                for (int jj = 0; jj < 16; jj++) {
+                    float f = si;
+                    if (a.inv_scale) {
                         const int j = j0 + cb * 16 + jj;
-                        if (j <= i && j < S) {
-                            float f = si;
-                            if (a.inv_scale) f *= __ldg(a.inv_scale + (int64_t)j * a.C + c);
-                            float2 v = make_float2(__uint_as_float(re[jj]) * f, __uint_as_float(im[jj]) * f);
-                            if (a.accumulate) {
-                                float2 o = out[j];
-                                v.x += o.x;
-                                v.y += o.y;
-                            }
-                            out[j] = v;
+                        f *= (j < S) ? __ldg(a.inv_scale + (int64_t)j * a.C + c) : 0.f;
+                    }
+                    stg[lane * 17 + jj] = make_float2(__uint_as_float(re[jj]) * f, __uint_as_float(im[jj]) * f);
+                }
+                __syncwarp();
+#pragma unroll 4
+                for (int it = 0; it < 16; it++) {
+                    const int rr = 2 * it + (lane >> 4), col = lane & 15;
+                    const int ii = i0 + 32 * q + rr, j = j0 + cb * 16 + col;
+                    if (ii < S && j <= ii) {
+                        float2 v = stg[rr * 17 + col];
+                        float2* o = a.vis + (int64_t)c * a.P + (int64_t)ii * (ii + 1) / 2 + j;
+                        if (a.accumulate) {
+                            const float2 old = *o;
+                            v.x += old.x;
+                            v.y += old.y;
                         }
+                        *o = v;
                     }
                 }
+                __syncwarp();
             }
         }
         tc_fence_before();

@@ -77,6 +77,14 @@ int cellspe_unpack2bit(const void* raw, long long nsamp, int nchan, int format,
 int cellspe_fft_c2c(const void* in, void* out, int n, long long batch, int memory);
 int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memory);
 
+/* ---- XF lag products -------------------------------------------------------
+ * lags[p][m] = scale * sum_c vis[p][c] exp(+2 pi i c m / C): the backward,
+ * unnormalised transform of each product's visibility spectrum, as zerocorr's
+ * FFTW_BACKWARD plan (mark5access examples/zerocorr.c:391, 626-645; lag j is
+ * element j for j >= 0 and j + C for j < 0; scale = 1/#FFTs there).
+ * vis, lags: complex64 [P][C] (baseline-major), C a power of two <= 16384. */
+int cellspe_vis_lags(const void* vis, void* lags, long long n_products, int n_channels, double scale, int memory);
+
 /* ---- K-d: X stage on precomputed spectra ----------------------------------
  * spectra complex64 [C][S][K] (FP32 mode) -> vis complex64 [C][P] (channel-major),
  * V_ij = sum_k X_i conj(X_j), j <= i, p = i(i+1)/2 + j.
@@ -92,7 +100,7 @@ typedef struct { int S, C, K, accumulate; } cellspe_xmac_params;
 /* ---- Full FX correlation: unpack -> FFT -> delay/fringe -> X --------------- */
 typedef struct {
     int    n_inputs;          /* S: stations x polarisations                       */
-    int    fft_points;        /* N: 1024 .. 32768, power of two; C = N/2 channels  */
+    int    fft_points;        /* N: 512 .. 32768, power of two; C = N/2 channels   */
     int    n_segments;        /* K: FFT segments integrated                        */
     int    x_mode;            /* CELLSPE_X_*                                        */
     int    vis_order;         /* CELLSPE_VIS_*                                      */
@@ -123,6 +131,34 @@ long long cellspe_fx_workspace_bytes(const cellspe_fx_params* p);
 int cellspe_fx_correlate_async(const cellspe_fx_params* p, const void* raw, const double* delay_poly,
                                void* vis, void* stream);
 int cellspe_release_workspace(void);
+
+/* ---- Correlation service: continuous batching ----------------------------
+ * Jobs (cellspe_fx_params + buffers) are queued on submit and return at once.
+ * max_streams worker threads, each with its own CUDA stream and device
+ * workspace, take the oldest queued job as soon as its device footprint
+ * (cellspe_fx_workspace_bytes) fits next to the jobs already running under
+ * hbm_budget_bytes, so jobs that arrive while others run are admitted as
+ * memory frees and their work overlaps on the GPU.  Results are identical to
+ * cellspe_fx_correlate on the same job (same kernels, deterministic order).
+ * Buffers must stay valid until cellspe_service_wait returns for the job. */
+typedef struct cellspe_service cellspe_service;
+typedef struct {
+    long long hbm_budget_bytes;   /* 0: 80% of free device memory            */
+    int       max_streams;        /* concurrent jobs (0: 8)                    */
+} cellspe_service_config;
+typedef struct {
+    long long completed, failed, queued;
+    int       running, max_running;
+    double    p50_ms, p99_ms;     /* submit -> done latency of completed jobs */
+    double    p99_queue_ms;       /* submit -> start                          */
+    long long budget_bytes;
+} cellspe_service_stats;
+cellspe_service* cellspe_service_create(const cellspe_service_config* cfg);
+int  cellspe_service_submit(cellspe_service* s, const cellspe_fx_params* p, const void* raw,
+                            const double* delay_poly, void* vis, long long* job_id);
+int  cellspe_service_wait(cellspe_service* s, long long job_id, double* latency_ms);
+int  cellspe_service_get_stats(cellspe_service* s, cellspe_service_stats* out);
+void cellspe_service_destroy(cellspe_service* s);
 
 /* ---- Spectrometer ----------------------------------------------------------
  * Restates TaskCoreIPP::doMaths (TaskCoreIPP.cpp:394-513) on the GPU for every

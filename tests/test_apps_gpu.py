@@ -1,0 +1,60 @@
+"""Entry-point programs: swspectrometer_gpu and minicorrelator_gpu (run as processes)."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+PKG = Path(__file__).resolve().parent.parent / "cellspe-tasklib_gb300"
+
+
+def test_swspectrometer_cli_matches_oracle(cg, orc, tmp_path):
+    import synth
+
+    N, K, fs, nspec, ch = 4096, 8, 32e6, 2, 3
+    words, _ = synth.mark5b_subbands(16, N * K * nspec, fs_hz=fs, seed=31, n_channels=N // 2, pcal_amp=0.2)
+    data = tmp_path / "scan.m5b"
+    words.tofile(data)
+    ini = tmp_path / "spec.ini"
+    ini.write_text(f"""[Spectrometer]
+FFTpoints = {N}
+FFTIntegrationTimeSec = {K * N / fs}
+FFToverlapFactor = 2
+WindowType = Cosine2
+BandwidthHz = {fs / 2}
+SourceFormat = Mark5B-1024-16-2
+BitsPerSample = 2
+SourceChannels = 16
+UseFile1Channel = {ch}
+ExtractPCal = 1
+PCalOffsetHz = 0
+BaseFilename1 = {tmp_path}/out
+""")
+    r = subprocess.run([str(PKG / "swspectrometer_gpu"), str(ini), str(data)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(tmp_path / "out_swspec.bin", np.float32).reshape(nspec, N // 2 + 1)
+    bins = np.fromfile(tmp_path / "out_pcal.bin", np.complex64).reshape(nspec, 32)
+    planes = orc.unpack2bit(words.view(np.uint8), N * K * nspec, 16, orc.MARK5B_LUT)
+    ref, ref_b = orc.spectrometer(planes[ch - 1], N, 2, 2, K, 32, 32, 0.0, fs)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+    assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < 1e-5
+
+
+def test_minicorrelator_cli_matches_oracle(cg, orc):
+    r = subprocess.run([str(PKG / "minicorrelator_gpu"), "3", "8"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "Gbit/s" in r.stdout
+    lines = [l for l in r.stdout.splitlines() if l.startswith(("auto", "baseline"))]
+    assert len(lines) == 6
+    # recompute the last integration of products (1,0) with the oracle
+    S, N, raw_bytes, nint = 3, 1024, 256 * 16384, 8
+    K = raw_bytes * 4 // N // nint
+    raw = np.array([[(17 * i + 3 * j) % 256 for j in range(raw_bytes)] for i in range(S)], dtype=np.uint8)
+    ref = orc.fx_fp32(raw, S, N, K, start_sample=(nint - 1) * K * N)
+    line = [l for l in lines if "1-0" in l][0]
+    nums = [float(x) for x in re.findall(r"[-+]?\d[\d.e+-]*", line.split(":")[1])]
+    v = ref[orc.tri_index(1, 0)]
+    assert np.allclose(nums[:4], v.real[:4], rtol=1e-4, atol=1e-3)
+    assert np.allclose(nums[4:8], v.imag[:4], rtol=1e-4, atol=1e-3)

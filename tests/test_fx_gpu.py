@@ -10,7 +10,8 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("S,N,K", [(2, 1024, 64), (4, 2048, 40), (3, 4096, 9), (5, 8192, 4), (2, 32768, 2)])
+@pytest.mark.parametrize("S,N,K", [(3, 512, 40), (2, 1024, 64), (4, 2048, 40), (3, 4096, 9), (5, 8192, 4),
+                                   (2, 32768, 2), (3, 2048, 13)])
 def test_fx_fp32_vs_cpu_path(cg, orc, S, N, K):
     import synth
 
@@ -112,3 +113,20 @@ def test_fx_rejects_bad_jobs(cg):
         assert e.value.code == cg.ERR_NOMEM
     finally:
         cg.lib().cellspe_set_hbm_budget(0)
+
+
+def test_xf_lags_match_backward_fft(cg, orc):
+    """zerocorr lags (examples/zerocorr.c:391, 626-645): FFTW_BACKWARD of the visibilities, scaled 1/n."""
+    import synth
+
+    S, N, K = 2, 1024, 512
+    raw = synth.stations_offset_binary(S, N * K, rho=0.2, lags=[0, 5], seed=21)
+    vis = np.zeros((3, N // 2), np.complex64)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_BASELINE_MAJOR), raw, vis)
+    lags = np.zeros_like(vis)
+    cg.vis_lags(vis, lags, scale=1.0 / K)
+    ref = np.fft.ifft(vis.astype(np.complex128), axis=1) * (N // 2) / K
+    assert np.linalg.norm(lags - ref) / np.linalg.norm(ref) < 1e-5
+    # the 5-sample lag of station 1 appears at channel-lag index 5 (x_1(t) = c(t-5))
+    cross = lags[orc.tri_index(1, 0)]
+    assert int(np.argmax(np.abs(cross))) in (5 // 2, 5 // 2 + 1, (N // 2) - 5 // 2)
