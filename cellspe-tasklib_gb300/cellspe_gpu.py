@@ -27,7 +27,8 @@ LEVELS_MARK5B, LEVELS_TWOBIT, LEVELS_OFFSET_BINARY = 0, 1, 2
 UNPACK_MSB_FIRST = 0x100
 X_FP32, X_TC_FP16 = 0, 1
 VIS_CHANNEL_MAJOR, VIS_BASELINE_MAJOR = 0, 1
-SPEC_INTERLEAVED, SPEC_PLANES = 0, 1
+SPEC_INTERLEAVED, SPEC_PLANES, SPEC_MARK5B_FRAMED = 0, 1, 2
+MARK5B_FRAME, MARK5B_PAYLOAD = 10016, 10000
 
 TASK_INCOMPLETE, TASK_OK, TASK_GENERICERROR, TASK_UNKOWNCOMMAND = 0xFFFF, 0, 1, 2
 TASK_FLAG_DEVPTR = 0x40000000
@@ -99,11 +100,17 @@ class ServiceStats(ctypes.Structure):
                 ("p99_ms", ctypes.c_double), ("p99_queue_ms", ctypes.c_double), ("budget_bytes", ctypes.c_longlong)]
 
 
+class Mark5bInfo(ctypes.Structure):
+    _fields_ = [("first_frame_offset", ctypes.c_longlong), ("frames", ctypes.c_longlong),
+                ("good_samples", ctypes.c_longlong), ("mjd", ctypes.c_int), ("seconds", ctypes.c_int),
+                ("frame_number", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
 class XmacParams(ctypes.Structure):
     _fields_ = [("S", ctypes.c_int), ("C", ctypes.c_int), ("K", ctypes.c_int), ("accumulate", ctypes.c_int)]
 
 
-assert ctypes.sizeof(FxParams) == 80 and ctypes.sizeof(SpecParams) == 88
+assert ctypes.sizeof(FxParams) == 80 and ctypes.sizeof(SpecParams) == 88 and ctypes.sizeof(Mark5bInfo) == 40
 
 
 # ---- library loading ----------------------------------------------------------
@@ -153,6 +160,8 @@ def lib() -> ctypes.CDLL:
             "cellspe_spectrometer": ([V, V, V, V, V], I),
             "cellspe_spectrometer_workspace_bytes": ([V], LL),
             "cellspe_spectrometer_noalloc": ([V, V, V, V, V, V], I),
+            "cellspe_mark5b_decode": ([V, LL, I, LL, V, I, V], I),
+            "cellspe_mark5b_deframe": ([V, LL, I, LL, V, V, I, V], I),
             "cellspe_service_create": ([V], V),
             "cellspe_service_submit": ([V, V, V, V, V, ctypes.POINTER(ctypes.c_longlong)], I),
             "cellspe_service_wait": ([V, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)], I),
@@ -306,6 +315,27 @@ def spectrometer(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None
                                       _ptr(pcal_bins)[0] if pcal_bins is not None else None,
                                       _ptr(pcal_tones)[0] if pcal_tones is not None else None))
     return power
+
+
+def mark5b_decode(framed, nchan: int, nsamp: int, out) -> Mark5bInfo:
+    """cellspe_mark5b_decode: framed Mark5B bytes -> out[nchan][nsamp] float32 (0.0 where blanked)."""
+    info = Mark5bInfo()
+    nbytes = framed.numel() if _is_torch_cuda(framed) else framed.size
+    _check(lib().cellspe_mark5b_decode(_ptr(framed)[0], nbytes, nchan, nsamp, _ptr(out)[0], _mem(framed, out),
+                                       ctypes.byref(info)))
+    return info
+
+
+def mark5b_deframe(framed, nchan: int, frames: int = 0, payload=None, valid_mask=None) -> Mark5bInfo:
+    """cellspe_mark5b_deframe: payload bytes back to back (+ validity bit per sample time).
+    With payload None only the frame search runs (info.frames tells the size)."""
+    info = Mark5bInfo()
+    nbytes = framed.numel() if _is_torch_cuda(framed) else framed.size
+    _check(lib().cellspe_mark5b_deframe(_ptr(framed)[0], nbytes, nchan, frames,
+                                        _ptr(payload)[0] if payload is not None else None,
+                                        _ptr(valid_mask)[0] if valid_mask is not None else None,
+                                        _mem(framed, payload, valid_mask), ctypes.byref(info)))
+    return info
 
 
 def spectrometer_noalloc(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None, stream: int = 0):

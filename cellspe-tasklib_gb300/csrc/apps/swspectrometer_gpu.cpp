@@ -19,7 +19,10 @@
 // Differences from the reference: a zero PCalOffsetHz uses the comb period as
 // rotator length (the reference divides by zero in Helpers::gcd), and the
 // data of one integration period are read per GPU call instead of buffers
-// sized by MaxSourceBufferMB.
+// sized by MaxSourceBufferMB.  The phase-cal windows therefore match a
+// reference run whose core buffers hold one spectrum each: the reference's
+// FFT count runs on across the spectra of one buffer, so with several spectra
+// per buffer and FFToverlapFactor > 1 its later spectra fold other windows.
 #include "../../../include/cellspe_gpu.h"
 
 #include <algorithm>

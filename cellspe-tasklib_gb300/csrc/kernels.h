@@ -98,9 +98,27 @@ struct CsSpecArgs {
     const float* win_table;     // window, N entries
     const float2* rot_table;    // pcal rotator, rotatorlen entries
     int ffts_per_chunk;         // FFTs per partial spectrum (0: default)
+    const uint32_t* valid_mask; // bit t: sample time t of the planes is data (null: all data)
 };
 int64_t cs_spectrometer_scratch_floats(const CsSpecArgs& a);
 int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st);
+
+// mark5b.cu (framed Mark5B input) ----------------------------------------
+// Frame search + per-frame valid byte ranges (fill-pattern blanking); the
+// offset of the first frame stays on the device (no frame found: >= 1 MiB).
+int cs_m5b_locate(const uint8_t* framed, int64_t bytes, int* d_offset, int2* ranges, int64_t nframes, cudaStream_t st);
+// mark5_stream_decode: nsamp samples per channel into nch float planes,
+// unblanked count added to *d_good (cleared first).
+int cs_m5b_decode(const uint8_t* framed, int64_t bytes, const int* d_offset, const int2* ranges, int nch, int64_t nsamp,
+                  const float lut[4], float* out, unsigned long long* d_good, cudaStream_t st);
+// Payload bytes back to back (nframes * 10000) and, if mask != null, one
+// validity bit per sample time.
+int cs_m5b_deframe(const uint8_t* framed, int64_t bytes, const int* d_offset, const int2* ranges, int64_t nframes,
+                   int nch, uint8_t* payload, uint32_t* mask, cudaStream_t st);
+// Per-channel 2-bit planes ([nch][ngroups] words of 16 samples) plus the
+// validity mask (ceil(ngroups/2) words), straight from the framed bytes.
+int cs_m5b_planes(const uint8_t* framed, int64_t bytes, const int* d_offset, const int2* ranges, int64_t nframes,
+                  int nch, int64_t ngroups, uint32_t* planes, uint32_t* mask, cudaStream_t st);
 
 // dsp.cu (task-API vector primitives) ---------------------------------------
 int cs_cmac(const float2* a, const float2* b, float2* acc, int64_t n, int conj_b, cudaStream_t st);

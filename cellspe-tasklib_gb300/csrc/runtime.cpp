@@ -475,6 +475,18 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     return rc;
 }
 
+constexpr long long M5B_FRAME = 10016, M5B_PAYLOAD = 10000;
+
+// Sample-time groups of 16 per channel plane for a framed Mark5B buffer: every
+// sample time of the frames that fit, rounded up to 64 so each plane is a
+// multiple of 16 bytes.
+long long m5b_groups(long long raw_bytes, int nch)
+{
+    const long long spf = M5B_PAYLOAD / (nch / 4);
+    const long long nsamp = (raw_bytes / M5B_FRAME) * spf;
+    return ((nsamp + 63) / 64) * 4;
+}
+
 long long spec_bytes(const cellspe_spec_params* p)
 {
     CsSpecArgs a{};
@@ -484,6 +496,10 @@ long long spec_bytes(const cellspe_spec_params* p)
     bool host = p->memory == CELLSPE_MEM_HOST;
     if (host) b += align256(p->raw_bytes);
     if (p->input_layout == CELLSPE_SPEC_INTERLEAVED && p->n_subbands > 1) b += align256(p->raw_bytes);
+    if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED) {
+        const long long g = m5b_groups(p->raw_bytes, std::max(p->n_subbands, 4));
+        b += align256(g * 4 * p->n_subbands) + align256((g + 1) / 2 * 4) + align256(p->raw_bytes / M5B_FRAME * 8) + 256;
+    }
     long long rows = (long long)p->n_subbands * p->n_spectra;
     if (host) b += align256(rows * (p->fft_points / 2 + 1) * 4) + 2 * align256(rows * std::max(p->pcal_tonebins, p->pcal_ntones) * 8);
     return b;
@@ -497,7 +513,18 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
     if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16)) return set_err(CELLSPE_ERR_ARG, "spectrometer: n_subbands must be 1, 4, 8 or 16");
     if (!pow2(p->fft_points) || p->fft_points < 1024 || p->fft_points > 65536)
         return set_err(CELLSPE_ERR_ARG, "spectrometer: fft_points must be a power of two in [1024, 65536]");
-    if (p->raw_bytes <= 0 || p->raw_bytes % (16 * nsub)) return set_err(CELLSPE_ERR_ARG, "spectrometer: raw_bytes must be a multiple of 16*n_subbands");
+    const bool framed = p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED;
+    if (framed) {
+        if (nsub == 1) return set_err(CELLSPE_ERR_ARG, "spectrometer: framed Mark5B input needs 4, 8 or 16 subbands");
+        if (p->raw_bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, "spectrometer: framed input shorter than two frames");
+        const long long avail = (p->raw_bytes / M5B_FRAME) * (M5B_PAYLOAD / (nsub / 4));
+        if ((long long)p->n_spectra * p->ffts_per_spectrum * p->fft_points > avail)
+            return set_err(CELLSPE_ERR_ARG, "spectrometer: spectra need more samples than the frames hold");
+    } else if (p->input_layout != CELLSPE_SPEC_INTERLEAVED && p->input_layout != CELLSPE_SPEC_PLANES) {
+        return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown input_layout");
+    } else if (p->raw_bytes <= 0 || p->raw_bytes % (16 * nsub)) {
+        return set_err(CELLSPE_ERR_ARG, "spectrometer: raw_bytes must be a multiple of 16*n_subbands");
+    }
     if (p->pcal_tonebins > 0 && !pcal_bins) return set_err(CELLSPE_ERR_ARG, "spectrometer: pcal enabled without pcal_bins");
     float lut[4];
     if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown level table");
@@ -507,9 +534,26 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
     const bool host = p->memory == CELLSPE_MEM_HOST;
     Job j(ws, host);
     const uint8_t* d_raw = (const uint8_t*)j.in(raw, (size_t)p->raw_bytes);
-    const long long bytes_per_sub = p->raw_bytes / nsub;
+    long long bytes_per_sub = p->raw_bytes / nsub;
     const uint8_t* planes = d_raw;
-    if (p->input_layout == CELLSPE_SPEC_INTERLEAVED && nsub > 1) {
+    const uint32_t* vmask = nullptr;
+    if (framed) {
+        const long long nframes = p->raw_bytes / M5B_FRAME, groups = m5b_groups(p->raw_bytes, nsub);
+        void* pl = j.scratch((size_t)(groups * 4 * nsub));
+        void* mk = j.scratch((size_t)((groups + 1) / 2 * 4));
+        void* rg = j.scratch((size_t)(nframes * 8));
+        void* off = j.scratch(sizeof(int));
+        if (!j.err) {
+            int rc = map_rc(cs_m5b_locate(d_raw, p->raw_bytes, (int*)off, (int2*)rg, nframes, ws.stream), "frame search");
+            if (!rc)
+                rc = map_rc(cs_m5b_planes(d_raw, p->raw_bytes, (const int*)off, (const int2*)rg, nframes, nsub, groups,
+                                          (uint32_t*)pl, (uint32_t*)mk, ws.stream), "deframe");
+            if (rc) j.err = rc;
+        }
+        planes = (const uint8_t*)pl;
+        vmask = (const uint32_t*)mk;
+        bytes_per_sub = groups * 4;
+    } else if (p->input_layout == CELLSPE_SPEC_INTERLEAVED && nsub > 1) {
         void* pl = j.scratch((size_t)p->raw_bytes);
         if (!j.err) {
             long long nsamp = p->raw_bytes * 4 / nsub;
@@ -519,7 +563,7 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
         planes = (const uint8_t*)pl;
     }
     CsSpecArgs a{};
-    a.planes = planes; a.bytes_per_sub = bytes_per_sub; a.nsub = nsub; a.N = p->fft_points;
+    a.planes = planes; a.bytes_per_sub = bytes_per_sub; a.nsub = nsub; a.N = p->fft_points; a.valid_mask = vmask;
     a.overlap = p->overlap; a.window = p->window; a.ffts_per_spectrum = p->ffts_per_spectrum; a.nspec = p->n_spectra;
     std::memcpy(a.lut, lut, sizeof lut);
     a.tonebins = p->pcal_tonebins; a.rotatorlen = p->pcal_rotatorlen; a.ntones = p->pcal_ntones;
@@ -542,6 +586,136 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
 // ---------------------------------------------------------------------------
 // correlation service: continuous batching over execution streams
 // ---------------------------------------------------------------------------
+// ---- framed Mark5B ----------------------------------------------------------
+// Header fields as FileSource::locateFirstHeader (FileSource.cpp:330-333) and
+// the mark5access frame-number field (bits 0..14 of header word 1).
+void m5b_header_info(const uint8_t h[16], cellspe_mark5b_info* info)
+{
+    info->mjd = 56000 + (h[11] >> 4) * 100 + (h[11] & 15) * 10 + (h[10] >> 4);
+    info->seconds = (h[10] & 15) * 10000 + (h[9] >> 4) * 1000 + (h[9] & 15) * 100 + (h[8] >> 4) * 10 + (h[8] & 15);
+    info->frame_number = h[4] | ((h[5] & 0x7f) << 8);
+}
+
+// Stages the framed bytes, finds the first frame and the valid ranges of
+// every frame, and brings the frame offset back (the callers need the frame
+// count on the host).  Fills info except good_samples.
+struct M5bLocated {
+    const uint8_t* d_framed = nullptr;
+    int* d_off = nullptr;
+    int2* d_ranges = nullptr;
+    long long off = -1, frames = 0;
+};
+
+int m5b_locate(Workspace& ws, Job& j, const void* framed, long long bytes, M5bLocated& L, cellspe_mark5b_info* info)
+{
+    const long long nmax = bytes / M5B_FRAME;
+    L.d_framed = (const uint8_t*)j.in(framed, (size_t)bytes);
+    L.d_off = (int*)j.scratch(sizeof(int));
+    L.d_ranges = (int2*)j.scratch((size_t)nmax * sizeof(int2));
+    if (j.err) return j.err;
+    int rc = map_rc(cs_m5b_locate(L.d_framed, bytes, L.d_off, L.d_ranges, nmax, ws.stream), "frame search");
+    if (rc) return rc;
+    int off = 0;
+    cudaError_t e = cudaMemcpyAsync(&off, L.d_off, sizeof off, cudaMemcpyDeviceToHost, ws.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ws.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "frame search");
+    if (off < 0 || off >= (1 << 20)) return set_err(CELLSPE_ERR_ARG, "mark5b: no frame found in the first MiB");
+    L.off = off;
+    L.frames = (bytes - off) / M5B_FRAME;
+    if (info) {
+        uint8_t h[16];
+        if (j.host) std::memcpy(h, (const uint8_t*)framed + off, 16);
+        else {
+            e = cudaMemcpyAsync(h, L.d_framed + off, 16, cudaMemcpyDeviceToHost, ws.stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ws.stream);
+            if (e != cudaSuccess) return cuda_fail(e, "header read");
+        }
+        info->first_frame_offset = off;
+        info->frames = L.frames;
+        info->good_samples = 0;
+        m5b_header_info(h, info);
+        info->reserved = 0;
+    }
+    return 0;
+}
+
+int m5b_check(const void* framed, long long bytes, int nchan, const char* who)
+{
+    if (!framed) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": null input");
+    if (!(nchan == 4 || nchan == 8 || nchan == 16))
+        return set_err(CELLSPE_ERR_ARG, std::string(who) + ": nchan must be 4, 8 or 16 (2-bit Mark5B)");
+    if (bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": fewer than two frames of input");
+    return 0;
+}
+
+int op_mark5b_decode(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, long long nsamp,
+                     float* out, cellspe_mark5b_info* info)
+{
+    if (int rc = m5b_check(framed, bytes, nchan, "mark5b_decode")) return rc;
+    if (!out || nsamp <= 0) return set_err(CELLSPE_ERR_ARG, "mark5b_decode: bad output");
+    const long long need = (host ? align256(bytes) + align256(nsamp * nchan * 4) : 0) + align256(bytes / M5B_FRAME * 8) + 512;
+    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "mark5b_decode: job exceeds the device memory budget");
+    cellspe_mark5b_info tmp{};
+    if (!info) info = &tmp;
+    Job j(ws, host);
+    M5bLocated L;
+    int rc = m5b_locate(ws, j, framed, bytes, L, info);
+    if (rc) { j.err = rc; return j.finish(); }
+    const long long spf = M5B_PAYLOAD / (nchan / 4);
+    const bool runs_out = nsamp >= L.frames * spf;
+    // past the last frame nothing is written: keep the caller's values there
+    float* d_out = (float*)j.out(out, (size_t)(nsamp * nchan * 4), runs_out);
+    auto* d_good = (unsigned long long*)j.scratch(sizeof(unsigned long long));
+    unsigned long long good = 0;
+    if (!j.err) {
+        float lut[4];
+        pick_levels(CELLSPE_LEVELS_MARK5B, nullptr, lut);
+        rc = map_rc(cs_m5b_decode(L.d_framed, bytes, L.d_off, L.d_ranges, nchan, nsamp, lut, d_out, d_good, ws.stream),
+                    "mark5b decode");
+        if (!rc) {
+            cudaError_t e = cudaMemcpyAsync(&good, d_good, sizeof good, cudaMemcpyDeviceToHost, ws.stream);
+            if (e != cudaSuccess) rc = cuda_fail(e, "mark5b decode");
+        }
+        if (rc) j.err = rc;
+    }
+    rc = j.finish();
+    if (!rc) info->good_samples = runs_out ? -1 : (long long)good;
+    return rc;
+}
+
+int op_mark5b_deframe(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, long long frames,
+                      void* payload, unsigned* mask, cellspe_mark5b_info* info)
+{
+    if (int rc = m5b_check(framed, bytes, nchan, "mark5b_deframe")) return rc;
+    if (frames < 0) return set_err(CELLSPE_ERR_ARG, "mark5b_deframe: negative frame count");
+    const long long nmax = bytes / M5B_FRAME, spf = M5B_PAYLOAD / (nchan / 4);
+    const long long mwords_max = (nmax * spf + 31) / 32;
+    const long long need = (host ? align256(bytes) + align256(nmax * M5B_PAYLOAD) + align256(mwords_max * 4) : 0) +
+                           align256(nmax * 8) + 256;
+    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "mark5b_deframe: job exceeds the device memory budget");
+    cellspe_mark5b_info tmp{};
+    if (!info) info = &tmp;
+    Job j(ws, host);
+    M5bLocated L;
+    int rc = m5b_locate(ws, j, framed, bytes, L, info);
+    if (rc) { j.err = rc; return j.finish(); }
+    if (frames == 0) frames = L.frames;
+    if (frames > L.frames) {
+        j.err = set_err(CELLSPE_ERR_ARG, "mark5b_deframe: fewer complete frames in the buffer than requested");
+        return j.finish();
+    }
+    if (payload) {
+        void* d_pay = j.out(payload, (size_t)(frames * M5B_PAYLOAD), false);
+        void* d_mask = mask ? j.out(mask, (size_t)((frames * spf + 31) / 32 * 4), false) : nullptr;
+        if (!j.err) {
+            rc = map_rc(cs_m5b_deframe(L.d_framed, bytes, L.d_off, L.d_ranges, frames, nchan, (uint8_t*)d_pay,
+                                       (uint32_t*)d_mask, ws.stream), "deframe");
+            if (rc) j.err = rc;
+        }
+    }
+    return j.finish();
+}
+
 struct SvcJob {
     long long id = 0;
     cellspe_fx_params p{};
@@ -1515,5 +1689,19 @@ int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* p
 }
 
 long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p) { return p ? spec_bytes(p) : -1; }
+
+int cellspe_mark5b_decode(const void* framed, long long bytes, int nchan, long long nsamp, float* out, int memory,
+                          cellspe_mark5b_info* info)
+{
+    DIRECT_PROLOGUE
+    return op_mark5b_decode(*ws, memory == CELLSPE_MEM_HOST, framed, bytes, nchan, nsamp, out, info);
+}
+
+int cellspe_mark5b_deframe(const void* framed, long long bytes, int nchan, long long frames, void* payload,
+                           unsigned int* valid_mask, int memory, cellspe_mark5b_info* info)
+{
+    DIRECT_PROLOGUE
+    return op_mark5b_deframe(*ws, memory == CELLSPE_MEM_HOST, framed, bytes, nchan, frames, payload, valid_mask, info);
+}
 
 }  // extern "C"

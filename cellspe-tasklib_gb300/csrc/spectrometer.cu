@@ -95,6 +95,19 @@ CS_DEV float lut_pick4(const float (&l)[4], unsigned c)
     return (c & 2u) ? hi : lo;
 }
 
+// Samples s and s+1 (s even) from a plane word; blanked samples (their bit
+// in the validity mask clear) are 0.0, as mark5access decodes them.
+CS_DEV float2 sample_pair(const float (&lut)[4], uint32_t w, int f, const uint32_t* __restrict__ vmask, int64_t s)
+{
+    float x0 = lut_pick4(lut, (w >> (2 * f)) & 3u), x1 = lut_pick4(lut, (w >> (2 * f + 2)) & 3u);
+    if (vmask) {
+        const uint32_t m = __ldg(vmask + (s >> 5)) >> (s & 31);
+        x0 = (m & 1u) ? x0 : 0.f;
+        x1 = (m & 2u) ? x1 : 0.f;
+    }
+    return make_float2(x0, x1);
+}
+
 template <int MC, int P>
 __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const float2* __restrict__ tw,
                                                             const float* __restrict__ win, int nchunk, int ch)
@@ -118,6 +131,7 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const
     const int hop = N / a.overlap;
     const uint32_t* plane = reinterpret_cast<const uint32_t*>(a.planes + (int64_t)sub * a.bytes_per_sub);
     const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
+    const uint32_t* vmask = a.valid_mask;
 
     for (int i = threadIdx.x; i < GROUPS * NACC; i += C::NT) acc_all[i] = 0.f;
     __syncthreads();
@@ -136,16 +150,16 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const
             if constexpr (P == 1) {
                 uint32_t w = __ldg(wsrc + (2 * n >> 4));
                 int f = (2 * n) & 15;
-                v[r] = make_float2(lut_pick4(lut, (w >> (2 * f)) & 3u) * __ldg(win + 2 * n),
-                                   lut_pick4(lut, (w >> (2 * f + 2)) & 3u) * __ldg(win + 2 * n + 1));
+                const float2 x = sample_pair(lut, w, f, vmask, start + 2 * n);
+                v[r] = make_float2(x.x * __ldg(win + 2 * n), x.y * __ldg(win + 2 * n + 1));
             } else {
                 const int n2 = n + MC;
                 uint32_t w1 = __ldg(wsrc + (2 * n >> 4)), w2 = __ldg(wsrc + (2 * n2 >> 4));
                 int f1 = (2 * n) & 15, f2 = (2 * n2) & 15;
-                float2 z1 = make_float2(lut_pick4(lut, (w1 >> (2 * f1)) & 3u) * __ldg(win + 2 * n),
-                                        lut_pick4(lut, (w1 >> (2 * f1 + 2)) & 3u) * __ldg(win + 2 * n + 1));
-                float2 z2 = make_float2(lut_pick4(lut, (w2 >> (2 * f2)) & 3u) * __ldg(win + 2 * n2),
-                                        lut_pick4(lut, (w2 >> (2 * f2 + 2)) & 3u) * __ldg(win + 2 * n2 + 1));
+                const float2 x1 = sample_pair(lut, w1, f1, vmask, start + 2 * n);
+                const float2 x2 = sample_pair(lut, w2, f2, vmask, start + 2 * n2);
+                float2 z1 = make_float2(x1.x * __ldg(win + 2 * n), x1.y * __ldg(win + 2 * n + 1));
+                float2 z2 = make_float2(x2.x * __ldg(win + 2 * n2), x2.y * __ldg(win + 2 * n2 + 1));
                 v[r] = p ? cmul(csub(z1, z2), twiddle(tw, 2 * n)) : cadd(z1, z2);
             }
         }
@@ -193,26 +207,38 @@ __global__ void k_spec_reduce(const float* __restrict__ partial, float* __restri
 }
 
 // PCal fold: thread-private accumulators in shared memory, [bin][thread].
+// TaskCoreIPP::doMaths folds the overlapped FFT windows whose running FFT
+// count is a multiple of the overlap factor (TaskCoreIPP.cpp:414-418), and the
+// count runs on across the spectra of one call (it starts at 0 once,
+// :358).  Spectrum s therefore folds windows j = j0, j0+ov, ... < novl with
+// j0 = (-s*novl) mod ov: cnt back-to-back stretches of N samples starting
+// j0*hop samples into the spectrum.  The rotator index restarts at every
+// window, which is the index relative to the fold start because N % L == 0.
 __global__ void k_pcal_fold(const uint8_t* __restrict__ planes, int64_t bytes_per_sub, int nspec, int64_t samp_per_spec,
-                            int T, int L, const float2* __restrict__ rot, float l0, float l1, float l2, float l3,
-                            float2* __restrict__ partial, int nblk_per_row)
+                            int N, int ov, int novl, int T, int L, const float2* __restrict__ rot, float l0, float l1,
+                            float l2, float l3, const uint32_t* __restrict__ vmask, float2* __restrict__ partial,
+                            int nblk_per_row)
 {
     extern __shared__ float2 pacc[];                 // [T][blockDim]
     const int row = blockIdx.y, sub = row / nspec, spec = row % nspec;
     const int nt = blockDim.x, tid = threadIdx.x;
     for (int b = 0; b < T; b++) pacc[b * nt + tid] = make_float2(0.f, 0.f);
     const uint32_t* plane = reinterpret_cast<const uint32_t*>(planes + (int64_t)sub * bytes_per_sub);
-    const int64_t w_begin = (int64_t)spec * samp_per_spec / 16;
-    const int64_t nwords = samp_per_spec / 16;
+    const int j0 = (ov - (int)(((int64_t)spec * novl) % ov)) % ov;
+    const int cnt = j0 < novl ? (novl - 1 - j0) / ov + 1 : 0;
+    const int64_t w_begin = ((int64_t)spec * samp_per_spec + (int64_t)j0 * (N / ov)) / 16;
+    const int64_t nwords = (int64_t)cnt * N / 16;
     const float lut[4] = {l0, l1, l2, l3};
     for (int64_t w = (int64_t)blockIdx.x * nt + tid; w < nwords; w += (int64_t)nblk_per_row * nt) {
         uint32_t word = __ldg(plane + w_begin + w);
-        int64_t n0 = w * 16;                         // sample index relative to spectrum start
+        const int64_t wg = w_begin + w;
+        const uint32_t valid = vmask ? __ldg(vmask + (wg >> 1)) >> ((wg & 1) * 16) : 0xffffu;
+        int64_t n0 = w * 16;                         // sample index relative to the fold start
 #pragma unroll
         for (int j = 0; j < 16; j++) {
             int64_t n = n0 + j;
             int li = (int)(n % L);
-            float x = lut_pick4(lut, (word >> (2 * j)) & 3u);
+            float x = (valid >> j) & 1u ? lut_pick4(lut, (word >> (2 * j)) & 3u) : 0.f;
             float2 r = __ldg(rot + li);
             float2& slot = pacc[(li % T) * nt + tid];
             slot.x += x * r.x;
@@ -333,8 +359,9 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
         int nt = PCAL_THREADS;
         size_t smem = (size_t)T * nt * sizeof(float2);
         CS_CUDA_TRY(cudaFuncSetAttribute(k_pcal_fold, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_pcal_fold<<<dim3(PCAL_BLOCKS, rows), nt, smem, st>>>(a.planes, a.bytes_per_sub, a.nspec, samp_per_spec, T, L,
-                                                               rot, a.lut[0], a.lut[1], a.lut[2], a.lut[3], pp,
+        k_pcal_fold<<<dim3(PCAL_BLOCKS, rows), nt, smem, st>>>(a.planes, a.bytes_per_sub, a.nspec, samp_per_spec, a.N,
+                                                               a.overlap, novl, T, L, rot, a.lut[0], a.lut[1], a.lut[2], a.lut[3],
+                                                               a.valid_mask, pp,
                                                                PCAL_BLOCKS), cs_count_launches(1);
         CS_CUDA_TRY(cudaGetLastError());
         k_pcal_reduce<<<(rows + 63) / 64, 64, 0, st>>>(pp, rows, PCAL_BLOCKS, T, a.ntones, a.pcal_bins, a.pcal_tones), cs_count_launches(1);

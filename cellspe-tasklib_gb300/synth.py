@@ -14,6 +14,10 @@ it.  These generators produce the inputs of the benchmark configurations:
 * ``device_stations`` -- the same statistics as stations_offset_binary,
   generated on the GPU with torch (for the 512-input configuration whose
   4.3 G samples would take minutes on the host).
+* ``mark5b_frames`` / ``mark5b_fill`` -- a payload byte stream wrapped into
+  Mark5B frames (16-byte header + 10000-byte payload) and fill-pattern
+  (0x11223344) zones written over parts of payloads, the way a recorder marks
+  missing data.
 """
 from __future__ import annotations
 
@@ -111,3 +115,47 @@ def device_stations(S: int, T: int, rho: float, seed: int, device="cuda", chunk:
             packed = (codes << shifts).sum(dim=-1, dtype=torch.uint8)
             out[s0:s1, t0 // 4 : (t0 + chunk) // 4] = packed
     return out
+
+
+MARK5B_FRAME = 10016
+MARK5B_PAYLOAD = 10000
+
+
+def _bcd(v: int, digits: int) -> int:
+    out = 0
+    for d in range(digits):
+        out |= (v % 10) << (4 * d)
+        v //= 10
+    return out
+
+
+def mark5b_frames(payload: np.ndarray, prefix: int = 0, first_frame: int = 0, seconds: int = 43210,
+                  mjd_digits: int = 789, frames_per_second: int = 6400) -> np.ndarray:
+    """Wrap payload bytes (a multiple of 10000) into Mark5B frames.
+
+    Header words (little-endian): sync 0xABADDEED; frame number within the
+    second in bits 0..14 of word 1; BCD time code JJJSSSSS in word 2 (last three
+    MJD digits, seconds of day); word 3 zero.  ``prefix`` zero bytes precede the
+    first frame.
+    """
+    payload = np.ascontiguousarray(payload, np.uint8).reshape(-1, MARK5B_PAYLOAD)
+    nf = payload.shape[0]
+    frames = np.zeros((nf, MARK5B_FRAME), np.uint8)
+    hdr = np.zeros((nf, 4), np.uint32)
+    n = first_frame + np.arange(nf)
+    hdr[:, 0] = 0xABADDEED
+    hdr[:, 1] = (n % frames_per_second).astype(np.uint32) & 0x7FFF
+    for f in range(nf):
+        sec = seconds + int(n[f] // frames_per_second)
+        hdr[f, 2] = (_bcd(mjd_digits, 3) << 20) | _bcd(sec, 5)
+    frames[:, :16] = hdr.view(np.uint8).reshape(nf, 16)
+    frames[:, 16:] = payload
+    return np.concatenate([np.zeros(prefix, np.uint8), frames.reshape(-1)])
+
+
+def mark5b_fill(framed: np.ndarray, frame: int, start: int, end: int, prefix: int = 0) -> None:
+    """Overwrite payload bytes [start, end) of one frame with the fill pattern
+    (32-bit words 0x11223344; start and end multiples of 4)."""
+    assert start % 4 == 0 and end % 4 == 0 and 0 <= start <= end <= MARK5B_PAYLOAD
+    o = prefix + frame * MARK5B_FRAME + 16
+    framed[o + start:o + end] = np.tile(np.array([0x44, 0x33, 0x22, 0x11], np.uint8), (end - start) // 4)

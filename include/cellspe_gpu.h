@@ -165,6 +165,11 @@ void cellspe_service_destroy(cellspe_service* s);
  * subband of a 2-bit stream. */
 #define CELLSPE_SPEC_INTERLEAVED 0  /* raw: nsub channels interleaved per sample time (Mark5B payload) */
 #define CELLSPE_SPEC_PLANES      1  /* raw: nsub planes of bytes_per_sub bytes, 1 channel each */
+#define CELLSPE_SPEC_MARK5B_FRAMED 2 /* raw: a framed Mark5B recording (16-byte headers, 10000-byte
+                                      * payloads, n_subbands = 4, 8 or 16 channels); headers are
+                                      * stripped and fill-pattern zones blanked (decoded as 0.0)
+                                      * on the device, as cellspe_mark5b_decode does; samples past
+                                      * the last complete frame are blanked too */
 typedef struct {
     int    fft_points;        /* N: 1024 .. 65536                                  */
     int    overlap;           /* fft_overlap_factor                                */
@@ -190,6 +195,46 @@ typedef struct {
 int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* power,
                          void* pcal_bins, void* pcal_tones);
 long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p);
+
+/* ---- framed Mark5B input ------------------------------------------------
+ * A Mark5B recording is a run of 10016-byte frames: a 16-byte header (sync
+ * word 0xABADDEED, frame number, BCD time code) and 10000 bytes of 2-bit
+ * samples, nchan channels interleaved per sample time (mark5access
+ * mark5_format_mark5b.c).  Missing data carry the fill pattern 0x11223344
+ * and are blanked per payload by the rules of blanker_mark5.c. */
+typedef struct {
+    long long first_frame_offset;  /* byte offset of the first frame (-1: none)        */
+    long long frames;              /* complete frames from there to the buffer end    */
+    long long good_samples;        /* cellspe_mark5b_decode: unblanked samples per
+                                    * channel, or -1 when the frames ran out (the
+                                    * value mark5_stream_decode returns)              */
+    int mjd;                       /* 56000 + BCD day digits of the first header, as
+                                    * FileSource::locateFirstHeader reads them        */
+    int seconds;                   /* BCD seconds of day of the first header          */
+    int frame_number;              /* 15-bit frame number within the second           */
+    int reserved;
+} cellspe_mark5b_info;
+
+/* new_mark5_stream_memory(framed, bytes) + mark5_stream_decode(nsamp):
+ * finds the first frame (sync word twice, 10016 bytes apart, within the first
+ * MiB; mark5_format_mark5b.c:98-131), strips the headers and decodes nsamp
+ * samples of each of nchan (4, 8, 16) channels into out[nchan][nsamp] with the
+ * mark5access levels {-3.3359, +1, -1, +3.3359}; blanked samples are 0.0.
+ * Like the library, it stops writing after the last complete frame and then
+ * reports good_samples = -1 (also when the last wanted sample ends the last
+ * frame).  Returns CELLSPE_ERR_ARG when no frame is found.  info may be NULL.
+ * memory = CELLSPE_MEM_HOST or _DEVICE for framed and out. */
+int cellspe_mark5b_decode(const void* framed, long long bytes, int nchan, long long nsamp, float* out,
+                          int memory, cellspe_mark5b_info* info);
+
+/* FileSource::read for framed data (spectrometer/src/FileSource.cpp:185-215):
+ * the payloads of `frames` frames from the first frame on, back to back,
+ * into payload[frames * 10000]; with valid_mask != NULL also one bit per
+ * sample time (bit t % 32 of word t / 32 set = unblanked), nchan channels per
+ * sample time.  frames = 0 takes every complete frame; payload and the mask
+ * must hold that many (see info->frames, filled first).  info may be NULL. */
+int cellspe_mark5b_deframe(const void* framed, long long bytes, int nchan, long long frames, void* payload,
+                           unsigned int* valid_mask, int memory, cellspe_mark5b_info* info);
 
 /* Spectrometer that allocates no device memory (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc when they run it:

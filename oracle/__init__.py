@@ -73,6 +73,10 @@ def lib() -> ctypes.CDLL:
         _lib.orc_pcal_tones.argtypes = [V, I, I, V]
         _lib.orc_fx_fp32.argtypes = [V, L, I, I, I, L, V, V, V, I, V, I]
         _lib.orc_fx_fstage_fp32.argtypes = [V, L, I, I, I, L, V, V, V, I, V, I]
+        _lib.orc_mark5b_find_first_frame.argtypes = [V, L]
+        _lib.orc_mark5b_valid_range.argtypes = [V, ctypes.POINTER(I), ctypes.POINTER(I)]
+        _lib.orc_mark5b_decode_framed.argtypes = [V, L, I, L, V]
+        _lib.orc_mark5b_decode_framed.restype = L
     return _lib
 
 
@@ -87,6 +91,28 @@ def ref_mark5() -> ctypes.CDLL:
         _ref_m5.ref_mark5_unpack.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     return _ref_m5
+
+
+def ref_mark5_decode_memory(fmt: bytes, framed: np.ndarray, nsamp: int):
+    """The reference's framed decode (mark5access memory stream + mark5_stream_decode)."""
+    m5 = ref_mark5()
+    m5.ref_mark5_decode_memory.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)]
+    buf = np.ascontiguousarray(framed, np.uint8).copy()
+    nch = int(fmt.split(b"-")[2])
+    out = np.zeros((nch, nsamp), np.float32)
+    c, off = ctypes.c_int(), ctypes.c_int()
+    rc = m5.ref_mark5_decode_memory(fmt, buf.ctypes.data, buf.size, nsamp, out.ctypes.data, ctypes.byref(c),
+                                    ctypes.byref(off))
+    return rc, out, off.value
+
+
+def mark5b_decode_framed(framed: np.ndarray, nchan: int, nsamp: int):
+    framed = np.ascontiguousarray(framed, np.uint8)
+    out = np.zeros((nchan, nsamp), np.float32)
+    good = lib().orc_mark5b_decode_framed(_ptr(framed), framed.size, nchan, nsamp, _ptr(out))
+    return good, out
 
 
 def ref_generic() -> ctypes.CDLL:

@@ -35,6 +35,93 @@ void orc_unpack2bit(const uint8_t* raw, int64_t nsamp, int nchan, int msb_first,
 }
 
 /* ---------------------------------------------------------------------- */
+/* Framed Mark5B: first frame, fill-pattern blanking, decode               */
+/* ---------------------------------------------------------------------- */
+#define M5B_FRAME 10016
+#define M5B_PAYLOAD 10000
+#define M5B_FILL64 0x1122334411223344ULL
+#define M5B_FILL32 0x11223344U
+
+int orc_mark5b_find_first_frame(const uint8_t* d, int64_t bytes)
+{
+    if (bytes > (1 << 20)) bytes = 1 << 20;
+    bytes -= M5B_FRAME + 4;
+    for (int64_t i = 0; i < bytes; i++)
+        if (d[i] == 0xED && d[i + 1] == 0xDE && d[i + 2] == 0xAD && d[i + 3] == 0xAB &&
+            d[i + M5B_FRAME] == 0xED && d[i + M5B_FRAME + 1] == 0xDE && d[i + M5B_FRAME + 2] == 0xAD &&
+            d[i + M5B_FRAME + 3] == 0xAB)
+            return (int)i;
+    return -1;
+}
+
+static uint64_t rd64(const uint8_t* p, int64_t i) { uint64_t v; memcpy(&v, p + 8 * i, 8); return v; }
+static uint32_t rd32(const uint8_t* p, int64_t i) { uint32_t v; memcpy(&v, p + 4 * i, 4); return v; }
+
+/* binary searches of blanker_mark5.c: boundary between data and fill words */
+static int first_invalid(const uint8_t* p, int start, int end)
+{
+    int n = end - start, i = n / 2, r = n - 1;
+    for (int s = n / 4; s > 0; s >>= 1) {
+        if (rd64(p, start + i) == M5B_FILL64) { r = i; i -= s; }
+        else i += s;
+    }
+    r = 8 * (start + r);
+    if (rd32(p, r / 4 - 1) == M5B_FILL32) r -= 4;
+    return r;
+}
+
+static int first_valid(const uint8_t* p, int start, int end)
+{
+    int n = end - start, i = n / 2, r = n - 1;
+    for (int s = n / 4; s > 0; s >>= 1) {
+        if (rd64(p, start + i) != M5B_FILL64) { r = i; i -= s; }
+        else i += s;
+    }
+    r = 8 * (start + r);
+    if (rd32(p, r / 4 - 2) == M5B_FILL32) r += 4;
+    return r;
+}
+
+void orc_mark5b_valid_range(const uint8_t* p, int* start, int* end)
+{
+    const int nword = M5B_PAYLOAD / 8;
+    int s_ok = rd64(p, 0) != M5B_FILL64, e_ok = rd64(p, nword - 1) != M5B_FILL64;
+    if (s_ok && e_ok) { *start = 0; *end = 1 << 30; }
+    else if (!s_ok && !e_ok) { *start = 1 << 30; *end = 0; }
+    else if (s_ok) { *start = 0; *end = first_invalid(p, 0, nword); }
+    else { *start = first_valid(p, 0, nword); *end = 1 << 30; }
+}
+
+int64_t orc_mark5b_decode_framed(const uint8_t* framed, int64_t bytes, int nchan, int64_t nsamp, float* out)
+{
+    static const float lut[4] = {-3.3359f, 1.0f, -1.0f, 3.3359f};
+    int off = orc_mark5b_find_first_frame(framed, bytes);
+    if (off < 0) return -1;
+    const int bps = nchan / 4;                       /* bytes per sample time */
+    const int spf = M5B_PAYLOAD / bps;
+    int64_t good = 0;
+    for (int64_t t = 0; t < nsamp; t++) {
+        int64_t f = t / spf;
+        int64_t fo = off + f * M5B_FRAME;
+        const uint8_t* p = framed + fo + 16;
+        int sv, ev;
+        orc_mark5b_valid_range(p, &sv, &ev);
+        int i = (int)(t % spf) * bps;
+        int valid = i >= sv && i < ev;
+        good += valid;
+        for (int c = 0; c < nchan; c++) {
+            unsigned code = (p[i + c / 4] >> (2 * (c % 4))) & 3u;
+            out[(int64_t)c * nsamp + t] = valid ? lut[code] : 0.0f;
+        }
+        /* the decoder moves to the next frame as soon as a payload is used
+         * up and fails when there is none (mark5_format_mark5b.c:1901-1908,
+         * mark5_stream_memory.c:59-71), also after the last wanted sample */
+        if (i + bps >= M5B_PAYLOAD && fo + 2 * M5B_FRAME > bytes) return -1;
+    }
+    return good;
+}
+
+/* ---------------------------------------------------------------------- */
 /* Generic complex MAC (architecture.h:405-433)                            */
 /* ---------------------------------------------------------------------- */
 void orc_addproduct_32fc(const orc_cf32* a, const orc_cf32* b, orc_cf32* acc, int n)

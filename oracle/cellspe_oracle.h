@@ -40,6 +40,23 @@ typedef struct { float re, im; } orc_cf32;
 void orc_unpack2bit(const uint8_t* raw, int64_t nsamp, int nchan, int msb_first,
                     const float lut[4], float* out);
 
+/* Framed Mark5B (10016-byte frames: 16-byte header + 10000-byte payload).
+ * orc_mark5b_find_first_frame restates findfirstframe
+ * (mark5_format_mark5b.c:98-131): the first offset where the sync word
+ * 0xABADDEED appears twice, 10016 bytes apart, searching at most 1 MiB.
+ * orc_mark5b_valid_range restates blanker_mark5 (blanker_mark5.c) for one
+ * 10000-byte payload (a single 32 KiB blanking zone): the byte range
+ * [start, end) outside of which samples are blanked (decoded as 0).
+ * orc_mark5b_decode_framed restates mark5_stream_decode on a memory stream:
+ * nsamp samples per channel from the first frame on, lut2bit values inside
+ * the valid range, 0.0 outside.  nchan = 4, 8 or 16 (2-bit).  Returns the
+ * number of unblanked samples, or -1 when the frames run out (the decoder
+ * steps to the next frame as soon as a payload is used up, so -1 also when
+ * the last wanted sample ends the last frame), or when no frame is found. */
+int orc_mark5b_find_first_frame(const uint8_t* data, int64_t bytes);
+void orc_mark5b_valid_range(const uint8_t* payload, int* start, int* end);
+int64_t orc_mark5b_decode_framed(const uint8_t* framed, int64_t bytes, int nchan, int64_t nsamp, float* out);
+
 /* acc[i] += a[i]*b[i]            architecture.h:405-421 (do_complex_mac)  */
 void orc_addproduct_32fc(const orc_cf32* a, const orc_cf32* b, orc_cf32* acc, int n);
 /* acc[i] += a[i]*conj(b[i])      architecture.h:427-433                   */

@@ -41,3 +41,25 @@ int ref_mark5_format_info(const char* format, int* nchan, int* nbit)
     delete_mark5_stream(ms);
     return 0;
 }
+
+/* Decodes nsamp samples per channel of a framed stream (headers included)
+ * through new_mark5_stream_memory() + mark5_stream_decode() -- the library's
+ * framed path with its fill-pattern blanking (blanker_mark5.c).  Returns the
+ * number of good (unblanked) samples, or a negative value on failure. */
+int ref_mark5_decode_memory(const char* format, void* data, unsigned int bytes, int nsamp,
+                            float* out, int* nchan_out, int* frameoffset_out)
+{
+    struct mark5_format_generic* f = new_mark5_format_generic_from_string(format);
+    if (!f) return -1;
+    struct mark5_stream* ms = new_mark5_stream(new_mark5_stream_memory(data, bytes), f);
+    if (!ms) return -2;
+    int nchan = ms->nchan;
+    float** planes = (float**)malloc(sizeof(float*) * nchan);
+    for (int c = 0; c < nchan; c++) planes[c] = out + (size_t)c * nsamp;
+    if (nchan_out) *nchan_out = nchan;
+    if (frameoffset_out) *frameoffset_out = ms->frameoffset;
+    int rc = mark5_stream_decode(ms, nsamp, planes);
+    free(planes);
+    delete_mark5_stream(ms);
+    return rc;
+}

@@ -31,6 +31,46 @@ def test_unpack_matches_live_mark5access(orc):
         assert np.array_equal(mine.view(np.uint32), ref.reshape(nch, n).view(np.uint32))
 
 
+FRAMED_LEVELS = np.array([-3.3359, 1.0, -1.0, 3.3359, 0.0], np.float32)
+
+
+@pytest.mark.parametrize("fmt,nch", [("Mark5B_512_16_2", 16), ("Mark5B_256_8_2", 8), ("Mark5B_128_4_2", 4)])
+def test_framed_mark5b_golden(orc, fmt, nch):
+    """Header strip + fill-pattern blanking + end-of-data rule vs the library's own decode."""
+    g = np.load(GOLD / "mark5b_framed.npz")
+    fr = g["framed"]
+    assert orc.lib().orc_mark5b_find_first_frame(fr.ctypes.data, fr.size) == 137
+    for k, ns in enumerate(g[f"{fmt}_nsamp"]):
+        good, out = orc.mark5b_decode_framed(fr, nch, int(ns))
+        assert good == int(g[f"{fmt}_rc{k}"])
+        assert np.array_equal(out.view(np.uint32), FRAMED_LEVELS[g[f"{fmt}_codes{k}"]].view(np.uint32))
+
+
+def test_framed_mark5b_live_reference(orc):
+    if not orc.have_ref():
+        pytest.skip("reference tree not compiled here")
+    import synth
+
+    rng = np.random.default_rng(17)
+    for fmt, nch in [(b"Mark5B-512-16-2", 16), (b"Mark5B-256-8-2", 8), (b"Mark5B-128-4-2", 4)]:
+        nf, pre = 6, int(rng.integers(0, 3000))
+        fr = synth.mark5b_frames(rng.integers(0, 256, nf * 10000, dtype=np.uint8), prefix=pre,
+                                 first_frame=int(rng.integers(0, 6400)))
+        for f in range(nf):
+            a = int(rng.integers(0, 2501)) * 4
+            kind = int(rng.integers(0, 4))
+            if kind == 1:
+                synth.mark5b_fill(fr, f, 0, a, pre)
+            elif kind == 2:
+                synth.mark5b_fill(fr, f, a, 10000, pre)
+        spf = 10000 // (nch // 4)
+        for ns in (int(rng.integers(1, nf * spf)), (nf - 1) * spf, nf * spf):
+            rc, ref, off = orc.ref_mark5_decode_memory(fmt, fr, ns)
+            good, mine = orc.mark5b_decode_framed(fr, nch, ns)
+            assert off == pre and good == rc
+            assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
 def test_generic_mac_golden(orc):
     g = np.load(GOLD / "generic_mac.npz")
     acc = g["acc0"].copy()

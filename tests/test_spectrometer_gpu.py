@@ -89,6 +89,29 @@ def test_spectrometer_pcal_offset_rotator(cg, orc):
     assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < TOL
 
 
+@pytest.mark.parametrize("overlap,K,nspec", [(2, 4, 3), (4, 3, 4), (1, 5, 2)])
+def test_spectrometer_pcal_running_fft_count(cg, orc, overlap, K, nspec):
+    """Several spectra in one call: the phase-cal fold follows the FFT count
+    that runs on across the spectra of one doMaths call, so with an odd
+    number of overlapped FFTs per spectrum later spectra fold other windows."""
+    import synth
+
+    nsub, N, fs = 4, 2048, 32e6
+    words, _ = synth.mark5b_subbands(16, N * K * nspec, fs_hz=fs, seed=40 + overlap, n_channels=N // 2, pcal_amp=0.3)
+    codes = np.stack([(words >> np.uint32(2 * c)) & np.uint32(3) for c in range(nsub)], axis=1)
+    raw = synth.pack2bit(codes.reshape(-1))
+    tb = 32
+    p = cg.spec_params(N, overlap, 2, K, nspec, nsub, raw.size, tonebins=tb, rotatorlen=tb, ntones=16, offset_hz=0.0,
+                       fs_hz=fs)
+    power = np.zeros((nsub, nspec, N // 2 + 1), np.float32)
+    bins = np.zeros((nsub, nspec, tb), np.complex64)
+    cg.spectrometer(p, raw, power, bins)
+    ref_p, ref_b = _oracle(orc, raw, nsub, N, overlap, 2, K, tb, tb, 0.0, fs)
+    assert np.linalg.norm(power - ref_p) / np.linalg.norm(ref_p) < TOL
+    for s in range(nspec):
+        assert np.linalg.norm(bins[:, s] - ref_b[:, s]) / np.linalg.norm(ref_b[:, s]) < TOL
+
+
 def test_spectrometer_planes_layout_and_device(cg):
     import torch
 
