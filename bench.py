@@ -62,11 +62,18 @@ class ClockSampler:
 
     def __init__(self, index: int):
         self.index, self.rows, self.proc = index, [], None
+        self.t0, self.t1 = None, None
+
+    def mark_start(self):
+        self.t0 = time.monotonic()
+
+    def mark_end(self):
+        self.t1 = time.monotonic()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
@@ -75,7 +82,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.monotonic(), [x.strip() for x in line.split(",")]))
 
     def __exit__(self, *a):
         if self.proc:
@@ -83,14 +90,17 @@ class ClockSampler:
             self.proc.wait(timeout=5)
 
     def summary(self):
-        if not self.rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        """Samples taken between mark_start and mark_end (the timed region)."""
+        rows = [r for t, r in self.rows
+                if (self.t0 is None or t >= self.t0) and (self.t1 is None or t <= self.t1)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
 
 
 def cpu_baseline(raw_host: np.ndarray, k_sample: int, nthreads: int):
@@ -184,7 +194,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="tc", choices=["tc", "fp32"])
@@ -196,6 +206,8 @@ def main():
                     help="length of the Poisson arrival window of the serving measurement (0 skips it)")
     ap.add_argument("--segments", type=int, default=K,
                     help="spectra per integration (smaller values make a profiling-sized case)")
+    ap.add_argument("--fft-points", type=int, default=N,
+                    help="FFT length (smaller values make a profiling-sized case with fewer channels)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -222,10 +234,13 @@ def main():
 
     x_mode = cg.X_TC_FP16 if args.mode == "tc" else cg.X_FP32
     K_run = args.segments
-    T_run = N * K_run
+    N_run = args.fft_points
+    C_run = N_run // 2
+    T_run = N_run * K_run
     raw = synth.device_stations(S, T_run, RHO, seed=4 + 1000 * rank)
-    vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
-    params = cg.fx_params(S, N, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+    vis = torch.empty((C_run, P), dtype=torch.complex64, device="cuda")
+    params = cg.fx_params(S, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+    clk = ClockSampler(local).__enter__()             # running before the timed region
     for _ in range(args.warmup):
         cg.fx_correlate(params, raw, vis)
 
@@ -234,14 +249,16 @@ def main():
     barrier()
     l0 = cg.kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        e0.record()
-        for _ in range(args.steps):
-            cg.fx_correlate(params, raw, vis)
-            stage_sum += np.array(cg.stage_times())
-        torch.cuda.synchronize()
-        e1.record()
-        e1.synchronize()
+    clk.mark_start()
+    e0.record()
+    for _ in range(args.steps):
+        cg.fx_correlate(params, raw, vis)
+        stage_sum += np.array(cg.stage_times())
+    torch.cuda.synchronize()
+    e1.record()
+    e1.synchronize()
+    clk.mark_end()
+    clk.__exit__(None, None, None)
     launches = cg.kernel_launches() - l0
     ms = e0.elapsed_time(e1)
     if dist:
@@ -258,9 +275,9 @@ def main():
     e2e_ms, e2e_value = None, None
     if not args.no_e2e:
         pin_raw = torch.from_numpy(raw_h).pin_memory()
-        pin_vis = torch.empty((C, P), dtype=torch.complex64).pin_memory()
+        pin_vis = torch.empty((C_run, P), dtype=torch.complex64).pin_memory()
         raw_np, vis_np = pin_raw.numpy(), pin_vis.numpy()
-        hparams = cg.fx_params(S, N, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+        hparams = cg.fx_params(S, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
         cg.fx_correlate(hparams, raw_np, vis_np)
         barrier()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -280,8 +297,8 @@ def main():
     # ---- roofline of the dominant kernel -----------------------------------
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
-    f_bytes = S * K_run * (N // 4 + C * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
-    x_flops = 8.0 * P * C * K_run                                              # 8 real flops per CMAC, triangle
+    f_bytes = S * K_run * (N_run // 4 + C_run * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
+    x_flops = 8.0 * P * C_run * K_run                                              # 8 real flops per CMAC, triangle
     stages = {"f_stage_ms": f_ms, "x_stage_ms": x_ms, "output_ms": stage_ms[3],
               "f_stage_gbs": f_bytes / (f_ms * 1e-3) / 1e9,
               "x_stage_tflops": x_flops / (x_ms * 1e-3) / 1e12}
@@ -299,7 +316,9 @@ def main():
                     "peak_source": f"{peak_kind} dense bf16 (burst)", "traffic": None}
     else:
         pk = peaks["hbm_gbs"]
-        roof = {"bound": "hbm", "kernel": "k_fx_fstage", "achieved": stages["f_stage_gbs"], "peak": pk,
+        tc_f = x_mode == cg.X_TC_FP16 and N_run == 2048 and os.environ.get("CELLSPE_FSTAGE_TC") == "1"
+        fk = "k_fx_fstage_tc" if tc_f else ("k_fx_fstage_w2048" if N_run == 2048 else "k_fx_fstage")
+        roof = {"bound": "hbm", "kernel": fk, "achieved": stages["f_stage_gbs"], "peak": pk,
                 "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
                 "traffic": None}
 
@@ -312,7 +331,7 @@ def main():
         nthreads = os.cpu_count() or 1
         v, dt = cpu_baseline(raw_h, args.cpu_segments, nthreads)
         cpu = {"value": v, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
-               "sample": f"{S} inputs x {args.cpu_segments} segments x {N} samples, {dt:.1f} s"}
+               "sample": f"{S} inputs x {args.cpu_segments} segments x {N_run} samples, {dt:.1f} s"}
 
     if rank == 0:
         line = {
@@ -321,13 +340,13 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f16-tc/f32-acc" if x_mode == cg.X_TC_FP16 else "f32",
             "data": "synthetic (seeded 2-bit offset binary, rho=0.02, generated on device)",
-            "config": {"workload": f"256-station dual-pol FX: S=512, N=2048, C=1024, K={K_run}",
-                       "inputs": S, "fft_points": N, "channels": C, "segments": K_run, "products": P,
+            "config": {"workload": f"256-station dual-pol FX: S=512, N={N_run}, C={C_run}, K={K_run}",
+                       "inputs": S, "fft_points": N_run, "channels": C_run, "segments": K_run, "products": P,
                        "x_mode": args.mode, "vis_order": "channel-major [C][P]",
                        "l2": "inputs larger than L2 (1.07 GB raw, spectra 8.6/17 GB, vis 1.07 GB)",
                        "parallelism": f"replicas x{world} (one job per GPU)"},
             "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(S * T_run // 4),
-                    "d2h_bytes_per_step": int(C * P * 8), "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": int(C_run * P * 8), "ms_per_step": e2e_ms},
             "gpu_launches": int(launches),
             "roofline": roof,
             "stages": stages,

@@ -26,6 +26,8 @@
 
 namespace {
 
+CS_DEV int out_pitch(const CsFStageArgs& a) { return a.kp ? a.kp : a.K; }
+
 template <int M> struct FCfg {
     static constexpr int T = M / 16;
     static constexpr int GROUPS = (T >= 256) ? 1 : 256 / T;
@@ -63,7 +65,7 @@ CS_DEV float lut_pick(const float (&l)[4], unsigned c)
 }
 
 template <int M, int FMT, bool PHASE>
-__global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const float2* __restrict__ tw)
+__global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
 {
     using Cfg = FCfg<M>;
     constexpr int T = Cfg::T, GROUPS = Cfg::GROUPS, N = 2 * M;
@@ -129,11 +131,11 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
             if (scl) X = cscale(X, __ldg(scl + c));
             if constexpr (DIRECT) {
                 if constexpr (FMT == CS_SPECTRA_F32) {
-                    reinterpret_cast<float2*>(a.out)[((int64_t)c * a.S + s) * a.K + k] = X;
+                    reinterpret_cast<float2*>(a.out)[((int64_t)c * a.S + s) * out_pitch(a) + k] = X;
                 } else {
                     __half* o = reinterpret_cast<__half*>(a.out);
-                    o[(((int64_t)c * 2 + 0) * a.S + s) * a.K + k] = __float2half_rn(X.x);
-                    o[(((int64_t)c * 2 + 1) * a.S + s) * a.K + k] = __float2half_rn(X.y);
+                    o[(((int64_t)c * 2 + 0) * a.S + s) * out_pitch(a) + k] = __float2half_rn(X.x);
+                    o[(((int64_t)c * 2 + 1) * a.S + s) * out_pitch(a) + k] = __float2half_rn(X.y);
                 }
             } else if constexpr (FMT == CS_SPECTRA_F32) {
                 reinterpret_cast<float2*>(stage)[c * (G + 1) + ls] = X;
@@ -163,28 +165,28 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
 
     // ---- write the staging tile out, corner-turned ----
     const int nvalid = min(G, a.K - k0);
-    const int S = a.S, K = a.K;
+    const int S = a.S, KP = out_pitch(a);
     if constexpr (FMT == CS_SPECTRA_F32) {
         const float2* st = reinterpret_cast<const float2*>(stage);
         float2* out = reinterpret_cast<float2*>(a.out);
-        if (nvalid == G && (G % 2 == 0) && (K % 2 == 0)) {
+        if (nvalid == G && (G % 2 == 0) && (KP % 2 == 0)) {
             constexpr int P2 = G / 2;
             for (int idx = threadIdx.x; idx < M * P2; idx += Cfg::NT) {
                 int c = idx / P2, l = 2 * (idx % P2);
                 float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
-                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * K + k0 + l) =
+                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * KP + k0 + l) =
                     make_float4(x0.x, x0.y, x1.x, x1.y);
             }
         } else {
             for (int idx = threadIdx.x; idx < M * G; idx += Cfg::NT) {
                 int c = idx / G, l = idx % G;
-                if (l < nvalid) out[((int64_t)c * S + s) * K + k0 + l] = st[c * (G + 1) + l];
+                if (l < nvalid) out[((int64_t)c * S + s) * KP + k0 + l] = st[c * (G + 1) + l];
             }
         }
     } else {
         const __half2* st = reinterpret_cast<const __half2*>(stage);
         __half* out = reinterpret_cast<__half*>(a.out);
-        if (nvalid == G && (G % 8 == 0) && (K % 8 == 0)) {
+        if (nvalid == G && (G % 8 == 0) && (KP % 8 == 0)) {
             constexpr int P8 = G / 8;
             for (int idx = threadIdx.x; idx < M * 2 * P8; idx += Cfg::NT) {
                 int l = 8 * (idx % P8);
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
                 // pick the Re (low) or Im (high) halves of 8 staged half2 words
                 const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + l);
                 const uint32_t sel = plane ? 0x7632u : 0x5410u;
-                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * K + k0 + l) =
+                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * KP + k0 + l) =
                     make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
                                __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
             }
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(CsFStageArgs a, const
                 int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
                 if (l < nvalid) {
                     __half2 x = st[c * (G + 1) + l];
-                    out[(((int64_t)c * 2 + plane) * S + s) * K + k0 + l] = plane ? __high2half(x) : __low2half(x);
+                    out[(((int64_t)c * 2 + plane) * S + s) * KP + k0 + l] = plane ? __high2half(x) : __low2half(x);
                 }
             }
         }
@@ -251,14 +253,14 @@ constexpr int W_G = 8, W_TP = 33;
 constexpr int W_RAWC = 2048 / 64 + 2;          // 16-byte chunks staged per segment (34 = 136 words)
 constexpr int W_RAWW = 4 * W_RAWC;
 
-template <int FMT, int WARPS>
+template <int FMT, int WARPS, int G>
 size_t w2048_smem()
 {
     size_t elem = (FMT == CS_SPECTRA_F32) ? 8 : 4;
     return (size_t)WARPS * 32 * W_TP * 8            // transpose tiles (complex)
            + (size_t)WARPS * 2 * W_RAWW * 4         // raw double buffers
            + 16 * 8                                 // pair LUT
-           + (size_t)1024 * (W_G + 1) * elem;       // staging tile
+           + (size_t)1024 * (G + 1) * elem;         // staging tile
 }
 
 CS_DEV void cp_async16(uint32_t dst, const void* src, bool valid)
@@ -270,10 +272,11 @@ CS_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memor
 template <int N_PENDING>
 CS_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N_PENDING) : "memory"); }
 
-template <int FMT, bool PHASE, int WARPS, int ROUNDS>
-__global__ void __launch_bounds__(32 * WARPS, (WARPS == 8) ? 2 : 3) k_fx_fstage_w2048(CsFStageArgs a, const float2* __restrict__ tw)
+template <int FMT, bool PHASE, int WARPS, int ROUNDS, int G>
+__global__ void __launch_bounds__(32 * WARPS, (WARPS == 16) ? 1 : (WARPS == 8) ? 2 : 3) k_fx_fstage_w2048(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
 {
-    constexpr int M = 1024, N = 2048, G = W_G, NT = 32 * WARPS, PER = G / WARPS;
+    constexpr int M = 1024, N = 2048, NT = 32 * WARPS, PER = G / WARPS;
+    static_assert(G % WARPS == 0 && G % 8 == 0, "segments per CTA");
     extern __shared__ __align__(16) unsigned char smem[];
     float2* tb_all = reinterpret_cast<float2*>(smem);
     uint32_t* rb_all = reinterpret_cast<uint32_t*>(tb_all + WARPS * 32 * W_TP);
@@ -412,32 +415,33 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 8) ? 2 : 3) k_fx_fstage_
 
     // corner-turned write-out of the G staged segments
     const int nvalid = max(0, min(G, a.K - k0));
-    const int S = a.S, K = a.K;
+    const int S = a.S, KP = out_pitch(a);
     if constexpr (FMT == CS_SPECTRA_F32) {
         const float2* st = reinterpret_cast<const float2*>(stage);
         float2* out = reinterpret_cast<float2*>(a.out);
-        if (nvalid == G && K % 2 == 0) {
+        if (nvalid == G && KP % 2 == 0) {
             for (int idx = threadIdx.x; idx < M * (G / 2); idx += NT) {
                 const int c = idx / (G / 2), l = 2 * (idx % (G / 2));
                 const float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
-                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * K + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
+                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * KP + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
             }
         } else {
             for (int idx = threadIdx.x; idx < M * G; idx += NT) {
                 const int c = idx / G, l = idx % G;
-                if (l < nvalid) out[((int64_t)c * S + s) * K + k0 + l] = st[c * (G + 1) + l];
+                if (l < nvalid) out[((int64_t)c * S + s) * KP + k0 + l] = st[c * (G + 1) + l];
             }
         }
     } else {
         const __half2* st = reinterpret_cast<const __half2*>(stage);
         __half* out = reinterpret_cast<__half*>(a.out);
-        if (nvalid == G && K % 8 == 0) {
-            for (int idx = threadIdx.x; idx < M * 2; idx += NT) {
-                const int plane = idx & 1, c = idx >> 1;
+        if (nvalid == G && KP % 8 == 0) {
+            constexpr int P8 = G / 8;                 // 16-byte pieces per output row
+            for (int idx = threadIdx.x; idx < M * 2 * P8; idx += NT) {
+                const int piece = idx % P8, plane = (idx / P8) & 1, c = idx / (2 * P8);
                 // pick the Re (low) or Im (high) halves of 8 staged half2 words
-                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1));
+                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + 8 * piece);
                 const uint32_t sel = plane ? 0x7632u : 0x5410u;
-                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * K + k0) =
+                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * KP + k0 + 8 * piece) =
                     make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
                                __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
             }
@@ -446,7 +450,7 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 8) ? 2 : 3) k_fx_fstage_
                 const int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
                 if (l < nvalid) {
                     const __half2 x = st[c * (G + 1) + l];
-                    out[(((int64_t)c * 2 + plane) * S + s) * K + k0 + l] = plane ? __high2half(x) : __low2half(x);
+                    out[(((int64_t)c * 2 + plane) * S + s) * KP + k0 + l] = plane ? __high2half(x) : __low2half(x);
                 }
             }
         }
@@ -455,18 +459,18 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 8) ? 2 : 3) k_fx_fstage_
     }
 }
 
-template <int FMT, bool PHASE, int WARPS, int ROUNDS>
+template <int FMT, bool PHASE, int WARPS, int ROUNDS, int G = W_G>
 int launch_w2048_variant(const CsFStageArgs& a, const float2* tw, cudaStream_t st)
 {
-    size_t smem = w2048_smem<FMT, WARPS>();
-    auto kern = k_fx_fstage_w2048<FMT, PHASE, WARPS, ROUNDS>;
+    size_t smem = w2048_smem<FMT, WARPS, G>();
+    auto kern = k_fx_fstage_w2048<FMT, PHASE, WARPS, ROUNDS, G>;
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((a.K + W_G * ROUNDS - 1) / (W_G * ROUNDS), a.S);
+    dim3 grid((a.K + G * ROUNDS - 1) / (G * ROUNDS), a.S);
     kern<<<grid, 32 * WARPS, smem, st>>>(a, tw), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
-constexpr int W_NVARIANTS = 3;
+constexpr int W_NVARIANTS = 4;
 
 template <int FMT, bool PHASE>
 int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cudaStream_t st)
@@ -474,6 +478,10 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
     switch (choice) {
         case 2: return launch_w2048_variant<FMT, PHASE, 4, 1>(a, tw, st);
         case 3: return launch_w2048_variant<FMT, PHASE, 8, 2>(a, tw, st);
+        case 4:
+            // 16 warps, 16 segments: 32-byte output runs (FP16 staging fits)
+            if constexpr (FMT == CS_SPECTRA_F16) return launch_w2048_variant<FMT, PHASE, 16, 1, 16>(a, tw, st);
+            return launch_w2048_variant<FMT, PHASE, 8, 1>(a, tw, st);
         default: return launch_w2048_variant<FMT, PHASE, 8, 1>(a, tw, st);
     }
 }
@@ -481,10 +489,12 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
 // Schedule choice per (format, phase): 1 = 8 warps, one segment each;
 // 2 = 4 warps, two segments each with the second prefetched; 3 = 8 warps,
 // two rounds of 8 segments per CTA (the second round's raw words prefetched
-// during the first).  Picked once per
-// process by timing both on a 64-input x 64-segment job of zero samples (the
-// FFT's arithmetic does not depend on the values), unless the environment
-// variable CELLSPE_FSTAGE_VARIANT forces 1, 2 or 3.
+// during the first); 4 = 16 warps and 16 segments per CTA, so that each
+// output row gets a 32-byte run (FP16 only).  Picked once per process by
+// timing all on a 64-input x 512-segment job of zero samples (the FFT's
+// arithmetic does not depend on the values; the spectra exceed the L2 cache
+// and use the padded row pitch of the FX path), unless the environment
+// variable CELLSPE_FSTAGE_VARIANT forces one.
 int g_w2048_choice[2][2] = {{0, 0}, {0, 0}};
 std::mutex g_w2048_mu;
 
@@ -493,9 +503,9 @@ int tune_w2048(const float2* tw, cudaStream_t st)
 {
     const char* env = getenv("CELLSPE_FSTAGE_VARIANT");
     if (env && env[0] >= '1' && env[0] <= '0' + W_NVARIANTS) return env[0] - '0';
-    const int S = 64, K = 64;
+    const int S = 64, K = 512, KP = K + 64;
     const size_t raw_bytes = (size_t)S * K * 2048 / 4;
-    const size_t out_bytes = (size_t)S * K * 1024 * (FMT == CS_SPECTRA_F32 ? 8 : 4);
+    const size_t out_bytes = (size_t)S * KP * 1024 * (FMT == CS_SPECTRA_F32 ? 8 : 4);
     const size_t ph_bytes = PHASE ? (size_t)S * K * 4 : 0;
     char* buf = nullptr;
     if (cudaMalloc(&buf, raw_bytes + out_bytes + 2 * ph_bytes) != cudaSuccess) return 1;
@@ -503,7 +513,7 @@ int tune_w2048(const float2* tw, cudaStream_t st)
     CsFStageArgs a{};
     a.raw = (const uint8_t*)buf;
     a.bytes_per_input = raw_bytes / S;
-    a.S = S; a.N = 2048; a.K = K;
+    a.S = S; a.N = 2048; a.K = K; a.kp = KP;
     a.phase0 = PHASE ? (const float*)(buf + raw_bytes + out_bytes) : nullptr;
     a.dphase = PHASE ? (const float*)(buf + raw_bytes + out_bytes + ph_bytes) : nullptr;
     a.lut[0] = -3.f; a.lut[1] = -1.f; a.lut[2] = 1.f; a.lut[3] = 3.f;
@@ -587,6 +597,14 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
 {
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
+    // The tensor-core F stage is opt-in (CELLSPE_FSTAGE_TC=1, read per call):
+    // its 8-segment units give 16-byte output runs, and on 512 inputs x 4096
+    // segments it measured 14.5 ms against 7.3 ms for the 16-segment warp
+    // FFT below.
+    if (cs_fstage_tc_supported(a)) {
+        const char* e = getenv("CELLSPE_FSTAGE_TC");
+        if (e && e[0] == '1') return cs_fx_fstage_tc(a, st);
+    }
     if (a.N == 2048 && !a.msb_first) {
         const bool ph = a.phase0 != nullptr;
         if (a.format == CS_SPECTRA_F32)

@@ -56,18 +56,28 @@ struct CsFStageArgs {
     float lut[4];
     int msb_first;
     int format;                 // CsSpectraFormat
-    void* out;                  // F32: float2 [C][S][K];  F16: __half [C][2][S][K]
+    void* out;                  // F32: float2 [C][S][kp];  F16: __half [C][2][S][kp]
+    int kp;                     // row pitch of out in elements (>= K; 0 = K)
 };
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
+// fstage_tc.cu: the N = 2048 FP16-output F stage on the tensor cores (both
+// DFT passes as tcgen05 MMAs).  cs_fx_fstage uses it for those arguments
+// when the environment sets CELLSPE_FSTAGE_TC=1.
+bool cs_fstage_tc_supported(const CsFStageArgs& a);
+int cs_fx_fstage_tc(const CsFStageArgs& a, cudaStream_t st);
+// Error code of the last tensor-core F-stage launch (0 = ok; 1, 2 = a wait
+// timed out).  Call after the stream has synchronised.
+int cs_fstage_tc_status(unsigned* code);
 
 // xstage.cu -----------------------------------------------------------------
-// FP32 CUDA-core X stage: spectra float2 [C][S][K] -> vis float2 [C][P],
-// P = S(S+1)/2, p = i(i+1)/2 + j (j <= i), V = sum_k X_i conj(X_j).
-int cs_xmac_f32(const float2* spectra, int S, int C, int K, float2* vis, int accumulate,
+// FP32 CUDA-core X stage: spectra float2 [C][S][kp] (K used) -> vis float2
+// [C][P], P = S(S+1)/2, p = i(i+1)/2 + j (j <= i), V = sum_k X_i conj(X_j).
+int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis, int accumulate,
                 cudaStream_t st);
 // Tensor-core (tcgen05, FP16 in, FP32 accumulate) X stage:
-// spectra __half [C][2][S][K] -> vis float2 [C][P]; inv_scale [S*C] or null.
-int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, float2* vis, const float* inv_scale,
+// spectra __half [C][2][S][kp] (K used; kp % 8 == 0) -> vis float2 [C][P];
+// inv_scale [S*C] or null.
+int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
                    int accumulate, cudaStream_t st);
 // Error code of the last tensor-core X-stage launch (0 = ok; 1..3 = a
 // pipeline wait timed out).  Call after the launching stream has synchronised.

@@ -314,7 +314,7 @@ int op_xmac(Workspace& ws, bool host, const void* spectra, int S, int C, int K, 
     const void* d_sp = j.in(spectra, (size_t)C * S * K * 8);
     void* d_vis = j.out(vis, (size_t)C * P * 8, accumulate != 0);
     if (!j.err) {
-        int rc = map_rc(cs_xmac_f32((const float2*)d_sp, S, C, K, (float2*)d_vis, accumulate, ws.stream), "xmac");
+        int rc = map_rc(cs_xmac_f32((const float2*)d_sp, S, C, K, K, (float2*)d_vis, accumulate, ws.stream), "xmac");
         if (rc) j.err = rc;
     }
     return j.finish();
@@ -329,7 +329,7 @@ int op_xmac_f16(Workspace& ws, bool host, const void* spectra, int S, int C, int
     const void* d_sp = j.in(spectra, (size_t)C * 2 * S * K * 2);
     void* d_vis = j.out(vis, (size_t)C * P * 8, accumulate != 0);
     if (!j.err) {
-        int rc = map_rc(cs_xmac_tc_f16(d_sp, S, C, K, (float2*)d_vis, nullptr, accumulate, ws.stream), "xmac_f16");
+        int rc = map_rc(cs_xmac_tc_f16(d_sp, S, C, K, K, (float2*)d_vis, nullptr, accumulate, ws.stream), "xmac_f16");
         if (rc) j.err = rc;
     }
     int rc = j.finish();
@@ -341,6 +341,14 @@ int op_xmac_f16(Workspace& ws, bool host, const void* spectra, int S, int C, int
     return rc;
 }
 
+// Row pitch (elements) of the internal spectra between the F and X stages:
+// K + 64 for long rows.  Unpadded, the F stage's corner-turn writes land on
+// rows a power-of-two number of bytes apart (4 MiB at 512 inputs x 4096
+// segments), which measured 16% slower; the pad keeps rows 128-byte aligned
+// for the X stage's TMA loads and costs at most 25% memory at K = 256 (1.6%
+// at K = 4096).
+long long spectra_pitch(long long K) { return K >= 256 ? K + 64 : K; }
+
 long long fx_bytes(const cellspe_fx_params* p, bool with_poly)
 {
     long long S = p->n_inputs, N = p->fft_points, K = p->n_segments, C = N / 2;
@@ -349,7 +357,7 @@ long long fx_bytes(const cellspe_fx_params* p, bool with_poly)
     long long b = 0;
     if (host) b += align256(S * p->bytes_per_input);
     if (with_poly) b += align256(S * 32) + 3 * align256(S * K * 4);
-    b += align256(C * S * K * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));
+    b += align256(C * S * spectra_pitch(K) * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));
     bool stage_vis = host || p->vis_order == CELLSPE_VIS_BASELINE_MAJOR || p->accumulate;
     if (stage_vis) b += 3 * align256(C * P * 8);
     if (p->x_mode != CELLSPE_X_FP32) b += 2 * align256(S * C * 4);
@@ -413,7 +421,9 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         }
         d_inv_scale = inv;
     }
-    fa.out = j.scratch((size_t)C * S * K * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
+    const int kp = (int)spectra_pitch(K);
+    fa.kp = kp;
+    fa.out = j.scratch((size_t)C * S * kp * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
     if (sync) cudaEventRecord(ws.sev[1], ws.stream);
     if (!j.err) {
         int rc = map_rc(cs_fx_fstage(fa, ws.stream), "F stage");
@@ -426,9 +436,9 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     if (!j.err) {
         int rc;
         if (p->x_mode == CELLSPE_X_FP32)
-            rc = cs_xmac_f32((const float2*)fa.out, S, C, K, vis_cp, 0, ws.stream);
+            rc = cs_xmac_f32((const float2*)fa.out, S, C, K, kp, vis_cp, 0, ws.stream);
         else
-            rc = cs_xmac_tc_f16(fa.out, S, C, K, vis_cp, d_inv_scale, 0, ws.stream);
+            rc = cs_xmac_tc_f16(fa.out, S, C, K, kp, vis_cp, d_inv_scale, 0, ws.stream);
         rc = map_rc(rc, "X stage");
         if (rc) j.err = rc;
     }
@@ -462,7 +472,10 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     int rc = j.finish(sync);
     if (sync && !rc && p->x_mode != CELLSPE_X_FP32) {
         unsigned code = 0;
-        if (cs_xmac_tc_status(&code) != 0 || code != 0)
+        if (cs_fstage_tc_status(&code) != 0 || code != 0)
+            rc = set_err(CELLSPE_ERR_CUDA, "F stage: tensor-core pipeline wait timed out (code " +
+                                               std::to_string(code) + ")");
+        else if (cs_xmac_tc_status(&code) != 0 || code != 0)
             rc = set_err(CELLSPE_ERR_CUDA, "X stage: tensor-core pipeline wait timed out (code " +
                                                std::to_string(code) + ")");
     }

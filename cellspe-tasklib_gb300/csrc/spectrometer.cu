@@ -109,7 +109,7 @@ CS_DEV float2 sample_pair(const float (&lut)[4], uint32_t w, int f, const uint32
 }
 
 template <int MC, int P>
-__global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(CsSpecArgs a, const float2* __restrict__ tw,
+__global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_constant__ CsSpecArgs a, const float2* __restrict__ tw,
                                                             const float* __restrict__ win, int nchunk, int ch)
 {
     using C = SCfg<MC>;

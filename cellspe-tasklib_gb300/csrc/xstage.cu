@@ -31,7 +31,7 @@ __device__ __forceinline__ void tile_coords(int t, int& bi, int& bj)
     bj = t - b * (b + 1) / 2;
 }
 
-__global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict__ spec, int S, int K,
+__global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict__ spec, int S, int K, int kp,
                                                       float2* __restrict__ vis, int64_t P, int accumulate)
 {
     __shared__ float2 As[2][XK][XLD];
@@ -43,13 +43,13 @@ __global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict_
     const int tid = threadIdx.x;
     const int ti = tid >> 3;          // 0..15 -> rows ti + 16a
     const int tj = tid & 7;           // 0..7  -> cols tj + 8b
-    const float2* base = spec + (int64_t)c * S * K;
+    const float2* base = spec + (int64_t)c * S * kp;
 
     // loader: thread -> (row = tid/2, 8 consecutive time samples)
     const int lrow = tid >> 1, lk = (tid & 1) * 8;
     const int ai = i0 + lrow, bjr = j0 + lrow;
-    const float2* pa = base + (int64_t)min(ai, S - 1) * K;
-    const float2* pb = base + (int64_t)min(bjr, S - 1) * K;
+    const float2* pa = base + (int64_t)min(ai, S - 1) * kp;
+    const float2* pb = base + (int64_t)min(bjr, S - 1) * kp;
     const bool va = ai < S, vb = bjr < S;
 
     float2 ra[8], rb[8];
@@ -145,15 +145,15 @@ __global__ void k_vis_transpose(const float2* __restrict__ in, float2* __restric
 }
 }  // namespace
 
-int cs_xmac_f32(const float2* spectra, int S, int C, int K, float2* vis, int accumulate, cudaStream_t st)
+int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis, int accumulate, cudaStream_t st)
 {
-    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0) return CS_ERR_ARG;
+    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || kp < K) return CS_ERR_ARG;
     int nb = (S + XT - 1) / XT;
     int64_t tiles = (int64_t)nb * (nb + 1) / 2;
     if (C > 65535) return CS_ERR_ARG;
     int64_t P = (int64_t)S * (S + 1) / 2;
     dim3 grid((unsigned)tiles, C);
-    k_xmac_f32<<<grid, XTHREADS, 0, st>>>(spectra, S, K, vis, P, accumulate), cs_count_launches(1);
+    k_xmac_f32<<<grid, XTHREADS, 0, st>>>(spectra, S, K, kp, vis, P, accumulate), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 

@@ -24,6 +24,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "tma.h"
 
 #include <mutex>
 #include <vector>
@@ -314,25 +315,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn()
-{
-    static EncodeTiledFn fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    });
-    return fn;
-}
-
 std::mutex g_tiles_mu;
 std::vector<std::pair<std::pair<int, int>, int2*>> g_tiles;   // ((device, S) -> device tile list)
 
@@ -357,12 +339,27 @@ const int2* tile_list(int S, int* ntiles)
 
 }  // namespace
 
-int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, float2* vis, const float* inv_scale, int accumulate,
-                   cudaStream_t st)
+CsEncodeTiledFn cs_encode_tiled()
 {
-    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || C > 65535) return CS_ERR_ARG;
-    if (K % 8 != 0 || (uintptr_t)spectra % 16) return CS_ERR_ARG;     // TMA: 16-byte row pitch and base
-    EncodeTiledFn enc = encode_fn();
+    static CsEncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CsEncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
+                   int accumulate, cudaStream_t st)
+{
+    if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || C > 65535 || kp < K) return CS_ERR_ARG;
+    if (K % 8 != 0 || kp % 8 != 0 || (uintptr_t)spectra % 16) return CS_ERR_ARG;   // TMA: 16-byte pitch and base
+    CsEncodeTiledFn enc = cs_encode_tiled();
     if (!enc) return CS_ERR_UNSUPPORTED;
     int ntiles = 0;
     const int2* tiles = tile_list(S, &ntiles);
@@ -370,7 +367,7 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, float2* vis, const 
 
     CUtensorMap tm;
     cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)C * 2 * S};
-    cuuint64_t gstride[1] = {(cuuint64_t)K * 2};
+    cuuint64_t gstride[1] = {(cuuint64_t)kp * 2};
     cuuint32_t box[2] = {BK, BM};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(spectra), gdim, gstride, box, estr,

@@ -103,3 +103,69 @@ def test_fx_tc_channel_scale(cg):
     scaled = _fx_pair(cg, raw, S, N, K, cg.X_TC_FP16, channel_scale=scale)
     rel = np.linalg.norm(scaled - base) / np.linalg.norm(base)
     assert rel < 1e-3
+
+
+def _tc_bars(orc, vis, X, pairs, K, sel=None, chans=None, cross_coverage=True):
+    """1e-3 relative amplitude per product, 0.05 deg phase above the 3-sigma noise floor."""
+    ref = orc.fx_vis_f64(X, pairs)
+    got = vis if sel is None else np.stack([vis[p][chans] for p in sel])
+    amp_err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert amp_err.max() < 1e-3, amp_err.max()
+    auto = {a: ref[pairs.index((a, a))].real for a, b in pairs if a == b}
+    floor = np.stack([3 * np.sqrt(auto[a] * auto[b] / K) for a, b in pairs])
+    mask = np.abs(ref) > floor
+    cross = np.array([a != b for a, b in pairs])
+    if cross_coverage:
+        assert mask[cross].mean() > 0.5
+    phase_deg = np.degrees(np.abs(np.angle(got * np.conj(ref))))[mask]
+    assert phase_deg.max() < 0.05, phase_deg.max()
+
+
+@pytest.fixture(params=["0", "1"], ids=["warp-fft", "tc-fstage"])
+def fstage_engine(request, monkeypatch):
+    """N = 2048 FP16 spectra from the warp FFT (default) or the tensor-core F stage."""
+    monkeypatch.setenv("CELLSPE_FSTAGE_TC", request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("S,K,rho", [(24, 64, 0.5), (9, 72, 0.6), (40, 136, 0.4)])
+def test_fx_tc_fstage_2048_vs_fp64(cg, orc, S, K, rho, fstage_engine):
+    """N = 2048 with either F stage (tensor-core one: units of 8 segments over 9
+    to 40 inputs; the X stage needs K % 8 == 0)."""
+    import synth
+
+    N = 2048
+    raw = synth.stations_offset_binary(S, N * K, rho=rho, lags=np.arange(S) % 3, seed=S + K)
+    p = cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=cg.VIS_BASELINE_MAJOR)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis)
+    inputs = list(range(min(S, 8)))
+    X = orc.fx_spectra_f64(raw, S, N, K, inputs=inputs)
+    pairs = [(a, b) for a in range(len(inputs)) for b in range(a + 1)]
+    sel = [orc.tri_index(inputs[a], inputs[b]) for a, b in pairs]
+    _tc_bars(orc, vis, X, pairs, K, sel=sel, chans=slice(None))
+
+
+def test_fx_tc_fstage_2048_delay_model(cg, orc, fstage_engine):
+    """Integer shifts (start offsets at every sample alignment) and the fringe /
+    fractional-delay phasor in the tensor-core F stage's epilogue."""
+    import synth
+
+    S, N, K = 5, 2048, 40
+    fs, lo = 32e6, 8.4e9
+    margin = 4096
+    raw = synth.stations_offset_binary(S, N * K + 2 * margin, rho=0.5, seed=21)
+    rng = np.random.default_rng(6)
+    poly = np.zeros((S, 4))
+    poly[:, 0] = rng.uniform(-40e-6, 40e-6, S)
+    poly[:, 1] = rng.uniform(-2e-3, 2e-3, S)          # fast rates: the shift walks through alignments
+    p = cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=cg.VIS_BASELINE_MAJOR,
+                     start_sample=margin, fs_hz=fs, lo_hz=lo)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis, delay_poly=poly)
+    shift, ph0, dph = orc.delay_state_f64(poly, N, K, fs, lo)
+    assert len(set((shift.ravel() + margin) % 64)) > 20          # many sample alignments
+    X = orc.fx_spectra_f64(raw, S, N, K, margin, shift, ph0, dph)
+    pairs = [(i, j) for i in range(S) for j in range(i + 1)]
+    # the random delays decorrelate the inputs: the phase bar covers the autos
+    _tc_bars(orc, vis, X, pairs, K, cross_coverage=False)
