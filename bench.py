@@ -295,6 +295,14 @@ def main():
         e2e_value = world * S * T_run / (e2e_ms * 1e-3) / 1e9
 
     # ---- roofline of the dominant kernel -----------------------------------
+    # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) measured by
+    # ncu --set full on cases larger than L2 with the same per-unit work, scaled
+    # by the units one launch here processes: the warp-FFT F stage moved 4,407 B
+    # per input-segment (512 inputs x 512 segments, N = 2048); the tensor-core
+    # X stage moved 9.63 MB per channel (512 inputs x 4096 segments x 256
+    # channels).  None where no capture of that kernel exists.
+    F_TRAFFIC_PER_SEGMENT = 4407.0 if N_run == 2048 else None
+    X_TRAFFIC_PER_CHANNEL = 9.63e6 * K_run / 4096.0
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
     f_bytes = S * K_run * (N_run // 4 + C_run * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
@@ -313,14 +321,17 @@ def main():
             pk = peaks["bf16_tflops"]
             roof = {"bound": "tensor", "kernel": "k_xmac_tc", "achieved": stages["x_stage_tflops"], "peak": pk,
                     "unit": "TFLOP/s", "frac": stages["x_stage_tflops"] / pk,
-                    "peak_source": f"{peak_kind} dense bf16 (burst)", "traffic": None}
+                    "peak_source": f"{peak_kind} dense bf16 (burst)",
+                    "traffic": X_TRAFFIC_PER_CHANNEL * C_run}
     else:
         pk = peaks["hbm_gbs"]
         tc_f = x_mode == cg.X_TC_FP16 and N_run == 2048 and os.environ.get("CELLSPE_FSTAGE_TC") == "1"
         fk = "k_fx_fstage_tc" if tc_f else ("k_fx_fstage_w2048" if N_run == 2048 else "k_fx_fstage")
         roof = {"bound": "hbm", "kernel": fk, "achieved": stages["f_stage_gbs"], "peak": pk,
                 "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
-                "traffic": None}
+                "traffic": (F_TRAFFIC_PER_SEGMENT * S * K_run
+                            if F_TRAFFIC_PER_SEGMENT and fk == "k_fx_fstage_w2048" else None),
+                "note": "F stage is bound by instruction issue and the shared-memory pipe (ncu), not HBM"}
 
     serving = None
     if args.serve_seconds > 0:

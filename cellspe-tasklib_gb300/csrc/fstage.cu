@@ -273,7 +273,7 @@ template <int N_PENDING>
 CS_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N_PENDING) : "memory"); }
 
 template <int FMT, bool PHASE, int WARPS, int ROUNDS, int G>
-__global__ void __launch_bounds__(32 * WARPS, (WARPS == 16) ? 1 : (WARPS == 8) ? 2 : 3) k_fx_fstage_w2048(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
+__global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WARPS == 8) ? 2 : 3) k_fx_fstage_w2048(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
 {
     constexpr int M = 1024, N = 2048, NT = 32 * WARPS, PER = G / WARPS;
     static_assert(G % WARPS == 0 && G % 8 == 0, "segments per CTA");
@@ -470,7 +470,7 @@ int launch_w2048_variant(const CsFStageArgs& a, const float2* tw, cudaStream_t s
     return (int)cudaGetLastError();
 }
 
-constexpr int W_NVARIANTS = 4;
+constexpr int W_NVARIANTS = 5;
 
 template <int FMT, bool PHASE>
 int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cudaStream_t st)
@@ -482,6 +482,10 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
             // 16 warps, 16 segments: 32-byte output runs (FP16 staging fits)
             if constexpr (FMT == CS_SPECTRA_F16) return launch_w2048_variant<FMT, PHASE, 16, 1, 16>(a, tw, st);
             return launch_w2048_variant<FMT, PHASE, 8, 1>(a, tw, st);
+        case 5:
+            // 8 warps, 32 segments (4 per warp): 64-byte output runs
+            if constexpr (FMT == CS_SPECTRA_F16) return launch_w2048_variant<FMT, PHASE, 8, 1, 32>(a, tw, st);
+            return launch_w2048_variant<FMT, PHASE, 8, 1>(a, tw, st);
         default: return launch_w2048_variant<FMT, PHASE, 8, 1>(a, tw, st);
     }
 }
@@ -490,7 +494,8 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
 // 2 = 4 warps, two segments each with the second prefetched; 3 = 8 warps,
 // two rounds of 8 segments per CTA (the second round's raw words prefetched
 // during the first); 4 = 16 warps and 16 segments per CTA, so that each
-// output row gets a 32-byte run (FP16 only).  Picked once per process by
+// output row gets a 32-byte run; 5 = 8 warps, 32 segments per CTA (64-byte
+// runs); 4 and 5 are FP16 only.  Picked once per process by
 // timing all on a 64-input x 512-segment job of zero samples (the FFT's
 // arithmetic does not depend on the values; the spectra exceed the L2 cache
 // and use the padded row pitch of the FX path), unless the environment
