@@ -158,6 +158,100 @@ def run_serving(cg, torch, seconds: float, rate: float, x_mode: int, seed: int =
             "job_mix": "S in {4,8,24,64,200}, C in {256,1024,4096,16384}, T = 2^U, U in [18,24]"}
 
 
+def _time_calls(torch, fn, steps: int, warmup: int) -> float:
+    """Milliseconds per call by CUDA events (device-resident buffers)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_configs(cg, torch, x_mode: int, with_cpu: bool):
+    """The other benchmark configurations, measured beside the headline: the FP32
+    path on the headline job, the Mark5B spectrometer (payload and framed
+    recordings) and the 16-station delay-tracked job, each with its CPU rate."""
+    out = {}
+    # -- FP32 CUDA-core path on the headline job (tensor-core vs FP32 ratio)
+    T = N * K
+    g = torch.Generator(device="cuda").manual_seed(4)
+    raw = torch.randint(0, 256, (S, T // 4), dtype=torch.uint8, device="cuda", generator=g)
+    vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
+    p32 = cg.fx_params(S, N, K, T // 4, x_mode=cg.X_FP32, vis_order=cg.VIS_CHANNEL_MAJOR)
+    ms = _time_calls(torch, lambda: cg.fx_correlate(p32, raw, vis), steps=3, warmup=1)
+    out["fp32_path"] = {"value": S * T / (ms * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms,
+                        "workload": "same as the headline, x_mode = FP32 CUDA cores"}
+    del raw, vis
+
+    # -- Mark5B spectrometer: 16 subbands x 2^25 samples, N = 65536, overlap 2, cosine^2, PCal
+    nsub, nsamp, NS, fs = 16, 1 << 25, 65536, 32e6
+    kspec = nsamp // NS
+    payload = torch.randint(0, 256, (nsamp * nsub // 4,), dtype=torch.uint8, device="cuda", generator=g)
+    power = torch.empty((nsub, 1, NS // 2 + 1), dtype=torch.float32, device="cuda")
+    bins = torch.empty((nsub, 1, 32), dtype=torch.complex64, device="cuda")
+    sp = cg.spec_params(NS, 2, 2, kspec, 1, nsub, payload.numel(), tonebins=32, rotatorlen=32, ntones=16,
+                        fs_hz=fs, memory=cg.MEM_DEVICE)
+    ms = _time_calls(torch, lambda: cg.spectrometer(sp, payload, power, bins), steps=5, warmup=2)
+    nffts = nsub * (2 * kspec - 1)
+    res = {"value": nsub * nsamp / (ms * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms,
+           "fft_tflops": nffts * 2.5 * NS * 16 / (ms * 1e-3) / 1e12,
+           "workload": "Mark5B 16 subbands x 2^25 samples (1 s at 32 MS/s), N=65536, overlap 2, cosine^2, PCal 32 bins"}
+    # framed recording: 16-byte headers per 10000-byte payload, blanking on
+    nf = -(-payload.numel() // 10000)
+    framed = torch.zeros((nf, 10016), dtype=torch.uint8, device="cuda")
+    framed[:, 0:4] = torch.tensor([0xED, 0xDE, 0xAD, 0xAB], dtype=torch.uint8, device="cuda")
+    flat = framed[:, 16:].reshape(-1)
+    flat[: payload.numel()] = payload
+    framed = framed.reshape(-1)
+    spf = cg.spec_params(NS, 2, 2, kspec, 1, nsub, framed.numel(), layout=cg.SPEC_MARK5B_FRAMED, tonebins=32,
+                         rotatorlen=32, ntones=16, fs_hz=fs, memory=cg.MEM_DEVICE)
+    ms_f = _time_calls(torch, lambda: cg.spectrometer(spf, framed, power, bins), steps=5, warmup=2)
+    res["framed_value"] = nsub * nsamp / (ms_f * 1e-3) / 1e9
+    res["framed_ms_per_step"] = ms_f
+    if with_cpu:
+        import oracle
+
+        # oracle spectrometer (single thread) on one subband, 16 FFT lengths
+        x = np.random.default_rng(2).standard_normal(16 * NS).astype(np.float32)
+        t0 = time.perf_counter()
+        oracle.spectrometer(x, NS, 2, 2, 16, 32, 32, 0.0, fs)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": x.size / dt / 1e9, "unit": "Gsamples/s", "cores": 1, "kind": "port",
+                               "sample": f"1 subband x {16 * NS} samples, {dt:.2f} s"}
+    out["mark5b_spectrometer"] = res
+    del payload, framed, power, bins
+
+    # -- 16-station dual-pol (32 inputs), N = 8192, K = 4096, cubic delay model, one subband
+    S3, N3, K3 = 32, 8192, 4096
+    T3 = N3 * K3
+    margin = 1 << 17
+    raw3 = torch.randint(0, 256, (S3, (T3 + 2 * margin) // 4), dtype=torch.uint8, device="cuda", generator=g)
+    rng = np.random.default_rng(3)
+    poly = np.zeros((S3, 4))
+    poly[:, 0] = rng.uniform(-2e-3, 2e-3, S3)
+    poly[:, 1] = rng.uniform(-3e-6, 3e-6, S3)
+    poly[:, 2] = rng.uniform(-1e-9, 1e-9, S3)
+    poly[:, 3] = rng.uniform(-1e-12, 1e-12, S3)
+    dpoly = torch.from_numpy(poly).cuda()
+    vis3 = torch.empty((N3 // 2, S3 * (S3 + 1) // 2), dtype=torch.complex64, device="cuda")
+    r3 = {"workload": "32 inputs, N=8192 (4096 channels), K=4096, cubic delay per input (a0 within +-2 ms), "
+                      "fs 32 MS/s, LO 8.4 GHz, one of 8 subbands"}
+    for name, mode in (("tc", cg.X_TC_FP16), ("fp32", cg.X_FP32)):
+        p3 = cg.fx_params(S3, N3, K3, raw3.shape[1], x_mode=mode, vis_order=cg.VIS_CHANNEL_MAJOR,
+                          start_sample=margin, fs_hz=32e6, lo_hz=8.4e9)
+        ms3 = _time_calls(torch, lambda: cg.fx_correlate(p3, raw3, vis3, delay_poly=dpoly), steps=3, warmup=1)
+        r3[name] = {"value": S3 * T3 / (ms3 * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms3}
+    out["fx_16station_delay"] = r3
+    del raw3, vis3
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args):
     """CPU implementation of the path (the oracle's FX restatement), all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -202,6 +296,8 @@ def main():
     ap.add_argument("--cpu-segments", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the FP32-path, spectrometer and delay-tracked measurements")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="length of the Poisson arrival window of the serving measurement (0 skips it)")
     ap.add_argument("--segments", type=int, default=K,
@@ -336,13 +432,19 @@ def main():
     serving = None
     if args.serve_seconds > 0:
         serving = run_serving(cg, torch, args.serve_seconds, 200.0, x_mode)
+    configs = None
+    if not args.no_configs and N_run == N:
+        configs = run_configs(cg, torch, x_mode, with_cpu=(rank == 0 and not args.no_cpu))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
         v, dt = cpu_baseline(raw_h, args.cpu_segments, nthreads)
+        v1, dt1 = cpu_baseline(raw_h, max(1, args.cpu_segments // 8), 1)
         cpu = {"value": v, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
-               "sample": f"{S} inputs x {args.cpu_segments} segments x {N_run} samples, {dt:.1f} s"}
+               "sample": f"{S} inputs x {args.cpu_segments} segments x {N_run} samples, {dt:.1f} s",
+               "value_1core": v1,
+               "sample_1core": f"{S} inputs x {max(1, args.cpu_segments // 8)} segments, {dt1:.1f} s"}
 
     if rank == 0:
         line = {
@@ -363,6 +465,7 @@ def main():
             "stages": stages,
             "clocks": clk.summary(),
             "serving": serving,
+            "configs": configs,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))

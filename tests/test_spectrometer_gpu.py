@@ -128,3 +128,20 @@ def test_spectrometer_planes_layout_and_device(cg):
     cg.spectrometer(cg.spec_params(N, 2, 2, K, 1, nsub, planes.size, layout=cg.SPEC_PLANES),
                     torch.from_numpy(planes).cuda(), b)
     assert np.array_equal(a, b.cpu().numpy())
+
+
+def test_spectrometer_config2_shape(cg, orc):
+    """The Mark5B spectrometer configuration's shape (16 subbands, N = 65536,
+    overlap 2, cosine^2, PCal at 1 MHz) on 64 FFT lengths per subband of random
+    2-bit codes; two subbands checked against the oracle."""
+    nsub, N, K, fs = 16, 65536, 64, 32e6
+    raw = np.random.default_rng(12).integers(0, 256, N * K * nsub // 4, dtype=np.uint8)
+    p = cg.spec_params(N, 2, 2, K, 1, nsub, raw.size, tonebins=32, rotatorlen=32, ntones=16, fs_hz=fs)
+    power = np.zeros((nsub, 1, N // 2 + 1), np.float32)
+    bins = np.zeros((nsub, 1, 32), np.complex64)
+    cg.spectrometer(p, raw, power, bins)
+    planes = orc.unpack2bit(raw, N * K, nsub, orc.MARK5B_LUT)
+    for c in (0, 11):
+        ref, ref_b = orc.spectrometer(planes[c], N, 2, 2, K, 32, 32, 0.0, fs)
+        assert np.linalg.norm(power[c] - ref) / np.linalg.norm(ref) < TOL
+        assert np.linalg.norm(bins[c] - ref_b) / np.linalg.norm(ref_b) < TOL
