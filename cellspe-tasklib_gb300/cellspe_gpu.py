@@ -161,6 +161,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_spectrometer_workspace_bytes": ([V], LL),
             "cellspe_spectrometer_noalloc": ([V, V, V, V, V, V], I),
             "cellspe_mark5b_decode": ([V, LL, I, LL, V, I, V], I),
+            "cellspe_spectrometer_xpol": ([V, V, V, I, I, V, V, V], I),
             "cellspe_mark5b_deframe": ([V, LL, I, LL, V, V, I, V], I),
             "cellspe_service_create": ([V], V),
             "cellspe_service_submit": ([V, V, V, V, V, ctypes.POINTER(ctypes.c_longlong)], I),
@@ -315,6 +316,15 @@ def spectrometer(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None
                                       _ptr(pcal_bins)[0] if pcal_bins is not None else None,
                                       _ptr(pcal_tones)[0] if pcal_tones is not None else None))
     return power
+
+
+def spectrometer_xpol(params: SpecParams, raw0, raw1, channel0: int, channel1: int, power, xpol, pcal_bins=None):
+    """cellspe_spectrometer_xpol: power [2][n][N/2+1], xpol [n][N/2+1] complex, pcal [2][n][T]."""
+    params.memory = _mem(raw0, raw1, power, xpol)
+    _check(lib().cellspe_spectrometer_xpol(ctypes.byref(params), _ptr(raw0)[0], _ptr(raw1)[0], channel0, channel1,
+                                           _ptr(power)[0], _ptr(xpol)[0],
+                                           _ptr(pcal_bins)[0] if pcal_bins is not None else None))
+    return power, xpol
 
 
 def mark5b_decode(framed, nchan: int, nsamp: int, out) -> Mark5bInfo:

@@ -10,7 +10,10 @@
 // plus the folded phase-cal bins to <BaseFilename>_pcal.bin when ExtractPCal
 // is set.  The arithmetic runs in cellspe_spectrometer (TaskCoreIPP::doMaths
 // on the GPU) for all subbands of the input at once; the file keeps the
-// subband named by UseFile1Channel / UseFile2Channel.
+// subband named by UseFile1Channel.  With two input files (two sources) the
+// spectra come from cellspe_spectrometer_xpol: the second source's auto
+// spectra go to <BaseFilename>_file2_swspec.bin and the cross-polarisation
+// spectrum (N/2+1 complex64 per spectrum) to <BaseFilename>_xpol_swspec.bin.
 //
 // Input: 2-bit samples (BitsPerSample = 2), SourceChannels channels
 // interleaved per sample time (Mark5B payload order, or the TwoBit order with
@@ -162,6 +165,54 @@ int main(int argc, char** argv)
     const long long bytes_per_spec = K * N * s.channels / 4;
     if (K < 1) { std::cerr << "Error: integration shorter than one FFT\n"; return -1; }
 
+    cellspe_spec_params p;
+    std::memset(&p, 0, sizeof p);
+    p.fft_points = (int)N; p.overlap = s.overlap; p.window = s.window; p.ffts_per_spectrum = (int)K;
+    p.n_spectra = 1; p.n_subbands = s.channels; p.input_layout = CELLSPE_SPEC_INTERLEAVED;
+    p.levels = s.mark5b ? CELLSPE_LEVELS_MARK5B : CELLSPE_LEVELS_TWOBIT;
+    p.raw_bytes = bytes_per_spec; p.pcal_tonebins = tonebins; p.pcal_rotatorlen = rotlen;
+    p.pcal_ntones = 0; p.pcal_offset_hz = s.pcal_offset; p.sample_rate_hz = s.fs; p.memory = CELLSPE_MEM_HOST;
+
+    if (argc == 4) {
+        // two sources: auto spectra of both plus the cross spectrum
+        // (TaskCoreIPP::doMaths with num_sources = 2, num_xpols = 1;
+        // swspectrometer.cpp:247-254, 341-358 name the outputs)
+        std::ifstream in0(argv[2], std::ios::binary), in1(argv[3], std::ios::binary);
+        if (!in0 || !in1) { std::cerr << "Error: cannot open the input files\n"; return -1; }
+        const std::string base1 = fill_pattern(s.base, s, s.use_ch[0]);
+        const std::string base2 = fill_pattern(s.base + "_file2", s, s.use_ch[1]);
+        std::ofstream out0(base1 + "_swspec.bin", std::ios::binary), out1(base2 + "_swspec.bin", std::ios::binary);
+        std::ofstream outx(base1 + "_xpol_swspec.bin", std::ios::binary);
+        std::ofstream pout0, pout1;
+        if (s.pcal) { pout0.open(base1 + "_pcal.bin", std::ios::binary); pout1.open(base2 + "_pcal.bin", std::ios::binary); }
+        void* raw0 = cellspe_host_alloc((size_t)bytes_per_spec);
+        void* raw1 = cellspe_host_alloc((size_t)bytes_per_spec);
+        if (!raw0 || !raw1) { std::cerr << "Error: " << cellspe_last_error() << "\n"; return -1; }
+        std::vector<float> power((size_t)2 * (N / 2 + 1)), xpol((size_t)2 * (N / 2 + 1));
+        std::vector<float> bins((size_t)2 * std::max(tonebins, 1) * 2);
+        long long nspec = 0;
+        int status = 0;
+        while (in0.read((char*)raw0, bytes_per_spec) && in0.gcount() == bytes_per_spec &&
+               in1.read((char*)raw1, bytes_per_spec) && in1.gcount() == bytes_per_spec) {
+            int rc = cellspe_spectrometer_xpol(&p, raw0, raw1, s.use_ch[0] - 1, s.use_ch[1] - 1, power.data(),
+                                               xpol.data(), s.pcal ? bins.data() : nullptr);
+            if (rc) { std::cerr << "Error: " << cellspe_last_error() << "\n"; status = -1; break; }
+            out0.write((const char*)power.data(), sizeof(float) * (N / 2 + 1));
+            out1.write((const char*)(power.data() + (N / 2 + 1)), sizeof(float) * (N / 2 + 1));
+            outx.write((const char*)xpol.data(), sizeof(float) * 2 * (N / 2 + 1));
+            if (s.pcal) {
+                pout0.write((const char*)bins.data(), sizeof(float) * 2 * tonebins);
+                pout1.write((const char*)(bins.data() + 2 * tonebins), sizeof(float) * 2 * tonebins);
+            }
+            nspec++;
+        }
+        std::cerr << nspec << " spectra of " << N << " points from two sources (channels " << s.use_ch[0] << ", "
+                  << s.use_ch[1] << ") -> " << base1 << "_xpol_swspec.bin\n";
+        cellspe_host_free(raw0);
+        cellspe_host_free(raw1);
+        return status;
+    }
+
     int status = 0;
     for (int f = 0; f < argc - 2; f++) {
         std::ifstream in(argv[2 + f], std::ios::binary);
@@ -175,13 +226,6 @@ int main(int argc, char** argv)
         std::vector<float> power((size_t)s.channels * (N / 2 + 1));
         std::vector<float> bins((size_t)s.channels * std::max(tonebins, 1) * 2);
         if (!raw) { std::cerr << "Error: " << cellspe_last_error() << "\n"; return -1; }
-        cellspe_spec_params p;
-        std::memset(&p, 0, sizeof p);
-        p.fft_points = (int)N; p.overlap = s.overlap; p.window = s.window; p.ffts_per_spectrum = (int)K;
-        p.n_spectra = 1; p.n_subbands = s.channels; p.input_layout = CELLSPE_SPEC_INTERLEAVED;
-        p.levels = s.mark5b ? CELLSPE_LEVELS_MARK5B : CELLSPE_LEVELS_TWOBIT;
-        p.raw_bytes = bytes_per_spec; p.pcal_tonebins = tonebins; p.pcal_rotatorlen = rotlen;
-        p.pcal_ntones = 0; p.pcal_offset_hz = s.pcal_offset; p.sample_rate_hz = s.fs; p.memory = CELLSPE_MEM_HOST;
         long long nspec = 0;
         while (in.read((char*)raw, bytes_per_spec) && in.gcount() == bytes_per_spec) {
             int rc = cellspe_spectrometer(&p, raw, power.data(), s.pcal ? bins.data() : nullptr, nullptr);

@@ -109,9 +109,26 @@ struct CsSpecArgs {
     const float2* rot_table;    // pcal rotator, rotatorlen entries
     int ffts_per_chunk;         // FFTs per partial spectrum (0: default)
     const uint32_t* valid_mask; // bit t: sample time t of the planes is data (null: all data)
+    int pcal_sources;           // sources sharing the call's FFT count (0 or 1: one)
+    int pcal_source;            // this source's index among them
+    int skip_power;             // 1: phase-cal only (no power spectra)
 };
 int64_t cs_spectrometer_scratch_floats(const CsSpecArgs& a);
+int64_t cs_spectrometer_pcal_floats(const CsSpecArgs& a);   // the phase-cal part of it
 int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st);
+// Window function of TaskCoreIPP::generate_windowfunction, n floats (cached).
+const float* cs_window_table(int type, int n);
+
+// spectrometer_xpol.cu: two sources and their cross spectrum.
+// Overlapped, windowed windows of one 2-bit plane (LSB first, optional
+// validity mask): out[nspec * novl][N] floats, window j of spectrum s from
+// sample s*K*N + j*N/overlap.
+int cs_spec_windows(const uint8_t* plane, const uint32_t* vmask, int N, int overlap, int K, int nspec, int window,
+                    const float lut[4], float* out, cudaStream_t st);
+// X0, X1: [nspec * novl][N/2+1] spectra -> power [2][nspec][N/2+1] (autos of
+// both sources) and xpol [nspec][N/2+1] (X0 conj X1, DC / Nyquist real).
+int cs_xpol_reduce(const float2* X0, const float2* X1, int N, int overlap, int K, int nspec, float* power,
+                   float2* xpol, cudaStream_t st);
 
 // mark5b.cu (framed Mark5B input) ----------------------------------------
 // Frame search + per-frame valid byte ranges (fill-pattern blanking); the

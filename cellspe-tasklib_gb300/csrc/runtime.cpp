@@ -518,39 +518,47 @@ long long spec_bytes(const cellspe_spec_params* p)
     return b;
 }
 
-int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw, float* power, void* pcal_bins,
-                    void* pcal_tones)
+// Checks shared by the spectrometer entry points ("who" names the caller).
+int spec_check(const cellspe_spec_params* p, const char* who)
 {
-    if (!p || !raw || !power) return set_err(CELLSPE_ERR_ARG, "spectrometer: null argument");
+    const std::string w(who);
     const int nsub = p->n_subbands;
-    if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16)) return set_err(CELLSPE_ERR_ARG, "spectrometer: n_subbands must be 1, 4, 8 or 16");
+    if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16)) return set_err(CELLSPE_ERR_ARG, w + ": n_subbands must be 1, 4, 8 or 16");
     if (!pow2(p->fft_points) || p->fft_points < 1024 || p->fft_points > 65536)
-        return set_err(CELLSPE_ERR_ARG, "spectrometer: fft_points must be a power of two in [1024, 65536]");
-    const bool framed = p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED;
-    if (framed) {
-        if (nsub == 1) return set_err(CELLSPE_ERR_ARG, "spectrometer: framed Mark5B input needs 4, 8 or 16 subbands");
-        if (p->raw_bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, "spectrometer: framed input shorter than two frames");
+        return set_err(CELLSPE_ERR_ARG, w + ": fft_points must be a power of two in [1024, 65536]");
+    if (p->overlap < 1 || p->ffts_per_spectrum < 1 || p->n_spectra < 1 || p->fft_points % (16 * p->overlap))
+        return set_err(CELLSPE_ERR_ARG, w + ": bad overlap, ffts_per_spectrum or n_spectra");
+    if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED) {
+        if (nsub == 1) return set_err(CELLSPE_ERR_ARG, w + ": framed Mark5B input needs 4, 8 or 16 subbands");
+        if (p->raw_bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, w + ": framed input shorter than two frames");
         const long long avail = (p->raw_bytes / M5B_FRAME) * (M5B_PAYLOAD / (nsub / 4));
         if ((long long)p->n_spectra * p->ffts_per_spectrum * p->fft_points > avail)
-            return set_err(CELLSPE_ERR_ARG, "spectrometer: spectra need more samples than the frames hold");
+            return set_err(CELLSPE_ERR_ARG, w + ": spectra need more samples than the frames hold");
     } else if (p->input_layout != CELLSPE_SPEC_INTERLEAVED && p->input_layout != CELLSPE_SPEC_PLANES) {
-        return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown input_layout");
+        return set_err(CELLSPE_ERR_ARG, w + ": unknown input_layout");
     } else if (p->raw_bytes <= 0 || p->raw_bytes % (16 * nsub)) {
-        return set_err(CELLSPE_ERR_ARG, "spectrometer: raw_bytes must be a multiple of 16*n_subbands");
+        return set_err(CELLSPE_ERR_ARG, w + ": raw_bytes must be a multiple of 16*n_subbands");
     }
-    if (p->pcal_tonebins > 0 && !pcal_bins) return set_err(CELLSPE_ERR_ARG, "spectrometer: pcal enabled without pcal_bins");
-    float lut[4];
-    if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown level table");
-    long long need = spec_bytes(p);
-    long long budget = job_limit(ws);
-    if (need > budget) return set_err(CELLSPE_ERR_NOMEM, "spectrometer: job exceeds the device memory budget");
-    const bool host = p->memory == CELLSPE_MEM_HOST;
-    Job j(ws, host);
-    const uint8_t* d_raw = (const uint8_t*)j.in(raw, (size_t)p->raw_bytes);
-    long long bytes_per_sub = p->raw_bytes / nsub;
-    const uint8_t* planes = d_raw;
+    return 0;
+}
+
+// One recording on the device as per-subband 2-bit planes (+ validity mask
+// for framed Mark5B): interleaved input is corner-turned, framed input is
+// searched, deframed and corner-turned in one pass, planes are used in place.
+struct SpecPlanes {
+    const uint8_t* planes = nullptr;
+    long long bytes_per_sub = 0;
     const uint32_t* vmask = nullptr;
-    if (framed) {
+};
+
+SpecPlanes spec_planes(Workspace& ws, Job& j, const cellspe_spec_params* p, const void* raw)
+{
+    const int nsub = p->n_subbands;
+    SpecPlanes r;
+    const uint8_t* d_raw = (const uint8_t*)j.in(raw, (size_t)p->raw_bytes);
+    r.planes = d_raw;
+    r.bytes_per_sub = p->raw_bytes / nsub;
+    if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED) {
         const long long nframes = p->raw_bytes / M5B_FRAME, groups = m5b_groups(p->raw_bytes, nsub);
         void* pl = j.scratch((size_t)(groups * 4 * nsub));
         void* mk = j.scratch((size_t)((groups + 1) / 2 * 4));
@@ -563,9 +571,9 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
                                           (uint32_t*)pl, (uint32_t*)mk, ws.stream), "deframe");
             if (rc) j.err = rc;
         }
-        planes = (const uint8_t*)pl;
-        vmask = (const uint32_t*)mk;
-        bytes_per_sub = groups * 4;
+        r.planes = (const uint8_t*)pl;
+        r.vmask = (const uint32_t*)mk;
+        r.bytes_per_sub = groups * 4;
     } else if (p->input_layout == CELLSPE_SPEC_INTERLEAVED && nsub > 1) {
         void* pl = j.scratch((size_t)p->raw_bytes);
         if (!j.err) {
@@ -573,15 +581,39 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
             int rc = map_rc(cs_cornerturn2bit(d_raw, nsamp, nsub, pl, ws.stream), "corner turn");
             if (rc) j.err = rc;
         }
-        planes = (const uint8_t*)pl;
+        r.planes = (const uint8_t*)pl;
     }
+    return r;
+}
+
+CsSpecArgs spec_args(const cellspe_spec_params* p, const SpecPlanes& sp, const float lut[4])
+{
     CsSpecArgs a{};
-    a.planes = planes; a.bytes_per_sub = bytes_per_sub; a.nsub = nsub; a.N = p->fft_points; a.valid_mask = vmask;
+    a.planes = sp.planes; a.bytes_per_sub = sp.bytes_per_sub; a.nsub = p->n_subbands; a.N = p->fft_points;
+    a.valid_mask = sp.vmask;
     a.overlap = p->overlap; a.window = p->window; a.ffts_per_spectrum = p->ffts_per_spectrum; a.nspec = p->n_spectra;
-    std::memcpy(a.lut, lut, sizeof lut);
+    std::memcpy(a.lut, lut, 4 * sizeof(float));
     a.tonebins = p->pcal_tonebins; a.rotatorlen = p->pcal_rotatorlen; a.ntones = p->pcal_ntones;
     a.pcal_offset_hz = p->pcal_offset_hz; a.fs_hz = p->sample_rate_hz;
-    const long long rows = (long long)nsub * p->n_spectra;
+    return a;
+}
+
+int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw, float* power, void* pcal_bins,
+                    void* pcal_tones)
+{
+    if (!p || !raw || !power) return set_err(CELLSPE_ERR_ARG, "spectrometer: null argument");
+    if (int rc = spec_check(p, "spectrometer")) return rc;
+    if (p->pcal_tonebins > 0 && !pcal_bins) return set_err(CELLSPE_ERR_ARG, "spectrometer: pcal enabled without pcal_bins");
+    float lut[4];
+    if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "spectrometer: unknown level table");
+    long long need = spec_bytes(p);
+    long long budget = job_limit(ws);
+    if (need > budget) return set_err(CELLSPE_ERR_NOMEM, "spectrometer: job exceeds the device memory budget");
+    const bool host = p->memory == CELLSPE_MEM_HOST;
+    Job j(ws, host);
+    const SpecPlanes sp = spec_planes(ws, j, p, raw);
+    CsSpecArgs a = spec_args(p, sp, lut);
+    const long long rows = (long long)p->n_subbands * p->n_spectra;
     a.power = (float*)j.out(power, (size_t)rows * (p->fft_points / 2 + 1) * 4, false);
     if (a.tonebins > 0) {
         a.pcal_bins = (float2*)j.out(pcal_bins, (size_t)rows * a.tonebins * 8, false);
@@ -590,6 +622,76 @@ int op_spectrometer(Workspace& ws, const cellspe_spec_params* p, const void* raw
     a.partial = (float*)j.scratch((size_t)cs_spectrometer_scratch_floats(a) * 4);
     if (!j.err) {
         int rc = map_rc(cs_spectrometer(a, ws.stream), "spectrometer");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
+// Device bytes of one cross-polarisation job: both recordings' planes, the
+// windows of one source and the spectra of both.
+long long spec_xpol_bytes(const cellspe_spec_params* p)
+{
+    const long long N = p->fft_points, nb = N / 2 + 1;
+    const long long nwin = (long long)p->n_spectra * (p->overlap * p->ffts_per_spectrum - (p->overlap - 1));
+    cellspe_spec_params one = *p;
+    one.n_subbands = p->n_subbands;
+    long long b = 2 * spec_bytes(&one);
+    b += align256(nwin * N * 4) + 2 * align256(nwin * nb * 8);
+    b += align256(3LL * p->n_spectra * nb * 8);
+    return b;
+}
+
+int op_spectrometer_xpol(Workspace& ws, const cellspe_spec_params* p, const void* raw0, const void* raw1, int ch0,
+                         int ch1, float* power, void* xpol, void* pcal_bins)
+{
+    const char* who = "spectrometer_xpol";
+    if (!p || !raw0 || !raw1 || !power || !xpol) return set_err(CELLSPE_ERR_ARG, "spectrometer_xpol: null argument");
+    if (int rc = spec_check(p, who)) return rc;
+    if (p->fft_points > 32768)
+        return set_err(CELLSPE_ERR_UNSUPPORTED, "spectrometer_xpol: fft_points above 32768 are not supported");
+    if (ch0 < 0 || ch0 >= p->n_subbands || ch1 < 0 || ch1 >= p->n_subbands)
+        return set_err(CELLSPE_ERR_ARG, "spectrometer_xpol: channel outside the recording's subbands");
+    if (p->pcal_tonebins > 0 && !pcal_bins) return set_err(CELLSPE_ERR_ARG, "spectrometer_xpol: pcal enabled without pcal_bins");
+    float lut[4];
+    if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "spectrometer_xpol: unknown level table");
+    if (spec_xpol_bytes(p) > job_limit(ws))
+        return set_err(CELLSPE_ERR_NOMEM, "spectrometer_xpol: job exceeds the device memory budget");
+    const bool host = p->memory == CELLSPE_MEM_HOST;
+    const int N = p->fft_points, nb = N / 2 + 1, nspec = p->n_spectra;
+    const long long nwin = (long long)nspec * (p->overlap * p->ffts_per_spectrum - (p->overlap - 1));
+    Job j(ws, host);
+    SpecPlanes sp[2] = {spec_planes(ws, j, p, raw0), spec_planes(ws, j, p, raw1)};
+    const int ch[2] = {ch0, ch1};
+    float* d_power = (float*)j.out(power, (size_t)2 * nspec * nb * 4, false);
+    float2* d_xpol = (float2*)j.out(xpol, (size_t)nspec * nb * 8, false);
+    float2* d_bins = p->pcal_tonebins > 0 ? (float2*)j.out(pcal_bins, (size_t)2 * nspec * p->pcal_tonebins * 8, false)
+                                          : nullptr;
+    float* win = (float*)j.scratch((size_t)(nwin * N * 4));
+    float2* X[2] = {(float2*)j.scratch((size_t)(nwin * nb * 8)), (float2*)j.scratch((size_t)(nwin * nb * 8))};
+    for (int s = 0; s < 2 && !j.err; s++) {
+        const uint8_t* plane = sp[s].planes + (long long)ch[s] * sp[s].bytes_per_sub;
+        if ((long long)nspec * p->ffts_per_spectrum * N > sp[s].bytes_per_sub * 4) {
+            j.err = set_err(CELLSPE_ERR_ARG, "spectrometer_xpol: spectra need more samples than the recording holds");
+            break;
+        }
+        int rc = map_rc(cs_spec_windows(plane, sp[s].vmask, N, p->overlap, p->ffts_per_spectrum, nspec, p->window, lut,
+                                        win, ws.stream), "windows");
+        if (!rc) rc = map_rc(cs_rfft_batch(win, X[s], N, nwin, ws.stream), "window FFTs");
+        if (!rc && d_bins) {
+            // phase-cal of this source alone: the FFT count advances after
+            // both sources' FFTs (two sources share it)
+            CsSpecArgs a = spec_args(p, sp[s], lut);
+            a.planes = plane; a.nsub = 1; a.skip_power = 1;
+            a.pcal_sources = 2; a.pcal_source = s;
+            a.pcal_bins = d_bins + (size_t)s * nspec * p->pcal_tonebins;
+            a.partial = (float*)j.scratch((size_t)cs_spectrometer_scratch_floats(a) * 4);
+            if (!j.err) rc = map_rc(cs_spectrometer(a, ws.stream), "phase-cal");
+        }
+        if (rc) j.err = rc;
+    }
+    if (!j.err) {
+        int rc = map_rc(cs_xpol_reduce(X[0], X[1], N, p->overlap, p->ffts_per_spectrum, nspec, d_power, d_xpol,
+                                       ws.stream), "cross spectrum");
         if (rc) j.err = rc;
     }
     return j.finish();
@@ -1702,6 +1804,13 @@ int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* p
 }
 
 long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p) { return p ? spec_bytes(p) : -1; }
+
+int cellspe_spectrometer_xpol(const cellspe_spec_params* p, const void* raw0, const void* raw1, int channel0,
+                              int channel1, float* power, void* xpol, void* pcal_bins)
+{
+    DIRECT_PROLOGUE
+    return op_spectrometer_xpol(*ws, p, raw0, raw1, channel0, channel1, power, xpol, pcal_bins);
+}
 
 int cellspe_mark5b_decode(const void* framed, long long bytes, int nchan, long long nsamp, float* out, int memory,
                           cellspe_mark5b_info* info)

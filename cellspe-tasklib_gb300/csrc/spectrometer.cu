@@ -208,36 +208,42 @@ __global__ void k_spec_reduce(const float* __restrict__ partial, float* __restri
 
 // PCal fold: thread-private accumulators in shared memory, [bin][thread].
 // TaskCoreIPP::doMaths folds the overlapped FFT windows whose running FFT
-// count is a multiple of the overlap factor (TaskCoreIPP.cpp:414-418), and the
-// count runs on across the spectra of one call (it starts at 0 once,
-// :358).  Spectrum s therefore folds windows j = j0, j0+ov, ... < novl with
-// j0 = (-s*novl) mod ov: cnt back-to-back stretches of N samples starting
-// j0*hop samples into the spectrum.  The rotator index restarts at every
-// window, which is the index relative to the fold start because N % L == 0.
+// count is a multiple of the overlap factor (TaskCoreIPP.cpp:414-418).  The
+// count starts at 0 once per call (:358), runs on across the spectra of the
+// call and advances after every source's FFT (:434-435), so with ns sources
+// source rs folds window j of spectrum s when (ns (s novl + j) + rs) % ov == 0:
+// an arithmetic progression j0, j0 + step, ... (step = ov / gcd(ns, ov)),
+// possibly empty.  Each window is folded from its own start (the rotator
+// index restarts), N samples from j * hop.
+CS_DEV int gcd_int(int a, int b) { while (b) { int t = a % b; a = b; b = t; } return a; }
+
 __global__ void k_pcal_fold(const uint8_t* __restrict__ planes, int64_t bytes_per_sub, int nspec, int64_t samp_per_spec,
-                            int N, int ov, int novl, int T, int L, const float2* __restrict__ rot, float l0, float l1,
-                            float l2, float l3, const uint32_t* __restrict__ vmask, float2* __restrict__ partial,
-                            int nblk_per_row)
+                            int N, int ov, int novl, int ns, int rs, int T, int L, const float2* __restrict__ rot,
+                            float l0, float l1, float l2, float l3, const uint32_t* __restrict__ vmask,
+                            float2* __restrict__ partial, int nblk_per_row)
 {
     extern __shared__ float2 pacc[];                 // [T][blockDim]
     const int row = blockIdx.y, sub = row / nspec, spec = row % nspec;
     const int nt = blockDim.x, tid = threadIdx.x;
     for (int b = 0; b < T; b++) pacc[b * nt + tid] = make_float2(0.f, 0.f);
     const uint32_t* plane = reinterpret_cast<const uint32_t*>(planes + (int64_t)sub * bytes_per_sub);
-    const int j0 = (ov - (int)(((int64_t)spec * novl) % ov)) % ov;
-    const int cnt = j0 < novl ? (novl - 1 - j0) / ov + 1 : 0;
-    const int64_t w_begin = ((int64_t)spec * samp_per_spec + (int64_t)j0 * (N / ov)) / 16;
-    const int64_t nwords = (int64_t)cnt * N / 16;
+    const int step = ov / gcd_int(ns, ov);
+    int j0 = -1;
+    for (int j = 0; j < step && j < novl; j++)
+        if (((int64_t)ns * ((int64_t)spec * novl + j) + rs) % ov == 0) { j0 = j; break; }
+    const int cnt = j0 >= 0 ? (novl - 1 - j0) / step + 1 : 0;
+    const int hop = N / ov, wpw = N / 16;            // 32-bit words per window
+    const int64_t nwords = (int64_t)cnt * wpw;
     const float lut[4] = {l0, l1, l2, l3};
     for (int64_t w = (int64_t)blockIdx.x * nt + tid; w < nwords; w += (int64_t)nblk_per_row * nt) {
-        uint32_t word = __ldg(plane + w_begin + w);
-        const int64_t wg = w_begin + w;
+        const int win = (int)(w / wpw), wi = (int)(w - (int64_t)win * wpw);
+        const int64_t wg = ((int64_t)spec * samp_per_spec + (int64_t)(j0 + win * step) * hop) / 16 + wi;
+        uint32_t word = __ldg(plane + wg);
         const uint32_t valid = vmask ? __ldg(vmask + (wg >> 1)) >> ((wg & 1) * 16) : 0xffffu;
-        int64_t n0 = w * 16;                         // sample index relative to the fold start
+        const int n0 = wi * 16;                      // sample index inside the window
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-            int64_t n = n0 + j;
-            int li = (int)(n % L);
+            int li = (n0 + j) % L;
             float x = (valid >> j) & 1u ? lut_pick4(lut, (word >> (2 * j)) & 3u) : 0.f;
             float2 r = __ldg(rot + li);
             float2& slot = pacc[(li % T) * nt + tid];
@@ -313,16 +319,30 @@ int spec_nchunk(const CsSpecArgs& a)
 }
 }  // namespace
 
+const float* cs_window_table(int type, int n) { return window_table(type, n); }
+
+// Scratch layout: chunk partial spectra, then (256-byte aligned: N/2+1 is
+// odd, and the phase-cal partials are float2) the phase-cal partials.
+int64_t power_partial_floats(const CsSpecArgs& a)
+{
+    const int64_t power = (int64_t)a.nsub * a.nspec * spec_nchunk(a) * (a.N / 2 + 1);
+    return (power + 63) / 64 * 64;
+}
+
+int64_t cs_spectrometer_pcal_floats(const CsSpecArgs& a)
+{
+    return a.tonebins > 0 ? (int64_t)a.nsub * a.nspec * PCAL_BLOCKS * a.tonebins * 2 : 0;
+}
+
 int64_t cs_spectrometer_scratch_floats(const CsSpecArgs& a)
 {
-    int64_t power = (int64_t)a.nsub * a.nspec * spec_nchunk(a) * (a.N / 2 + 1);
-    int64_t pcal = a.tonebins > 0 ? (int64_t)a.nsub * a.nspec * PCAL_BLOCKS * a.tonebins * 2 : 0;
-    return power + pcal;
+    return power_partial_floats(a) + cs_spectrometer_pcal_floats(a);
 }
 
 int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
 {
-    if (!a.planes || !a.power || !a.partial || a.nsub <= 0 || a.nspec <= 0 || a.ffts_per_spectrum <= 0)
+    if (!a.planes || (!a.power && !a.skip_power) || !a.partial || a.nsub <= 0 || a.nspec <= 0 ||
+        a.ffts_per_spectrum <= 0)
         return CS_ERR_ARG;
     if (a.overlap < 1 || a.N % (16 * a.overlap) != 0) return CS_ERR_ARG;
     if ((uintptr_t)a.planes % 16 || a.bytes_per_sub % 16) return CS_ERR_ARG;
@@ -330,8 +350,8 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
     if ((int64_t)a.nspec * a.ffts_per_spectrum * a.N > a.bytes_per_sub * 4) return CS_ERR_ARG;
     if (a.nsub * a.nspec > 65535) return CS_ERR_ARG;
     const int nchunk = spec_nchunk(a);
-    int rc;
-    switch (a.N) {
+    int rc = 0;
+    if (!a.skip_power) switch (a.N) {
         case 1024: rc = launch_power<512, 1>(a, nchunk, st); break;
         case 2048: rc = launch_power<1024, 1>(a, nchunk, st); break;
         case 4096: rc = launch_power<2048, 1>(a, nchunk, st); break;
@@ -344,24 +364,28 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
     if (rc) return rc;
     const int rows = a.nsub * a.nspec, nb = a.N / 2 + 1;
     const int novl = a.overlap * a.ffts_per_spectrum - (a.overlap - 1);
-    const float scale = (float)(1.0 / (double)novl);
-    int64_t tot = (int64_t)rows * nb;
-    k_spec_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a.partial, a.power, rows, nchunk, nb, scale), cs_count_launches(1);
-    CS_CUDA_TRY(cudaGetLastError());
+    if (!a.skip_power) {
+        const float scale = (float)(1.0 / (double)novl);
+        int64_t tot = (int64_t)rows * nb;
+        k_spec_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a.partial, a.power, rows, nchunk, nb, scale),
+            cs_count_launches(1);
+        CS_CUDA_TRY(cudaGetLastError());
+    }
 
     if (a.tonebins > 0) {
         const int T = a.tonebins, L = a.rotatorlen;
         if (L <= 0 || L % T != 0 || a.N % L != 0 || T > 128 || !a.pcal_bins) return CS_ERR_ARG;
         const float2* rot = a.rot_table ? a.rot_table : rotator_table(L, a.pcal_offset_hz, a.fs_hz);
         if (!rot) return CS_ERR_ARG;
-        float2* pp = reinterpret_cast<float2*>(a.partial + (int64_t)rows * nchunk * nb);
+        float2* pp = reinterpret_cast<float2*>(a.partial + power_partial_floats(a));
         int64_t samp_per_spec = (int64_t)a.ffts_per_spectrum * a.N;
         int nt = PCAL_THREADS;
         size_t smem = (size_t)T * nt * sizeof(float2);
         CS_CUDA_TRY(cudaFuncSetAttribute(k_pcal_fold, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int ns = a.pcal_sources > 0 ? a.pcal_sources : 1;
         k_pcal_fold<<<dim3(PCAL_BLOCKS, rows), nt, smem, st>>>(a.planes, a.bytes_per_sub, a.nspec, samp_per_spec, a.N,
-                                                               a.overlap, novl, T, L, rot, a.lut[0], a.lut[1], a.lut[2], a.lut[3],
-                                                               a.valid_mask, pp,
+                                                               a.overlap, novl, ns, a.pcal_source, T, L, rot, a.lut[0],
+                                                               a.lut[1], a.lut[2], a.lut[3], a.valid_mask, pp,
                                                                PCAL_BLOCKS), cs_count_launches(1);
         CS_CUDA_TRY(cudaGetLastError());
         k_pcal_reduce<<<(rows + 63) / 64, 64, 0, st>>>(pp, rows, PCAL_BLOCKS, T, a.ntones, a.pcal_bins, a.pcal_tones), cs_count_launches(1);

@@ -139,9 +139,8 @@ extern "C" int cellspe_spectrometer_noalloc(const cellspe_spec_params* p, const 
     a.ffts_per_chunk = 0;
     if ((size_t)cs_spectrometer_scratch_floats(a) > CS_NOALLOC_SCRATCH_FLOATS) {
         const long long rows = (long long)nsub * p->n_spectra, nb = N / 2 + 1;
-        const long long pcal = p->pcal_tonebins > 0 ? cs_spectrometer_scratch_floats(a) - rows * nb *
-                                                       ((novl + 31) / 32)
-                                                    : 0;
+        // phase-cal partials + 64 floats of alignment between the two parts
+        const long long pcal = cs_spectrometer_pcal_floats(a) + 64;
         const long long max_chunks = ((long long)CS_NOALLOC_SCRATCH_FLOATS - pcal) / (rows * nb);
         if (max_chunks < 1)
             return cs_set_error(CELLSPE_ERR_ARG,

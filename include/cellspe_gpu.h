@@ -196,6 +196,23 @@ int cellspe_spectrometer(const cellspe_spec_params* p, const void* raw, float* p
                          void* pcal_bins, void* pcal_tones);
 long long cellspe_spectrometer_workspace_bytes(const cellspe_spec_params* p);
 
+/* Two recordings (sources) and their cross-polarisation spectrum:
+ * TaskCoreIPP::doMaths with two sources and one cross product
+ * (spectrometer/src/IA-32/TaskCoreIPP.cpp:394-513).  raw0 and raw1 are two
+ * recordings in the layout p describes (p->raw_bytes each, p->n_subbands
+ * channels); channel0 / channel1 pick the subband of each (UseFile1Channel - 1,
+ * UseFile2Channel - 1).  Outputs, n = p->n_spectra, nb = fft_points/2 + 1:
+ *   power     [2][n][nb] float     auto spectra of source 0 and source 1
+ *   xpol      [n][nb] complex64    sum X0 conj(X1) over the overlapped FFTs;
+ *                                  bins 0 and nb-1 real (Re X0 Re X1)
+ *   pcal_bins [2][n][tonebins] complex64 or NULL; as in the reference the FFT
+ *             count advances after each source's FFT, so with overlap 2 source
+ *             0 folds every overlapped window and source 1 none.
+ * All spectra are scaled by 1/(overlap*K - (overlap-1)).  fft_points up to
+ * 32768. */
+int cellspe_spectrometer_xpol(const cellspe_spec_params* p, const void* raw0, const void* raw1, int channel0,
+                              int channel1, float* power, void* xpol, void* pcal_bins);
+
 /* ---- framed Mark5B input ------------------------------------------------
  * A Mark5B recording is a run of 10016-byte frames: a 16-byte header (sync
  * word 0xABADDEED, frame number, BCD time code) and 10000 bytes of 2-bit

@@ -69,6 +69,8 @@ def lib() -> ctypes.CDLL:
         _lib.orc_rfft_f32.argtypes = [V, V, I]
         _lib.orc_spectrometer.argtypes = [V, L, V, V, V]
         _lib.orc_spectrometer.restype = I
+        _lib.orc_spectrometer_xpol.argtypes = [V, V, L, V, V, V, V]
+        _lib.orc_spectrometer_xpol.restype = I
         _lib.orc_spec_window.argtypes = [I, I, V]
         _lib.orc_pcal_tones.argtypes = [V, I, I, V]
         _lib.orc_fx_fp32.argtypes = [V, L, I, I, I, L, V, V, V, I, V, I]
@@ -179,6 +181,23 @@ def spectrometer(samples: np.ndarray, N: int, overlap: int, window: int, K: int,
     n = lib().orc_spectrometer(_ptr(samples), samples.size, ctypes.byref(cfg), _ptr(power),
                                _ptr(pc) if tonebins else None)
     return power[:n], (pc[:n] if tonebins else None)
+
+
+def spectrometer_xpol(s0: np.ndarray, s1: np.ndarray, N: int, overlap: int, window: int, K: int,
+                      tonebins: int = 0, rotatorlen: int = 0, offset_hz: float = 0.0, fs_hz: float = 1.0):
+    """Two sources: (power [2][nspec][N/2+1], xpol [nspec][N/2+1], pcal [2][nspec][tonebins] or None)."""
+    s0 = np.ascontiguousarray(s0, np.float32)
+    s1 = np.ascontiguousarray(s1, np.float32)
+    assert s0.size == s1.size
+    cfg = SpecCfg(N, overlap, window, K, tonebins, rotatorlen, offset_hz, fs_hz)
+    nspec = s0.size // (N * K)
+    power = np.zeros((2, nspec, N // 2 + 1), np.float32)
+    xpol = np.zeros((nspec, N // 2 + 1), np.complex64)
+    pc = np.zeros((2, nspec, max(tonebins, 1)), np.complex64)
+    n = lib().orc_spectrometer_xpol(_ptr(s0), _ptr(s1), s0.size, ctypes.byref(cfg), _ptr(power), _ptr(xpol),
+                                    _ptr(pc) if tonebins else None)
+    assert n == nspec
+    return power, xpol, (pc if tonebins else None)
 
 
 def window(kind: int, n: int) -> np.ndarray:

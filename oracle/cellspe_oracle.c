@@ -313,6 +313,87 @@ int orc_spectrometer(const float* samples, int64_t nsamp, const orc_spec_cfg* cf
     return spec;
 }
 
+/* Two sources and their cross spectrum: TaskCoreIPP::doMaths with
+ * num_sources = 2, num_xpols = 1 (TaskCoreIPP.cpp:394-513).  Per hop, each
+ * source in turn: phase-cal fold when the FFT count (starting at 0 once,
+ * advanced after every source's FFT) is a multiple of the overlap
+ * (:414-418, :434-435), window, real FFT, auto power with DC/Nyquist as real
+ * products (:437-447); then the cross spectrum X0 conj(X1) for bins
+ * 1..N/2-1 through ippsConj + ippsAddProduct, with DC and Nyquist as real
+ * products and zero imaginary parts (:456-487).  Spectra are scaled by
+ * 1/core_overlapped_ffts (:491-499). */
+int orc_spectrometer_xpol(const float* s0, const float* s1, int64_t nsamp, const orc_spec_cfg* cfg,
+                          float* power, orc_cf32* xpol, orc_cf32* pcal_bins)
+{
+    const int N = cfg->fft_points, nb = N / 2 + 1;
+    const int hop = N / cfg->overlap;
+    const int novl = orc_spec_overlapped_ffts(cfg);
+    const float scale = (float)(1.0 / (double)novl);
+    const int nspec_max = (int)(nsamp / ((int64_t)N * cfg->ffts_per_spectrum));
+    float* w = (float*)malloc(sizeof(float) * (size_t)N);
+    float* xw = (float*)malloc(sizeof(float) * (size_t)N);
+    orc_cf32* X[2];
+    X[0] = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)nb);
+    X[1] = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)nb);
+    orc_cf32* conj1 = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)nb);
+    orc_cf32* rot = NULL;
+    orc_spec_window(cfg->window, N, w);
+    if (cfg->pcal_tonebins > 0) {
+        rot = (orc_cf32*)malloc(sizeof(orc_cf32) * (size_t)cfg->pcal_rotatorlen);
+        double dphi = 2 * M_PI * (-cfg->pcal_offset_hz / cfg->sample_rate_hz);
+        for (int i = 0; i < cfg->pcal_rotatorlen; i++) {
+            rot[i].re = (float)cos(dphi * (double)i);
+            rot[i].im = (float)sin(dphi * (double)i);
+        }
+    }
+    const size_t psz = (size_t)nspec_max * nb, tsz = (size_t)nspec_max * (size_t)cfg->pcal_tonebins;
+    memset(power, 0, sizeof(float) * 2 * psz);
+    memset(xpol, 0, sizeof(orc_cf32) * psz);
+    if (pcal_bins && rot) memset(pcal_bins, 0, sizeof(orc_cf32) * 2 * tsz);
+    int64_t pos = 0, remaining = nsamp;
+    int acc = 0, spec = 0, curr = 0;
+    while (remaining >= N && spec < nspec_max) {
+        for (int rs = 0; rs < 2; rs++) {
+            const float* x = (rs ? s1 : s0) + pos;
+            float* P = power + (size_t)rs * psz + (size_t)spec * nb;
+            if (rot && pcal_bins && (curr % cfg->overlap) == 0)
+                pcal_fold(x, N, cfg, rot, pcal_bins + (size_t)rs * tsz + (size_t)spec * cfg->pcal_tonebins);
+            for (int i = 0; i < N; i++) xw[i] = w[i] * x[i];
+            orc_rfft_f32(xw, X[rs], N);
+            curr++;
+            float re0 = X[rs][0].re, reN2 = X[rs][N / 2].re;
+            float acc0 = P[0] + re0 * re0;
+            float accN = P[nb - 1] + reN2 * reN2;
+            for (int k = 1; k < nb - 1; k++) P[k] += X[rs][k].re * X[rs][k].re + X[rs][k].im * X[rs][k].im;
+            P[0] = acc0; P[nb - 1] = accN;
+        }
+        orc_cf32* XP = xpol + (size_t)spec * nb;
+        float old0 = XP[0].re, oldN = XP[nb - 1].re;
+        for (int k = 1; k < nb - 1; k++) { conj1[k].re = X[1][k].re; conj1[k].im = -X[1][k].im; }
+        orc_addproduct_32fc(X[0] + 1, conj1 + 1, XP + 1, nb - 2);
+        XP[0].re = old0 + X[0][0].re * X[1][0].re;
+        XP[0].im = 0.0f;
+        XP[nb - 1].re = oldN + X[0][N / 2].re * X[1][N / 2].re;
+        XP[nb - 1].im = 0.0f;
+        pos += hop;
+        remaining -= hop;
+        if (++acc >= novl) {
+            float* P0 = power + (size_t)spec * nb;
+            float* P1 = power + psz + (size_t)spec * nb;
+            for (int k = 0; k < nb; k++) {
+                P0[k] *= scale;
+                P1[k] *= scale;
+                XP[k].re *= scale;
+                XP[k].im *= scale;
+            }
+            spec++; acc = 0;
+            pos += N - hop; remaining -= N - hop;
+        }
+    }
+    free(w); free(xw); free(X[0]); free(X[1]); free(conj1); free(rot);
+    return spec;
+}
+
 void orc_pcal_tones(const orc_cf32* bins, int nbins, int ntones, orc_cf32* tones)
 {
     for (int k = 0; k < ntones; k++) {

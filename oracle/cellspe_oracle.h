@@ -99,6 +99,16 @@ void orc_spec_window(int type, int n, float* w);
 int orc_spectrometer(const float* samples, int64_t nsamp, const orc_spec_cfg* cfg,
                      float* power, orc_cf32* pcal_bins);
 
+/* Two sources and their cross spectrum (TaskCoreIPP::doMaths with
+ * num_sources = 2, num_xpols = 1, TaskCoreIPP.cpp:394-513).  power:
+ * [2][nspec][N/2+1]; xpol: [nspec][N/2+1] complex (bins 1..N/2-1:
+ * sum X0 conj(X1); DC and Nyquist real); pcal_bins: [2][nspec][tonebins] or
+ * NULL, folded where the FFT count (advanced after every source's FFT) is a
+ * multiple of the overlap.  nspec = nsamp / (N * K) spectra are written;
+ * returns the number computed. */
+int orc_spectrometer_xpol(const float* s0, const float* s1, int64_t nsamp, const orc_spec_cfg* cfg,
+                          float* power, orc_cf32* xpol, orc_cf32* pcal_bins);
+
 /* Phase-cal tones from folded bins: DFT of the bins scaled by 1/Nbins
  * (IPP_FFT_DIV_FWD_BY_N), first ntones outputs.  PCal.cpp:280-300. FP64. */
 void orc_pcal_tones(const orc_cf32* bins, int nbins, int ntones, orc_cf32* tones);

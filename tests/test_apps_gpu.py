@@ -61,3 +61,48 @@ def test_minicorrelator_cli_matches_oracle(cg, orc):
     v = ref[orc.tri_index(1, 0)]
     assert np.allclose(nums[:4], v.real[:4], rtol=1e-4, atol=1e-3)
     assert np.allclose(nums[4:8], v.imag[:4], rtol=1e-4, atol=1e-3)
+
+
+def test_swspectrometer_cli_two_sources(cg, orc, tmp_path):
+    """Two input files: both auto spectra and the cross-polarisation spectrum."""
+    import synth
+
+    N, K, fs, nspec, nsub = 2048, 4, 32e6, 2, 4
+    rng = np.random.default_rng(3)
+    common = rng.standard_normal((N * K * nspec, nsub))
+    files = []
+    for f in range(2):
+        x = 0.6 * common + 0.8 * rng.standard_normal(common.shape)
+        raw = synth.pack2bit(synth.quantize_mark5b(x.astype(np.float32)).reshape(-1))
+        path = tmp_path / f"src{f}.m5b"
+        raw.tofile(path)
+        files.append((path, raw))
+    ini = tmp_path / "spec.ini"
+    ini.write_text(f"""[Spectrometer]
+FFTpoints = {N}
+FFTIntegrationTimeSec = {K * N / fs}
+FFToverlapFactor = 2
+WindowType = Cosine2
+BandwidthHz = {fs / 2}
+SourceFormat = Mark5B-512-4-2
+BitsPerSample = 2
+SourceChannels = {nsub}
+UseFile1Channel = 2
+UseFile2Channel = 2
+BaseFilename1 = {tmp_path}/out
+""")
+    r = subprocess.run([str(PKG / "swspectrometer_gpu"), str(ini), str(files[0][0]), str(files[1][0])],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nb = N // 2 + 1
+    a0 = np.fromfile(tmp_path / "out_swspec.bin", np.float32).reshape(nspec, nb)
+    a1 = np.fromfile(tmp_path / "out_file2_swspec.bin", np.float32).reshape(nspec, nb)
+    xp = np.fromfile(tmp_path / "out_xpol_swspec.bin", np.complex64).reshape(nspec, nb)
+    for s in range(nspec):
+        sl = slice(s * N * K, (s + 1) * N * K)
+        x0 = orc.unpack2bit(files[0][1], N * K * nspec, nsub, orc.MARK5B_LUT)[1][sl]
+        x1 = orc.unpack2bit(files[1][1], N * K * nspec, nsub, orc.MARK5B_LUT)[1][sl]
+        rp, rx, _ = orc.spectrometer_xpol(x0, x1, N, 2, 2, K)
+        assert np.linalg.norm(a0[s] - rp[0, 0]) / np.linalg.norm(rp[0, 0]) < 1e-5
+        assert np.linalg.norm(a1[s] - rp[1, 0]) / np.linalg.norm(rp[1, 0]) < 1e-5
+        assert np.linalg.norm(xp[s] - rx[0]) / np.linalg.norm(rx[0]) < 1e-5
