@@ -147,7 +147,10 @@ CS_DEV float2 twiddle(const float2* __restrict__ tw, int m) { return __ldg(tw + 
 //   codelet and writes back (Stockham autosort: the result ends up in natural
 //   order).  The caller provides the group-wide barrier.
 // ---------------------------------------------------------------------------
-template <int M> struct CtaFft {
+// TWREC: each butterfly loads one twiddle w from the table and forms w^2..w^15
+// by a balanced recurrence (w^2e = (w^e)^2, w^(2e+1) = w^2e w: at most four
+// products deep), trading table loads for FMA work.
+template <int M, bool TWREC = false> struct CtaFft {
     static_assert(M >= 16 && (M & (M - 1)) == 0, "M must be a power of two >= 16");
     static constexpr int T = M / 16;
 
@@ -181,8 +184,17 @@ template <int M> struct CtaFft {
             int j = t + q * T;
             int k = j & (NS - 1);
             constexpr int STEP = M / (NS * R);
+            if constexpr (TWREC) {
+                float2 wp[R];
+                wp[1] = twiddle(tw, k * STEP * tws);
 #pragma unroll
-            for (int r = 1; r < R; r++) v[q][r] = cmul(v[q][r], twiddle(tw, (r * k) * STEP * tws));
+                for (int e = 2; e < R; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], wp[1]) : cmul(wp[e / 2], wp[e / 2]);
+#pragma unroll
+                for (int r = 1; r < R; r++) v[q][r] = cmul(v[q][r], wp[r]);
+            } else {
+#pragma unroll
+                for (int r = 1; r < R; r++) v[q][r] = cmul(v[q][r], twiddle(tw, (r * k) * STEP * tws));
+            }
             Dft<R>::run(v[q]);
             int base = (j - k) * R + k;
 #pragma unroll

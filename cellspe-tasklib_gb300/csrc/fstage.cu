@@ -27,6 +27,7 @@
 namespace {
 
 CS_DEV int out_pitch(const CsFStageArgs& a) { return a.kp ? a.kp : a.K; }
+CS_DEV int out_rows(const CsFStageArgs& a) { return a.S_out ? a.S_out : a.S; }
 
 template <int M> struct FCfg {
     static constexpr int T = M / 16;
@@ -131,11 +132,11 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
             if (scl) X = cscale(X, __ldg(scl + c));
             if constexpr (DIRECT) {
                 if constexpr (FMT == CS_SPECTRA_F32) {
-                    reinterpret_cast<float2*>(a.out)[((int64_t)c * a.S + s) * out_pitch(a) + k] = X;
+                    reinterpret_cast<float2*>(a.out)[((int64_t)c * out_rows(a) + s) * out_pitch(a) + k] = X;
                 } else {
                     __half* o = reinterpret_cast<__half*>(a.out);
-                    o[(((int64_t)c * 2 + 0) * a.S + s) * out_pitch(a) + k] = __float2half_rn(X.x);
-                    o[(((int64_t)c * 2 + 1) * a.S + s) * out_pitch(a) + k] = __float2half_rn(X.y);
+                    o[(((int64_t)c * 2 + 0) * out_rows(a) + s) * out_pitch(a) + k] = __float2half_rn(X.x);
+                    o[(((int64_t)c * 2 + 1) * out_rows(a) + s) * out_pitch(a) + k] = __float2half_rn(X.y);
                 }
             } else if constexpr (FMT == CS_SPECTRA_F32) {
                 reinterpret_cast<float2*>(stage)[c * (G + 1) + ls] = X;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
 
     // ---- write the staging tile out, corner-turned ----
     const int nvalid = min(G, a.K - k0);
-    const int S = a.S, KP = out_pitch(a);
+    const int S = out_rows(a), KP = out_pitch(a);      // output layout
     if constexpr (FMT == CS_SPECTRA_F32) {
         const float2* st = reinterpret_cast<const float2*>(stage);
         float2* out = reinterpret_cast<float2*>(a.out);
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
 
     // corner-turned write-out of the G staged segments
     const int nvalid = max(0, min(G, a.K - k0));
-    const int S = a.S, KP = out_pitch(a);
+    const int S = out_rows(a), KP = out_pitch(a);      // output layout
     if constexpr (FMT == CS_SPECTRA_F32) {
         const float2* st = reinterpret_cast<const float2*>(stage);
         float2* out = reinterpret_cast<float2*>(a.out);

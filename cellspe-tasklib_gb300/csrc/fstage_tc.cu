@@ -543,7 +543,8 @@ int cs_fx_fstage_tc(const CsFStageArgs& a, cudaStream_t st)
     const cuuint64_t gdim[3] = {(cuuint64_t)a.K, (cuuint64_t)a.S, (cuuint64_t)FC * 2};
     const int kp = a.kp ? a.kp : a.K;
     if (kp < a.K || kp % 8) return CS_ERR_ARG;
-    const cuuint64_t gstride[2] = {(cuuint64_t)kp * 2, (cuuint64_t)kp * a.S * 2};
+    const int s_rows = a.S_out ? a.S_out : a.S;
+    const cuuint64_t gstride[2] = {(cuuint64_t)kp * 2, (cuuint64_t)kp * s_rows * 2};
     const cuuint32_t box[3] = {G, 1, 256};
     const cuuint32_t estr[3] = {1, 1, 1};
     if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, a.out, gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,

@@ -58,6 +58,9 @@ struct CsFStageArgs {
     int format;                 // CsSpectraFormat
     void* out;                  // F32: float2 [C][S][kp];  F16: __half [C][2][S][kp]
     int kp;                     // row pitch of out in elements (>= K; 0 = K)
+    int S_out;                  // inputs in the output layout (0 = S): a launch over a
+                                // block of inputs writes at out + s0 * kp with rows
+                                // (c, plane) S_out * kp apart
 };
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
 // fstage_tc.cu: the N = 2048 FP16-output F stage on the tensor cores (both
@@ -78,7 +81,7 @@ int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis,
 // spectra __half [C][2][S][kp] (K used; kp % 8 == 0) -> vis float2 [C][P];
 // inv_scale [S*C] or null.
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
-                   int accumulate, cudaStream_t st);
+                   int scale_stride, int accumulate, cudaStream_t st);   // inv_scale[s * scale_stride + c]
 // Error code of the last tensor-core X-stage launch (0 = ok; 1..3 = a
 // pipeline wait timed out).  Call after the launching stream has synchronised.
 int cs_xmac_tc_status(unsigned* code);

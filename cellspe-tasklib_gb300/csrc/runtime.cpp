@@ -129,10 +129,14 @@ struct Arena {
     }
 };
 
+constexpr int PIPE_CHUNKS = 8;        // host-buffer FX jobs: input / output chunks
+
 struct Workspace {
     cudaStream_t stream = nullptr;
+    cudaStream_t copy = nullptr;      // host <-> device copies overlapping the kernels
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t sev[5] = {};          // stage boundaries of the last FX job
+    cudaEvent_t cev[2 * PIPE_CHUNKS + 2] = {};   // copy / compute hand-offs
     Arena arena;
     bool own_stream = true;
     struct Out { void* host; const void* dev; size_t bytes; };
@@ -143,10 +147,13 @@ struct Workspace {
         int rc = ensure_device();
         if (rc) return rc;
         cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreate(&ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&ev1);
         for (auto& ev : sev)
             if (e == cudaSuccess) e = cudaEventCreate(&ev);
+        for (auto& ev : cev)
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
         return e == cudaSuccess ? 0 : cuda_fail(e, "stream setup");
     }
     void destroy()
@@ -157,6 +164,9 @@ struct Workspace {
         if (ev1) cudaEventDestroy(ev1);
         for (auto& ev : sev)
             if (ev) cudaEventDestroy(ev), ev = nullptr;
+        for (auto& ev : cev)
+            if (ev) cudaEventDestroy(ev), ev = nullptr;
+        if (copy) cudaStreamSynchronize(copy), cudaStreamDestroy(copy), copy = nullptr;
         if (stream && own_stream) cudaStreamDestroy(stream);
         stream = nullptr;
         ev0 = ev1 = nullptr;
@@ -329,7 +339,7 @@ int op_xmac_f16(Workspace& ws, bool host, const void* spectra, int S, int C, int
     const void* d_sp = j.in(spectra, (size_t)C * 2 * S * K * 2);
     void* d_vis = j.out(vis, (size_t)C * P * 8, accumulate != 0);
     if (!j.err) {
-        int rc = map_rc(cs_xmac_tc_f16(d_sp, S, C, K, K, (float2*)d_vis, nullptr, accumulate, ws.stream), "xmac_f16");
+        int rc = map_rc(cs_xmac_tc_f16(d_sp, S, C, K, K, (float2*)d_vis, nullptr, 0, accumulate, ws.stream), "xmac_f16");
         if (rc) j.err = rc;
     }
     int rc = j.finish();
@@ -386,8 +396,28 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
                                               std::to_string(budget));
     const bool host = p->memory == CELLSPE_MEM_HOST;
     const long long P = (long long)S * (S + 1) / 2;
+    const long long bpi = p->bytes_per_input;
+    // Host buffers of large jobs move in chunks on the copy stream: input
+    // blocks of inputs while the F stage transforms the blocks already there,
+    // channel blocks of visibilities while the X stage computes later ones.
+    const int nsc = (host && sync && S * bpi >= (64LL << 20)) ? std::min(S, PIPE_CHUNKS) : 1;
+    const bool stream_out = nsc > 1 && !p->accumulate && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR;
+    const int ncb = stream_out ? std::min(C, PIPE_CHUNKS) : 1;
     Job j(ws, host);
-    const uint8_t* d_raw = (const uint8_t*)j.in(raw, (size_t)S * p->bytes_per_input);
+    const uint8_t* d_raw = nsc > 1 ? (const uint8_t*)j.scratch((size_t)(S * bpi))
+                                   : (const uint8_t*)j.in(raw, (size_t)(S * bpi));
+    if (nsc > 1 && !j.err) {
+        // the copy stream starts after everything queued before this job
+        cudaEventRecord(ws.cev[2 * PIPE_CHUNKS], ws.stream);
+        cudaStreamWaitEvent(ws.copy, ws.cev[2 * PIPE_CHUNKS], 0);
+        for (int i = 0; i < nsc && !j.err; i++) {
+            const long long s0 = (long long)S * i / nsc, s1 = (long long)S * (i + 1) / nsc;
+            cudaError_t e = cudaMemcpyAsync((void*)(d_raw + s0 * bpi), (const uint8_t*)raw + s0 * bpi,
+                                            (size_t)((s1 - s0) * bpi), cudaMemcpyHostToDevice, ws.copy);
+            if (e == cudaSuccess) e = cudaEventRecord(ws.cev[i], ws.copy);
+            if (e != cudaSuccess) j.err = cuda_fail(e, "host to device copy");
+        }
+    }
     if (sync) cudaEventRecord(ws.sev[0], ws.stream);
     CsFStageArgs fa{};
     fa.raw = d_raw;
@@ -425,25 +455,54 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     fa.kp = kp;
     fa.out = j.scratch((size_t)C * S * kp * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
     if (sync) cudaEventRecord(ws.sev[1], ws.stream);
-    if (!j.err) {
-        int rc = map_rc(cs_fx_fstage(fa, ws.stream), "F stage");
+    // bytes of one spectra element: F32 rows [C][S][kp] of float2, F16 rows [C][2][S][kp] of half
+    const long long el_bytes = fa.format == CS_SPECTRA_F32 ? 8 : 2;
+    for (int i = 0; i < nsc && !j.err; i++) {
+        CsFStageArgs fb = fa;
+        if (nsc > 1) {
+            const long long s0 = (long long)S * i / nsc, s1 = (long long)S * (i + 1) / nsc;
+            cudaStreamWaitEvent(ws.stream, ws.cev[i], 0);
+            fb.raw = d_raw + s0 * bpi;
+            fb.S = (int)(s1 - s0);
+            fb.S_out = S;
+            fb.out = (char*)fa.out + s0 * kp * el_bytes;          // input s0's row in every (c, plane) block
+            if (fa.shift) fb.shift = fa.shift + s0 * K;
+            if (fa.phase0) fb.phase0 = fa.phase0 + s0 * K, fb.dphase = fa.dphase + s0 * K;
+            if (fa.scale) fb.scale = fa.scale + s0 * C;
+        }
+        int rc = map_rc(cs_fx_fstage(fb, ws.stream), "F stage");
         if (rc) j.err = rc;
     }
     if (sync) cudaEventRecord(ws.sev[2], ws.stream);
     // X stage into a channel-major buffer
     const bool direct = !host && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR && !p->accumulate;
     float2* vis_cp = direct ? (float2*)vis : (float2*)j.scratch((size_t)C * P * 8);
-    if (!j.err) {
+    for (int b = 0; b < ncb && !j.err; b++) {
+        const long long c0 = (long long)C * b / ncb, c1 = (long long)C * (b + 1) / ncb, cn = c1 - c0;
         int rc;
         if (p->x_mode == CELLSPE_X_FP32)
-            rc = cs_xmac_f32((const float2*)fa.out, S, C, K, kp, vis_cp, 0, ws.stream);
+            rc = cs_xmac_f32((const float2*)fa.out + c0 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P, 0, ws.stream);
         else
-            rc = cs_xmac_tc_f16(fa.out, S, C, K, kp, vis_cp, d_inv_scale, 0, ws.stream);
+            rc = cs_xmac_tc_f16((const uint16_t*)fa.out + c0 * 2 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P,
+                                d_inv_scale ? d_inv_scale + c0 : nullptr, C, 0, ws.stream);
         rc = map_rc(rc, "X stage");
+        if (!rc && stream_out) {
+            cudaError_t e = cudaEventRecord(ws.cev[PIPE_CHUNKS + b], ws.stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.copy, ws.cev[PIPE_CHUNKS + b], 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync((float2*)vis + c0 * P, vis_cp + c0 * P, (size_t)(cn * P * 8), cudaMemcpyDeviceToHost,
+                                    ws.copy);
+            if (e != cudaSuccess) rc = cuda_fail(e, "device to host copy");
+        }
         if (rc) j.err = rc;
     }
+    if (nsc > 1) {
+        // the job ends when the copy stream's work has ended too
+        cudaEventRecord(ws.cev[2 * PIPE_CHUNKS + 1], ws.copy);
+        cudaStreamWaitEvent(ws.stream, ws.cev[2 * PIPE_CHUNKS + 1], 0);
+    }
     if (sync) cudaEventRecord(ws.sev[3], ws.stream);
-    if (!direct && !j.err) {
+    if (!direct && !stream_out && !j.err) {
         float2* result = vis_cp;
         if (p->vis_order == CELLSPE_VIS_BASELINE_MAJOR) {
             float2* t = (float2*)j.scratch((size_t)C * P * 8);
@@ -469,6 +528,8 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         }
     }
     if (sync) cudaEventRecord(ws.sev[4], ws.stream);
+    // after a failure the copy stream may still hold copies into the workspace
+    if (nsc > 1 && j.err) cudaStreamSynchronize(ws.copy);
     int rc = j.finish(sync);
     if (sync && !rc && p->x_mode != CELLSPE_X_FP32) {
         unsigned code = 0;

@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
 
     const int j_begin = chunk * ch, j_end = min(novl, j_begin + ch);
     auto bar = [] { __syncthreads(); };
+    // P = 2, odd outputs: sample pair n = t + r T is rotated by W_N^(2n) =
+    // W_N^(2t) W_32^r (2T = N/32), one table load for all windows
+    const float2 tw_t = (P == 2) ? twiddle(tw, 2 * t) : make_float2(1.f, 0.f);
     for (int j0 = j_begin; j0 < j_end; j0 += GROUPS) {
         const int j = j0 + g;
         const bool valid = j < j_end;
@@ -147,23 +150,27 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
 #pragma unroll
         for (int r = 0; r < 16; r++) {
             const int n = t + r * T;                 // index into the transformed sequence
+            // window values of samples 2n, 2n+1 as one 8-byte load
+            const float2* win2 = reinterpret_cast<const float2*>(win);
             if constexpr (P == 1) {
                 uint32_t w = __ldg(wsrc + (2 * n >> 4));
                 int f = (2 * n) & 15;
                 const float2 x = sample_pair(lut, w, f, vmask, start + 2 * n);
-                v[r] = make_float2(x.x * __ldg(win + 2 * n), x.y * __ldg(win + 2 * n + 1));
+                const float2 wn = __ldg(win2 + n);
+                v[r] = make_float2(x.x * wn.x, x.y * wn.y);
             } else {
                 const int n2 = n + MC;
                 uint32_t w1 = __ldg(wsrc + (2 * n >> 4)), w2 = __ldg(wsrc + (2 * n2 >> 4));
                 int f1 = (2 * n) & 15, f2 = (2 * n2) & 15;
                 const float2 x1 = sample_pair(lut, w1, f1, vmask, start + 2 * n);
                 const float2 x2 = sample_pair(lut, w2, f2, vmask, start + 2 * n2);
-                float2 z1 = make_float2(x1.x * __ldg(win + 2 * n), x1.y * __ldg(win + 2 * n + 1));
-                float2 z2 = make_float2(x2.x * __ldg(win + 2 * n2), x2.y * __ldg(win + 2 * n2 + 1));
-                v[r] = p ? cmul(csub(z1, z2), twiddle(tw, 2 * n)) : cadd(z1, z2);
+                const float2 wa = __ldg(win2 + n), wb = __ldg(win2 + n2);
+                float2 z1 = make_float2(x1.x * wa.x, x1.y * wa.y);
+                float2 z2 = make_float2(x2.x * wb.x, x2.y * wb.y);
+                v[r] = p ? cmul(csub(z1, z2), rot32(tw_t, r)) : cadd(z1, z2);
             }
         }
-        CtaFft<MC>::run(fb, t, v, tw, N / MC, bar);
+        CtaFft<MC, (MC >= 8192)>::run(fb, t, v, tw, N / MC, bar);
         if (valid) {
             const int mmax = (P == 1) ? MC / 2 : (p ? MC / 2 - 1 : MC / 2);
             for (int m = t; m <= mmax; m += T) {

@@ -148,7 +148,8 @@ struct TcArgs {
     int64_t P;
     const int2* tiles;          // (i0, j0) per tile
     float2* vis;
-    const float* inv_scale;     // [S][C] or null
+    const float* inv_scale;     // [S][scale_stride] or null
+    int scale_stride;
     int accumulate;
 };
 
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
             // store instruction writes two 128-byte runs of one output row.
             float2* stg = reinterpret_cast<float2*>(smem) + (warp - 2) * 32 * 17;
             const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-            const float si = (a.inv_scale && i < S) ? __ldg(a.inv_scale + (int64_t)i * a.C + c) : 1.f;
+            const float si = (a.inv_scale && i < S) ? __ldg(a.inv_scale + (int64_t)i * a.scale_stride + c) : 1.f;
             const int ncb = (int)(n_eff / 16);
             for (int cb = 0; cb < ncb; cb++) {
                 uint32_t re[16], im[16];
@@ -280,7 +281,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                     float f = si;
                     if (a.inv_scale) {
                         const int j = j0 + cb * 16 + jj;
-                        f *= (j < S) ? __ldg(a.inv_scale + (int64_t)j * a.C + c) : 0.f;
+                        f *= (j < S) ? __ldg(a.inv_scale + (int64_t)j * a.scale_stride + c) : 0.f;
                     }
                     stg[lane * 17 + jj] = make_float2(__uint_as_float(re[jj]) * f, __uint_as_float(im[jj]) * f);
                 }
@@ -355,7 +356,7 @@ CsEncodeTiledFn cs_encode_tiled()
 }
 
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
-                   int accumulate, cudaStream_t st)
+                   int scale_stride, int accumulate, cudaStream_t st)
 {
     if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || C > 65535 || kp < K) return CS_ERR_ARG;
     if (K % 8 != 0 || kp % 8 != 0 || (uintptr_t)spectra % 16) return CS_ERR_ARG;   // TMA: 16-byte pitch and base
@@ -379,7 +380,8 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
     CS_CUDA_TRY(cudaGetSymbolAddress(&errp, g_tc_error));
     CS_CUDA_TRY(cudaMemsetAsync(errp, 0, sizeof(unsigned), st));
 
-    TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, accumulate};
+    TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, scale_stride > 0 ? scale_stride : C,
+             accumulate};
     const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
     CS_CUDA_TRY(cudaFuncSetAttribute(k_xmac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(ntiles, C);
