@@ -48,11 +48,11 @@ constexpr int stage_g()
     return g >= 16 ? 16 : (g >= 8 ? 8 : (g >= 4 ? 4 : (g >= 2 ? 2 : 1)));
 }
 
-template <int M, int FMT>
+template <int M, int FMT, bool SEGMAJ>
 size_t fstage_smem()
 {
     using C = FCfg<M>;
-    constexpr int G = stage_g<M, FMT>();
+    constexpr int G = SEGMAJ ? 1 : stage_g<M, FMT>();
     size_t elem = (FMT == CS_SPECTRA_F32) ? 8 : 4;
     size_t stage = (G == 1) ? 0 : (size_t)M * (G + 1) * elem;   // G == 1: direct stores
     return (size_t)C::GROUPS * fpad_size(M) * 8 + (size_t)C::GROUPS * C::RAWW * 4 + stage;
@@ -65,12 +65,12 @@ CS_DEV float lut_pick(const float (&l)[4], unsigned c)
     return (c & 2u) ? hi : lo;
 }
 
-template <int M, int FMT, bool PHASE>
+template <int M, int FMT, bool PHASE, bool SEGMAJ>
 __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
 {
     using Cfg = FCfg<M>;
     constexpr int T = Cfg::T, GROUPS = Cfg::GROUPS, N = 2 * M;
-    constexpr int G = stage_g<M, FMT>();
+    constexpr int G = SEGMAJ ? 1 : stage_g<M, FMT>();
     extern __shared__ __align__(16) unsigned char smem[];
     float2* fbuf_all = reinterpret_cast<float2*>(smem);
     uint32_t* rbuf_all = reinterpret_cast<uint32_t*>(fbuf_all + GROUPS * fpad_size(M));
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
             unsigned c1 = code2(rb[n1 >> 4], n1 & 15, msb);
             v[r] = make_float2(lut_pick(lut, c0), lut_pick(lut, c1));
         }
-        CtaFft<M>::run(fb, t, v, tw, 2, bar);
+        CtaFft<M, (M >= 8192)>::run(fb, t, v, tw, 2, bar);
 
         // phasor recurrences: channel kk = t + q*T and its mirror M - kk
         float2 A = make_float2(1.f, 0.f), B = A, D = A, AM = A;
@@ -130,7 +130,11 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
         auto emit = [&](int c, float2 X) {
             if (!valid) return;
             if (scl) X = cscale(X, __ldg(scl + c));
-            if constexpr (DIRECT) {
+            if constexpr (SEGMAJ) {
+                const int64_t i = ((int64_t)s * a.K + k) * M + c;      // [S][K][C], coalesced in c
+                if constexpr (FMT == CS_SPECTRA_F32) reinterpret_cast<float2*>(a.out)[i] = X;
+                else reinterpret_cast<__half2*>(a.out)[i] = __floats2half2_rn(X.x, X.y);
+            } else if constexpr (DIRECT) {
                 if constexpr (FMT == CS_SPECTRA_F32) {
                     reinterpret_cast<float2*>(a.out)[((int64_t)c * out_rows(a) + s) * out_pitch(a) + k] = X;
                 } else {
@@ -212,28 +216,43 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
     }
 }
 
-template <int M, int FMT, bool PHASE>
+template <int M, int FMT, bool PHASE, bool SEGMAJ>
 int launch_fstage(const CsFStageArgs& a, cudaStream_t st)
 {
     using Cfg = FCfg<M>;
-    constexpr int G = stage_g<M, FMT>();
+    constexpr int G = SEGMAJ ? 1 : stage_g<M, FMT>();
     const float2* tw = cs_twiddles(2 * M);
     if (!tw) return CS_ERR_ARG;
-    size_t smem = fstage_smem<M, FMT>();
-    auto kern = k_fx_fstage<M, FMT, PHASE>;
+    size_t smem = fstage_smem<M, FMT, SEGMAJ>();
+    auto kern = k_fx_fstage<M, FMT, PHASE, SEGMAJ>;
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((a.K + G - 1) / G, a.S);
     kern<<<grid, Cfg::NT, smem, st>>>(a, tw), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
-template <int M>
-int dispatch_fstage(const CsFStageArgs& a, cudaStream_t st)
+template <int M, bool SEGMAJ>
+int dispatch_fstage2(const CsFStageArgs& a, cudaStream_t st)
 {
     bool ph = a.phase0 != nullptr;
     if (a.format == CS_SPECTRA_F32)
-        return ph ? launch_fstage<M, CS_SPECTRA_F32, true>(a, st) : launch_fstage<M, CS_SPECTRA_F32, false>(a, st);
-    return ph ? launch_fstage<M, CS_SPECTRA_F16, true>(a, st) : launch_fstage<M, CS_SPECTRA_F16, false>(a, st);
+        return ph ? launch_fstage<M, CS_SPECTRA_F32, true, SEGMAJ>(a, st)
+                  : launch_fstage<M, CS_SPECTRA_F32, false, SEGMAJ>(a, st);
+    return ph ? launch_fstage<M, CS_SPECTRA_F16, true, SEGMAJ>(a, st)
+              : launch_fstage<M, CS_SPECTRA_F16, false, SEGMAJ>(a, st);
+}
+
+// Segment-major output only from 2048-point complex transforms (N >= 4096):
+// the staged corner turn there holds at most 4 segments (8-byte runs).
+template <int M>
+int dispatch_fstage(const CsFStageArgs& a, cudaStream_t st)
+{
+    if constexpr (M >= 2048) {
+        if (a.seg_major) return dispatch_fstage2<M, true>(a, st);
+    } else {
+        if (a.seg_major) return CS_ERR_ARG;
+    }
+    return dispatch_fstage2<M, false>(a, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -627,4 +646,69 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
         case 32768: return dispatch_fstage<16384>(a, st);
         default: return CS_ERR_UNSUPPORTED;
     }
+}
+
+namespace {
+
+// [S][K][C] -> channel-major rows.  Tile of 64 segments x 64 channels per
+// CTA: 256-byte reads along channels, 128- (F16) or 512-byte (F32) writes
+// along segments.
+constexpr int TT = 64;
+
+__global__ void __launch_bounds__(256) k_transpose_f16(const __half2* __restrict__ in, int K, int C, int kp, int S_out,
+                                                       __half* __restrict__ out)
+{
+    __shared__ __half2 tile[TT][TT + 1];
+    const int s = blockIdx.z, k0 = blockIdx.y * TT, c0 = blockIdx.x * TT;
+    for (int i = threadIdx.x; i < TT * TT; i += 256) {
+        const int kk = i / TT, cc = i % TT, k = k0 + kk, c = c0 + cc;
+        tile[kk][cc] = (k < K && c < C) ? in[((int64_t)s * K + k) * C + c] : __floats2half2_rn(0.f, 0.f);
+    }
+    __syncthreads();
+    // row (c, plane): 64 halves of k as 32 half pairs
+    for (int i = threadIdx.x; i < TT * 2 * (TT / 2); i += 256) {
+        const int w = i % (TT / 2), row = i / (TT / 2), cc = row >> 1, plane = row & 1;
+        const int c = c0 + cc, k = k0 + 2 * w;
+        if (c >= C || k >= K) continue;
+        const __half2 a = tile[2 * w][cc], b = tile[2 * w + 1][cc];
+        __half* o = out + (((int64_t)c * 2 + plane) * S_out + s) * kp + k;
+        if (k + 1 < K) {
+            *reinterpret_cast<__half2*>(o) = plane ? __halves2half2(__high2half(a), __high2half(b))
+                                                   : __halves2half2(__low2half(a), __low2half(b));
+        } else {
+            *o = plane ? __high2half(a) : __low2half(a);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_transpose_f32(const float2* __restrict__ in, int K, int C, int kp, int S_out,
+                                                       float2* __restrict__ out)
+{
+    __shared__ float2 tile[TT][TT + 1];
+    const int s = blockIdx.z, k0 = blockIdx.y * TT, c0 = blockIdx.x * TT;
+    for (int i = threadIdx.x; i < TT * TT; i += 256) {
+        const int kk = i / TT, cc = i % TT, k = k0 + kk, c = c0 + cc;
+        tile[kk][cc] = (k < K && c < C) ? in[((int64_t)s * K + k) * C + c] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < TT * TT; i += 256) {
+        const int kk = i % TT, cc = i / TT, c = c0 + cc, k = k0 + kk;
+        if (c < C && k < K) out[((int64_t)c * S_out + s) * kp + k] = tile[kk][cc];
+    }
+}
+
+}  // namespace
+
+int cs_spectra_transpose(const void* tmp, int S, int K, int C, int kp, int S_out, int format, void* out, cudaStream_t st)
+{
+    if (!tmp || !out || S <= 0 || K <= 0 || C <= 0 || kp < K || S_out < S || S > 65535) return CS_ERR_ARG;
+    const dim3 grid((C + TT - 1) / TT, (K + TT - 1) / TT, S);
+    if (grid.y > 65535) return CS_ERR_ARG;
+    if (format == CS_SPECTRA_F32) {
+        k_transpose_f32<<<grid, 256, 0, st>>>((const float2*)tmp, K, C, kp, S_out, (float2*)out), cs_count_launches(1);
+    } else {
+        if ((uintptr_t)out % 4 || kp % 2) return CS_ERR_ARG;
+        k_transpose_f16<<<grid, 256, 0, st>>>((const __half2*)tmp, K, C, kp, S_out, (__half*)out), cs_count_launches(1);
+    }
+    return (int)cudaGetLastError();
 }

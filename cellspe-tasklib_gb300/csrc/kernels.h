@@ -61,8 +61,16 @@ struct CsFStageArgs {
     int S_out;                  // inputs in the output layout (0 = S): a launch over a
                                 // block of inputs writes at out + s0 * kp with rows
                                 // (c, plane) S_out * kp apart
+    int seg_major;              // 1: out is [S][K][C] (F32 float2, F16 half2 Re|Im), each
+                                // segment's spectrum contiguous; cs_spectra_transpose then
+                                // makes the channel-major layout (the generic kernels only)
 };
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
+// Segment-major spectra [S][K][C] (tmp) -> the X stage's layout at out:
+// F32 float2 rows (c, s), F16 half rows (c, plane, s); row pitch kp, S_out
+// inputs per (c[, plane]) block (tmp and out already offset to the block).
+int cs_spectra_transpose(const void* tmp, int S, int K, int C, int kp, int S_out, int format, void* out,
+                         cudaStream_t st);
 // fstage_tc.cu: the N = 2048 FP16-output F stage on the tensor cores (both
 // DFT passes as tcgen05 MMAs).  cs_fx_fstage uses it for those arguments
 // when the environment sets CELLSPE_FSTAGE_TC=1.

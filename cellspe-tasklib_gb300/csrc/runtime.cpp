@@ -368,6 +368,7 @@ long long fx_bytes(const cellspe_fx_params* p, bool with_poly)
     if (host) b += align256(S * p->bytes_per_input);
     if (with_poly) b += align256(S * 32) + 3 * align256(S * K * 4);
     b += align256(C * S * spectra_pitch(K) * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));
+    if (N >= 4096) b += align256(C * S * K * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));   // segment-major spectra
     bool stage_vis = host || p->vis_order == CELLSPE_VIS_BASELINE_MAJOR || p->accumulate;
     if (stage_vis) b += 3 * align256(C * P * 8);
     if (p->x_mode != CELLSPE_X_FP32) b += 2 * align256(S * C * 4);
@@ -457,10 +458,16 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     if (sync) cudaEventRecord(ws.sev[1], ws.stream);
     // bytes of one spectra element: F32 rows [C][S][kp] of float2, F16 rows [C][2][S][kp] of half
     const long long el_bytes = fa.format == CS_SPECTRA_F32 ? 8 : 2;
+    // 4096-point and longer transforms stage at most 4 segments per CTA, so
+    // their spectra are written segment-major and transposed in 64 x 64 tiles
+    const bool segmaj = N >= 4096;
+    const long long seg_bytes = fa.format == CS_SPECTRA_F32 ? 8 : 4;       // one channel of one segment
+    char* seg_tmp = segmaj ? (char*)j.scratch((size_t)((long long)S * K * C * seg_bytes)) : nullptr;
     for (int i = 0; i < nsc && !j.err; i++) {
         CsFStageArgs fb = fa;
+        long long s0 = 0, s1 = S;
         if (nsc > 1) {
-            const long long s0 = (long long)S * i / nsc, s1 = (long long)S * (i + 1) / nsc;
+            s0 = (long long)S * i / nsc, s1 = (long long)S * (i + 1) / nsc;
             cudaStreamWaitEvent(ws.stream, ws.cev[i], 0);
             fb.raw = d_raw + s0 * bpi;
             fb.S = (int)(s1 - s0);
@@ -470,7 +477,15 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
             if (fa.phase0) fb.phase0 = fa.phase0 + s0 * K, fb.dphase = fa.dphase + s0 * K;
             if (fa.scale) fb.scale = fa.scale + s0 * C;
         }
+        void* rows_out = fb.out;
+        if (segmaj) {
+            fb.seg_major = 1;
+            fb.out = seg_tmp + s0 * K * C * seg_bytes;
+        }
         int rc = map_rc(cs_fx_fstage(fb, ws.stream), "F stage");
+        if (!rc && segmaj)
+            rc = map_rc(cs_spectra_transpose(fb.out, (int)(s1 - s0), K, C, kp, S, fa.format, rows_out, ws.stream),
+                        "spectra transpose");
         if (rc) j.err = rc;
     }
     if (sync) cudaEventRecord(ws.sev[2], ws.stream);
