@@ -149,7 +149,8 @@ CS_DEV float2 twiddle(const float2* __restrict__ tw, int m) { return __ldg(tw + 
 // ---------------------------------------------------------------------------
 // TWREC: each butterfly loads one twiddle w from the table and forms w^2..w^15
 // by a balanced recurrence (w^2e = (w^e)^2, w^(2e+1) = w^2e w: at most four
-// products deep), trading table loads for FMA work.
+// products deep), trading table loads for FMA work.  Used for transforms of
+// 2048 points and more, whose tables no longer stay in L1.
 template <int M, bool TWREC = false> struct CtaFft {
     static_assert(M >= 16 && (M & (M - 1)) == 0, "M must be a power of two >= 16");
     static constexpr int T = M / 16;

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(BCfg<M>::NT) k_fft_batch(const void* __restric
     auto bar = [] { __syncthreads(); };
     // REAL: the M-point transform of pairs uses the 2M-point table (stride 2);
     // complex: the M-point table is the 2M table at stride 2 as well.
-    CtaFft<M, (M >= 8192)>::run(fb, t, v, tw, 2, bar);
+    CtaFft<M, (M >= 2048)>::run(fb, t, v, tw, 2, bar);
     if (!valid) return;
     if constexpr (!REAL) {
 #pragma unroll

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
             unsigned c1 = code2(rb[n1 >> 4], n1 & 15, msb);
             v[r] = make_float2(lut_pick(lut, c0), lut_pick(lut, c1));
         }
-        CtaFft<M, (M >= 8192)>::run(fb, t, v, tw, 2, bar);
+        CtaFft<M, (M >= 2048)>::run(fb, t, v, tw, 2, bar);
 
         // phasor recurrences: channel kk = t + q*T and its mirror M - kk
         float2 A = make_float2(1.f, 0.f), B = A, D = A, AM = A;

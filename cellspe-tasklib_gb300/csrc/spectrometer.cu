@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
                 v[r] = p ? cmul(csub(z1, z2), rot32(tw_t, r)) : cadd(z1, z2);
             }
         }
-        CtaFft<MC, (MC >= 8192)>::run(fb, t, v, tw, N / MC, bar);
+        CtaFft<MC, (MC >= 2048)>::run(fb, t, v, tw, N / MC, bar);
         if (valid) {
             const int mmax = (P == 1) ? MC / 2 : (p ? MC / 2 - 1 : MC / 2);
             for (int m = t; m <= mmax; m += T) {
