@@ -23,11 +23,11 @@ LIB_PATH = PKG / "libcellspe_gpu.so"
 # ---- constants (cellspe_gpu.h, cellspe-tasklib*.h) --------------------------
 MEM_HOST, MEM_DEVICE = 0, 1
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_NOMEM, ERR_CUDA, ERR_INJECTED = range(6)
-LEVELS_MARK5B, LEVELS_TWOBIT, LEVELS_OFFSET_BINARY = 0, 1, 2
+LEVELS_MARK5B, LEVELS_TWOBIT, LEVELS_OFFSET_BINARY, LEVELS_VDIF = 0, 1, 2, 3
 UNPACK_MSB_FIRST = 0x100
 X_FP32, X_TC_FP16 = 0, 1
 VIS_CHANNEL_MAJOR, VIS_BASELINE_MAJOR = 0, 1
-SPEC_INTERLEAVED, SPEC_PLANES, SPEC_MARK5B_FRAMED = 0, 1, 2
+SPEC_INTERLEAVED, SPEC_PLANES, SPEC_MARK5B_FRAMED, SPEC_VDIF_FRAMED = 0, 1, 2, 3
 MARK5B_FRAME, MARK5B_PAYLOAD = 10016, 10000
 
 TASK_INCOMPLETE, TASK_OK, TASK_GENERICERROR, TASK_UNKOWNCOMMAND = 0xFFFF, 0, 1, 2
@@ -106,11 +106,20 @@ class Mark5bInfo(ctypes.Structure):
                 ("frame_number", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
+class VdifInfo(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_longlong), ("good_samples", ctypes.c_longlong),
+                ("blanked_frames", ctypes.c_longlong), ("frame_bytes", ctypes.c_int),
+                ("header_bytes", ctypes.c_int), ("mjd", ctypes.c_int), ("seconds", ctypes.c_int),
+                ("ns", ctypes.c_int), ("frame_number", ctypes.c_int), ("nchan_header", ctypes.c_int),
+                ("thread_id", ctypes.c_int), ("station_id", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
 class XmacParams(ctypes.Structure):
     _fields_ = [("S", ctypes.c_int), ("C", ctypes.c_int), ("K", ctypes.c_int), ("accumulate", ctypes.c_int)]
 
 
 assert ctypes.sizeof(FxParams) == 80 and ctypes.sizeof(SpecParams) == 88 and ctypes.sizeof(Mark5bInfo) == 40
+assert ctypes.sizeof(VdifInfo) == 64
 
 
 # ---- library loading ----------------------------------------------------------
@@ -163,6 +172,8 @@ def lib() -> ctypes.CDLL:
             "cellspe_mark5b_decode": ([V, LL, I, LL, V, I, V], I),
             "cellspe_spectrometer_xpol": ([V, V, V, I, I, V, V, V], I),
             "cellspe_mark5b_deframe": ([V, LL, I, LL, V, V, I, V], I),
+            "cellspe_vdif_decode": ([V, LL, I, I, LL, V, I, V], I),
+            "cellspe_vdif_deframe": ([V, LL, I, I, LL, V, V, I, V], I),
             "cellspe_service_create": ([V], V),
             "cellspe_service_submit": ([V, V, V, V, V, ctypes.POINTER(ctypes.c_longlong)], I),
             "cellspe_service_wait": ([V, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)], I),
@@ -333,6 +344,27 @@ def mark5b_decode(framed, nchan: int, nsamp: int, out) -> Mark5bInfo:
     nbytes = framed.numel() if _is_torch_cuda(framed) else framed.size
     _check(lib().cellspe_mark5b_decode(_ptr(framed)[0], nbytes, nchan, nsamp, _ptr(out)[0], _mem(framed, out),
                                        ctypes.byref(info)))
+    return info
+
+
+def vdif_decode(framed, nchan: int, mbps: int, nsamp: int, out) -> VdifInfo:
+    """cellspe_vdif_decode: framed VDIF bytes -> out[nchan][nsamp] float32 (0.0 where blanked)."""
+    info = VdifInfo()
+    nbytes = framed.numel() if _is_torch_cuda(framed) else framed.size
+    _check(lib().cellspe_vdif_decode(_ptr(framed)[0], nbytes, nchan, mbps, nsamp, _ptr(out)[0], _mem(framed, out),
+                                     ctypes.byref(info)))
+    return info
+
+
+def vdif_deframe(framed, nchan: int, mbps: int, frames: int = 0, payload=None, valid_mask=None) -> VdifInfo:
+    """cellspe_vdif_deframe: the payloads the decoder reads, back to back (+ validity bit per
+    sample time).  With payload None only the frame checks run (info.frames tells the size)."""
+    info = VdifInfo()
+    nbytes = framed.numel() if _is_torch_cuda(framed) else framed.size
+    _check(lib().cellspe_vdif_deframe(_ptr(framed)[0], nbytes, nchan, mbps, frames,
+                                      _ptr(payload)[0] if payload is not None else None,
+                                      _ptr(valid_mask)[0] if valid_mask is not None else None,
+                                      _mem(framed, payload, valid_mask), ctypes.byref(info)))
     return info
 
 

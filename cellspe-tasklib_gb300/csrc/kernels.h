@@ -141,22 +141,48 @@ int cs_spec_windows(const uint8_t* plane, const uint32_t* vmask, int N, int over
 int cs_xpol_reduce(const float2* X0, const float2* X1, int N, int overlap, int K, int nspec, float* power,
                    float2* xpol, cudaStream_t st);
 
-// mark5b.cu (framed Mark5B input) ----------------------------------------
+// framed.cu (framed Mark5B and VDIF input) --------------------------------
+// Geometry of a framed stream: frame f starts at offset + f * frame_bytes
+// (offset on the device for Mark5B, 0 for VDIF), its payload at
+// payload_offset bytes into the frame (frame0_payload_offset for frame 0).
+struct CsFraming {
+    int64_t frame_bytes;
+    int payload_bytes;
+    int payload_offset;
+    int frame0_payload_offset;
+    int nch;                      // 2-bit channels per sample time: 1, 2, 4, 8, 16
+};
+// VDIF header-time check (mark5_format_vdif_validate): frames whose number is
+// a multiple of `granularity` must carry the time predicted from frame 0.
+struct CsVdifClock {
+    CsFraming fmt;
+    double frame_ns;              // payload bits * 1000 / Mbps
+    long long step_ns;            // gframens / granularity (integer division)
+    int granularity;
+    int mjd0, sec0, ns0;          // time of frame 0
+    int epoch_mjd[64];            // MJD of each VDIF reference epoch
+};
 // Frame search + per-frame valid byte ranges (fill-pattern blanking); the
 // offset of the first frame stays on the device (no frame found: >= 1 MiB).
 int cs_m5b_locate(const uint8_t* framed, int64_t bytes, int* d_offset, int2* ranges, int64_t nframes, cudaStream_t st);
+// VDIF validity per frame (all or nothing): header time, invalid bit and
+// fill pattern; blanked frames counted into *d_blanked (cleared first).
+int cs_vdif_locate(const uint8_t* framed, int64_t bytes, const CsVdifClock& clk, int2* ranges, int64_t nframes,
+                   unsigned long long* d_blanked, cudaStream_t st);
 // mark5_stream_decode: nsamp samples per channel into nch float planes,
-// unblanked count added to *d_good (cleared first).
-int cs_m5b_decode(const uint8_t* framed, int64_t bytes, const int* d_offset, const int2* ranges, int nch, int64_t nsamp,
-                  const float lut[4], float* out, unsigned long long* d_good, cudaStream_t st);
-// Payload bytes back to back (nframes * 10000) and, if mask != null, one
-// validity bit per sample time.
-int cs_m5b_deframe(const uint8_t* framed, int64_t bytes, const int* d_offset, const int2* ranges, int64_t nframes,
-                   int nch, uint8_t* payload, uint32_t* mask, cudaStream_t st);
+// unblanked count added to *d_good (cleared first).  d_offset null = 0.
+int cs_framed_decode(const uint8_t* framed, int64_t bytes, const CsFraming& fmt, const int* d_offset,
+                     const int2* ranges, int64_t nsamp, const float lut[4], float* out, unsigned long long* d_good,
+                     cudaStream_t st);
+// Payload bytes back to back (nframes * payload_bytes) and, if mask != null,
+// one validity bit per sample time.
+int cs_framed_deframe(const uint8_t* framed, int64_t bytes, const CsFraming& fmt, const int* d_offset,
+                      const int2* ranges, int64_t nframes, uint8_t* payload, uint32_t* mask, cudaStream_t st);
 // Per-channel 2-bit planes ([nch][ngroups] words of 16 samples) plus the
 // validity mask (ceil(ngroups/2) words), straight from the framed bytes.
-int cs_m5b_planes(const uint8_t* framed, int64_t bytes, const int* d_offset, const int2* ranges, int64_t nframes,
-                  int nch, int64_t ngroups, uint32_t* planes, uint32_t* mask, cudaStream_t st);
+int cs_framed_planes(const uint8_t* framed, int64_t bytes, const CsFraming& fmt, const int* d_offset,
+                     const int2* ranges, int64_t nframes, int64_t ngroups, uint32_t* planes, uint32_t* mask,
+                     cudaStream_t st);
 
 // dsp.cu (task-API vector primitives) ---------------------------------------
 int cs_cmac(const float2* a, const float2* b, float2* acc, int64_t n, int conj_b, cudaStream_t st);

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <deque>
 #include <unordered_map>
 #include <condition_variable>
@@ -263,6 +264,7 @@ bool pick_levels(int format, const float* custom, float out[4])
     static const float mk5b[4] = {-3.3359f, 1.0f, -1.0f, 3.3359f};
     static const float twob[4] = {1.0f, -1.0f, 3.3359f, -3.3359f};
     static const float offb[4] = {-3.336f, -1.0f, 1.0f, 3.336f};
+    static const float vdif[4] = {-3.3359f, -1.0f, 1.0f, 3.3359f};
     if (custom) {
         std::memcpy(out, custom, 4 * sizeof(float));
         return true;
@@ -271,6 +273,7 @@ bool pick_levels(int format, const float* custom, float out[4])
         case CELLSPE_LEVELS_MARK5B: std::memcpy(out, mk5b, sizeof mk5b); return true;
         case CELLSPE_LEVELS_TWOBIT: std::memcpy(out, twob, sizeof twob); return true;
         case CELLSPE_LEVELS_OFFSET_BINARY: std::memcpy(out, offb, sizeof offb); return true;
+        case CELLSPE_LEVELS_VDIF: std::memcpy(out, vdif, sizeof vdif); return true;
         default: return false;
     }
 }
@@ -576,6 +579,336 @@ long long m5b_groups(long long raw_bytes, int nch)
     return ((nsamp + 63) / 64) * 4;
 }
 
+// ---- framed Mark5B / VDIF ---------------------------------------------------
+// Header fields as FileSource::locateFirstHeader (FileSource.cpp:330-333) and
+// the mark5access frame-number field (bits 0..14 of header word 1).
+void m5b_header_info(const uint8_t h[16], cellspe_mark5b_info* info)
+{
+    info->mjd = 56000 + (h[11] >> 4) * 100 + (h[11] & 15) * 10 + (h[10] >> 4);
+    info->seconds = (h[10] & 15) * 10000 + (h[9] >> 4) * 1000 + (h[9] & 15) * 100 + (h[8] >> 4) * 10 + (h[8] & 15);
+    info->frame_number = h[4] | ((h[5] & 0x7f) << 8);
+}
+
+// A framed stream staged on the device with its frame geometry and the valid
+// byte range of every complete frame (Mark5B: the first-frame offset stays on
+// the device in d_off; VDIF: frames from byte 0, d_off null).
+struct Located {
+    const uint8_t* d_framed = nullptr;
+    int* d_off = nullptr;
+    int2* d_ranges = nullptr;
+    unsigned long long* d_blanked = nullptr;
+    CsFraming fmt{};
+    long long off = -1, frames = 0, bytes = 0;
+};
+
+CsFraming m5b_framing(int nch) { return CsFraming{M5B_FRAME, (int)M5B_PAYLOAD, 16, 16, nch}; }
+
+// Reads n bytes at offset off of a host or device buffer into h.
+int read_head(Workspace& ws, bool host, const void* src, const uint8_t* d_src, long long off, void* h, size_t n,
+              const char* what)
+{
+    if (host) {
+        std::memcpy(h, (const uint8_t*)src + off, n);
+        return 0;
+    }
+    cudaError_t e = cudaMemcpyAsync(h, d_src + off, n, cudaMemcpyDeviceToHost, ws.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ws.stream);
+    return e == cudaSuccess ? 0 : cuda_fail(e, what);
+}
+
+// Stages the framed bytes, finds the first frame and the valid ranges of
+// every frame, and brings the frame offset back (the callers need the frame
+// count on the host).  Fills info except good_samples.
+int m5b_locate(Workspace& ws, Job& j, const void* framed, long long bytes, int nch, Located& L,
+               cellspe_mark5b_info* info)
+{
+    const long long nmax = bytes / M5B_FRAME;
+    L.fmt = m5b_framing(nch);
+    L.bytes = bytes;
+    L.d_framed = (const uint8_t*)j.in(framed, (size_t)bytes);
+    L.d_off = (int*)j.scratch(sizeof(int));
+    L.d_ranges = (int2*)j.scratch((size_t)nmax * sizeof(int2));
+    if (j.err) return j.err;
+    int rc = map_rc(cs_m5b_locate(L.d_framed, bytes, L.d_off, L.d_ranges, nmax, ws.stream), "frame search");
+    if (rc) return rc;
+    int off = 0;
+    if ((rc = read_head(ws, false, nullptr, (const uint8_t*)L.d_off, 0, &off, sizeof off, "frame search"))) return rc;
+    if (off < 0 || off >= (1 << 20)) return set_err(CELLSPE_ERR_ARG, "mark5b: no frame found in the first MiB");
+    L.off = off;
+    L.frames = (bytes - off) / M5B_FRAME;
+    if (info) {
+        uint8_t h[16];
+        if ((rc = read_head(ws, j.host, framed, L.d_framed, off, h, 16, "header read"))) return rc;
+        info->first_frame_offset = off;
+        info->frames = L.frames;
+        info->good_samples = 0;
+        m5b_header_info(h, info);
+        info->reserved = 0;
+    }
+    return 0;
+}
+
+// MJD of the VDIF reference epoch e: 1 January (even e) or 1 July (odd e) of
+// year 2000 + e / 2, counted from the proleptic Gregorian calendar (days
+// since 1 March of year 0 shifted to MJD 0 = 1858-11-17).
+int vdif_epoch_mjd(int e)
+{
+    long y = 2000 + e / 2;
+    const int month = (e & 1) ? 7 : 1;
+    if (month <= 2) y -= 1;
+    const long mp = month > 2 ? month - 3 : month + 9;           // months since March
+    const long days = 365 * y + y / 4 - y / 100 + y / 400 + (153 * mp + 2) / 5;  // day 1 of the month
+    return (int)(days - 678881);                                 // 1858-11-17 = day 678881
+}
+
+// The stream geometry and the header-time model of a VDIF buffer opened as
+// mark5access does with the format "VDIF_<payload>-<mbps>-<nch>-2"
+// (mark5_format_vdif_init, format_vdif.c:2121-2257): frame length and legacy
+// flag from the first header; frame duration payload * 8000 / mbps ns with
+// the smallest power-of-two granularity (< 128) that makes a whole number of
+// ns (32-bit products, as the library computes them); frame 0's payload 32
+// bytes into the frame whatever the header length.
+int vdif_model(const uint8_t h[32], long long bytes, int nch, int mbps, CsVdifClock& c, cellspe_vdif_info* info,
+               const char* who)
+{
+    const std::string w(who);
+    if (!(nch == 1 || nch == 2 || nch == 4 || nch == 8 || nch == 16))
+        return set_err(CELLSPE_ERR_ARG, w + ": nchan must be 1, 2, 4, 8 or 16 (2-bit VDIF)");
+    if (mbps <= 0) return set_err(CELLSPE_ERR_ARG, w + ": Mbps must be positive");
+    auto word = [&](int k) {
+        return (uint32_t)h[4 * k] | ((uint32_t)h[4 * k + 1] << 8) | ((uint32_t)h[4 * k + 2] << 16) |
+               ((uint32_t)h[4 * k + 3] << 24);
+    };
+    const int hsize = (h[3] & 0x40) ? 16 : 32;
+    const long long frame = (long long)(word(2) & 0x00FFFFFF) * 8;
+    const long long payload = frame - hsize;
+    if (payload < 8) return set_err(CELLSPE_ERR_ARG, w + ": first VDIF header gives no payload");
+    if (payload * 8000 > INT32_MAX) return set_err(CELLSPE_ERR_UNSUPPORTED, w + ": VDIF payload above 268435 bytes");
+    if (payload * 4 % nch) return set_err(CELLSPE_ERR_ARG, w + ": payload does not hold whole sample times");
+    if (bytes < 2 * frame) return set_err(CELLSPE_ERR_ARG, w + ": fewer than two VDIF frames of input");
+    c = CsVdifClock{};
+    c.fmt = CsFraming{frame, (int)payload, hsize, 32, nch};
+    const int num = (int)(payload * 8000), den = mbps;
+    c.frame_ns = (double)num / (double)den;
+    int g = 1;
+    for (; g < 128; g *= 2)
+        if ((int32_t)((uint32_t)g * (uint32_t)num) % den == 0) break;
+    if (g >= 128) g = 1;
+    c.granularity = g;
+    const int gframe_ns = (int)(g * c.frame_ns + 0.5);
+    c.step_ns = gframe_ns / g;
+    for (int e = 0; e < 64; e++) c.epoch_mjd[e] = vdif_epoch_mjd(e);
+    const uint32_t w0 = word(0), w1 = word(1);
+    int sec = (int)(w0 & 0x3FFFFFFF);
+    const int days = sec / 86400;
+    sec -= days * 86400;
+    c.mjd0 = days + c.epoch_mjd[(w1 >> 24) & 0x3F];
+    c.sec0 = sec;
+    c.ns0 = (int)((double)(w1 & 0x00FFFFFF) * c.frame_ns + 0.5);
+    if (info) {
+        *info = cellspe_vdif_info{};
+        info->frames = bytes / frame;
+        info->frame_bytes = (int)frame;
+        info->header_bytes = hsize;
+        info->mjd = c.mjd0;
+        info->seconds = c.sec0;
+        info->ns = c.ns0;
+        info->frame_number = (int)(w1 & 0x00FFFFFF);
+        info->nchan_header = 1 << ((word(2) >> 24) & 0x1F);
+        info->thread_id = (int)((word(3) >> 16) & 0x3FF);
+        info->station_id = (int)(word(3) & 0xFFFF);
+    }
+    return 0;
+}
+
+// Stages a VDIF buffer, builds its model from the first header and marks
+// every frame used or blanked on the device.  Fills info except
+// good_samples and blanked_frames (read back with the results).
+int vdif_locate(Workspace& ws, Job& j, const void* framed, long long bytes, int nch, int mbps, Located& L,
+                cellspe_vdif_info* info, const char* who)
+{
+    if (bytes < 32) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": input shorter than a VDIF header");
+    L.d_framed = (const uint8_t*)j.in(framed, (size_t)bytes);
+    if (j.err) return j.err;
+    uint8_t h[32];
+    int rc = read_head(ws, j.host, framed, L.d_framed, 0, h, 32, "header read");
+    if (rc) return rc;
+    CsVdifClock c;
+    if ((rc = vdif_model(h, bytes, nch, mbps, c, info, who))) return rc;
+    L.fmt = c.fmt;
+    L.off = 0;
+    L.bytes = bytes;
+    L.frames = bytes / c.fmt.frame_bytes;
+    L.d_ranges = (int2*)j.scratch((size_t)L.frames * sizeof(int2));
+    L.d_blanked = (unsigned long long*)j.scratch(sizeof(unsigned long long));
+    if (j.err) return j.err;
+    return map_rc(cs_vdif_locate(L.d_framed, bytes, c, L.d_ranges, L.frames, L.d_blanked, ws.stream), "VDIF frames");
+}
+
+int m5b_check(const void* framed, long long bytes, int nchan, const char* who)
+{
+    if (!framed) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": null input");
+    if (!(nchan == 4 || nchan == 8 || nchan == 16))
+        return set_err(CELLSPE_ERR_ARG, std::string(who) + ": nchan must be 4, 8 or 16 (2-bit Mark5B)");
+    if (bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": fewer than two frames of input");
+    return 0;
+}
+
+long long samples_per_frame(const CsFraming& f) { return (long long)f.payload_bytes * 4 / f.nch; }
+
+// mark5_stream_decode over a located stream: the unblanked sample count, or
+// -1 when the frames run out (nothing is written past the last frame, so the
+// caller's values stay there).
+int framed_decode(Workspace& ws, Job& j, const Located& L, long long nsamp, const float lut[4], float* out,
+                  long long* good_out, const char* who)
+{
+    const bool runs_out = nsamp >= L.frames * samples_per_frame(L.fmt);
+    float* d_out = (float*)j.out(out, (size_t)(nsamp * L.fmt.nch * 4), runs_out);
+    auto* d_good = (unsigned long long*)j.scratch(sizeof(unsigned long long));
+    unsigned long long good = 0, blanked = 0;
+    if (!j.err) {
+        int rc = map_rc(cs_framed_decode(L.d_framed, L.bytes, L.fmt, L.d_off, L.d_ranges, nsamp, lut, d_out, d_good, ws.stream), who);
+        if (!rc) {
+            cudaError_t e = cudaMemcpyAsync(&good, d_good, sizeof good, cudaMemcpyDeviceToHost, ws.stream);
+            if (e == cudaSuccess && L.d_blanked)
+                e = cudaMemcpyAsync(&blanked, L.d_blanked, sizeof blanked, cudaMemcpyDeviceToHost, ws.stream);
+            if (e != cudaSuccess) rc = cuda_fail(e, who);
+        }
+        if (rc) j.err = rc;
+    }
+    int rc = j.finish();
+    if (!rc) {
+        good_out[0] = runs_out ? -1 : (long long)good;
+        good_out[1] = (long long)blanked;
+    }
+    return rc;
+}
+
+int op_mark5b_decode(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, long long nsamp,
+                     float* out, cellspe_mark5b_info* info)
+{
+    if (int rc = m5b_check(framed, bytes, nchan, "mark5b_decode")) return rc;
+    if (!out || nsamp <= 0) return set_err(CELLSPE_ERR_ARG, "mark5b_decode: bad output");
+    const long long need = (host ? align256(bytes) + align256(nsamp * nchan * 4) : 0) + align256(bytes / M5B_FRAME * 8) + 512;
+    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "mark5b_decode: job exceeds the device memory budget");
+    cellspe_mark5b_info tmp{};
+    if (!info) info = &tmp;
+    Job j(ws, host);
+    Located L;
+    int rc = m5b_locate(ws, j, framed, bytes, nchan, L, info);
+    if (rc) { j.err = rc; return j.finish(); }
+    float lut[4];
+    pick_levels(CELLSPE_LEVELS_MARK5B, nullptr, lut);
+    long long res[2] = {0, 0};
+    rc = framed_decode(ws, j, L, nsamp, lut, out, res, "mark5b decode");
+    if (!rc) info->good_samples = res[0];
+    return rc;
+}
+
+int op_vdif_decode(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, int mbps,
+                   long long nsamp, float* out, cellspe_vdif_info* info)
+{
+    if (!framed || !out || nsamp <= 0) return set_err(CELLSPE_ERR_ARG, "vdif_decode: null input or bad output");
+    if (nchan < 4 && nchan > 0 && nsamp % (4 / nchan))
+        return set_err(CELLSPE_ERR_ARG, "vdif_decode: nsamp must be a multiple of the samples per byte");
+    const long long need = (host ? align256(bytes) + align256(nsamp * nchan * 4) : 0) + align256(bytes / 24 * 8) + 768;
+    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "vdif_decode: job exceeds the device memory budget");
+    cellspe_vdif_info tmp{};
+    if (!info) info = &tmp;
+    Job j(ws, host);
+    Located L;
+    int rc = vdif_locate(ws, j, framed, bytes, nchan, mbps, L, info, "vdif_decode");
+    if (rc) { j.err = rc; return j.finish(); }
+    float lut[4];
+    pick_levels(CELLSPE_LEVELS_VDIF, nullptr, lut);
+    long long res[2] = {0, 0};
+    rc = framed_decode(ws, j, L, nsamp, lut, out, res, "vdif decode");
+    if (!rc) {
+        info->good_samples = res[0];
+        info->blanked_frames = res[1];
+    }
+    return rc;
+}
+
+// Payloads (and validity mask) of `frames` located frames; frames = 0 takes
+// them all.  Returns the blanked-frame count through *blanked when asked.
+int framed_deframe(Workspace& ws, Job& j, const Located& L, long long frames, void* payload,
+                   unsigned* mask, long long* blanked, const char* who)
+{
+    if (frames > L.frames) {
+        j.err = set_err(CELLSPE_ERR_ARG, std::string(who) + ": fewer complete frames in the buffer than requested");
+        return j.finish();
+    }
+    unsigned long long nb = 0;
+    if (payload) {
+        const long long spf = samples_per_frame(L.fmt);
+        void* d_pay = j.out(payload, (size_t)(frames * L.fmt.payload_bytes), false);
+        void* d_mask = mask ? j.out(mask, (size_t)((frames * spf + 31) / 32 * 4), false) : nullptr;
+        if (!j.err) {
+            int rc = map_rc(cs_framed_deframe(L.d_framed, L.bytes, L.fmt, L.d_off, L.d_ranges, frames, (uint8_t*)d_pay,
+                                              (uint32_t*)d_mask, ws.stream), "deframe");
+            if (rc) j.err = rc;
+        }
+    }
+    if (!j.err && blanked && L.d_blanked) {
+        cudaError_t e = cudaMemcpyAsync(&nb, L.d_blanked, sizeof nb, cudaMemcpyDeviceToHost, ws.stream);
+        if (e != cudaSuccess) j.err = cuda_fail(e, who);
+    }
+    int rc = j.finish();
+    if (!rc && blanked) *blanked = (long long)nb;
+    return rc;
+}
+
+int op_mark5b_deframe(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, long long frames,
+                      void* payload, unsigned* mask, cellspe_mark5b_info* info)
+{
+    if (int rc = m5b_check(framed, bytes, nchan, "mark5b_deframe")) return rc;
+    if (frames < 0) return set_err(CELLSPE_ERR_ARG, "mark5b_deframe: negative frame count");
+    const long long nmax = bytes / M5B_FRAME, spf = M5B_PAYLOAD / (nchan / 4);
+    const long long mwords_max = (nmax * spf + 31) / 32;
+    const long long need = (host ? align256(bytes) + align256(nmax * M5B_PAYLOAD) + align256(mwords_max * 4) : 0) +
+                           align256(nmax * 8) + 256;
+    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "mark5b_deframe: job exceeds the device memory budget");
+    cellspe_mark5b_info tmp{};
+    if (!info) info = &tmp;
+    Job j(ws, host);
+    Located L;
+    int rc = m5b_locate(ws, j, framed, bytes, nchan, L, info);
+    if (rc) { j.err = rc; return j.finish(); }
+    return framed_deframe(ws, j, L, frames == 0 ? L.frames : frames, payload, mask, nullptr, "mark5b_deframe");
+}
+
+int op_vdif_deframe(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, int mbps,
+                    long long frames, void* payload, unsigned* mask, cellspe_vdif_info* info)
+{
+    if (!framed) return set_err(CELLSPE_ERR_ARG, "vdif_deframe: null input");
+    if (frames < 0) return set_err(CELLSPE_ERR_ARG, "vdif_deframe: negative frame count");
+    const long long need = (host ? 2 * align256(bytes) + align256(bytes / 4 + 4) : 0) + align256(bytes / 24 * 8) + 512;
+    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "vdif_deframe: job exceeds the device memory budget");
+    cellspe_vdif_info tmp{};
+    if (!info) info = &tmp;
+    Job j(ws, host);
+    Located L;
+    int rc = vdif_locate(ws, j, framed, bytes, nchan, mbps, L, info, "vdif_deframe");
+    if (rc) { j.err = rc; return j.finish(); }
+    long long blanked = 0;
+    rc = framed_deframe(ws, j, L, frames == 0 ? L.frames : frames, payload, mask, &blanked, "vdif_deframe");
+    if (!rc) info->blanked_frames = blanked;
+    return rc;
+}
+
+// Smallest VDIF frame the spectrometer takes (bounds its frame table).
+constexpr long long VDIF_SPEC_MIN_FRAME = 528;
+
+// Mbps of a VDIF stream carrying the spectrometer's subbands: 2 bits per
+// sample, nsub channels at sample_rate_hz (0 when that is not a whole number).
+int vdif_spec_mbps(const cellspe_spec_params* p)
+{
+    const double mbps = p->sample_rate_hz * 2.0 * p->n_subbands / 1e6;
+    const long long r = std::llround(mbps);
+    return (r > 0 && r < INT32_MAX && std::fabs(mbps - (double)r) < 1e-6) ? (int)r : 0;
+}
+
 long long spec_bytes(const cellspe_spec_params* p)
 {
     CsSpecArgs a{};
@@ -588,6 +921,11 @@ long long spec_bytes(const cellspe_spec_params* p)
     if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED) {
         const long long g = m5b_groups(p->raw_bytes, std::max(p->n_subbands, 4));
         b += align256(g * 4 * p->n_subbands) + align256((g + 1) / 2 * 4) + align256(p->raw_bytes / M5B_FRAME * 8) + 256;
+    } else if (p->input_layout == CELLSPE_SPEC_VDIF_FRAMED) {
+        // bounds: every byte a payload byte, frames of at least VDIF_SPEC_MIN_FRAME bytes
+        const long long g = ((p->raw_bytes * 4 / p->n_subbands + 63) / 64) * 4;
+        b += align256(g * 4 * p->n_subbands) + align256((g + 1) / 2 * 4) +
+             align256(p->raw_bytes / VDIF_SPEC_MIN_FRAME * 8) + 512;
     }
     long long rows = (long long)p->n_subbands * p->n_spectra;
     if (host) b += align256(rows * (p->fft_points / 2 + 1) * 4) + 2 * align256(rows * std::max(p->pcal_tonebins, p->pcal_ntones) * 8);
@@ -610,6 +948,10 @@ int spec_check(const cellspe_spec_params* p, const char* who)
         const long long avail = (p->raw_bytes / M5B_FRAME) * (M5B_PAYLOAD / (nsub / 4));
         if ((long long)p->n_spectra * p->ffts_per_spectrum * p->fft_points > avail)
             return set_err(CELLSPE_ERR_ARG, w + ": spectra need more samples than the frames hold");
+    } else if (p->input_layout == CELLSPE_SPEC_VDIF_FRAMED) {
+        if (!vdif_spec_mbps(p))
+            return set_err(CELLSPE_ERR_ARG, w + ": VDIF input needs sample_rate_hz giving a whole number of Mbps");
+        if (p->raw_bytes < 2 * VDIF_SPEC_MIN_FRAME) return set_err(CELLSPE_ERR_ARG, w + ": framed input shorter than two frames");
     } else if (p->input_layout != CELLSPE_SPEC_INTERLEAVED && p->input_layout != CELLSPE_SPEC_PLANES) {
         return set_err(CELLSPE_ERR_ARG, w + ": unknown input_layout");
     } else if (p->raw_bytes <= 0 || p->raw_bytes % (16 * nsub)) {
@@ -643,8 +985,41 @@ SpecPlanes spec_planes(Workspace& ws, Job& j, const cellspe_spec_params* p, cons
         if (!j.err) {
             int rc = map_rc(cs_m5b_locate(d_raw, p->raw_bytes, (int*)off, (int2*)rg, nframes, ws.stream), "frame search");
             if (!rc)
-                rc = map_rc(cs_m5b_planes(d_raw, p->raw_bytes, (const int*)off, (const int2*)rg, nframes, nsub, groups,
-                                          (uint32_t*)pl, (uint32_t*)mk, ws.stream), "deframe");
+                rc = map_rc(cs_framed_planes(d_raw, p->raw_bytes, m5b_framing(nsub), (const int*)off, (const int2*)rg,
+                                             nframes, groups, (uint32_t*)pl, (uint32_t*)mk, ws.stream), "deframe");
+            if (rc) j.err = rc;
+        }
+        r.planes = (const uint8_t*)pl;
+        r.vmask = (const uint32_t*)mk;
+        r.bytes_per_sub = groups * 4;
+    } else if (p->input_layout == CELLSPE_SPEC_VDIF_FRAMED) {
+        // the frame length comes from the first header: read it before sizing
+        uint8_t h[32];
+        CsVdifClock c;
+        int rc = j.err;
+        if (!rc) rc = read_head(ws, j.host, raw, d_raw, 0, h, 32, "header read");
+        if (!rc) rc = vdif_model(h, p->raw_bytes, nsub, vdif_spec_mbps(p), c, nullptr, "spectrometer");
+        if (!rc && c.fmt.frame_bytes < VDIF_SPEC_MIN_FRAME)
+            rc = set_err(CELLSPE_ERR_ARG, "spectrometer: VDIF frames shorter than 528 bytes");
+        const long long nframes = rc ? 0 : p->raw_bytes / c.fmt.frame_bytes;
+        const long long spf = rc ? 0 : samples_per_frame(c.fmt);
+        if (!rc && (long long)p->n_spectra * p->ffts_per_spectrum * p->fft_points > nframes * spf)
+            rc = set_err(CELLSPE_ERR_ARG, "spectrometer: spectra need more samples than the frames hold");
+        if (rc) {
+            if (!j.err) j.err = rc;
+            return r;
+        }
+        const long long groups = ((nframes * spf + 63) / 64) * 4;
+        void* pl = j.scratch((size_t)(groups * 4 * nsub));
+        void* mk = j.scratch((size_t)((groups + 1) / 2 * 4));
+        void* rg = j.scratch((size_t)(nframes * 8));
+        void* nb = j.scratch(sizeof(unsigned long long));
+        if (!j.err) {
+            rc = map_rc(cs_vdif_locate(d_raw, p->raw_bytes, c, (int2*)rg, nframes, (unsigned long long*)nb, ws.stream),
+                        "VDIF frames");
+            if (!rc)
+                rc = map_rc(cs_framed_planes(d_raw, p->raw_bytes, c.fmt, nullptr, (const int2*)rg, nframes, groups,
+                                             (uint32_t*)pl, (uint32_t*)mk, ws.stream), "deframe");
             if (rc) j.err = rc;
         }
         r.planes = (const uint8_t*)pl;
@@ -777,136 +1152,6 @@ int op_spectrometer_xpol(Workspace& ws, const cellspe_spec_params* p, const void
 // ---------------------------------------------------------------------------
 // correlation service: continuous batching over execution streams
 // ---------------------------------------------------------------------------
-// ---- framed Mark5B ----------------------------------------------------------
-// Header fields as FileSource::locateFirstHeader (FileSource.cpp:330-333) and
-// the mark5access frame-number field (bits 0..14 of header word 1).
-void m5b_header_info(const uint8_t h[16], cellspe_mark5b_info* info)
-{
-    info->mjd = 56000 + (h[11] >> 4) * 100 + (h[11] & 15) * 10 + (h[10] >> 4);
-    info->seconds = (h[10] & 15) * 10000 + (h[9] >> 4) * 1000 + (h[9] & 15) * 100 + (h[8] >> 4) * 10 + (h[8] & 15);
-    info->frame_number = h[4] | ((h[5] & 0x7f) << 8);
-}
-
-// Stages the framed bytes, finds the first frame and the valid ranges of
-// every frame, and brings the frame offset back (the callers need the frame
-// count on the host).  Fills info except good_samples.
-struct M5bLocated {
-    const uint8_t* d_framed = nullptr;
-    int* d_off = nullptr;
-    int2* d_ranges = nullptr;
-    long long off = -1, frames = 0;
-};
-
-int m5b_locate(Workspace& ws, Job& j, const void* framed, long long bytes, M5bLocated& L, cellspe_mark5b_info* info)
-{
-    const long long nmax = bytes / M5B_FRAME;
-    L.d_framed = (const uint8_t*)j.in(framed, (size_t)bytes);
-    L.d_off = (int*)j.scratch(sizeof(int));
-    L.d_ranges = (int2*)j.scratch((size_t)nmax * sizeof(int2));
-    if (j.err) return j.err;
-    int rc = map_rc(cs_m5b_locate(L.d_framed, bytes, L.d_off, L.d_ranges, nmax, ws.stream), "frame search");
-    if (rc) return rc;
-    int off = 0;
-    cudaError_t e = cudaMemcpyAsync(&off, L.d_off, sizeof off, cudaMemcpyDeviceToHost, ws.stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ws.stream);
-    if (e != cudaSuccess) return cuda_fail(e, "frame search");
-    if (off < 0 || off >= (1 << 20)) return set_err(CELLSPE_ERR_ARG, "mark5b: no frame found in the first MiB");
-    L.off = off;
-    L.frames = (bytes - off) / M5B_FRAME;
-    if (info) {
-        uint8_t h[16];
-        if (j.host) std::memcpy(h, (const uint8_t*)framed + off, 16);
-        else {
-            e = cudaMemcpyAsync(h, L.d_framed + off, 16, cudaMemcpyDeviceToHost, ws.stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(ws.stream);
-            if (e != cudaSuccess) return cuda_fail(e, "header read");
-        }
-        info->first_frame_offset = off;
-        info->frames = L.frames;
-        info->good_samples = 0;
-        m5b_header_info(h, info);
-        info->reserved = 0;
-    }
-    return 0;
-}
-
-int m5b_check(const void* framed, long long bytes, int nchan, const char* who)
-{
-    if (!framed) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": null input");
-    if (!(nchan == 4 || nchan == 8 || nchan == 16))
-        return set_err(CELLSPE_ERR_ARG, std::string(who) + ": nchan must be 4, 8 or 16 (2-bit Mark5B)");
-    if (bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, std::string(who) + ": fewer than two frames of input");
-    return 0;
-}
-
-int op_mark5b_decode(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, long long nsamp,
-                     float* out, cellspe_mark5b_info* info)
-{
-    if (int rc = m5b_check(framed, bytes, nchan, "mark5b_decode")) return rc;
-    if (!out || nsamp <= 0) return set_err(CELLSPE_ERR_ARG, "mark5b_decode: bad output");
-    const long long need = (host ? align256(bytes) + align256(nsamp * nchan * 4) : 0) + align256(bytes / M5B_FRAME * 8) + 512;
-    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "mark5b_decode: job exceeds the device memory budget");
-    cellspe_mark5b_info tmp{};
-    if (!info) info = &tmp;
-    Job j(ws, host);
-    M5bLocated L;
-    int rc = m5b_locate(ws, j, framed, bytes, L, info);
-    if (rc) { j.err = rc; return j.finish(); }
-    const long long spf = M5B_PAYLOAD / (nchan / 4);
-    const bool runs_out = nsamp >= L.frames * spf;
-    // past the last frame nothing is written: keep the caller's values there
-    float* d_out = (float*)j.out(out, (size_t)(nsamp * nchan * 4), runs_out);
-    auto* d_good = (unsigned long long*)j.scratch(sizeof(unsigned long long));
-    unsigned long long good = 0;
-    if (!j.err) {
-        float lut[4];
-        pick_levels(CELLSPE_LEVELS_MARK5B, nullptr, lut);
-        rc = map_rc(cs_m5b_decode(L.d_framed, bytes, L.d_off, L.d_ranges, nchan, nsamp, lut, d_out, d_good, ws.stream),
-                    "mark5b decode");
-        if (!rc) {
-            cudaError_t e = cudaMemcpyAsync(&good, d_good, sizeof good, cudaMemcpyDeviceToHost, ws.stream);
-            if (e != cudaSuccess) rc = cuda_fail(e, "mark5b decode");
-        }
-        if (rc) j.err = rc;
-    }
-    rc = j.finish();
-    if (!rc) info->good_samples = runs_out ? -1 : (long long)good;
-    return rc;
-}
-
-int op_mark5b_deframe(Workspace& ws, bool host, const void* framed, long long bytes, int nchan, long long frames,
-                      void* payload, unsigned* mask, cellspe_mark5b_info* info)
-{
-    if (int rc = m5b_check(framed, bytes, nchan, "mark5b_deframe")) return rc;
-    if (frames < 0) return set_err(CELLSPE_ERR_ARG, "mark5b_deframe: negative frame count");
-    const long long nmax = bytes / M5B_FRAME, spf = M5B_PAYLOAD / (nchan / 4);
-    const long long mwords_max = (nmax * spf + 31) / 32;
-    const long long need = (host ? align256(bytes) + align256(nmax * M5B_PAYLOAD) + align256(mwords_max * 4) : 0) +
-                           align256(nmax * 8) + 256;
-    if (need > job_limit(ws)) return set_err(CELLSPE_ERR_NOMEM, "mark5b_deframe: job exceeds the device memory budget");
-    cellspe_mark5b_info tmp{};
-    if (!info) info = &tmp;
-    Job j(ws, host);
-    M5bLocated L;
-    int rc = m5b_locate(ws, j, framed, bytes, L, info);
-    if (rc) { j.err = rc; return j.finish(); }
-    if (frames == 0) frames = L.frames;
-    if (frames > L.frames) {
-        j.err = set_err(CELLSPE_ERR_ARG, "mark5b_deframe: fewer complete frames in the buffer than requested");
-        return j.finish();
-    }
-    if (payload) {
-        void* d_pay = j.out(payload, (size_t)(frames * M5B_PAYLOAD), false);
-        void* d_mask = mask ? j.out(mask, (size_t)((frames * spf + 31) / 32 * 4), false) : nullptr;
-        if (!j.err) {
-            rc = map_rc(cs_m5b_deframe(L.d_framed, bytes, L.d_off, L.d_ranges, frames, nchan, (uint8_t*)d_pay,
-                                       (uint32_t*)d_mask, ws.stream), "deframe");
-            if (rc) j.err = rc;
-        }
-    }
-    return j.finish();
-}
-
 struct SvcJob {
     long long id = 0;
     cellspe_fx_params p{};
@@ -1900,6 +2145,21 @@ int cellspe_mark5b_deframe(const void* framed, long long bytes, int nchan, long 
 {
     DIRECT_PROLOGUE
     return op_mark5b_deframe(*ws, memory == CELLSPE_MEM_HOST, framed, bytes, nchan, frames, payload, valid_mask, info);
+}
+
+int cellspe_vdif_decode(const void* framed, long long bytes, int nchan, int mbps, long long nsamp, float* out,
+                        int memory, cellspe_vdif_info* info)
+{
+    DIRECT_PROLOGUE
+    return op_vdif_decode(*ws, memory == CELLSPE_MEM_HOST, framed, bytes, nchan, mbps, nsamp, out, info);
+}
+
+int cellspe_vdif_deframe(const void* framed, long long bytes, int nchan, int mbps, long long frames, void* payload,
+                         unsigned int* valid_mask, int memory, cellspe_vdif_info* info)
+{
+    DIRECT_PROLOGUE
+    return op_vdif_deframe(*ws, memory == CELLSPE_MEM_HOST, framed, bytes, nchan, mbps, frames, payload, valid_mask,
+                           info);
 }
 
 }  // extern "C"

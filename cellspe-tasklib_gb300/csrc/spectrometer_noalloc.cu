@@ -102,6 +102,8 @@ extern "C" int cellspe_spectrometer_noalloc(const cellspe_spec_params* p, const 
     const int nsub = p->n_subbands;
     if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16))
         return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: n_subbands must be 1, 4, 8 or 16");
+    if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED || p->input_layout == CELLSPE_SPEC_VDIF_FRAMED)
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: framed input needs deframing scratch");
     if (nsub > 1 && p->input_layout != CELLSPE_SPEC_PLANES)
         return cs_set_error(CELLSPE_ERR_ARG,
                             "spectrometer_noalloc: needs CELLSPE_SPEC_PLANES input (the corner turn needs a raw-sized buffer)");

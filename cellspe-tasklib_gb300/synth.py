@@ -159,3 +159,46 @@ def mark5b_fill(framed: np.ndarray, frame: int, start: int, end: int, prefix: in
     assert start % 4 == 0 and end % 4 == 0 and 0 <= start <= end <= MARK5B_PAYLOAD
     o = prefix + frame * MARK5B_FRAME + 16
     framed[o + start:o + end] = np.tile(np.array([0x44, 0x33, 0x22, 0x11], np.uint8), (end - start) // 4)
+
+
+def vdif_frames(payload: np.ndarray, databytes: int = 8000, nchan: int = 4, mbps: int = 512,
+                legacy: bool = False, seconds: int = 7654321, ref_epoch: int = 40, first_frame: int = 0,
+                thread: int = 0, station: int = 0x4D62) -> np.ndarray:
+    """Wrap payload bytes (a multiple of ``databytes``) into VDIF frames.
+
+    Header words (little-endian, VDIF 1.0): word 0 = seconds from the reference
+    epoch (bits 0..29), legacy flag (bit 30), invalid flag (bit 31, clear);
+    word 1 = frame number within the second (bits 0..23), reference epoch
+    (bits 24..29, half years since 2000); word 2 = frame length in 8-byte
+    units (bits 0..23), log2(nchan) (bits 24..28); word 3 = bits per sample - 1
+    (bits 26..30, 2-bit samples: 1), thread (bits 16..25), station (bits
+    0..15); words 4..7 (non-legacy) zero.  Frames per second follow from mbps:
+    mbps * 1e6 / (8 * databytes), which must be a whole number here.
+    """
+    hsize = 16 if legacy else 32
+    fps = mbps * 1_000_000 // (8 * databytes)
+    assert fps * 8 * databytes == mbps * 1_000_000, "frame rate must be whole"
+    assert (databytes + hsize) % 8 == 0
+    payload = np.ascontiguousarray(payload, np.uint8).reshape(-1, databytes)
+    nf = payload.shape[0]
+    n = first_frame + np.arange(nf, dtype=np.int64)
+    hdr = np.zeros((nf, hsize // 4), np.uint32)
+    hdr[:, 0] = ((seconds + n // fps) & 0x3FFFFFFF).astype(np.uint32) | (np.uint32(1 << 30) if legacy else 0)
+    hdr[:, 1] = ((n % fps) & 0xFFFFFF).astype(np.uint32) | np.uint32((ref_epoch & 0x3F) << 24)
+    hdr[:, 2] = np.uint32(((databytes + hsize) // 8) | ((nchan.bit_length() - 1) << 24))
+    hdr[:, 3] = np.uint32((1 << 26) | ((thread & 0x3FF) << 16) | (station & 0xFFFF))
+    frames = np.concatenate([hdr.view(np.uint8).reshape(nf, hsize), payload], axis=1)
+    return frames.reshape(-1)
+
+
+def vdif_set_invalid(framed: np.ndarray, frame: int, framebytes: int) -> None:
+    """Set the invalid-data bit (word 0 bit 31) of one VDIF frame."""
+    framed[frame * framebytes + 3] |= 0x80
+
+
+def vdif_fill(framed: np.ndarray, frame: int, framebytes: int, hsize: int, start: int, end: int) -> None:
+    """Overwrite payload bytes [start, end) of one VDIF frame with the fill
+    pattern (32-bit words 0x11223344; start and end multiples of 4)."""
+    assert start % 4 == 0 and end % 4 == 0 and 0 <= start <= end <= framebytes - hsize
+    o = frame * framebytes + hsize
+    framed[o + start:o + end] = np.tile(np.array([0x44, 0x33, 0x22, 0x11], np.uint8), (end - start) // 4)

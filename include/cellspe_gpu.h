@@ -34,6 +34,7 @@ extern "C" {
 #define CELLSPE_LEVELS_MARK5B        0  /* {-3.3359, +1, -1, +3.3359}  mark5_format_mark5b.c:63  */
 #define CELLSPE_LEVELS_TWOBIT        1  /* {+1, -1, +3.3359, -3.3359}  DataUnpackers.cpp:195     */
 #define CELLSPE_LEVELS_OFFSET_BINARY 2  /* {-3.336, -1, +1, +3.336}    synthetic offset binary    */
+#define CELLSPE_LEVELS_VDIF          3  /* {-3.3359, -1, +1, +3.3359}  format_vdif.c:70          */
 #define CELLSPE_UNPACK_MSB_FIRST     0x100  /* single channel: sample 0 in bits 7:6 */
 
 /* X-stage arithmetic */
@@ -170,6 +171,11 @@ void cellspe_service_destroy(cellspe_service* s);
                                       * stripped and fill-pattern zones blanked (decoded as 0.0)
                                       * on the device, as cellspe_mark5b_decode does; samples past
                                       * the last complete frame are blanked too */
+#define CELLSPE_SPEC_VDIF_FRAMED   3 /* raw: a framed VDIF recording from byte 0 (n_subbands = 1, 4, 8
+                                      * or 16 channels, 2-bit, frames of at least 528 bytes); frames
+                                      * are validated and blanked as cellspe_vdif_decode does, with
+                                      * Mbps = sample_rate_hz * 2 * n_subbands / 1e6 (a whole number);
+                                      * levels should be CELLSPE_LEVELS_VDIF */
 typedef struct {
     int    fft_points;        /* N: 1024 .. 65536                                  */
     int    overlap;           /* fft_overlap_factor                                */
@@ -253,6 +259,60 @@ int cellspe_mark5b_decode(const void* framed, long long bytes, int nchan, long l
 int cellspe_mark5b_deframe(const void* framed, long long bytes, int nchan, long long frames, void* payload,
                            unsigned int* valid_mask, int memory, cellspe_mark5b_info* info);
 
+/* ---- framed VDIF input ---------------------------------------------------
+ * A VDIF recording is a run of frames from byte 0, each a 32-byte header (16
+ * with the legacy bit, word 0 bit 30) and a payload of 2-bit samples, nchan
+ * channels interleaved per sample time, channel c in bits 2c..2c+1 of the
+ * sample time's bit field (mark5access format_vdif.c).  The frame length is
+ * word 2 of the first header.  The decode restates a mark5access memory
+ * stream opened with the format "VDIF_<payload>-<mbps>-<nchan>-2"
+ * (new_mark5_stream_memory + mark5_stream_decode):
+ *   - a frame is used whole or blanked whole (decoded as 0.0);
+ *   - frames after the first are blanked when the invalid bit (word 0 bit 31)
+ *     is set, or when, on frame numbers that are multiples of the frame-time
+ *     granularity, the header time (reference epoch + seconds + frame number
+ *     x frame duration) differs from the time predicted from the first frame
+ *     (mark5_format_vdif_validate, format_vdif.c:2299-2337; frame duration
+ *     payload * 8000 / mbps ns; its integer-ns granularity and the integer
+ *     step per frame as the library computes them);
+ *   - any frame is blanked when the first or last 64-bit word of its payload
+ *     is the fill pattern 0x1122334411223344 (blanker_vdif);
+ *   - like the library, frame 0 of a legacy stream is read from byte 32 of
+ *     the frame (the library sets the first payload pointer before it learns
+ *     the header is 16 bytes, format_vdif.c:2196-2220).
+ * At least two frames are required. */
+typedef struct {
+    long long frames;          /* complete frames in the buffer                     */
+    long long good_samples;    /* cellspe_vdif_decode: unblanked samples per channel,
+                                * or -1 when the frames ran out (the value
+                                * mark5_stream_decode returns)                      */
+    long long blanked_frames;  /* frames of the buffer that are blanked             */
+    int frame_bytes;           /* header + payload, from the first header           */
+    int header_bytes;          /* 32, or 16 with the legacy bit                     */
+    int mjd, seconds, ns;      /* time of the first frame (ns rounded)              */
+    int frame_number;          /* of the first frame, within its second             */
+    int nchan_header;          /* 2^(word 2 bits 24..28)                            */
+    int thread_id, station_id;
+    int reserved;
+} cellspe_vdif_info;
+
+/* Decodes nsamp samples of each of nchan (1, 2, 4, 8, 16) channels into
+ * out[nchan][nsamp] with the VDIF levels {-3.3359, -1, +1, +3.3359}; nsamp a
+ * multiple of 4 / nchan for nchan < 4.  Like the library, it stops writing
+ * after the last complete frame and then reports good_samples = -1 (also when
+ * the last wanted sample ends the last frame).  mbps: the stream's total bit
+ * rate in Mbit/s.  memory = CELLSPE_MEM_HOST or _DEVICE for framed and out;
+ * info may be NULL. */
+int cellspe_vdif_decode(const void* framed, long long bytes, int nchan, int mbps, long long nsamp, float* out,
+                        int memory, cellspe_vdif_info* info);
+
+/* The payloads the decoder reads, of `frames` frames (0 = every complete
+ * frame), back to back into payload[frames * payload bytes]; with
+ * valid_mask != NULL also one bit per sample time (bit t % 32 of word t / 32
+ * set = used).  info is filled first (frames, frame_bytes, header_bytes). */
+int cellspe_vdif_deframe(const void* framed, long long bytes, int nchan, int mbps, long long frames, void* payload,
+                         unsigned int* valid_mask, int memory, cellspe_vdif_info* info);
+
 /* Spectrometer that allocates no device memory (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc when they run it:
  * real-time loops that must not stall on the allocator (cudaMalloc/cudaFree
@@ -261,7 +321,7 @@ int cellspe_mark5b_deframe(const void* framed, long long bytes, int nchan, long 
  * cellspe_spectrometer (within FP32 summation order), enqueued on `stream`
  * (a cudaStream_t, NULL = default stream) without synchronising.
  * Requirements: memory = CELLSPE_MEM_DEVICE (raw, power, pcal_* are device
- * pointers); input_layout = CELLSPE_SPEC_PLANES unless n_subbands == 1;
+ * pointers); input_layout = CELLSPE_SPEC_PLANES unless n_subbands == 1 (never framed);
  * fft_points <= 65536; pcal_rotatorlen <= 65536.
  * Scratch: a fixed static device array of 4,194,304 floats (16 MiB) plus
  * 1.25 MiB of tables, held by every GPU that loads the library until exit.

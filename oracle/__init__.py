@@ -79,6 +79,10 @@ def lib() -> ctypes.CDLL:
         _lib.orc_mark5b_valid_range.argtypes = [V, ctypes.POINTER(I), ctypes.POINTER(I)]
         _lib.orc_mark5b_decode_framed.argtypes = [V, L, I, L, V]
         _lib.orc_mark5b_decode_framed.restype = L
+        _lib.orc_vdif_frame_ok.argtypes = [V, L, I, L]
+        _lib.orc_vdif_decode_framed.argtypes = [V, L, I, I, L, V]
+        _lib.orc_vdif_decode_framed.restype = L
+        _lib.orc_vdif_first_time.argtypes = [V, L, I, V, V, V]
     return _lib
 
 
@@ -115,6 +119,41 @@ def mark5b_decode_framed(framed: np.ndarray, nchan: int, nsamp: int):
     out = np.zeros((nchan, nsamp), np.float32)
     good = lib().orc_mark5b_decode_framed(_ptr(framed), framed.size, nchan, nsamp, _ptr(out))
     return good, out
+
+
+def vdif_decode_framed(framed: np.ndarray, nchan: int, mbps: int, nsamp: int):
+    """(good samples or -1/-2/-3, out[nchan][nsamp]) of a framed VDIF buffer."""
+    framed = np.ascontiguousarray(framed, np.uint8)
+    out = np.zeros((nchan, nsamp), np.float32)
+    good = lib().orc_vdif_decode_framed(_ptr(framed), framed.size, nchan, mbps, nsamp, _ptr(out))
+    return good, out
+
+
+def vdif_first_time(framed: np.ndarray, mbps: int):
+    """(mjd, seconds, ns) of frame 0 as the memory stream reads it."""
+    framed = np.ascontiguousarray(framed, np.uint8)
+    t = (ctypes.c_int * 3)()
+    rc = lib().orc_vdif_first_time(_ptr(framed), framed.size, mbps, ctypes.byref(t, 0), ctypes.byref(t, 4),
+                                   ctypes.byref(t, 8))
+    assert rc == 0
+    return tuple(t)
+
+
+def ref_mark5_stream_time(fmt: bytes, framed: np.ndarray):
+    """(mjd, seconds, ns) of the first frame as the compiled library reads it."""
+    m5 = ref_mark5()
+    m5.ref_mark5_stream_time.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint] + [ctypes.c_void_p] * 3
+    buf = np.ascontiguousarray(framed, np.uint8).copy()
+    t = (ctypes.c_int * 3)()
+    rc = m5.ref_mark5_stream_time(fmt, buf.ctypes.data, buf.size, ctypes.byref(t, 0), ctypes.byref(t, 4),
+                                  ctypes.byref(t, 8))
+    assert rc == 0, rc
+    return tuple(t)
+
+
+def vdif_frame_ok(framed: np.ndarray, mbps: int, frame: int) -> int:
+    framed = np.ascontiguousarray(framed, np.uint8)
+    return lib().orc_vdif_frame_ok(_ptr(framed), framed.size, mbps, frame)
 
 
 def ref_generic() -> ctypes.CDLL:

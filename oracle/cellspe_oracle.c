@@ -122,6 +122,147 @@ int64_t orc_mark5b_decode_framed(const uint8_t* framed, int64_t bytes, int nchan
 }
 
 /* ---------------------------------------------------------------------- */
+/* Framed VDIF (mark5access format_vdif.c, blanker_mark5.c:282-316)         */
+/* ---------------------------------------------------------------------- */
+static uint32_t le32(const uint8_t* p)
+{
+    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+
+/* MJD of 1 January (even e) or 1 July (odd e) of year 2000 + e/2: the VDIF
+ * reference epochs (format_vdif.c:145-155 tabulates them), from the civil
+ * calendar: days since 1970-01-01 by the era/day-of-era method, + 40587. */
+static int vdif_epoch_mjd(int e)
+{
+    int y = 2000 + e / 2, m = (e & 1) ? 7 : 1, d = 1;
+    y -= m <= 2;
+    const int era = y / 400, yoe = y - era * 400;
+    const int doy = (153 * (m + (m > 2 ? -3 : 9)) + 2) / 5 + d - 1;
+    const int doe = yoe * 365 + yoe / 4 - yoe / 100 + doy;
+    return era * 146097 + doe - 719468 + 40587;
+}
+
+typedef struct {
+    int hsize, databytes, framebytes;
+    double framens;
+    int fg, gframens;
+    int mjd0, sec0, ns0;
+} orc_vdif_stream;
+
+/* mark5_stream_frame_time_vdif (format_vdif.c:135-200), leap seconds 0 */
+static void vdif_frame_time(const uint8_t* h, double framens, int* mjd, int* sec, double* ns)
+{
+    const uint32_t w0 = le32(h), w1 = le32(h + 4);
+    int seconds = (int)(w0 & 0x3FFFFFFF);
+    int days = seconds / 86400;
+    seconds -= days * 86400;
+    *mjd = days + vdif_epoch_mjd((int)((w1 >> 24) & 0x3F));
+    *sec = seconds;
+    *ns = (double)(w1 & 0x00FFFFFF) * framens;
+}
+
+/* mark5_format_vdif_init (format_vdif.c:2121-2257) with the header-derived
+ * payload size also used for the frame duration */
+static int vdif_open(const uint8_t* d, int64_t bytes, int mbps, orc_vdif_stream* s)
+{
+    if (bytes < 32 || mbps <= 0) return -2;
+    s->hsize = (d[3] & 0x40) ? 16 : 32;
+    s->framebytes = (int)(le32(d + 8) & 0x00FFFFFF) * 8;
+    s->databytes = s->framebytes - s->hsize;
+    if (s->databytes < 8 || bytes < 2 * (int64_t)s->framebytes) return -2;
+    const int num = s->databytes * 8 * 1000, den = mbps;
+    s->framens = (double)num / (double)den;
+    for (s->fg = 1; s->fg < 128; s->fg *= 2)
+        if ((int)((unsigned)s->fg * (unsigned)num) % den == 0) break;
+    if (s->fg >= 128) s->fg = 1;
+    s->gframens = (int)(s->fg * s->framens + 0.5);
+    double dns;
+    vdif_frame_time(d, s->framens, &s->mjd0, &s->sec0, &dns);
+    s->ns0 = (int)(dns + 0.5);
+    return 0;
+}
+
+/* Payload offset of frame f.  The format name "VDIF_..." opens the stream
+ * with 32-byte headers; on a legacy header mark5_format_vdif_init switches to
+ * 16 bytes (format_vdif.c:2209-2220) after it has already pointed the first
+ * payload 32 bytes into frame 0 (:2196), so frame 0 of a legacy stream is
+ * read from byte 32 on (its last 16 bytes come from the next frame). */
+static int vdif_payload_offset(const orc_vdif_stream* s, int64_t f)
+{
+    return f == 0 ? 32 : s->hsize;
+}
+
+static int vdif_ok(const uint8_t* framed, int64_t bytes, const orc_vdif_stream* s, int64_t f)
+{
+    if ((f + 1) * (int64_t)s->framebytes > bytes) return 0;
+    const uint8_t* h = framed + f * (int64_t)s->framebytes;
+    if (f > 0) {
+        if (s->mjd0 && f % s->fg == 0) {
+            int mjd_d, sec_d;
+            double ns_d;
+            vdif_frame_time(h, s->framens, &mjd_d, &sec_d, &ns_d);
+            long long ns_t = f * (long long)(s->gframens / s->fg) + (long long)s->ns0;
+            int sec_t = (int)(ns_t / 1000000000LL);
+            ns_t -= (long long)sec_t * 1000000000LL;
+            sec_t += s->sec0;
+            int mjd_t = sec_t / 86400;
+            sec_t -= mjd_t * 86400;
+            mjd_t += s->mjd0;
+            if (mjd_t != mjd_d || sec_t != sec_d || fabs((double)ns_t - ns_d) > 0.000001) return 0;
+        }
+        if ((le32(h) >> 31) & 1u) return 0;
+    }
+    const uint8_t* p = h + vdif_payload_offset(s, f);
+    const int nword = s->databytes / 8;
+    if (rd64(p, 0) == M5B_FILL64 || rd64(p, nword - 1) == M5B_FILL64) return 0;
+    return 1;
+}
+
+int orc_vdif_first_time(const uint8_t* framed, int64_t bytes, int mbps, int* mjd, int* sec, int* ns)
+{
+    orc_vdif_stream s;
+    if (vdif_open(framed, bytes, mbps, &s)) return -2;
+    *mjd = s.mjd0;
+    *sec = s.sec0;
+    *ns = s.ns0;
+    return 0;
+}
+
+int orc_vdif_frame_ok(const uint8_t* framed, int64_t bytes, int mbps, int64_t f)
+{
+    orc_vdif_stream s;
+    if (vdif_open(framed, bytes, mbps, &s)) return -2;
+    return vdif_ok(framed, bytes, &s, f);
+}
+
+int64_t orc_vdif_decode_framed(const uint8_t* framed, int64_t bytes, int nchan, int mbps, int64_t nsamp, float* out)
+{
+    static const float lut[4] = {-3.3359f, -1.0f, 1.0f, 3.3359f};
+    if (!(nchan == 1 || nchan == 2 || nchan == 4 || nchan == 8 || nchan == 16)) return -2;
+    orc_vdif_stream s;
+    if (vdif_open(framed, bytes, mbps, &s)) return -2;
+    if (nchan < 4 && nsamp % (4 / nchan)) return -3;
+    if ((s.databytes * 4) % nchan) return -2;
+    const int64_t spf = (int64_t)s.databytes * 4 / nchan;
+    int64_t good = 0, fcur = -1;
+    int ok = 0;
+    for (int64_t t = 0; t < nsamp; t++) {
+        const int64_t f = t / spf, st = t % spf;
+        if (f != fcur) { fcur = f; ok = vdif_ok(framed, bytes, &s, f); }
+        const uint8_t* p = framed + f * (int64_t)s.framebytes + vdif_payload_offset(&s, f);
+        good += ok;
+        for (int c = 0; c < nchan; c++) {
+            const int64_t bit = (st * nchan + c) * 2;
+            const unsigned code = (p[bit >> 3] >> (bit & 7)) & 3u;
+            out[(int64_t)c * nsamp + t] = ok ? lut[code] : 0.0f;
+        }
+        /* next frame as soon as a payload is used up (format_vdif.c:684-692) */
+        if (st == spf - 1 && (f + 2) * (int64_t)s.framebytes > bytes) return -1;
+    }
+    return good;
+}
+
+/* ---------------------------------------------------------------------- */
 /* Generic complex MAC (architecture.h:405-433)                            */
 /* ---------------------------------------------------------------------- */
 void orc_addproduct_32fc(const orc_cf32* a, const orc_cf32* b, orc_cf32* acc, int n)

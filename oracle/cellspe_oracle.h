@@ -57,6 +57,29 @@ int orc_mark5b_find_first_frame(const uint8_t* data, int64_t bytes);
 void orc_mark5b_valid_range(const uint8_t* payload, int* start, int* end);
 int64_t orc_mark5b_decode_framed(const uint8_t* framed, int64_t bytes, int nchan, int64_t nsamp, float* out);
 
+/* Framed VDIF, 2-bit real samples, as a mark5access memory stream opened with
+ * the format "VDIF_<databytes>-<mbps>-<nchan>-2" (format_vdif.c 1.4.3).
+ * The first frame starts at byte 0; word 2 of its header gives the frame
+ * length (8-byte units) and the legacy bit (word 0 bit 30) a 16-byte instead
+ * of a 32-byte header (mark5_format_vdif_init, format_vdif.c:2121-2257).
+ * orc_vdif_frame_ok restates, for frame f >= 1, mark5_format_vdif_validate
+ * (format_vdif.c:2299-2337: header time against the time predicted from the
+ * first frame on frames f % framegranularity == 0, then the invalid bit) and
+ * for every frame blanker_vdif (blanker_mark5.c:282-316: fill pattern in the
+ * first or the last 64-bit payload word blanks the frame); frame 0 is not
+ * validated (mark5_stream_next_frame, mark5_stream.c:144-193, runs only on
+ * the frames after it).  orc_vdif_decode_framed decodes nsamp samples per
+ * channel (nchan = 1, 2, 4, 8, 16) with the VDIF levels {-H, -1, +1, +H};
+ * returns the unblanked sample count, -1 when the frames run out (also when
+ * the last wanted sample ends the last frame), -2 on a header it cannot use
+ * or a buffer shorter than two frames, -3 when nsamp is not a multiple of the
+ * samples per byte.  Frame 0 of a legacy (16-byte header) stream is read from
+ * byte 32, as the library does when the format name is "VDIF_...". */
+int orc_vdif_frame_ok(const uint8_t* framed, int64_t bytes, int mbps, int64_t f);
+/* time of frame 0 as the stream reads it (ms->mjd, ms->sec, ms->ns) */
+int orc_vdif_first_time(const uint8_t* framed, int64_t bytes, int mbps, int* mjd, int* sec, int* ns);
+int64_t orc_vdif_decode_framed(const uint8_t* framed, int64_t bytes, int nchan, int mbps, int64_t nsamp, float* out);
+
 /* acc[i] += a[i]*b[i]            architecture.h:405-421 (do_complex_mac)  */
 void orc_addproduct_32fc(const orc_cf32* a, const orc_cf32* b, orc_cf32* acc, int n);
 /* acc[i] += a[i]*conj(b[i])      architecture.h:427-433                   */

@@ -63,3 +63,19 @@ int ref_mark5_decode_memory(const char* format, void* data, unsigned int bytes, 
     delete_mark5_stream(ms);
     return rc;
 }
+
+/* Time of the first frame as the library reads it when it opens a memory
+ * stream (ms->mjd, ms->sec, ms->ns after mark5_format_init).  Returns 0, or a
+ * negative value when the stream does not open. */
+int ref_mark5_stream_time(const char* format, void* data, unsigned int bytes, int* mjd, int* sec, int* ns)
+{
+    struct mark5_format_generic* f = new_mark5_format_generic_from_string(format);
+    if (!f) return -1;
+    struct mark5_stream* ms = new_mark5_stream(new_mark5_stream_memory(data, bytes), f);
+    if (!ms) return -2;
+    *mjd = ms->mjd;
+    *sec = ms->sec;
+    *ns = ms->ns;
+    delete_mark5_stream(ms);
+    return 0;
+}

@@ -71,6 +71,86 @@ def test_framed_mark5b_live_reference(orc):
             assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
 
 
+VDIF_LEVELS = np.array([-3.3359, -1.0, 1.0, 3.3359, 0.0], np.float32)
+VDIF_GOLDEN = {"v4ch": (4, 128), "v8ch_legacy": (8, 256), "v16ch_granularity": (16, 8192), "v1ch_day": (1, 128),
+               "v2ch_legacy": (2, 64)}
+
+
+@pytest.mark.parametrize("name", sorted(VDIF_GOLDEN))
+def test_framed_vdif_golden(orc, name):
+    """VDIF validation (invalid bit, header time, fill) + legacy headers + end-of-data rule
+    vs the library's own decode of the same bytes."""
+    nch, mbps = VDIF_GOLDEN[name]
+    g = np.load(GOLD / "vdif_framed.npz")
+    fr = g[f"{name}_framed"]
+    for k, ns in enumerate(g[f"{name}_nsamp"]):
+        good, out = orc.vdif_decode_framed(fr, nch, mbps, int(ns))
+        assert good == int(g[f"{name}_rc{k}"])
+        assert np.array_equal(out.view(np.uint32), VDIF_LEVELS[g[f"{name}_codes{k}"]].view(np.uint32))
+
+
+def test_vdif_golden_covers_each_blanking_rule():
+    """The fixtures hold what they are meant to: an invalid-bit frame 0 that stays
+    (frame 0 is not validated), blanked invalid / time-glitch / fill frames, and the
+    frame the library blanks because its frame time is not a whole number of ns."""
+    g = np.load(GOLD / "vdif_framed.npz")
+
+    def blanked(name, nch, db):
+        spf = db * 4 // nch
+        c = g[f"{name}_codes1"]
+        return [bool((c[:, f * spf:(f + 1) * spf] == 4).all()) for f in range(c.shape[1] // spf)]
+
+    assert blanked("v4ch", 4, 2000) == [False, False, True, True, False, True, True]
+    assert blanked("v16ch_granularity", 16, 2000)[8] and not any(blanked("v16ch_granularity", 16, 2000)[4:8])
+    assert blanked("v1ch_day", 1, 1024) == [False, False, False, False, True]
+
+
+def test_vdif_first_frame_time_every_epoch(orc):
+    """The calendar-computed reference epochs against the library's table, all 64."""
+    import synth
+
+    want = np.load(GOLD / "vdif_framed.npz")["epoch_times"]
+    for e in range(64):
+        fr = synth.vdif_frames(np.zeros(2 * 1024, np.uint8), 1024, 4, 128, ref_epoch=e, seconds=5 * 86400 + 7,
+                               first_frame=3)
+        assert orc.vdif_first_time(fr, 128) == tuple(int(v) for v in want[e]), e
+        if orc.have_ref():
+            assert orc.ref_mark5_stream_time(b"VDIF_1024-128-4-2", fr) == tuple(int(v) for v in want[e])
+
+
+def test_framed_vdif_live_reference(orc):
+    if not orc.have_ref():
+        pytest.skip("reference tree not compiled here")
+    import synth
+
+    rng = np.random.default_rng(23)
+    for db, nch, mbps, legacy in [(8000, 4, 512, False), (8000, 16, 2048, True), (8000, 1, 128, False),
+                                  (8000, 2, 256, False), (8000, 8, 8192, False), (1024, 4, 1024, False),
+                                  (5000, 8, 4000, True), (8192, 16, 4096, False)]:
+        hs = 16 if legacy else 32
+        fb, nf = db + hs, 9
+        fr = synth.vdif_frames(rng.integers(0, 256, nf * db, dtype=np.uint8), db, nch, mbps, legacy=legacy,
+                               ref_epoch=int(rng.integers(0, 64)), seconds=int(rng.integers(0, 1 << 30)),
+                               first_frame=int(rng.integers(0, 8)))
+        for f in rng.choice(nf, 4, replace=False):
+            kind = int(rng.integers(0, 4))
+            if kind == 0:
+                synth.vdif_set_invalid(fr, int(f), fb)
+            elif kind == 1:
+                fr[int(f) * fb + 4] ^= 1
+            elif kind == 2:
+                synth.vdif_fill(fr, int(f), fb, hs, 0, 8)
+            else:
+                synth.vdif_fill(fr, int(f), fb, hs, db - 8, db)
+        spf = db * 4 // nch
+        fmt = f"VDIF_{db}-{mbps}-{nch}-2".encode()
+        for ns in (3 * spf + 16, (nf - 1) * spf, nf * spf, nf * spf - 4):
+            rc, ref, off = orc.ref_mark5_decode_memory(fmt, fr, ns)
+            good, mine = orc.vdif_decode_framed(fr, nch, mbps, ns)
+            assert off == 0 and good == rc, (fmt, ns)
+            assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32)), (fmt, ns)
+
+
 def test_generic_mac_golden(orc):
     g = np.load(GOLD / "generic_mac.npz")
     acc = g["acc0"].copy()
