@@ -213,6 +213,25 @@ def run_configs(cg, torch, x_mode: int, with_cpu: bool):
     ms_f = _time_calls(torch, lambda: cg.spectrometer(spf, framed, power, bins), steps=5, warmup=2)
     res["framed_value"] = nsub * nsamp / (ms_f * 1e-3) / 1e9
     res["framed_ms_per_step"] = ms_f
+    del framed
+    # the same samples as a VDIF recording: 32-byte headers per 8000-byte payload
+    # (1024 Mbps, 16000 frames per second), every frame validated on the device
+    import synth
+
+    nfv = -(-payload.numel() // 8000)
+    mbps = int(fs * 2 * nsub / 1e6)
+    hdr = synth.vdif_frames(np.zeros(nfv * 8000, np.uint8), 8000, nsub, mbps).reshape(nfv, 8032)[:, :32]
+    vdif = torch.zeros((nfv, 8032), dtype=torch.uint8, device="cuda")
+    vdif[:, :32] = torch.from_numpy(hdr).cuda()
+    vflat = vdif[:, 32:].reshape(-1)
+    vflat[: payload.numel()] = payload
+    vdif = vdif.reshape(-1)
+    spv = cg.spec_params(NS, 2, 2, kspec, 1, nsub, vdif.numel(), layout=cg.SPEC_VDIF_FRAMED, levels=cg.LEVELS_VDIF,
+                         tonebins=32, rotatorlen=32, ntones=16, fs_hz=fs, memory=cg.MEM_DEVICE)
+    ms_v = _time_calls(torch, lambda: cg.spectrometer(spv, vdif, power, bins), steps=5, warmup=2)
+    res["vdif_value"] = nsub * nsamp / (ms_v * 1e-3) / 1e9
+    res["vdif_ms_per_step"] = ms_v
+    del vdif
     if with_cpu:
         import oracle
 
@@ -224,7 +243,7 @@ def run_configs(cg, torch, x_mode: int, with_cpu: bool):
         res["cpu_baseline"] = {"value": x.size / dt / 1e9, "unit": "Gsamples/s", "cores": 1, "kind": "port",
                                "sample": f"1 subband x {16 * NS} samples, {dt:.2f} s"}
     out["mark5b_spectrometer"] = res
-    del payload, framed, power, bins
+    del payload, power, bins
 
     # -- 16-station dual-pol (32 inputs), N = 8192, K = 4096, cubic delay model, one subband
     S3, N3, K3 = 32, 8192, 4096

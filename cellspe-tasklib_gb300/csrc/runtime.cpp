@@ -138,6 +138,7 @@ struct Workspace {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t sev[5] = {};          // stage boundaries of the last FX job
     cudaEvent_t cev[2 * PIPE_CHUNKS + 2] = {};   // copy / compute hand-offs
+    cudaEvent_t ev_legacy = nullptr;  // ordering after the legacy default stream
     Arena arena;
     bool own_stream = true;
     struct Out { void* host; const void* dev; size_t bytes; };
@@ -155,7 +156,20 @@ struct Workspace {
             if (e == cudaSuccess) e = cudaEventCreate(&ev);
         for (auto& ev : cev)
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_legacy, cudaEventDisableTiming);
         return e == cudaSuccess ? 0 : cuda_fail(e, "stream setup");
+    }
+    // The library's streams are non-blocking, so a call that reads device
+    // buffers first waits (on the device, not the host) for everything issued
+    // so far to the legacy default stream -- which itself waits for all
+    // blocking streams -- so buffers that the caller's earlier work fills there
+    // are complete.  Work on the caller's own non-blocking streams is the
+    // caller's to synchronise.
+    int after_legacy_stream()
+    {
+        cudaError_t e = cudaEventRecord(ev_legacy, cudaStreamLegacy);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ev_legacy, 0);
+        return e == cudaSuccess ? 0 : cuda_fail(e, "stream ordering");
     }
     void destroy()
     {
@@ -163,6 +177,7 @@ struct Workspace {
         arena.release();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (ev_legacy) cudaEventDestroy(ev_legacy);
         for (auto& ev : sev)
             if (ev) cudaEventDestroy(ev), ev = nullptr;
         for (auto& ev : cev)
@@ -404,6 +419,10 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     // Host buffers of large jobs move in chunks on the copy stream: input
     // blocks of inputs while the F stage transforms the blocks already there,
     // channel blocks of visibilities while the X stage computes later ones.
+    // (Kernels reading and writing page-locked host buffers in place over the
+    // CPU-GPU link measured slower here: the link carries ~193 GB/s to the host
+    // and ~211 GB/s from it whether copy engines or SMs drive it, and SM
+    // writes then stretch the X stage.)
     const int nsc = (host && sync && S * bpi >= (64LL << 20)) ? std::min(S, PIPE_CHUNKS) : 1;
     const bool stream_out = nsc > 1 && !p->accumulate && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR;
     const int ncb = stream_out ? std::min(C, PIPE_CHUNKS) : 1;
@@ -1159,6 +1178,7 @@ struct SvcJob {
     const double* poly = nullptr;
     void* vis = nullptr;
     long long footprint = 0;
+    cudaEvent_t ready = nullptr;      // device buffers complete (legacy stream at submit)
     std::chrono::steady_clock::time_point t_submit, t_start, t_done;
     int status = 0;
     bool done = false;
@@ -1204,7 +1224,16 @@ void service_worker(cellspe_service* sv)
         lk.unlock();
         sv->cv_work.notify_all();
         j->t_start = std::chrono::steady_clock::now();
-        int rc = init ? init : op_fx(ws, &j->p, j->raw, j->poly, j->vis, true);
+        int rc = init;
+        if (!rc && j->ready) {
+            cudaError_t e = cudaStreamWaitEvent(ws.stream, j->ready, 0);
+            if (e != cudaSuccess) rc = cuda_fail(e, "service job ordering");
+        }
+        if (!rc) rc = op_fx(ws, &j->p, j->raw, j->poly, j->vis, true);
+        if (j->ready) {
+            cudaEventDestroy(j->ready);
+            j->ready = nullptr;
+        }
         j->t_done = std::chrono::steady_clock::now();
         lk.lock();
         sv->in_flight -= j->footprint;
@@ -1952,12 +1981,18 @@ static int direct_gate()
     return 0;
 }
 
-#define DIRECT_PROLOGUE                         \
+// Synchronous direct calls: the thread's workspace, its stream ordered after
+// the legacy default stream.  Calls on a caller's stream (the async entry
+// point, which may run under stream capture) take the workspace only.
+#define DIRECT_WORKSPACE                        \
     int _g = direct_gate();                     \
     if (_g) return _g;                          \
     int _rc = 0;                                \
     Workspace* ws = thread_ws(&_rc);            \
     if (!ws) return _rc;
+#define DIRECT_PROLOGUE                         \
+    DIRECT_WORKSPACE                            \
+    if ((_rc = ws->after_legacy_stream())) return _rc;
 
 int cellspe_unpack2bit(const void* raw, long long nsamp, int nchan, int format, const float* custom_levels, float* out,
                        int memory)
@@ -2018,7 +2053,7 @@ long long cellspe_fx_workspace_bytes(const cellspe_fx_params* p) { return p ? fx
 int cellspe_fx_correlate_async(const cellspe_fx_params* p, const void* raw, const double* delay_poly, void* vis,
                                void* stream)
 {
-    DIRECT_PROLOGUE
+    DIRECT_WORKSPACE
     if (!p || p->memory != CELLSPE_MEM_DEVICE) return set_err(CELLSPE_ERR_ARG, "fx async: device memory only");
     cudaStream_t saved = ws->stream;
     ws->stream = (cudaStream_t)stream;
@@ -2066,6 +2101,16 @@ int cellspe_service_submit(cellspe_service* sv, const cellspe_fx_params* p, cons
     if (j->footprint > sv->budget)
         return set_err(CELLSPE_ERR_NOMEM, "service_submit: job footprint exceeds the service HBM budget");
     j->t_submit = std::chrono::steady_clock::now();
+    // the job's buffers may be filled by work the caller issued before submit:
+    // the worker's stream waits for the legacy default stream as it was now
+    if (p->memory == CELLSPE_MEM_DEVICE) {
+        cudaError_t e = cudaEventCreateWithFlags(&j->ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(j->ready, cudaStreamLegacy);
+        if (e != cudaSuccess) {
+            if (j->ready) cudaEventDestroy(j->ready);
+            return cuda_fail(e, "service_submit");
+        }
+    }
     {
         std::lock_guard<std::mutex> lk(sv->mu);
         j->id = sv->next_id++;
@@ -2115,6 +2160,8 @@ void cellspe_service_destroy(cellspe_service* sv)
     }
     sv->cv_work.notify_all();
     for (auto& t : sv->workers) t.join();
+    for (auto& j : sv->queue)              // never started
+        if (j->ready) cudaEventDestroy(j->ready), j->ready = nullptr;
     delete sv;
 }
 

@@ -8,8 +8,12 @@
  * inputs to the GPU and results back; pinned memory from cellspe_host_alloc
  * is fastest) or CELLSPE_MEM_DEVICE (device pointers on the engine's GPU).
  * Calls from several host threads are safe; each thread uses its own stream
- * and workspace.  There is no CPU fallback: without a usable GPU every call
- * fails with CELLSPE_ERR_CUDA and cellspe_last_error() says why.
+ * and workspace.  A call's first kernel waits (on the device) for all work
+ * issued before the call to the legacy default stream, so device buffers
+ * filled there, or on blocking streams, are ready; work on the caller's own
+ * non-blocking streams must be synchronised by the caller.  There is no CPU
+ * fallback: without a usable GPU every call fails with CELLSPE_ERR_CUDA and
+ * cellspe_last_error() says why.
  */
 #ifndef CELLSPE_GPU_H
 #define CELLSPE_GPU_H

@@ -156,3 +156,28 @@ def test_fx_host_buffers_streamed_match_device(cg, mode):
     vb = np.zeros((P, C), np.complex64)              # baseline-major: streamed in only
     cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=x_mode, vis_order=cg.VIS_BASELINE_MAJOR), raw, vb)
     assert np.array_equal(vb, ref.T)
+
+
+def test_direct_call_waits_for_prior_default_stream_work(cg):
+    """A synchronous call on device buffers sees the data that work queued just
+    before it on the default stream writes (the library's streams are
+    non-blocking; each call first waits on the device for that stream)."""
+    import torch
+
+    import synth
+
+    S, N, K = 64, 2048, 1024
+    P, C = S * (S + 1) // 2, N // 2
+    src = synth.device_stations(S, N * K, 0.1, seed=13)
+    p = cg.fx_params(S, N, K, src.shape[1])
+    want = torch.empty((C, P), dtype=torch.complex64, device="cuda")
+    cg.fx_correlate(p, src, want)
+    for _ in range(3):
+        raw = torch.zeros_like(src)
+        busy = torch.randn((4096, 4096), device="cuda")
+        for _ in range(8):                       # keep the default stream busy for a while
+            busy = busy @ busy.T / 4096.0
+        raw.copy_(src)                           # queued behind the products, not yet done
+        vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
+        cg.fx_correlate(p, raw, vis)
+        assert torch.equal(vis, want)
