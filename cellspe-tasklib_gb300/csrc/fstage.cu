@@ -395,39 +395,59 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
             __syncwarp();
             Dft<32>::run(v);                                    // over n1 -> k2: v[k2] = Z[lane + 32 k2]
 
-            float2 B = make_float2(1.f, 0.f), D = B;
+            // Real-FFT split, one pair (k, 1024 - k) per lane and step: with
+            // s = Z[k] + conj(Z[1024-k]), d = Z[k] - conj(Z[1024-k]) and
+            // t = (W_2048^k / 2) d,
+            //     X[k] = s/2 - i t,     X[1024-k] = conj(s/2 + i t)
+            // (W_2048^(1024-k) = -conj(W_2048^k)).  Lane l, step k2 < 16 takes
+            // k = l + 32 k2, whose partner Z[1024-k] is lane (32-l) mod 32's
+            // register 31-k2 (lane 0: its own register (32-k2) mod 32); lane 0
+            // adds the self-paired k = 512.  X[1024] (k = 0's partner) is not a
+            // channel.  Optional per-channel phasor exp(i (ph0 + c dph)) and
+            // scale, then the staging store.
+            float2 B = make_float2(1.f, 0.f), D = B, B2 = B;
             if constexpr (PHASE) {
                 const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);
                 float sn, cs;
                 sincosf(ph0 + (float)lane * dph, &sn, &cs);
-                B = make_float2(cs, sn);
+                B = make_float2(cs, sn);                         // channel lane + 32 k2
+                sincosf(ph0 + (float)(M - lane) * dph, &sn, &cs);
+                B2 = make_float2(cs, sn);                        // channel 1024 - lane - 32 k2
                 sincosf(32.f * dph, &sn, &cs);
                 D = make_float2(cs, sn);
             }
             const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
-#pragma unroll
-            for (int k2 = 0; k2 < 32; k2++) {
-                float2 zb;
-                zb.x = __shfl_sync(0xffffffffu, v[31 - k2].x, src_lane);
-                zb.y = __shfl_sync(0xffffffffu, v[31 - k2].y, src_lane);
-                if (lane == 0) zb = v[(32 - k2) & 31];
-                const float2 za = v[k2];
-                // X = E + W O with E = (a + b*)/2, O = (a - b*)/(2i):
-                // X = s/2 - i (W/2) d,  s = a + b*, d = a - b*
-                const float2 sm = make_float2(za.x + zb.x, za.y - zb.y);
-                const float2 df = make_float2(za.x - zb.x, za.y + zb.y);
-                const float2 t = cmul(cmul(whalf, w64c(k2)), df);
-                float2 X = make_float2(fmaf(0.5f, sm.x, t.y), fmaf(0.5f, sm.y, -t.x));
-                const int c = lane + 32 * k2;
-                if constexpr (PHASE) {
-                    X = cmul(X, B);
-                    B = cmul(B, D);
-                }
+            auto put = [&](int c, float2 X) {
                 if (scl) X = cscale(X, __ldg(scl + c));
                 if constexpr (FMT == CS_SPECTRA_F32)
                     reinterpret_cast<float2*>(stage)[c * (G + 1) + ls] = X;
                 else
                     reinterpret_cast<__half2*>(stage)[c * (G + 1) + ls] = __floats2half2_rn(X.x, X.y);
+            };
+#pragma unroll
+            for (int k2 = 0; k2 <= 16; k2++) {
+                if (k2 == 16 && lane != 0) break;
+                float2 zb;
+                if (k2 < 16) {
+                    zb.x = __shfl_sync(0xffffffffu, v[31 - k2].x, src_lane);
+                    zb.y = __shfl_sync(0xffffffffu, v[31 - k2].y, src_lane);
+                }
+                if (lane == 0) zb = v[(32 - k2) & 31];
+                const float2 za = v[k2];
+                const float2 sm = make_float2(za.x + zb.x, za.y - zb.y);
+                const float2 df = make_float2(za.x - zb.x, za.y + zb.y);
+                const float2 t = cmul(cmul(whalf, w64c(k2)), df);
+                float2 X1 = make_float2(fmaf(0.5f, sm.x, t.y), fmaf(0.5f, sm.y, -t.x));
+                float2 X2 = make_float2(fmaf(0.5f, sm.x, -t.y), -fmaf(0.5f, sm.y, t.x));
+                const int c1 = lane + 32 * k2, c2 = M - c1;
+                if constexpr (PHASE) {
+                    X1 = cmul(X1, B);
+                    X2 = cmul(X2, B2);
+                    B = cmul(B, D);
+                    B2 = cmul_conj(B2, D);
+                }
+                put(c1, X1);
+                if (k2 < 16 && c1 != 0) put(c2, X2);
             }
         }
     }
