@@ -330,6 +330,7 @@ def main():
     import torch
 
     import cellspe_gpu as cg
+    import replicas
     import synth
 
     rank = int(os.environ.get("RANK", "0"))
@@ -352,7 +353,7 @@ def main():
     N_run = args.fft_points
     C_run = N_run // 2
     T_run = N_run * K_run
-    raw = synth.device_stations(S, T_run, RHO, seed=4 + 1000 * rank)
+    raw = synth.device_stations(S, T_run, RHO, seed=replicas.job_seed(rank))
     vis = torch.empty((C_run, P), dtype=torch.complex64, device="cuda")
     params = cg.fx_params(S, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
     clk = ClockSampler(local).__enter__()             # running before the timed region
@@ -375,13 +376,9 @@ def main():
     clk.mark_end()
     clk.__exit__(None, None, None)
     launches = cg.kernel_launches() - l0
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1), dist, device="cuda")
     ms_step = ms / args.steps
-    value = world * S * T_run / (ms_step * 1e-3) / 1e9
+    value = replicas.aggregate_gsamples(world, S * T_run, ms_step)
     stage_ms = stage_sum / args.steps
 
     # ---- end to end through the C ABI with host buffers --------------------
@@ -402,12 +399,8 @@ def main():
         torch.cuda.synchronize()
         f1.record()
         f1.synchronize()
-        e2e_ms = f0.elapsed_time(f1) / args.e2e_steps
-        if dist:
-            t = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e_value = world * S * T_run / (e2e_ms * 1e-3) / 1e9
+        e2e_ms = replicas.max_over_ranks(f0.elapsed_time(f1) / args.e2e_steps, dist, device="cuda")
+        e2e_value = replicas.aggregate_gsamples(world, S * T_run, e2e_ms)
 
     # ---- roofline of the dominant kernel -----------------------------------
     # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) measured by
