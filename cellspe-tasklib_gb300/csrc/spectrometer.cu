@@ -242,22 +242,54 @@ __global__ void k_pcal_fold(const uint8_t* __restrict__ planes, int64_t bytes_pe
     const int hop = N / ov, wpw = N / 16;            // 32-bit words per window
     const int64_t nwords = (int64_t)cnt * wpw;
     const float lut[4] = {l0, l1, l2, l3};
-    for (int64_t w = (int64_t)blockIdx.x * nt + tid; w < nwords; w += (int64_t)nblk_per_row * nt) {
-        const int win = (int)(w / wpw), wi = (int)(w - (int64_t)win * wpw);
-        const int64_t wg = ((int64_t)spec * samp_per_spec + (int64_t)(j0 + win * step) * hop) / 16 + wi;
-        uint32_t word = __ldg(plane + wg);
-        const uint32_t valid = vmask ? __ldg(vmask + (wg >> 1)) >> ((wg & 1) * 16) : 0xffffu;
-        const int n0 = wi * 16;                      // sample index inside the window
+    // Sample j of word wi of a window has rotator index (16 wi + j) mod L and
+    // bin that mod T.  A thread keeps the 16 rotator values and bins of its
+    // current wi in registers and sums each j over the windows in a register,
+    // adding the sums into its shared-memory slots when wi changes (for
+    // N = 65536, whose windows have 4096 words like the 32 x 128 threads of
+    // a row, never: each thread owns one wi).
+    float2 acc[16], rj[16];
+    int bj[16];
+    int cur = -1;
+    auto flush = [&]() {
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-            int li = (n0 + j) % L;
-            float x = (valid >> j) & 1u ? lut_pick4(lut, (word >> (2 * j)) & 3u) : 0.f;
-            float2 r = __ldg(rot + li);
-            float2& slot = pacc[(li % T) * nt + tid];
-            slot.x += x * r.x;
-            slot.y += x * r.y;
+            if (cur >= 0) {
+                float2& slot = pacc[bj[j] * nt + tid];
+                slot.x += acc[j].x;
+                slot.y += acc[j].y;
+            }
+            acc[j] = make_float2(0.f, 0.f);
+        }
+    };
+    flush();
+    for (int64_t w = (int64_t)blockIdx.x * nt + tid; w < nwords; w += (int64_t)nblk_per_row * nt) {
+        const int win = (int)(w / wpw), wi = (int)(w - (int64_t)win * wpw);
+        if (wi != cur) {
+            flush();
+            cur = wi;
+            int li = (wi * 16) % L, bi = li % T;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                rj[j] = __ldg(rot + li);
+                bj[j] = bi;
+                li++;
+                bi++;
+                if (li == L) li = 0, bi = 0;
+                else if (bi == T) bi = 0;
+            }
+        }
+        const int64_t wg = ((int64_t)spec * samp_per_spec + (int64_t)(j0 + win * step) * hop) / 16 + wi;
+        const uint32_t word = __ldg(plane + wg);
+        const uint32_t valid = vmask ? __ldg(vmask + (wg >> 1)) >> ((wg & 1) * 16) : 0xffffu;
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const float x = (valid >> j) & 1u ? lut_pick4(lut, (word >> (2 * j)) & 3u) : 0.f;
+            acc[j].x += x * rj[j].x;
+            acc[j].y += x * rj[j].y;
         }
     }
+    flush();
     __syncthreads();
     for (int b = tid; b < T; b += nt) {
         float2 s = make_float2(0.f, 0.f);
