@@ -164,7 +164,10 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
                 int f1 = (2 * n) & 15, f2 = (2 * n2) & 15;
                 const float2 x1 = sample_pair(lut, w1, f1, vmask, start + 2 * n);
                 const float2 x2 = sample_pair(lut, w2, f2, vmask, start + 2 * n2);
-                const float2 wa = __ldg(win2 + n), wb = __ldg(win2 + n2);
+                // cosine^2: w(i + N/2) = sin^2 = 1 - w(i), so one table read
+                // serves both halves (the table pair differs by <= 2^-24)
+                const float2 wa = __ldg(win2 + n);
+                const float2 wb = (a.window == 2) ? make_float2(1.f - wa.x, 1.f - wa.y) : __ldg(win2 + n2);
                 float2 z1 = make_float2(x1.x * wa.x, x1.y * wa.y);
                 float2 z2 = make_float2(x2.x * wb.x, x2.y * wb.y);
                 v[r] = p ? cmul(csub(z1, z2), rot32(tw_t, r)) : cadd(z1, z2);
