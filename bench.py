@@ -312,7 +312,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="tc", choices=["tc", "fp32"])
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-segments", type=int, default=64)
+    ap.add_argument("--cpu-segments", type=int, default=64,
+                    help="segments per step of the reference arm (--impl reference)")
+    ap.add_argument("--cpu-baseline-segments", type=int, default=768,
+                    help="segments of this arm's cpu_baseline sample (~10 s on 16 cores; 1 core: 1/16 of it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
@@ -451,12 +454,13 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
-        v, dt = cpu_baseline(raw_h, args.cpu_segments, nthreads)
-        v1, dt1 = cpu_baseline(raw_h, max(1, args.cpu_segments // 8), 1)
+        kb = min(args.cpu_baseline_segments, K_run)
+        v, dt = cpu_baseline(raw_h, kb, nthreads)
+        v1, dt1 = cpu_baseline(raw_h, max(1, kb // 16), 1)
         cpu = {"value": v, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
-               "sample": f"{S} inputs x {args.cpu_segments} segments x {N_run} samples, {dt:.1f} s",
+               "sample": f"{S} inputs x {kb} segments x {N_run} samples, {dt:.1f} s",
                "value_1core": v1,
-               "sample_1core": f"{S} inputs x {max(1, args.cpu_segments // 8)} segments, {dt1:.1f} s"}
+               "sample_1core": f"{S} inputs x {max(1, kb // 16)} segments, {dt1:.1f} s"}
 
     if rank == 0:
         line = {

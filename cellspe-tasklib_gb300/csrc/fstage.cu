@@ -536,10 +536,11 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
 // during the first); 4 = 16 warps and 16 segments per CTA, so that each
 // output row gets a 32-byte run; 5 = 8 warps, 32 segments per CTA (64-byte
 // runs); 4 and 5 are FP16 only.  Picked once per process by
-// timing all on a 64-input x 512-segment job of zero samples (the FFT's
-// arithmetic does not depend on the values; the spectra exceed the L2 cache
-// and use the padded row pitch of the FX path), unless the environment
-// variable CELLSPE_FSTAGE_VARIANT forces one.
+// timing all on a 128-input x 1024-segment job of zero samples (the FFT's
+// arithmetic does not depend on the values; the spectra, 0.57 GB, exceed the
+// L2 cache and use the padded row pitch of the FX path), fastest of four
+// timed launches each after one warm-up, unless the environment variable
+// CELLSPE_FSTAGE_VARIANT forces one.
 int g_w2048_choice[2][2] = {{0, 0}, {0, 0}};
 std::mutex g_w2048_mu;
 
@@ -548,7 +549,7 @@ int tune_w2048(const float2* tw, cudaStream_t st)
 {
     const char* env = getenv("CELLSPE_FSTAGE_VARIANT");
     if (env && env[0] >= '1' && env[0] <= '0' + W_NVARIANTS) return env[0] - '0';
-    const int S = 64, K = 512, KP = K + 64;
+    const int S = 128, K = 1024, KP = K + 64;
     const size_t raw_bytes = (size_t)S * K * 2048 / 4;
     const size_t out_bytes = (size_t)S * KP * 1024 * (FMT == CS_SPECTRA_F32 ? 8 : 4);
     const size_t ph_bytes = PHASE ? (size_t)S * K * 4 : 0;
@@ -570,8 +571,8 @@ int tune_w2048(const float2* tw, cudaStream_t st)
     float best = 1e30f;
     int choice = 1;
     for (int v = 1; v <= W_NVARIANTS; v++) {
-        float total = 0.f;
-        for (int rep = 0; rep < 3; rep++) {
+        float fastest = 1e30f;
+        for (int rep = 0; rep < 5; rep++) {
             cudaEventRecord(e0, st);
             int rc = launch_w2048_choice<FMT, PHASE>(v, a, tw, st);
             cudaEventRecord(e1, st);
@@ -579,9 +580,9 @@ int tune_w2048(const float2* tw, cudaStream_t st)
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
             if (rc) ms = 1e30f;
-            if (rep > 0) total += ms;
+            if (rep > 0) fastest = fminf(fastest, ms);
         }
-        if (total < best) { best = total; choice = v; }
+        if (fastest < best) { best = fastest; choice = v; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
