@@ -16,9 +16,20 @@
 // spectrum (N/2+1 complex64 per spectrum) to <BaseFilename>_xpol_swspec.bin.
 //
 // Input: 2-bit samples (BitsPerSample = 2), SourceChannels channels
-// interleaved per sample time (Mark5B payload order, or the TwoBit order with
-// ChannelOrderIncreasing; the level table follows SourceFormat: "Mark5B..."
-// uses the mark5access table, anything else the TwoBitUnpacker table).
+// interleaved per sample time.  SourceFormat selects the framing as
+// FileSource::open does (FileSource.cpp:40-62): "Mark5B" is a framed Mark5B
+// recording (16-byte headers, 10000-byte payloads, first frame searched for),
+// "VDIF" a framed VDIF recording (frames from byte 0, frame length from the
+// first header; Mbps = 2 x BandwidthHz x 2 bits x SourceChannels); headers are
+// stripped and invalid or fill-pattern data blanked on the GPU, as mark5access
+// decodes them (FileSource passes fill bytes through as samples, and the
+// reference has no VDIF unpacker).  A framed file is read whole and its
+// spectra computed in one call, so the phase-cal FFT count runs on across
+// them as in a reference core buffer holding the whole file.  Any other
+// SourceFormat is headerless payload (Mark5B payload order, or the TwoBit
+// order with ChannelOrderIncreasing; names starting with "Mark5B" use the
+// mark5access level table, anything else the TwoBitUnpacker table), read one
+// integration period per call.
 // Differences from the reference: a zero PCalOffsetHz uses the comb period as
 // rotator length (the reference divides by zero in Helpers::gcd), and the
 // data of one integration period are read per GPU call instead of buffers
@@ -31,6 +42,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <cstring>
 #include <fstream>
 #include <iostream>
@@ -211,6 +223,98 @@ int main(int argc, char** argv)
         cellspe_host_free(raw0);
         cellspe_host_free(raw1);
         return status;
+    }
+
+    const std::string fmt_l = lower(s.format);
+    if (fmt_l == "mark5b" || fmt_l == "vdif") {
+        // framed recordings: whole files, headers stripped on the GPU
+        const bool vdif = fmt_l == "vdif";
+        const int nsrc = argc - 2;
+        std::vector<void*> bufs(nsrc, nullptr);
+        long long nspec = -1, bytes = 0;
+        for (int f = 0; f < nsrc; f++) {
+            std::ifstream in(argv[2 + f], std::ios::binary | std::ios::ate);
+            if (!in) { std::cerr << "Error: cannot open " << argv[2 + f] << "\n"; return -1; }
+            const long long sz = (long long)in.tellg();
+            in.seekg(0);
+            if (f == 0) bytes = sz;
+            if (sz != bytes) { std::cerr << "Error: the two framed inputs differ in size\n"; return -1; }
+            bufs[f] = cellspe_host_alloc((size_t)std::max(sz, 1LL));
+            if (!bufs[f] || !in.read((char*)bufs[f], sz)) { std::cerr << "Error: cannot read " << argv[2 + f] << "\n"; return -1; }
+            long long samples = 0;
+            if (vdif) {
+                cellspe_vdif_info info;
+                const int mbps = (int)llround(s.fs * 2.0 * s.channels / 1e6);
+                if (cellspe_vdif_deframe(bufs[f], sz, s.channels, mbps, 0, nullptr, nullptr, CELLSPE_MEM_HOST, &info)) {
+                    std::cerr << "Error: " << cellspe_last_error() << "\n";
+                    return -1;
+                }
+                samples = info.frames * ((long long)(info.frame_bytes - info.header_bytes) * 4 / s.channels);
+            } else {
+                cellspe_mark5b_info info;
+                if (cellspe_mark5b_deframe(bufs[f], sz, s.channels, 0, nullptr, nullptr, CELLSPE_MEM_HOST, &info)) {
+                    std::cerr << "Error: " << cellspe_last_error() << "\n";
+                    return -1;
+                }
+                samples = info.frames * (10000LL * 4 / s.channels);
+            }
+            const long long n = samples / (K * N);
+            nspec = nspec < 0 ? n : std::min(nspec, n);
+        }
+        if (nspec < 1) { std::cerr << "Error: the framed input holds less than one integration period\n"; return -1; }
+        p.input_layout = vdif ? CELLSPE_SPEC_VDIF_FRAMED : CELLSPE_SPEC_MARK5B_FRAMED;
+        p.levels = vdif ? CELLSPE_LEVELS_VDIF : CELLSPE_LEVELS_MARK5B;
+        p.raw_bytes = bytes;
+        p.n_spectra = (int)nspec;
+        const long long nb = N / 2 + 1;
+        const std::string base1 = fill_pattern(s.base, s, s.use_ch[0]);
+        int rc;
+        if (nsrc == 2) {
+            const std::string base2 = fill_pattern(s.base + "_file2", s, s.use_ch[1]);
+            std::vector<float> power((size_t)2 * nspec * nb), xpol((size_t)2 * nspec * nb);
+            std::vector<float> bins((size_t)2 * nspec * std::max(tonebins, 1) * 2);
+            rc = cellspe_spectrometer_xpol(&p, bufs[0], bufs[1], s.use_ch[0] - 1, s.use_ch[1] - 1, power.data(),
+                                           xpol.data(), s.pcal ? bins.data() : nullptr);
+            if (!rc) {
+                std::ofstream(base1 + "_swspec.bin", std::ios::binary).write((const char*)power.data(), sizeof(float) * nspec * nb);
+                std::ofstream(base2 + "_swspec.bin", std::ios::binary)
+                    .write((const char*)(power.data() + nspec * nb), sizeof(float) * nspec * nb);
+                std::ofstream(base1 + "_xpol_swspec.bin", std::ios::binary)
+                    .write((const char*)xpol.data(), sizeof(float) * 2 * nspec * nb);
+                if (s.pcal) {
+                    std::ofstream(base1 + "_pcal.bin", std::ios::binary).write((const char*)bins.data(), sizeof(float) * 2 * nspec * tonebins);
+                    std::ofstream(base2 + "_pcal.bin", std::ios::binary)
+                        .write((const char*)(bins.data() + 2 * nspec * tonebins), sizeof(float) * 2 * nspec * tonebins);
+                }
+            }
+        } else {
+            const int ch = s.use_ch[0];
+            std::vector<float> power((size_t)s.channels * nspec * nb);
+            std::vector<float> bins((size_t)s.channels * nspec * std::max(tonebins, 1) * 2);
+            rc = cellspe_spectrometer(&p, bufs[0], power.data(), s.pcal ? bins.data() : nullptr, nullptr);
+            if (!rc) {
+                std::ofstream out(base1 + "_swspec.bin", s.ascii ? std::ios::out : std::ios::binary);
+                for (long long sp = 0; sp < nspec; sp++) {
+                    const float* spec = power.data() + ((size_t)(ch - 1) * nspec + sp) * nb;
+                    if (s.ascii) {
+                        out << "// --------------------- DATA SET TIMESTAMP xxxx ---------------------\n";
+                        out << "// FFT bins 0.." << (N / 2) << " + Nyquist\n";
+                        for (long long k = 0; k < nb; k++) out << spec[k] << "\n";
+                    } else {
+                        out.write((const char*)spec, sizeof(float) * nb);
+                    }
+                }
+                if (s.pcal)
+                    std::ofstream(base1 + "_pcal.bin", std::ios::binary)
+                        .write((const char*)(bins.data() + (size_t)(ch - 1) * nspec * tonebins * 2),
+                               sizeof(float) * 2 * nspec * tonebins);
+            }
+        }
+        for (void* b : bufs) cellspe_host_free(b);
+        if (rc) { std::cerr << "Error: " << cellspe_last_error() << "\n"; return -1; }
+        std::cerr << nspec << " spectra of " << N << " points from framed " << s.format << " input -> " << base1
+                  << "_swspec.bin\n";
+        return 0;
     }
 
     int status = 0;

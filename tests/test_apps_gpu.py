@@ -106,3 +106,55 @@ BaseFilename1 = {tmp_path}/out
         assert np.linalg.norm(a0[s] - rp[0, 0]) / np.linalg.norm(rp[0, 0]) < 1e-5
         assert np.linalg.norm(a1[s] - rp[1, 0]) / np.linalg.norm(rp[1, 0]) < 1e-5
         assert np.linalg.norm(xp[s] - rx[0]) / np.linalg.norm(rx[0]) < 1e-5
+
+
+def _spec_ini(tmp_path, N, K, fs, fmt, nsub, ch):
+    ini = tmp_path / "spec.ini"
+    ini.write_text(f"""[Spectrometer]
+FFTpoints = {N}
+FFTIntegrationTimeSec = {K * N / fs}
+FFToverlapFactor = 2
+WindowType = Cosine2
+BandwidthHz = {fs / 2}
+SourceFormat = {fmt}
+BitsPerSample = 2
+SourceChannels = {nsub}
+UseFile1Channel = {ch}
+ExtractPCal = 1
+PCalOffsetHz = 0
+BaseFilename1 = {tmp_path}/out
+""")
+    return ini
+
+
+@pytest.mark.parametrize("fmt", ["Mark5B", "VDIF"])
+def test_swspectrometer_cli_framed_recording(cg, orc, tmp_path, fmt):
+    """SourceFormat = Mark5B / VDIF: a framed recording (headers, a blanked frame),
+    headers stripped and blanking applied on the GPU; all spectra in one call."""
+    import synth
+
+    N, K, fs, nspec, nsub, ch = 4096, 8, 32e6, 3, 16, 5
+    words, _ = synth.mark5b_subbands(16, N * K * nspec + 20000, fs_hz=fs, seed=41, n_channels=N // 2, pcal_amp=0.2)
+    payload = words.view(np.uint8)
+    if fmt == "Mark5B":
+        nf = payload.size // 10000
+        fr = synth.mark5b_frames(payload[: nf * 10000], prefix=777)
+        synth.mark5b_fill(fr, 2, 0, 4000, prefix=777)
+        good, planes = orc.mark5b_decode_framed(fr, nsub, N * K * nspec)
+    else:
+        mbps = int(fs * 2 * nsub / 1e6)
+        nf = payload.size // 8000
+        fr = synth.vdif_frames(payload[: nf * 8000], 8000, nsub, mbps, first_frame=5)
+        synth.vdif_set_invalid(fr, 3, 8032)
+        good, planes = orc.vdif_decode_framed(fr, nsub, mbps, N * K * nspec)
+    assert good > 0
+    data = tmp_path / "scan.bin"
+    fr.tofile(data)
+    ini = _spec_ini(tmp_path, N, K, fs, fmt, nsub, ch)
+    r = subprocess.run([str(PKG / "swspectrometer_gpu"), str(ini), str(data)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(tmp_path / "out_swspec.bin", np.float32).reshape(nspec, N // 2 + 1)
+    bins = np.fromfile(tmp_path / "out_pcal.bin", np.complex64).reshape(nspec, 32)
+    ref, ref_b = orc.spectrometer(planes[ch - 1], N, 2, 2, K, 32, 32, 0.0, fs)   # one call, all spectra
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+    assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < 1e-5
