@@ -677,27 +677,57 @@ namespace {
 constexpr int TT = 64;
 
 __global__ void __launch_bounds__(256) k_transpose_f16(const __half2* __restrict__ in, int K, int C, int kp, int S_out,
-                                                       __half* __restrict__ out)
+                                                       __half* __restrict__ out, int vec)
 {
-    __shared__ __half2 tile[TT][TT + 1];
+    __shared__ uint32_t tile[TT][TT + 1];            // half2 bits; the odd row stride keeps both passes conflict-free
     const int s = blockIdx.z, k0 = blockIdx.y * TT, c0 = blockIdx.x * TT;
-    for (int i = threadIdx.x; i < TT * TT; i += 256) {
-        const int kk = i / TT, cc = i % TT, k = k0 + kk, c = c0 + cc;
-        tile[kk][cc] = (k < K && c < C) ? in[((int64_t)s * K + k) * C + c] : __floats2half2_rn(0.f, 0.f);
+    // vec: 16-byte aligned rows in and out (C % 4 == 0, kp % 8 == 0, aligned bases)
+    const bool full = vec && k0 + TT <= K && c0 + TT <= C;
+    if (full) {
+        // 64 rows x 16 uint4 (4 channels each)
+        for (int i = threadIdx.x; i < TT * (TT / 4); i += 256) {
+            const int kk = i / (TT / 4), q = i % (TT / 4);
+            const uint4 v = *reinterpret_cast<const uint4*>(in + ((int64_t)s * K + k0 + kk) * C + c0 + 4 * q);
+            tile[kk][4 * q] = v.x;
+            tile[kk][4 * q + 1] = v.y;
+            tile[kk][4 * q + 2] = v.z;
+            tile[kk][4 * q + 3] = v.w;
+        }
+    } else {
+        for (int i = threadIdx.x; i < TT * TT; i += 256) {
+            const int kk = i / TT, cc = i % TT, k = k0 + kk, c = c0 + cc;
+            const __half2 x = (k < K && c < C) ? in[((int64_t)s * K + k) * C + c] : __floats2half2_rn(0.f, 0.f);
+            tile[kk][cc] = *reinterpret_cast<const uint32_t*>(&x);
+        }
     }
     __syncthreads();
+    if (full) {
+        // rows (c, plane) of 64 halves as 8 pieces of 16 bytes: the Re (low) or
+        // Im (high) halves of 8 consecutive segments
+        for (int i = threadIdx.x; i < TT * 2 * (TT / 8); i += 256) {
+            const int pc = i % (TT / 8), row = i / (TT / 8), cc = row >> 1, plane = row & 1;
+            uint32_t w[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) w[j] = tile[8 * pc + j][cc];
+            const uint32_t sel = plane ? 0x7632u : 0x5410u;
+            *reinterpret_cast<uint4*>(out + (((int64_t)(c0 + cc) * 2 + plane) * S_out + s) * kp + k0 + 8 * pc) =
+                make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel), __byte_perm(w[4], w[5], sel),
+                           __byte_perm(w[6], w[7], sel));
+        }
+        return;
+    }
     // row (c, plane): 64 halves of k as 32 half pairs
     for (int i = threadIdx.x; i < TT * 2 * (TT / 2); i += 256) {
         const int w = i % (TT / 2), row = i / (TT / 2), cc = row >> 1, plane = row & 1;
         const int c = c0 + cc, k = k0 + 2 * w;
         if (c >= C || k >= K) continue;
-        const __half2 a = tile[2 * w][cc], b = tile[2 * w + 1][cc];
+        const uint32_t a = tile[2 * w][cc], b = tile[2 * w + 1][cc];
         __half* o = out + (((int64_t)c * 2 + plane) * S_out + s) * kp + k;
         if (k + 1 < K) {
-            *reinterpret_cast<__half2*>(o) = plane ? __halves2half2(__high2half(a), __high2half(b))
-                                                   : __halves2half2(__low2half(a), __low2half(b));
+            *reinterpret_cast<uint32_t*>(o) = __byte_perm(a, b, plane ? 0x7632u : 0x5410u);
         } else {
-            *o = plane ? __high2half(a) : __low2half(a);
+            const uint32_t h = plane ? (a >> 16) : (a & 0xFFFFu);
+            *reinterpret_cast<unsigned short*>(o) = (unsigned short)h;
         }
     }
 }
@@ -729,7 +759,9 @@ int cs_spectra_transpose(const void* tmp, int S, int K, int C, int kp, int S_out
         k_transpose_f32<<<grid, 256, 0, st>>>((const float2*)tmp, K, C, kp, S_out, (float2*)out), cs_count_launches(1);
     } else {
         if ((uintptr_t)out % 4 || kp % 2) return CS_ERR_ARG;
-        k_transpose_f16<<<grid, 256, 0, st>>>((const __half2*)tmp, K, C, kp, S_out, (__half*)out), cs_count_launches(1);
+        const int vec = (C % 4 == 0 && kp % 8 == 0 && (uintptr_t)tmp % 16 == 0 && (uintptr_t)out % 16 == 0) ? 1 : 0;
+        k_transpose_f16<<<grid, 256, 0, st>>>((const __half2*)tmp, K, C, kp, S_out, (__half*)out, vec),
+            cs_count_launches(1);
     }
     return (int)cudaGetLastError();
 }
