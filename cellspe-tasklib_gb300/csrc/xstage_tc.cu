@@ -151,13 +151,19 @@ struct TcArgs {
     const float* inv_scale;     // [S][scale_stride] or null
     int scale_stride;
     int accumulate;
+    int box_rows;               // rows per TMA box: BM, or S rounded up to 8 when S < BM
+    int small;                  // S <= BM: one tile per channel whose B operand is its A operand
+    uint32_t tmem_cols;         // TMEM columns: Re V in [0, cols/2), Im V in [cols/2, cols)
 };
 
-__global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant__ CUtensorMap tmap, TcArgs a)
+__global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant__ CUtensorMap tmap,
+                                                           const __grid_constant__ TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);   // full[S], empty[S], acc
+    // S <= BM: a stage holds Ar and Ai only (the tile is diagonal, B = A)
+    const uint32_t stage_bytes = a.small ? 2 * A_BYTES : STAGE_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);   // full[S], empty[S], acc
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
     const uint32_t sbase = smem_u32(smem);
     const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, accb = full0 + 16 * STAGES;
@@ -172,7 +178,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     const int n_need = min(min(j0 + BN, i0 + BM), S) - j0;
     const uint32_t n_eff = (uint32_t)((n_need + 15) & ~15);
     const bool half_b = n_eff <= (uint32_t)BM;      // only the first 128 B rows are loaded
-    const uint32_t stage_tx = half_b ? 4 * A_BYTES : STAGE_BYTES;
+    // S < 128: the boxes hold the S (rounded up to 8) rows that exist, so a
+    // channel's planes are read once; the rows of the operand tiles past them
+    // only feed accumulator rows and columns that are never stored
+    const uint32_t stage_tx = a.small ? 2u * (uint32_t)a.box_rows * BK * 2
+                              : half_b ? 4u * (uint32_t)a.box_rows * BK * 2 : STAGE_BYTES;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -185,7 +195,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(TMEM_COLS)
+                     "r"(a.tmem_cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -205,14 +215,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 const int s = kc % STAGES;
                 const uint32_t ph = (kc / STAGES) & 1;
                 if (!mbar_wait(empty0 + 8 * s, ph ^ 1, ERR_EMPTY_WAIT)) { ok = false; break; }
-                const uint32_t st = sbase + s * STAGE_BYTES;
+                const uint32_t st = sbase + s * stage_bytes;
                 const uint32_t fb = full0 + 8 * s;
                 mbar_expect_tx(fb, stage_tx);
                 const int x = kc * BK;
                 tma_load_2d(st, &tmap, x, rowA_re, fb);
                 tma_load_2d(st + A_BYTES, &tmap, x, rowA_im, fb);
-                tma_load_2d(st + 2 * A_BYTES, &tmap, x, rowB_re, fb);
-                tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tmap, x, rowB_im, fb);
+                if (!a.small) {
+                    tma_load_2d(st + 2 * A_BYTES, &tmap, x, rowB_re, fb);
+                    tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tmap, x, rowB_im, fb);
+                }
                 if (!half_b) {
                     tma_load_2d(st + 2 * A_BYTES + A_BYTES, &tmap, x, rowB_re + BM, fb);
                     tma_load_2d(st + 2 * A_BYTES + B_BYTES + A_BYTES, &tmap, x, rowB_im + BM, fb);
@@ -227,19 +239,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             const uint32_t id_pos = make_idesc(false, n_eff), id_neg = make_idesc(true, n_eff);
-            const uint32_t d_re = tmem, d_im = tmem + BN;
+            const uint32_t d_re = tmem, d_im = tmem + a.tmem_cols / 2;
             bool ok = true;
             for (int kc = 0; kc < nk; kc++) {
                 const int s = kc % STAGES;
                 if (!mbar_wait(full0 + 8 * s, (kc / STAGES) & 1, ERR_FULL_WAIT)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t st = sbase + s * STAGE_BYTES;
+                const uint32_t st = sbase + s * stage_bytes;
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; kk++) {
                     const uint32_t off = kk * 32;                  // 16 FP16 along K
                     const uint64_t ar = sw64_desc(st + off), ai = sw64_desc(st + A_BYTES + off);
-                    const uint64_t br = sw64_desc(st + 2 * A_BYTES + off);
-                    const uint64_t bi = sw64_desc(st + 2 * A_BYTES + B_BYTES + off);
+                    const uint64_t br = a.small ? ar : sw64_desc(st + 2 * A_BYTES + off);
+                    const uint64_t bi = a.small ? ai : sw64_desc(st + 2 * A_BYTES + B_BYTES + off);
                     const uint32_t acc = (kc | kk) ? 1u : 0u;
                     umma_f16(d_re, ar, br, id_pos, acc);           // Re += Ar Br^T
                     umma_f16(d_re, ai, bi, id_pos, 1u);            // Re += Ai Bi^T
@@ -274,7 +286,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
             for (int cb = 0; cb < ncb; cb++) {
                 uint32_t re[16], im[16];
                 tmem_ld16(lane_base + cb * 16, re);
-                tmem_ld16(lane_base + BN + cb * 16, im);
+                tmem_ld16(lane_base + a.tmem_cols / 2 + cb * 16, im);
                 tmem_ld_wait();
 #pragma unroll
                 for (int jj = 0; jj < 16; jj++) {
@@ -309,7 +321,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
     }
 }
 
@@ -369,7 +381,8 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
     CUtensorMap tm;
     cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)C * 2 * S};
     cuuint64_t gstride[1] = {(cuuint64_t)kp * 2};
-    cuuint32_t box[2] = {BK, BM};
+    const int box_rows = S < BM ? (S + 7) / 8 * 8 : BM;
+    cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(spectra), gdim, gstride, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -380,9 +393,18 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
     CS_CUDA_TRY(cudaGetSymbolAddress(&errp, g_tc_error));
     CS_CUDA_TRY(cudaMemsetAsync(errp, 0, sizeof(unsigned), st));
 
+    // S <= 128: one diagonal tile per channel, B = A, 16 KB stages and only the
+    // TMEM columns the tile needs, so several CTAs share an SM
+    const int small = S <= BM ? 1 : 0;
+    uint32_t cols = TMEM_COLS;
+    if (small) {
+        const uint32_t n_eff = (uint32_t)((S + 15) & ~15);
+        cols = 32;
+        while (cols < 2 * n_eff) cols *= 2;
+    }
     TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, scale_stride > 0 ? scale_stride : C,
-             accumulate};
-    const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+             accumulate, box_rows, small, cols};
+    const size_t smem = (size_t)STAGES * (small ? 2 * A_BYTES : STAGE_BYTES) + 1024 + 256;
     CS_CUDA_TRY(cudaFuncSetAttribute(k_xmac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(ntiles, C);
     k_xmac_tc<<<grid, TC_THREADS, smem, st>>>(tm, a), cs_count_launches(1);
