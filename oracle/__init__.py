@@ -14,8 +14,10 @@ Contents
 * ``ref_generic()`` -- the reference's GENERIC kernels of ``architecture.h``.
 * FP64 numpy models: ``fx_spectra_f64``, ``fx_vis_f64``, ``delay_state_f64``.
 
-Parity status: the 2-bit decode and the complex MAC are pinned bit-for-bit
-to the reference (mark5access, architecture.h GENERIC).  The FFT is not
+Parity status: the 2-bit decode, the framed Mark5B and VDIF memory-stream
+decodes (header strip, validation, blanking, end-of-data rule) and the
+complex MAC are pinned bit-for-bit to the reference (mark5access,
+architecture.h GENERIC), live and through the golden vectors in tests/golden.  The FFT is not
 pinned by the reference (FFTW/IPP/Cell SDK absent): it is checked against an
 FP64 DFT and analytic known answers.  The phase-cal fold is pinned by the
 reference's own PCal unit-test recipe (tone phase within 0.1 degree).
