@@ -314,8 +314,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-segments", type=int, default=64,
                     help="segments per step of the reference arm (--impl reference)")
-    ap.add_argument("--cpu-baseline-segments", type=int, default=768,
-                    help="segments of this arm's cpu_baseline sample (~10 s on 16 cores; 1 core: 1/16 of it)")
+    ap.add_argument("--cpu-baseline-segments", type=int, default=1024,
+                    help="segments of this arm's cpu_baseline sample (~11 s on 16 cores; 1 core: 1/16 of it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
