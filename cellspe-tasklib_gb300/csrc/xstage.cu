@@ -7,7 +7,8 @@
 // S(S+1)/2 products of every channel at once.  Per channel it is a Hermitian
 // rank-K update, so it is tiled like a GEMM: a CTA owns a 64x64 block of
 // (i, j) for one channel and streams 16 time samples per stage through
-// shared memory; each of its 128 threads keeps 4x8 complex accumulators.
+// shared memory; each of its 128 threads keeps 4x8 complex accumulators
+// (32x32 blocks of 32 threads when S <= 32).
 // Only blocks on or below the diagonal are launched.
 //
 // Layout in:  float2 spectra[C][S][K]   (time innermost)
@@ -16,10 +17,7 @@
 #include "kernels.h"
 
 namespace {
-constexpr int XT = 64;      // tile edge (inputs)
 constexpr int XK = 16;      // time samples per stage
-constexpr int XTHREADS = 128;
-constexpr int XLD = XT + 1; // padded shared row (float2)
 
 __device__ __forceinline__ void tile_coords(int t, int& bi, int& bj)
 {
@@ -31,9 +29,15 @@ __device__ __forceinline__ void tile_coords(int t, int& bi, int& bj)
     bj = t - b * (b + 1) / 2;
 }
 
-__global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict__ spec, int S, int K, int kp,
-                                                      float2* __restrict__ vis, int64_t P, int accumulate)
+// Tile edge XT (64, or 32 for S <= 32 so that small arrays do not compute
+// three empty quarters of every tile); XT^2/32 threads, each keeping 4 x 8
+// complex accumulators: rows ti + TI a, columns tj + TJ b.
+template <int XT>
+__global__ void __launch_bounds__(XT * XT / 32) k_xmac_f32(const float2* __restrict__ spec, int S, int K, int kp,
+                                                          float2* __restrict__ vis, int64_t P, int accumulate)
 {
+    constexpr int NT = XT * XT / 32, TI = XT / 4, TJ = XT / 8, XLD = XT + 1;
+    constexpr int ITER = 2 * XT / NT;                // (row, 8-sample chunk) loads per thread per stage
     __shared__ float2 As[2][XK][XLD];
     __shared__ float2 Bs[2][XK][XLD];
     const int c = blockIdx.y;
@@ -41,32 +45,36 @@ __global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict_
     tile_coords(blockIdx.x, bi, bj);
     const int i0 = bi * XT, j0 = bj * XT;
     const int tid = threadIdx.x;
-    const int ti = tid >> 3;          // 0..15 -> rows ti + 16a
-    const int tj = tid & 7;           // 0..7  -> cols tj + 8b
+    const int ti = tid / TJ;          // rows ti + TI a
+    const int tj = tid % TJ;          // cols tj + TJ b
     const float2* base = spec + (int64_t)c * S * kp;
 
-    // loader: thread -> (row = tid/2, 8 consecutive time samples)
-    const int lrow = tid >> 1, lk = (tid & 1) * 8;
-    const int ai = i0 + lrow, bjr = j0 + lrow;
-    const float2* pa = base + (int64_t)min(ai, S - 1) * kp;
-    const float2* pb = base + (int64_t)min(bjr, S - 1) * kp;
-    const bool va = ai < S, vb = bjr < S;
-
-    float2 ra[8], rb[8];
+    float2 ra[ITER][8], rb[ITER][8];
     auto gload = [&](int k0) {
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            int k = k0 + lk + u;
-            bool kin = k < K;
-            ra[u] = (va && kin) ? __ldg(pa + k) : make_float2(0.f, 0.f);
-            rb[u] = (vb && kin) ? __ldg(pb + k) : make_float2(0.f, 0.f);
+        for (int it = 0; it < ITER; it++) {
+            const int q = tid + it * NT, lrow = q >> 1, lk = (q & 1) * 8;
+            const int ai = i0 + lrow, bjr = j0 + lrow;
+            const float2* pa = base + (int64_t)min(ai, S - 1) * kp;
+            const float2* pb = base + (int64_t)min(bjr, S - 1) * kp;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int k = k0 + lk + u;
+                const bool kin = k < K;
+                ra[it][u] = (ai < S && kin) ? __ldg(pa + k) : make_float2(0.f, 0.f);
+                rb[it][u] = (bjr < S && kin) ? __ldg(pb + k) : make_float2(0.f, 0.f);
+            }
         }
     };
     auto sstore = [&](int buf) {
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            As[buf][lk + u][lrow] = ra[u];
-            Bs[buf][lk + u][lrow] = rb[u];
+        for (int it = 0; it < ITER; it++) {
+            const int q = tid + it * NT, lrow = q >> 1, lk = (q & 1) * 8;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                As[buf][lk + u][lrow] = ra[it][u];
+                Bs[buf][lk + u][lrow] = rb[it][u];
+            }
         }
     };
 
@@ -87,9 +95,9 @@ __global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict_
         for (int kk = 0; kk < XK; kk++) {
             float2 av[4], bv[8];
 #pragma unroll
-            for (int a = 0; a < 4; a++) av[a] = As[cur][kk][ti + 16 * a];
+            for (int a = 0; a < 4; a++) av[a] = As[cur][kk][ti + TI * a];
 #pragma unroll
-            for (int b = 0; b < 8; b++) bv[b] = Bs[cur][kk][tj + 8 * b];
+            for (int b = 0; b < 8; b++) bv[b] = Bs[cur][kk][tj + TJ * b];
 #pragma unroll
             for (int a = 0; a < 4; a++)
 #pragma unroll
@@ -107,11 +115,11 @@ __global__ void __launch_bounds__(XTHREADS) k_xmac_f32(const float2* __restrict_
     float2* out = vis + (int64_t)c * P;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-        int i = i0 + ti + 16 * a;
+        int i = i0 + ti + TI * a;
         if (i >= S) continue;
 #pragma unroll
         for (int b = 0; b < 8; b++) {
-            int j = j0 + tj + 8 * b;
+            int j = j0 + tj + TJ * b;
             if (j > i) continue;
             int64_t p = (int64_t)i * (i + 1) / 2 + j;
             float2 v = make_float2(accr[a][b], acci[a][b]);
@@ -148,12 +156,17 @@ __global__ void k_vis_transpose(const float2* __restrict__ in, float2* __restric
 int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis, int accumulate, cudaStream_t st)
 {
     if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || kp < K) return CS_ERR_ARG;
-    int nb = (S + XT - 1) / XT;
-    int64_t tiles = (int64_t)nb * (nb + 1) / 2;
     if (C > 65535) return CS_ERR_ARG;
+    const int xt = S <= 32 ? 32 : 64;
+    int nb = (S + xt - 1) / xt;
+    int64_t tiles = (int64_t)nb * (nb + 1) / 2;
     int64_t P = (int64_t)S * (S + 1) / 2;
     dim3 grid((unsigned)tiles, C);
-    k_xmac_f32<<<grid, XTHREADS, 0, st>>>(spectra, S, K, kp, vis, P, accumulate), cs_count_launches(1);
+    if (xt == 32)
+        k_xmac_f32<32><<<grid, 32, 0, st>>>(spectra, S, K, kp, vis, P, accumulate);
+    else
+        k_xmac_f32<64><<<grid, 128, 0, st>>>(spectra, S, K, kp, vis, P, accumulate);
+    cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
