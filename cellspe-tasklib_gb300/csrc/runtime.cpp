@@ -130,14 +130,17 @@ struct Arena {
     }
 };
 
-constexpr int PIPE_CHUNKS = 8;        // host-buffer FX jobs: input / output chunks
+// Host-buffer FX jobs move their input in PIPE_IN blocks of inputs and their
+// visibilities in PIPE_OUT blocks of channels: more input blocks shorten the
+// wait for the first one; output blocks stay large enough to fill the GPU.
+constexpr int PIPE_IN = 16, PIPE_OUT = 8;
 
 struct Workspace {
     cudaStream_t stream = nullptr;
     cudaStream_t copy = nullptr;      // host <-> device copies overlapping the kernels
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t sev[5] = {};          // stage boundaries of the last FX job
-    cudaEvent_t cev[2 * PIPE_CHUNKS + 2] = {};   // copy / compute hand-offs
+    cudaEvent_t cev[PIPE_IN + PIPE_OUT + 2] = {};   // copy / compute hand-offs
     cudaEvent_t ev_legacy = nullptr;  // ordering after the legacy default stream
     Arena arena;
     bool own_stream = true;
@@ -423,16 +426,16 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     // CPU-GPU link measured slower here: the link carries ~193 GB/s to the host
     // and ~211 GB/s from it whether copy engines or SMs drive it, and SM
     // writes then stretch the X stage.)
-    const int nsc = (host && sync && S * bpi >= (64LL << 20)) ? std::min(S, PIPE_CHUNKS) : 1;
+    const int nsc = (host && sync && S * bpi >= (64LL << 20)) ? std::min(S, PIPE_IN) : 1;
     const bool stream_out = nsc > 1 && !p->accumulate && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR;
-    const int ncb = stream_out ? std::min(C, PIPE_CHUNKS) : 1;
+    const int ncb = stream_out ? std::min(C, PIPE_OUT) : 1;
     Job j(ws, host);
     const uint8_t* d_raw = nsc > 1 ? (const uint8_t*)j.scratch((size_t)(S * bpi))
                                    : (const uint8_t*)j.in(raw, (size_t)(S * bpi));
     if (nsc > 1 && !j.err) {
         // the copy stream starts after everything queued before this job
-        cudaEventRecord(ws.cev[2 * PIPE_CHUNKS], ws.stream);
-        cudaStreamWaitEvent(ws.copy, ws.cev[2 * PIPE_CHUNKS], 0);
+        cudaEventRecord(ws.cev[PIPE_IN + PIPE_OUT], ws.stream);
+        cudaStreamWaitEvent(ws.copy, ws.cev[PIPE_IN + PIPE_OUT], 0);
         for (int i = 0; i < nsc && !j.err; i++) {
             const long long s0 = (long long)S * i / nsc, s1 = (long long)S * (i + 1) / nsc;
             cudaError_t e = cudaMemcpyAsync((void*)(d_raw + s0 * bpi), (const uint8_t*)raw + s0 * bpi,
@@ -515,7 +518,14 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     const bool direct = !host && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR && !p->accumulate;
     float2* vis_cp = direct ? (float2*)vis : (float2*)j.scratch((size_t)C * P * 8);
     for (int b = 0; b < ncb && !j.err; b++) {
-        const long long c0 = (long long)C * b / ncb, c1 = (long long)C * (b + 1) / ncb, cn = c1 - c0;
+        // streamed output: a small first block (1/16 of the channels) starts the
+        // copy out early; the rest in equal blocks
+        auto cbound = [&](int i) -> long long {
+            if (ncb == 1) return i ? C : 0;
+            const long long first = std::max(1LL, (long long)C / 16);
+            return i == 0 ? 0 : first + (long long)(C - first) * (i - 1) / (ncb - 1);
+        };
+        const long long c0 = cbound(b), c1 = cbound(b + 1), cn = c1 - c0;
         int rc;
         if (p->x_mode == CELLSPE_X_FP32)
             rc = cs_xmac_f32((const float2*)fa.out + c0 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P, 0, ws.stream);
@@ -524,8 +534,8 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
                                 d_inv_scale ? d_inv_scale + c0 : nullptr, C, 0, ws.stream);
         rc = map_rc(rc, "X stage");
         if (!rc && stream_out) {
-            cudaError_t e = cudaEventRecord(ws.cev[PIPE_CHUNKS + b], ws.stream);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.copy, ws.cev[PIPE_CHUNKS + b], 0);
+            cudaError_t e = cudaEventRecord(ws.cev[PIPE_IN + b], ws.stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.copy, ws.cev[PIPE_IN + b], 0);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync((float2*)vis + c0 * P, vis_cp + c0 * P, (size_t)(cn * P * 8), cudaMemcpyDeviceToHost,
                                     ws.copy);
@@ -535,8 +545,8 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     }
     if (nsc > 1) {
         // the job ends when the copy stream's work has ended too
-        cudaEventRecord(ws.cev[2 * PIPE_CHUNKS + 1], ws.copy);
-        cudaStreamWaitEvent(ws.stream, ws.cev[2 * PIPE_CHUNKS + 1], 0);
+        cudaEventRecord(ws.cev[PIPE_IN + PIPE_OUT + 1], ws.copy);
+        cudaStreamWaitEvent(ws.stream, ws.cev[PIPE_IN + PIPE_OUT + 1], 0);
     }
     if (sync) cudaEventRecord(ws.sev[3], ws.stream);
     if (!direct && !stream_out && !j.err) {
