@@ -342,6 +342,14 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
         sincospif(-(float)lane / 1024.0f, &sn, &cs);
         whalf = make_float2(0.5f * cs, 0.5f * sn);
     }
+    // W_1024^(lane e), e < 16, by a balanced recurrence (w^2e = (w^e)^2,
+    // w^(2e+1) = w^2e w), and W_1024^(16 lane), kept for all segments
+    float2 wp[16];
+    wp[0] = make_float2(1.f, 0.f);
+    wp[1] = w1;
+#pragma unroll
+    for (int e = 2; e < 16; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], w1) : cmul(wp[e / 2], wp[e / 2]);
+    const float2 w16p = cmul(wp[8], wp[8]);
     __syncthreads();
     const int src_lane = (32 - lane) & 31;
 
@@ -373,20 +381,12 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
                 v[n2] = lut16[bits & 15u];
             }
             Dft<32>::run(v);                                    // over n2 -> k1
-            // v[k1] *= W_1024^(lane k1): powers of w1 by a balanced recurrence
-            // (w^2e = (w^e)^2, w^(2e+1) = w^2e w), applied on the fly
-            {
-                float2 wp[16];
-                wp[1] = w1;
+            // v[k1] *= W_1024^(lane k1), the powers formed once per thread
 #pragma unroll
-                for (int e = 2; e < 16; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], w1) : cmul(wp[e / 2], wp[e / 2]);
+            for (int e = 1; e < 16; e++) v[e] = cmul(v[e], wp[e]);
+            v[16] = cmul(v[16], w16p);
 #pragma unroll
-                for (int e = 1; e < 16; e++) v[e] = cmul(v[e], wp[e]);
-                const float2 w16p = cmul(wp[8], wp[8]);
-                v[16] = cmul(v[16], w16p);
-#pragma unroll
-                for (int e = 17; e < 32; e++) v[e] = cmul(v[e], cmul(w16p, wp[e - 16]));
-            }
+            for (int e = 17; e < 32; e++) v[e] = cmul(v[e], cmul(w16p, wp[e - 16]));
 #pragma unroll
             for (int e = 0; e < 32; e++) tb[e * W_TP + lane] = v[e];
             __syncwarp();
