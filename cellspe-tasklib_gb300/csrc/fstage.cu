@@ -474,6 +474,13 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
     } else {
         const __half2* st = reinterpret_cast<const __half2*>(stage);
         __half* out = reinterpret_cast<__half*>(a.out);
+        // element (c, plane, s, k): channel-major planes [C][2][S][KP], or
+        // k-blocked [C][S][KP/32][2][32] (the Re and Im halves of 32 segments
+        // side by side: a 32-segment tile writes 128 contiguous bytes per channel)
+        auto at = [&](int c, int plane, int k) -> int64_t {
+            if (a.kblock) return ((((int64_t)c * S + s) * (KP / 32) + k / 32) * 2 + plane) * 32 + (k % 32);
+            return (((int64_t)c * 2 + plane) * S + s) * KP + k;
+        };
         if (nvalid == G && KP % 8 == 0) {
             constexpr int P8 = G / 8;                 // 16-byte pieces per output row
             for (int idx = threadIdx.x; idx < M * 2 * P8; idx += NT) {
@@ -481,7 +488,7 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
                 // pick the Re (low) or Im (high) halves of 8 staged half2 words
                 const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + 8 * piece);
                 const uint32_t sel = plane ? 0x7632u : 0x5410u;
-                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * KP + k0 + 8 * piece) =
+                *reinterpret_cast<uint4*>(out + at(c, plane, k0 + 8 * piece)) =
                     make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
                                __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
             }
@@ -490,7 +497,7 @@ __global__ void __launch_bounds__(32 * WARPS, (WARPS == 16 || G > 16) ? 1 : (WAR
                 const int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
                 if (l < nvalid) {
                     const __half2 x = st[c * (G + 1) + l];
-                    out[(((int64_t)c * 2 + plane) * S + s) * KP + k0 + l] = plane ? __high2half(x) : __low2half(x);
+                    out[at(c, plane, k0 + l)] = plane ? __high2half(x) : __low2half(x);
                 }
             }
         }
@@ -564,6 +571,7 @@ int tune_w2048(const float2* tw, cudaStream_t st)
     a.dphase = PHASE ? (const float*)(buf + raw_bytes + out_bytes + ph_bytes) : nullptr;
     a.lut[0] = -3.f; a.lut[1] = -1.f; a.lut[2] = 1.f; a.lut[3] = 3.f;
     a.format = FMT;
+    a.kblock = cs_fstage_kblocked(a) ? 1 : 0;    // FP16: the layout the FX path writes
     a.out = buf + raw_bytes;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -639,15 +647,23 @@ int cs_delay_state(const double* poly, int S, int N, int K, double fs_hz, double
     return (int)cudaGetLastError();
 }
 
+bool cs_fstage_kblocked(const CsFStageArgs& a)
+{
+    const int kp = a.kp ? a.kp : a.K;
+    return a.format == CS_SPECTRA_F16 && a.N == 2048 && !a.msb_first && !a.seg_major && a.K % 32 == 0 &&
+           kp % 32 == 0;
+}
+
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
 {
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
+    if (a.kblock && !cs_fstage_kblocked(a)) return CS_ERR_ARG;
     // The tensor-core F stage is opt-in (CELLSPE_FSTAGE_TC=1, read per call):
     // its 8-segment units give 16-byte output runs, and on 512 inputs x 4096
     // segments it measured 14.5 ms against 7.3 ms for the 16-segment warp
-    // FFT below.
-    if (cs_fstage_tc_supported(a)) {
+    // FFT below.  It writes the channel-major planes only.
+    if (!a.kblock && cs_fstage_tc_supported(a)) {
         const char* e = getenv("CELLSPE_FSTAGE_TC");
         if (e && e[0] == '1') return cs_fx_fstage_tc(a, st);
     }

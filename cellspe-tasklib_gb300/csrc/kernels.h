@@ -64,8 +64,16 @@ struct CsFStageArgs {
     int seg_major;              // 1: out is [S][K][C] (F32 float2, F16 half2 Re|Im), each
                                 // segment's spectrum contiguous; cs_spectra_transpose then
                                 // makes the channel-major layout (the generic kernels only)
+    int kblock;                 // F16 only, 1: k-blocked rows, see cs_fstage_kblocked
 };
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
+// True when the F stage for these arguments writes FP16 spectra k-blocked:
+// __half [C][S_out][kp/32][2][32], i.e. for each (channel, input) and block of
+// 32 segments the 32 Re halves then the 32 Im halves (128 contiguous bytes, the
+// 2048-point warp F stage's 32-segment tiles).  Needs N = 2048, K and kp
+// multiples of 32; the X stage then reads the same layout (kblock = 1).  A
+// launch over a block of inputs writes at out + s0 * kp * 4 bytes.
+bool cs_fstage_kblocked(const CsFStageArgs& a);
 // Segment-major spectra [S][K][C] (tmp) -> the X stage's layout at out:
 // F32 float2 rows (c, s), F16 half rows (c, plane, s); row pitch kp, S_out
 // inputs per (c[, plane]) block (tmp and out already offset to the block).
@@ -86,10 +94,12 @@ int cs_fstage_tc_status(unsigned* code);
 int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis, int accumulate,
                 cudaStream_t st);
 // Tensor-core (tcgen05, FP16 in, FP32 accumulate) X stage:
-// spectra __half [C][2][S][kp] (K used; kp % 8 == 0) -> vis float2 [C][P];
+// spectra __half [C][2][S][kp] (K used; kp % 8 == 0), or k-blocked
+// [C][S][kp/32][2][32] with kblock = 1 (K, kp % 32 == 0) -> vis float2 [C][P];
 // inv_scale [S*C] or null.
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
-                   int scale_stride, int accumulate, cudaStream_t st);   // inv_scale[s * scale_stride + c]
+                   int scale_stride, int accumulate, cudaStream_t st,
+                   int kblock = 0);   // inv_scale[s * scale_stride + c]
 // Error code of the last tensor-core X-stage launch (0 = ok; 1..3 = a
 // pipeline wait timed out).  Call after the launching stream has synchronised.
 int cs_xmac_tc_status(unsigned* code);

@@ -479,6 +479,7 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     }
     const int kp = (int)spectra_pitch(K);
     fa.kp = kp;
+    fa.kblock = cs_fstage_kblocked(fa) ? 1 : 0;        // FP16, N = 2048: 128-byte rows per 32 segments
     fa.out = j.scratch((size_t)C * S * kp * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
     if (sync) cudaEventRecord(ws.sev[1], ws.stream);
     // bytes of one spectra element: F32 rows [C][S][kp] of float2, F16 rows [C][2][S][kp] of half
@@ -497,7 +498,8 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
             fb.raw = d_raw + s0 * bpi;
             fb.S = (int)(s1 - s0);
             fb.S_out = S;
-            fb.out = (char*)fa.out + s0 * kp * el_bytes;          // input s0's row in every (c, plane) block
+            // input s0's row in every (c, plane) block, or its k-blocked rows in every channel
+            fb.out = (char*)fa.out + s0 * kp * el_bytes * (fa.kblock ? 2 : 1);
             if (fa.shift) fb.shift = fa.shift + s0 * K;
             if (fa.phase0) fb.phase0 = fa.phase0 + s0 * K, fb.dphase = fa.dphase + s0 * K;
             if (fa.scale) fb.scale = fa.scale + s0 * C;
@@ -531,7 +533,7 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
             rc = cs_xmac_f32((const float2*)fa.out + c0 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P, 0, ws.stream);
         else
             rc = cs_xmac_tc_f16((const uint16_t*)fa.out + c0 * 2 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P,
-                                d_inv_scale ? d_inv_scale + c0 : nullptr, C, 0, ws.stream);
+                                d_inv_scale ? d_inv_scale + c0 : nullptr, C, 0, ws.stream, fa.kblock);
         rc = map_rc(rc, "X stage");
         if (!rc && stream_out) {
             cudaError_t e = cudaEventRecord(ws.cev[PIPE_IN + b], ws.stream);

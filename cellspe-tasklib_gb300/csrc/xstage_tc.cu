@@ -92,6 +92,16 @@ CS_DEV void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int x, int y, uint3
         : "memory");
 }
 
+// k-blocked spectra: coordinates (k within the block, plane, block, row)
+CS_DEV void tma_load_4d(uint32_t dst, const CUtensorMap* tm, int x, int p, int kb, int row, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(p), "r"(kb), "r"(row), "r"(bar)
+        : "memory");
+}
+
 CS_DEV void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 CS_DEV void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -154,6 +164,7 @@ struct TcArgs {
     int box_rows;               // rows per TMA box: BM, or S rounded up to 8 when S < BM
     int small;                  // S <= BM: one tile per channel whose B operand is its A operand
     uint32_t tmem_cols;         // TMEM columns: Re V in [0, cols/2), Im V in [cols/2, cols)
+    int kblock;                 // spectra k-blocked [C][S][kp/32][2][32] (4-D tensor map)
 };
 
 __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant__ CUtensorMap tmap,
@@ -209,6 +220,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
         if (lane == 0) {
             const int rowA_re = (c * 2 + 0) * S + i0, rowA_im = (c * 2 + 1) * S + i0;
             const int rowB_re = (c * 2 + 0) * S + j0, rowB_im = (c * 2 + 1) * S + j0;
+            // k-blocked: rows (c, s) with the plane a coordinate of its own
+            const int krowA = c * S + i0, krowB = c * S + j0;
+            auto load = [&](uint32_t dst, int kc, int plane, int row2d, int rowk, uint32_t bar) {
+                if (a.kblock) tma_load_4d(dst, &tmap, 0, plane, kc, rowk, bar);
+                else tma_load_2d(dst, &tmap, kc * BK, row2d, bar);
+            };
             int issued = 0;
             bool ok = true;
             for (int kc = 0; kc < nk && ok; kc++) {
@@ -218,16 +235,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 const uint32_t st = sbase + s * stage_bytes;
                 const uint32_t fb = full0 + 8 * s;
                 mbar_expect_tx(fb, stage_tx);
-                const int x = kc * BK;
-                tma_load_2d(st, &tmap, x, rowA_re, fb);
-                tma_load_2d(st + A_BYTES, &tmap, x, rowA_im, fb);
+                load(st, kc, 0, rowA_re, krowA, fb);
+                load(st + A_BYTES, kc, 1, rowA_im, krowA, fb);
                 if (!a.small) {
-                    tma_load_2d(st + 2 * A_BYTES, &tmap, x, rowB_re, fb);
-                    tma_load_2d(st + 2 * A_BYTES + B_BYTES, &tmap, x, rowB_im, fb);
+                    load(st + 2 * A_BYTES, kc, 0, rowB_re, krowB, fb);
+                    load(st + 2 * A_BYTES + B_BYTES, kc, 1, rowB_im, krowB, fb);
                 }
                 if (!half_b) {
-                    tma_load_2d(st + 2 * A_BYTES + A_BYTES, &tmap, x, rowB_re + BM, fb);
-                    tma_load_2d(st + 2 * A_BYTES + B_BYTES + A_BYTES, &tmap, x, rowB_im + BM, fb);
+                    load(st + 2 * A_BYTES + A_BYTES, kc, 0, rowB_re + BM, krowB + BM, fb);
+                    load(st + 2 * A_BYTES + B_BYTES + A_BYTES, kc, 1, rowB_im + BM, krowB + BM, fb);
                 }
                 issued = kc + 1;
             }
@@ -368,10 +384,11 @@ CsEncodeTiledFn cs_encode_tiled()
 }
 
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
-                   int scale_stride, int accumulate, cudaStream_t st)
+                   int scale_stride, int accumulate, cudaStream_t st, int kblock)
 {
     if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || C > 65535 || kp < K) return CS_ERR_ARG;
     if (K % 8 != 0 || kp % 8 != 0 || (uintptr_t)spectra % 16) return CS_ERR_ARG;   // TMA: 16-byte pitch and base
+    if (kblock && (K % 32 != 0 || kp % 32 != 0)) return CS_ERR_ARG;
     CsEncodeTiledFn enc = cs_encode_tiled();
     if (!enc) return CS_ERR_UNSUPPORTED;
     int ntiles = 0;
@@ -384,9 +401,23 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
     const int box_rows = S < BM ? (S + 7) / 8 * 8 : BM;
     cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(spectra), gdim, gstride, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r;
+    if (!kblock) {
+        r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(spectra), gdim, gstride, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    } else {
+        // [C*S rows][K/32 used of kp/32 blocks][2 planes][32 halves]: a box of
+        // (32 halves, 1 plane, 1 block, box_rows rows) lands in shared memory as
+        // the same [rows][32] tile as the channel-major map's box
+        cuuint64_t g4[4] = {32, 2, (cuuint64_t)K / 32, (cuuint64_t)C * S};
+        cuuint64_t s4[3] = {64, 128, (cuuint64_t)kp / 32 * 128};
+        cuuint32_t b4[4] = {32, 1, 1, (cuuint32_t)box_rows};
+        cuuint32_t e4[4] = {1, 1, 1, 1};
+        r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<void*>(spectra), g4, s4, b4, e4,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    }
     if (r != CUDA_SUCCESS) return CS_ERR_ARG;
 
     void* errp = nullptr;
@@ -403,7 +434,7 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
         while (cols < 2 * n_eff) cols *= 2;
     }
     TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, scale_stride > 0 ? scale_stride : C,
-             accumulate, box_rows, small, cols};
+             accumulate, box_rows, small, cols, kblock ? 1 : 0};
     const size_t smem = (size_t)STAGES * (small ? 2 * A_BYTES : STAGE_BYTES) + 1024 + 256;
     CS_CUDA_TRY(cudaFuncSetAttribute(k_xmac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(ntiles, C);
