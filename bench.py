@@ -408,12 +408,13 @@ def main():
     # ---- roofline of the dominant kernel -----------------------------------
     # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) measured by
     # ncu --set full on cases larger than L2 with the same per-unit work, scaled
-    # by the units one launch here processes: the warp-FFT F stage moved 4,407 B
-    # per input-segment (512 inputs x 512 segments, N = 2048); the tensor-core
-    # X stage moved 9.63 MB per channel (512 inputs x 4096 segments x 256
-    # channels).  None where no capture of that kernel exists.
-    F_TRAFFIC_PER_SEGMENT = 4407.0 if N_run == 2048 else None
-    X_TRAFFIC_PER_CHANNEL = 9.63e6 * K_run / 4096.0
+    # by the units one launch here processes: the warp-FFT F stage moved 4,375 B
+    # per input-segment (512 inputs x 512 segments, N = 2048, k-blocked FP16
+    # spectra); the tensor-core X stage read 2,049 B per (channel, segment) and
+    # wrote 1.02 MB of visibilities per channel (512 inputs x 1024 segments x
+    # 1024 channels).  None where no capture of that kernel exists.
+    F_TRAFFIC_PER_SEGMENT = 4375.0 if N_run == 2048 else None
+    X_TRAFFIC_PER_CHANNEL = 2049.0 * K_run + 1.0175e6
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
     f_bytes = S * K_run * (N_run // 4 + C_run * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
