@@ -650,6 +650,10 @@ int cs_delay_state(const double* poly, int S, int N, int K, double fs_hz, double
 bool cs_fstage_kblocked(const CsFStageArgs& a)
 {
     const int kp = a.kp ? a.kp : a.K;
+    if (cs_fstage_tc_supported(a)) {             // the opt-in tensor-core F stage writes the planes
+        const char* e = getenv("CELLSPE_FSTAGE_TC");
+        if (e && e[0] == '1') return false;
+    }
     return a.format == CS_SPECTRA_F16 && a.N == 2048 && !a.msb_first && !a.seg_major && a.K % 32 == 0 &&
            kp % 32 == 0;
 }
