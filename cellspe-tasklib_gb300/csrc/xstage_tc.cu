@@ -4,13 +4,15 @@
 // of the S x K spectra matrix X = Xr + i Xi (the conjugate MAC of
 // genericAddProduct_32fc_conj, architecture.h:427-433, for every product):
 //     Re V = Xr Xr^T + Xi Xi^T,      Im V = Xi Xr^T - Xr Xi^T.
-// A CTA owns one 128 (i) x 256 (j) tile of one channel that touches the lower
+// A CTA owns one 128 (i) x 128 (j) tile of one channel that touches the lower
 // triangle.  Its two FP32 accumulators live in tensor memory (TMEM): columns
-// 0..255 hold Re V, 256..511 hold Im V, lane = row i.  Each k-step issues four
-// kind::f16 MMAs (M=128, N=256, K=16); the minus sign of the last product is
-// the instruction descriptor's negate-A bit, so no negated copy of the data
+// 0..127 hold Re V, 128..255 hold Im V, lane = row i, so two CTAs share an
+// SM's TMEM and one's epilogue overlaps the other's MMAs.  Each k-step issues
+// four kind::f16 MMAs (M=128, N=128, K=16); the minus sign of the last product
+// is the instruction descriptor's negate-A bit, so no negated copy of the data
 // exists.  Operands are K-major (time innermost), loaded by TMA with 64-byte
-// swizzle into a 4-stage shared-memory ring guarded by mbarriers.
+// swizzle into a 3-stage shared-memory ring (32 KB stages) guarded by
+// mbarriers.
 //
 // Warp roles (6 warps): warp 0 = TMA producer, warp 1 = TMEM owner and MMA
 // issuer, warps 2..5 = epilogue (TMEM -> registers -> global; warp w reads
@@ -18,7 +20,8 @@
 // kernel records an error code, drains its own copies (bounded), frees TMEM
 // and returns, and the host reports the failure.
 //
-// Layout in:  __half spectra[C][2][S][K]  (plane 0 = Re, plane 1 = Im)
+// Layout in:  __half spectra[C][2][S][K]  (plane 0 = Re, plane 1 = Im), or
+//             k-blocked [C][S][K/32][2][32] (4-D tensor map)
 // Layout out: float2 vis[C][P], p = i(i+1)/2 + j, j <= i
 #include <cuda.h>
 
@@ -31,13 +34,13 @@
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 32;          // tile and k-chunk (64 B of FP16 = one swizzle row)
-constexpr int STAGES = 4;
+constexpr int BM = 128, BN = 128, BK = 32;          // tile and k-chunk (64 B of FP16 = one swizzle row)
+constexpr int STAGES = 3;
 constexpr int A_BYTES = BM * BK * 2;                // 8 KB
-constexpr int B_BYTES = BN * BK * 2;                // 16 KB
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // Ar, Ai, Br, Bi = 48 KB
+constexpr int B_BYTES = BN * BK * 2;                // 8 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // Ar, Ai, Br, Bi = 32 KB
 constexpr int TC_THREADS = 192;
-constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t TMEM_COLS = 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;     // ~2 s at 2 GHz
 
 // error codes written to g_tc_error
