@@ -95,17 +95,20 @@ CS_DEV float lut_pick4(const float (&l)[4], unsigned c)
     return (c & 2u) ? hi : lo;
 }
 
-// Samples s and s+1 (s even) from a plane word; blanked samples (their bit
-// in the validity mask clear) are 0.0, as mark5access decodes them.
-CS_DEV float2 sample_pair(const float (&lut)[4], uint32_t w, int f, const uint32_t* __restrict__ vmask, int64_t s)
+// Samples s and s+1 (s even) of a plane word through a 16-entry table of
+// level pairs (one shared-memory read instead of two 4-way selects); blanked
+// samples (their bit in the validity mask clear) are 0.0, as mark5access
+// decodes them.
+CS_DEV float2 sample_pair16(const float2* __restrict__ lut16, uint32_t w, int f, const uint32_t* __restrict__ vmask,
+                            int64_t s)
 {
-    float x0 = lut_pick4(lut, (w >> (2 * f)) & 3u), x1 = lut_pick4(lut, (w >> (2 * f + 2)) & 3u);
+    float2 x = lut16[(w >> (2 * f)) & 15u];
     if (vmask) {
         const uint32_t m = __ldg(vmask + (s >> 5)) >> (s & 31);
-        x0 = (m & 1u) ? x0 : 0.f;
-        x1 = (m & 2u) ? x1 : 0.f;
+        x.x = (m & 1u) ? x.x : 0.f;
+        x.y = (m & 2u) ? x.y : 0.f;
     }
-    return make_float2(x0, x1);
+    return x;
 }
 
 template <int MC, int P>
@@ -133,6 +136,8 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
     const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
     const uint32_t* vmask = a.valid_mask;
 
+    __shared__ float2 lut16[16];                     // level pairs: entry bits = code0 + 4 code1
+    if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(lut[threadIdx.x & 3], lut[threadIdx.x >> 2]);
     for (int i = threadIdx.x; i < GROUPS * NACC; i += C::NT) acc_all[i] = 0.f;
     __syncthreads();
 
@@ -155,15 +160,15 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
             if constexpr (P == 1) {
                 uint32_t w = __ldg(wsrc + (2 * n >> 4));
                 int f = (2 * n) & 15;
-                const float2 x = sample_pair(lut, w, f, vmask, start + 2 * n);
+                const float2 x = sample_pair16(lut16, w, f, vmask, start + 2 * n);
                 const float2 wn = __ldg(win2 + n);
                 v[r] = make_float2(x.x * wn.x, x.y * wn.y);
             } else {
                 const int n2 = n + MC;
                 uint32_t w1 = __ldg(wsrc + (2 * n >> 4)), w2 = __ldg(wsrc + (2 * n2 >> 4));
                 int f1 = (2 * n) & 15, f2 = (2 * n2) & 15;
-                const float2 x1 = sample_pair(lut, w1, f1, vmask, start + 2 * n);
-                const float2 x2 = sample_pair(lut, w2, f2, vmask, start + 2 * n2);
+                const float2 x1 = sample_pair16(lut16, w1, f1, vmask, start + 2 * n);
+                const float2 x2 = sample_pair16(lut16, w2, f2, vmask, start + 2 * n2);
                 // cosine^2: w(i + N/2) = sin^2 = 1 - w(i), so one table read
                 // serves both halves (the table pair differs by <= 2^-24)
                 const float2 wa = __ldg(win2 + n);
