@@ -90,6 +90,10 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
     const bool msb = a.msb_first != 0;
     const float lut[4] = {a.lut[0], a.lut[1], a.lut[2], a.lut[3]};
     constexpr bool DIRECT = (G == 1);
+    // LSB-first input: a sample pair's 4 bits index a table of level pairs
+    __shared__ float2 lut16[16];
+    if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(lut[threadIdx.x & 3], lut[threadIdx.x >> 2]);
+    __syncthreads();
 
     // every group runs the same number of rounds (barriers stay uniform);
     // segments past K are computed on zeros and not stored
@@ -100,19 +104,27 @@ __global__ void __launch_bounds__(FCfg<M>::NT) k_fx_fstage(const __grid_constant
         int64_t start = a.start_sample + (int64_t)(valid ? k : 0) * N + (a.shift ? a.shift[sk] : 0);
         int64_t w0 = start >> 4;                   // floor for negative starts too
         int off = (int)(start & 15);
-        for (int i = t; i < M / 8 + 1; i += T) {
+        for (int i = t; i < Cfg::RAWW; i += T) {
             int64_t wi = w0 + i;
             rb[i] = (valid && wi >= 0 && wi < words) ? __ldg(src_in + wi) : 0u;
         }
         bar();
         float2 v[16];
+        if (!msb) {
 #pragma unroll
-        for (int r = 0; r < 16; r++) {
-            int n0 = off + 2 * (t + r * T);
-            int n1 = n0 + 1;
-            unsigned c0 = code2(rb[n0 >> 4], n0 & 15, msb);
-            unsigned c1 = code2(rb[n1 >> 4], n1 & 15, msb);
-            v[r] = make_float2(lut_pick(lut, c0), lut_pick(lut, c1));
+            for (int r = 0; r < 16; r++) {
+                const int n0 = off + 2 * (t + r * T);         // the pair may straddle two words
+                v[r] = lut16[__funnelshift_r(rb[n0 >> 4], rb[(n0 >> 4) + 1], 2 * (n0 & 15)) & 15u];
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                int n0 = off + 2 * (t + r * T);
+                int n1 = n0 + 1;
+                unsigned c0 = code2(rb[n0 >> 4], n0 & 15, msb);
+                unsigned c1 = code2(rb[n1 >> 4], n1 & 15, msb);
+                v[r] = make_float2(lut_pick(lut, c0), lut_pick(lut, c1));
+            }
         }
         CtaFft<M, (M >= 2048)>::run(fb, t, v, tw, 2, bar);
 
