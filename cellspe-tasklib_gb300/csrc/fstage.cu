@@ -554,59 +554,48 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
 // two rounds of 8 segments per CTA (the second round's raw words prefetched
 // during the first); 4 = 16 warps and 16 segments per CTA, so that each
 // output row gets a 32-byte run; 5 = 8 warps, 32 segments per CTA (64-byte
-// runs); 4 and 5 are FP16 only.  Picked once per process by
-// timing all on a 128-input x 1024-segment job of zero samples (the FFT's
-// arithmetic does not depend on the values; the spectra, 0.57 GB, exceed the
-// L2 cache and use the padded row pitch of the FX path), fastest of four
-// timed launches each after one warm-up, unless the environment variable
-// CELLSPE_FSTAGE_VARIANT forces one.
-int g_w2048_choice[2][2] = {{0, 0}, {0, 0}};
+// runs, 128 in the k-blocked layout); 4 and 5 are FP16 only.
+// The choice is timed on the caller's own job: every schedule computes the
+// same values, so each is launched on the job's arguments (one warm-up and
+// one timed launch) and the fastest kept; the job's own launch follows.
+// Small jobs do not rank the schedules the way large ones do (on 128 inputs
+// x 1024 segments schedules 2 and 5 are within 2 %, on 512 x 4096 they are
+// 5 % apart), so a job with more than four times the segments of the one
+// that was timed times them again.  Not while the stream is being captured
+// (the timing synchronises); the environment variable CELLSPE_FSTAGE_VARIANT
+// forces one.
+struct W2048Choice {
+    int variant = 0;
+    int64_t work = 0;            // input-segments of the job it was timed on
+};
+W2048Choice g_w2048_choice[2][2];
 std::mutex g_w2048_mu;
 
 template <int FMT, bool PHASE>
-int tune_w2048(const float2* tw, cudaStream_t st)
+int tune_w2048(const CsFStageArgs& a, const float2* tw, cudaStream_t st)
 {
-    const char* env = getenv("CELLSPE_FSTAGE_VARIANT");
-    if (env && env[0] >= '1' && env[0] <= '0' + W_NVARIANTS) return env[0] - '0';
-    const int S = 128, K = 1024, KP = K + 64;
-    const size_t raw_bytes = (size_t)S * K * 2048 / 4;
-    const size_t out_bytes = (size_t)S * KP * 1024 * (FMT == CS_SPECTRA_F32 ? 8 : 4);
-    const size_t ph_bytes = PHASE ? (size_t)S * K * 4 : 0;
-    char* buf = nullptr;
-    if (cudaMalloc(&buf, raw_bytes + out_bytes + 2 * ph_bytes) != cudaSuccess) return 1;
-    cudaMemsetAsync(buf, 0, raw_bytes + out_bytes + 2 * ph_bytes, st);
-    CsFStageArgs a{};
-    a.raw = (const uint8_t*)buf;
-    a.bytes_per_input = raw_bytes / S;
-    a.S = S; a.N = 2048; a.K = K; a.kp = KP;
-    a.phase0 = PHASE ? (const float*)(buf + raw_bytes + out_bytes) : nullptr;
-    a.dphase = PHASE ? (const float*)(buf + raw_bytes + out_bytes + ph_bytes) : nullptr;
-    a.lut[0] = -3.f; a.lut[1] = -1.f; a.lut[2] = 1.f; a.lut[3] = 3.f;
-    a.format = FMT;
-    a.kblock = cs_fstage_kblocked(a) ? 1 : 0;    // FP16: the layout the FX path writes
-    a.out = buf + raw_bytes;
     cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    if (cudaEventCreate(&e0) != cudaSuccess) return 5;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return 5;
+    }
     float best = 1e30f;
-    int choice = 1;
+    int choice = 5;
     for (int v = 1; v <= W_NVARIANTS; v++) {
-        float fastest = 1e30f;
-        for (int rep = 0; rep < 5; rep++) {
+        if (FMT == CS_SPECTRA_F32 && v >= 4) break;        // 4 and 5 fall back to 1 for FP32
+        float ms = 1e30f;
+        if (launch_w2048_choice<FMT, PHASE>(v, a, tw, st) == 0) {
             cudaEventRecord(e0, st);
-            int rc = launch_w2048_choice<FMT, PHASE>(v, a, tw, st);
+            const int rc = launch_w2048_choice<FMT, PHASE>(v, a, tw, st);
             cudaEventRecord(e1, st);
-            cudaEventSynchronize(e1);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (rc) ms = 1e30f;
-            if (rep > 0) fastest = fminf(fastest, ms);
+            if (cudaEventSynchronize(e1) == cudaSuccess && rc == 0) cudaEventElapsedTime(&ms, e0, e1);
         }
-        if (fastest < best) { best = fastest; choice = v; }
+        cudaGetLastError();
+        if (ms < best) { best = ms; choice = v; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(buf);
     return choice;
 }
 
@@ -615,12 +604,28 @@ int launch_w2048(const CsFStageArgs& a, cudaStream_t st)
 {
     const float2* tw = cs_twiddles(2048);
     if (!tw) return CS_ERR_ARG;
-    int& choice = g_w2048_choice[FMT == CS_SPECTRA_F16][PHASE ? 1 : 0];
-    if (!choice) {
+    const char* env = getenv("CELLSPE_FSTAGE_VARIANT");
+    if (env && env[0] >= '1' && env[0] <= '0' + W_NVARIANTS)
+        return launch_w2048_choice<FMT, PHASE>(env[0] - '0', a, tw, st);
+    W2048Choice& c = g_w2048_choice[FMT == CS_SPECTRA_F16][PHASE ? 1 : 0];
+    const int64_t work = (int64_t)a.S * a.K;
+    int variant;
+    {
         std::lock_guard<std::mutex> lk(g_w2048_mu);
-        if (!choice) choice = tune_w2048<FMT, PHASE>(tw, st);
+        if (!c.variant || work > 4 * c.work) {
+            cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+                c.variant = tune_w2048<FMT, PHASE>(a, tw, st);
+                c.work = work;
+            } else if (!c.variant) {
+                cudaGetLastError();
+                variant = FMT == CS_SPECTRA_F16 ? 5 : 1;      // untimed default while capturing
+                return launch_w2048_choice<FMT, PHASE>(variant, a, tw, st);
+            }
+        }
+        variant = c.variant;
     }
-    return launch_w2048_choice<FMT, PHASE>(choice, a, tw, st);
+    return launch_w2048_choice<FMT, PHASE>(variant, a, tw, st);
 }
 
 // FP64 delay model (kept in FP64 on the GPU: the fringe phase 2 pi f_LO tau
