@@ -557,31 +557,39 @@ int launch_w2048_choice(int choice, const CsFStageArgs& a, const float2* tw, cud
 // runs, 128 in the k-blocked layout); 4 and 5 are FP16 only.
 // The choice is timed on the caller's own job: every schedule computes the
 // same values, so each is launched on the job's arguments (one warm-up and
-// one timed launch) and the fastest kept; the job's own launch follows.
-// Small jobs do not rank the schedules the way large ones do (on 128 inputs
-// x 1024 segments schedules 2 and 5 are within 2 %, on 512 x 4096 they are
-// 5 % apart), so a job with more than four times the segments of the one
-// that was timed times them again.  Not while the stream is being captured
-// (the timing synchronises); the environment variable CELLSPE_FSTAGE_VARIANT
-// forces one.
+// one timed launch) and the fastest kept (schedule 5 unless another is more
+// than 2 % faster); the job's own launch follows.  Small jobs do not rank the
+// schedules the way large ones do (on 128 inputs x 1024 segments schedules 2
+// and 5 are within 2 %, on 512 x 4096 they are 5 % apart), so jobs under
+// 2^16 input-segments never time, and a job with more than four times the
+// segments of the one that was timed times them again.  The timing runs
+// outside the lock: other threads keep launching the current choice
+// meanwhile.  Never while the stream is being captured (the timing
+// synchronises), nor on threads that turned timing off (the correlation
+// service's workers: timing would add ten F-stage launches to a live job's
+// latency); the environment variable CELLSPE_FSTAGE_VARIANT forces one.
 struct W2048Choice {
     int variant = 0;
     int64_t work = 0;            // input-segments of the job it was timed on
+    bool timing = false;         // a thread is timing the schedules now
 };
 W2048Choice g_w2048_choice[2][2];
 std::mutex g_w2048_mu;
+thread_local bool t_w2048_timing_allowed = true;
+constexpr int64_t W_TUNE_MIN_WORK = 1 << 16;
 
 template <int FMT, bool PHASE>
 int tune_w2048(const CsFStageArgs& a, const float2* tw, cudaStream_t st)
 {
+    const int dflt = FMT == CS_SPECTRA_F16 ? 5 : 1;
     cudaEvent_t e0, e1;
-    if (cudaEventCreate(&e0) != cudaSuccess) return 5;
+    if (cudaEventCreate(&e0) != cudaSuccess) return dflt;
     if (cudaEventCreate(&e1) != cudaSuccess) {
         cudaEventDestroy(e0);
-        return 5;
+        return dflt;
     }
     float best = 1e30f;
-    int choice = 5;
+    int choice = dflt;
     for (int v = 1; v <= W_NVARIANTS; v++) {
         if (FMT == CS_SPECTRA_F32 && v >= 4) break;        // 4 and 5 fall back to 1 for FP32
         float ms = 1e30f;
@@ -592,6 +600,7 @@ int tune_w2048(const CsFStageArgs& a, const float2* tw, cudaStream_t st)
             if (cudaEventSynchronize(e1) == cudaSuccess && rc == 0) cudaEventElapsedTime(&ms, e0, e1);
         }
         cudaGetLastError();
+        if (v == dflt) ms *= 0.98f;
         if (ms < best) { best = ms; choice = v; }
     }
     cudaEventDestroy(e0);
@@ -610,23 +619,33 @@ int launch_w2048(const CsFStageArgs& a, cudaStream_t st)
     W2048Choice& c = g_w2048_choice[FMT == CS_SPECTRA_F16][PHASE ? 1 : 0];
     const int64_t work = (int64_t)a.S * a.K;
     int variant;
+    bool time_now = false;
     {
         std::lock_guard<std::mutex> lk(g_w2048_mu);
-        if (!c.variant || work > 4 * c.work) {
+        variant = c.variant ? c.variant : (FMT == CS_SPECTRA_F16 ? 5 : 1);
+        if (t_w2048_timing_allowed && !c.timing && work >= W_TUNE_MIN_WORK && (!c.variant || work > 4 * c.work)) {
             cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-            if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
-                c.variant = tune_w2048<FMT, PHASE>(a, tw, st);
-                c.work = work;
-            } else if (!c.variant) {
+            if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+                time_now = c.timing = true;
+            else
                 cudaGetLastError();
-                variant = FMT == CS_SPECTRA_F16 ? 5 : 1;      // untimed default while capturing
-                return launch_w2048_choice<FMT, PHASE>(variant, a, tw, st);
-            }
         }
-        variant = c.variant;
+    }
+    if (time_now) {
+        variant = tune_w2048<FMT, PHASE>(a, tw, st);
+        std::lock_guard<std::mutex> lk(g_w2048_mu);
+        c.variant = variant;
+        c.work = work;
+        c.timing = false;
     }
     return launch_w2048_choice<FMT, PHASE>(variant, a, tw, st);
 }
+
+}  // namespace
+
+void cs_fstage_allow_timing(bool allow) { t_w2048_timing_allowed = allow; }
+
+namespace {
 
 // FP64 delay model (kept in FP64 on the GPU: the fringe phase 2 pi f_LO tau
 // spans ~1e7 cycles for millisecond delays at GHz sky frequencies, far beyond

@@ -67,6 +67,10 @@ struct CsFStageArgs {
     int kblock;                 // F16 only, 1: k-blocked rows, see cs_fstage_kblocked
 };
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
+// Per host thread: whether the 2048-point F stage may time its schedules on
+// this thread's jobs (default true; the correlation service's workers turn it
+// off and use the last timed schedule).
+void cs_fstage_allow_timing(bool allow);
 // True when the F stage for these arguments writes FP16 spectra k-blocked:
 // __half [C][S_out][kp/32][2][32], i.e. for each (channel, input) and block of
 // 32 segments the 32 Re halves then the 32 Im halves (128 contiguous bytes, the

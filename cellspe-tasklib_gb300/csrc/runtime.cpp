@@ -80,10 +80,18 @@ size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
 // Device workspace: a bump arena over one or more blocks.  After a job that
 // needed several blocks, reset() merges them into one, so steady-state jobs of
 // the same size allocate nothing.
+// Device scratch of one workspace: bump allocation in the newest block; a
+// request that does not fit takes a new block of at least 64 MiB, and the
+// next reset() merges the blocks into one as large as the last job needed.
+// Blocks come from the stream-ordered allocator on the workspace's stream
+// (cudaMallocAsync / cudaFreeAsync): cudaFree would wait for the whole
+// device, which in the correlation service holds one job up behind every
+// other job's kernels.
 struct Arena {
     std::vector<std::pair<char*, size_t>> blocks;
     size_t used = 0;
     size_t total_taken = 0;
+    cudaStream_t stream = nullptr;    // the stream the blocks are ordered on
     size_t capacity() const
     {
         size_t c = 0;
@@ -97,7 +105,7 @@ struct Arena {
         if (blocks.empty() || used + n > blocks.back().second) {
             char* p = nullptr;
             size_t sz = std::max(n, (size_t)64 << 20);
-            cudaError_t e = cudaMalloc(&p, sz);
+            cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), sz, stream);
             if (e != cudaSuccess) {
                 *err = e;
                 return nullptr;
@@ -109,22 +117,29 @@ struct Arena {
         used += n;
         return r;
     }
-    // stream must be idle
+    // the blocks' last users have finished (stream synchronised)
     void reset()
     {
         if (blocks.size() > 1) {
             size_t want = std::max(total_taken, capacity());
-            for (auto& b : blocks) cudaFree(b.first);
+            for (auto& b : blocks) cudaFreeAsync(b.first, stream);
             blocks.clear();
             char* p = nullptr;
-            if (cudaMalloc(&p, want) == cudaSuccess) blocks.push_back({p, want});
+            if (cudaMallocAsync(reinterpret_cast<void**>(&p), want, stream) == cudaSuccess) blocks.push_back({p, want});
+            else cudaGetLastError();
         }
+        rewind();
+    }
+    // start the next job in the same blocks (no allocator calls: safe while
+    // a CUDA graph is being captured)
+    void rewind()
+    {
         used = 0;
         total_taken = 0;
     }
     void release()
     {
-        for (auto& b : blocks) cudaFree(b.first);
+        for (auto& b : blocks) cudaFreeAsync(b.first, stream);
         blocks.clear();
         used = total_taken = 0;
     }
@@ -177,7 +192,9 @@ struct Workspace {
     void destroy()
     {
         if (stream) cudaStreamSynchronize(stream);
+        arena.stream = stream;
         arena.release();
+        if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (ev_legacy) cudaEventDestroy(ev_legacy);
@@ -226,7 +243,11 @@ struct Job {
     Workspace& ws;
     bool host;
     int err = 0;
-    Job(Workspace& w, bool h) : ws(w), host(h) { ws.outs.clear(); }
+    Job(Workspace& w, bool h) : ws(w), host(h)
+    {
+        ws.outs.clear();
+        ws.arena.stream = ws.stream;        // scratch is ordered on the stream the job runs on
+    }
     void* scratch(size_t bytes)
     {
         cudaError_t e = cudaSuccess;
@@ -1193,6 +1214,7 @@ struct SvcJob {
     cudaEvent_t ready = nullptr;      // device buffers complete (legacy stream at submit)
     std::chrono::steady_clock::time_point t_submit, t_start, t_done;
     int status = 0;
+    std::string error;                // the worker's message when status != 0
     bool done = false;
 };
 
@@ -1206,6 +1228,7 @@ struct cellspe_service {
     std::vector<std::thread> workers;
     std::vector<double> latency_ms, queue_ms;
     long long budget = 0, in_flight = 0, next_id = 1, completed = 0, failed = 0;
+    long long priority_samples = 0;   // smaller jobs run on a high-priority stream (<= 0: none)
     int running = 0, max_running = 0;
     bool stop = false;
 };
@@ -1216,6 +1239,17 @@ void service_worker(cellspe_service* sv)
 {
     Workspace ws;
     int init = ws.init();
+    cs_fstage_allow_timing(false);       // no schedule timing inside a live job
+    // small jobs go to a stream of the greatest priority: the block scheduler
+    // then dispatches their thread blocks before the waiting blocks of large
+    // jobs' kernels, instead of after the whole grid
+    cudaStream_t lo = ws.stream, hi = nullptr;
+    int least = 0, greatest = 0;
+    if (!init && sv->priority_samples > 0 && cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
+        greatest < least && cudaStreamCreateWithPriority(&hi, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+        hi = nullptr;
+        cudaGetLastError();
+    }
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
         // admit the oldest job as soon as its device footprint fits next to the
@@ -1237,11 +1271,14 @@ void service_worker(cellspe_service* sv)
         sv->cv_work.notify_all();
         j->t_start = std::chrono::steady_clock::now();
         int rc = init;
+        const long long samples = (long long)j->p.n_inputs * j->p.fft_points * j->p.n_segments;
+        ws.stream = (hi && samples < sv->priority_samples) ? hi : lo;
         if (!rc && j->ready) {
             cudaError_t e = cudaStreamWaitEvent(ws.stream, j->ready, 0);
             if (e != cudaSuccess) rc = cuda_fail(e, "service job ordering");
         }
         if (!rc) rc = op_fx(ws, &j->p, j->raw, j->poly, j->vis, true);
+        ws.stream = lo;
         if (j->ready) {
             cudaEventDestroy(j->ready);
             j->ready = nullptr;
@@ -1251,6 +1288,7 @@ void service_worker(cellspe_service* sv)
         sv->in_flight -= j->footprint;
         sv->running--;
         j->status = rc;
+        if (rc) j->error = t_err;
         j->done = true;
         if (rc) sv->failed++;
         else {
@@ -1262,6 +1300,7 @@ void service_worker(cellspe_service* sv)
         sv->cv_work.notify_all();
     }
     lk.unlock();
+    if (hi) cudaStreamSynchronize(hi), cudaStreamDestroy(hi);
     ws.destroy();
 }
 
@@ -2069,8 +2108,7 @@ int cellspe_fx_correlate_async(const cellspe_fx_params* p, const void* raw, cons
     if (!p || p->memory != CELLSPE_MEM_DEVICE) return set_err(CELLSPE_ERR_ARG, "fx async: device memory only");
     cudaStream_t saved = ws->stream;
     ws->stream = (cudaStream_t)stream;
-    ws->arena.used = 0;
-    ws->arena.total_taken = 0;
+    ws->arena.rewind();
     int rc = op_fx(*ws, p, raw, delay_poly, vis, false);
     ws->stream = saved;
     return rc;
@@ -2096,6 +2134,7 @@ cellspe_service* cellspe_service_create(const cellspe_service_config* cfg)
     long long b = (cfg && cfg->hbm_budget_bytes > 0) ? cfg->hbm_budget_bytes : (long long)(0.8 * (double)budget_bytes() / 0.9);
     sv->budget = b;
     int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 8;
+    sv->priority_samples = !cfg || cfg->priority_samples == 0 ? (1LL << 24) : cfg->priority_samples;
     for (int i = 0; i < n; i++) sv->workers.emplace_back(service_worker, sv);
     return sv;
 }
@@ -2144,7 +2183,8 @@ int cellspe_service_wait(cellspe_service* sv, long long job_id, double* latency_
     sv->cv_done.wait(lk, [&] { return j->done; });
     sv->jobs.erase(job_id);
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count();
-    return j->status;
+    if (j->status) return set_err(j->status, "service job " + std::to_string(job_id) + ": " + j->error);
+    return 0;
 }
 
 int cellspe_service_get_stats(cellspe_service* sv, cellspe_service_stats* out)

@@ -145,11 +145,17 @@ int cellspe_release_workspace(void);
  * hbm_budget_bytes, so jobs that arrive while others run are admitted as
  * memory frees and their work overlaps on the GPU.  Results are identical to
  * cellspe_fx_correlate on the same job (same kernels, deterministic order).
+ * Jobs of fewer than priority_samples samples (inputs x points x segments)
+ * run on a high-priority stream, so the GPU schedules their thread blocks
+ * ahead of the waiting blocks of larger jobs' kernels.  Workers use the F-stage
+ * schedule that a direct call has timed (they time none themselves).
  * Buffers must stay valid until cellspe_service_wait returns for the job. */
 typedef struct cellspe_service cellspe_service;
 typedef struct {
     long long hbm_budget_bytes;   /* 0: 80% of free device memory            */
     int       max_streams;        /* concurrent jobs (0: 8)                    */
+    int       reserved;
+    long long priority_samples;   /* 0: 2^24; < 0: one priority for all jobs */
 } cellspe_service_config;
 typedef struct {
     long long completed, failed, queued;

@@ -37,10 +37,11 @@ def test_task_descriptor_layout_matches_header(tmp_path):
 #include <stddef.h>
 #include "cellspe_gpu.h"
 int main(void){
- printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(CellDSPTask_t), offsetof(CellDSPTask_t, completed_flag),
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(CellDSPTask_t), offsetof(CellDSPTask_t, completed_flag),
    offsetof(CellDSPTask_t, inputvector_ptrs), offsetof(CellDSPTask_t, outputvector_ptrs),
    offsetof(CellDSPTask_t, subcontext), offsetof(CellDSPTask_t, next_task), sizeof(cellspe_fx_params),
-   sizeof(cellspe_spec_params));
+   sizeof(cellspe_spec_params), sizeof(cellspe_service_config), offsetof(cellspe_service_config, priority_samples),
+   sizeof(cellspe_service_stats), sizeof(cellspe_vdif_info));
  return 0; }''')
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
@@ -48,7 +49,9 @@ int main(void){
     T = cellspe_gpu.CellDSPTask
     assert vals == [ctypes.sizeof(T), T.completed_flag.offset, T.inputvector_ptrs.offset,
                     T.outputvector_ptrs.offset, T.subcontext.offset, T.next_task.offset,
-                    ctypes.sizeof(cellspe_gpu.FxParams), ctypes.sizeof(cellspe_gpu.SpecParams)]
+                    ctypes.sizeof(cellspe_gpu.FxParams), ctypes.sizeof(cellspe_gpu.SpecParams),
+                    ctypes.sizeof(cellspe_gpu.ServiceConfig), cellspe_gpu.ServiceConfig.priority_samples.offset,
+                    ctypes.sizeof(cellspe_gpu.ServiceStats), ctypes.sizeof(cellspe_gpu.VdifInfo)]
     assert vals[0] == 256 and vals[5] == 240
 
 

@@ -181,3 +181,28 @@ def test_direct_call_waits_for_prior_default_stream_work(cg):
         vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
         cg.fx_correlate(p, raw, vis)
         assert torch.equal(vis, want)
+
+
+@pytest.mark.parametrize("mode", ["tc", "fp32"])
+@pytest.mark.parametrize("K", [160, 104])
+def test_fx_w2048_schedules_identical(cg, mode, K, monkeypatch):
+    """The 2048-point F stage's CTA schedules, between which the autotuner
+    picks by time alone, compute the same values: every forced schedule gives
+    bit-identical visibilities (K = 160: whole 32-segment tiles; K = 104: a
+    partial last tile and the planar layout)."""
+    import torch
+
+    import synth
+
+    S, N = 16, 2048
+    x_mode = cg.X_TC_FP16 if mode == "tc" else cg.X_FP32
+    raw = synth.device_stations(S, N * K, 0.2, seed=17)
+    P, C = S * (S + 1) // 2, N // 2
+    outs = []
+    for v in "12345":
+        monkeypatch.setenv("CELLSPE_FSTAGE_VARIANT", v)
+        vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
+        cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=x_mode), raw, vis)
+        outs.append(vis)
+    for o in outs[1:]:
+        assert torch.equal(o, outs[0])

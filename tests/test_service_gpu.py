@@ -25,14 +25,18 @@ def _jobs():
     return jobs
 
 
-def test_service_mix_equals_solo(cg):
+@pytest.mark.parametrize("priority_samples", [0, -1, 1 << 17], ids=["default", "one-priority", "split"])
+def test_service_mix_equals_solo(cg, priority_samples):
+    """Identical results whichever stream priority a job runs at (default: all
+    these jobs are small; split: one on the high-priority stream, the rest not;
+    one-priority: no high-priority stream)."""
     jobs = _jobs()
     solo = []
     for S, N, K, mode, raw in jobs:
         vis = np.zeros((N // 2, S * (S + 1) // 2), np.complex64)
         cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=mode), raw, vis)
         solo.append(vis)
-    svc = cg.Service(max_streams=4)
+    svc = cg.Service(max_streams=4, priority_samples=priority_samples)
     try:
         outs, ids = [], []
         for S, N, K, mode, raw in jobs:
