@@ -92,7 +92,7 @@ class SpecParams(ctypes.Structure):
 
 class ServiceConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_streams", ctypes.c_int), ("reserved", ctypes.c_int),
-                ("priority_samples", ctypes.c_longlong)]
+                ("priority_samples", ctypes.c_longlong), ("large_samples", ctypes.c_longlong)]
 
 
 class ServiceStats(ctypes.Structure):
@@ -394,8 +394,9 @@ def spectrometer_noalloc(params: SpecParams, raw, power, pcal_bins=None, pcal_to
 class Service:
     """cellspe_service_*: continuous-batching correlation service."""
 
-    def __init__(self, hbm_budget_bytes: int = 0, max_streams: int = 8, priority_samples: int = 0):
-        cfg = ServiceConfig(hbm_budget_bytes, max_streams, 0, priority_samples)
+    def __init__(self, hbm_budget_bytes: int = 0, max_streams: int = 8, priority_samples: int = 0,
+                 large_samples: int = 0):
+        cfg = ServiceConfig(hbm_budget_bytes, max_streams, 0, priority_samples, large_samples)
         self._h = lib().cellspe_service_create(ctypes.byref(cfg))
         if not self._h:
             raise CellspeError(ERR_CUDA, last_error())

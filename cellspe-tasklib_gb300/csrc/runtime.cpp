@@ -1214,6 +1214,7 @@ struct SvcJob {
     cudaEvent_t ready = nullptr;      // device buffers complete (legacy stream at submit)
     std::chrono::steady_clock::time_point t_submit, t_start, t_done;
     int status = 0;
+    bool large = false;               // runs while no other large job does
     std::string error;                // the worker's message when status != 0
     bool done = false;
 };
@@ -1229,6 +1230,8 @@ struct cellspe_service {
     std::vector<double> latency_ms, queue_ms;
     long long budget = 0, in_flight = 0, next_id = 1, completed = 0, failed = 0;
     long long priority_samples = 0;   // smaller jobs run on a high-priority stream (<= 0: none)
+    long long large_samples = 0;      // jobs this large run one at a time (<= 0: no limit)
+    int large_running = 0;
     int running = 0, max_running = 0;
     bool stop = false;
 };
@@ -1252,18 +1255,24 @@ void service_worker(cellspe_service* sv)
     }
     std::unique_lock<std::mutex> lk(sv->mu);
     for (;;) {
-        // admit the oldest job as soon as its device footprint fits next to the
-        // jobs already running (a lone job is always admitted)
-        sv->cv_work.wait(lk, [&] {
-            if (sv->stop) return true;
-            if (sv->queue.empty()) return false;
-            const auto& h = sv->queue.front();
-            return sv->in_flight == 0 || sv->in_flight + h->footprint <= sv->budget;
-        });
-        if (sv->stop && sv->queue.empty()) break;
+        // admit the oldest job whose device footprint fits next to the jobs
+        // already running (a lone job always fits); with a large-job limit,
+        // a large job is passed over while another large job runs.
+        auto pick = [&]() -> std::deque<std::shared_ptr<SvcJob>>::iterator {
+            for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it) {
+                const SvcJob& q = **it;
+                if (q.large && sv->large_running > 0) continue;
+                if (sv->in_flight == 0 || sv->in_flight + q.footprint <= sv->budget) return it;
+                return sv->queue.end();          // memory goes to the oldest job that needs it
+            }
+            return sv->queue.end();
+        };
+        std::deque<std::shared_ptr<SvcJob>>::iterator at;
+        sv->cv_work.wait(lk, [&] { return sv->stop || (at = pick()) != sv->queue.end(); });
         if (sv->stop) break;
-        std::shared_ptr<SvcJob> j = sv->queue.front();
-        sv->queue.pop_front();
+        std::shared_ptr<SvcJob> j = *at;
+        sv->queue.erase(at);
+        if (j->large) sv->large_running++;
         sv->in_flight += j->footprint;
         sv->running++;
         sv->max_running = std::max(sv->max_running, sv->running);
@@ -1285,6 +1294,7 @@ void service_worker(cellspe_service* sv)
         }
         j->t_done = std::chrono::steady_clock::now();
         lk.lock();
+        if (j->large) sv->large_running--;
         sv->in_flight -= j->footprint;
         sv->running--;
         j->status = rc;
@@ -2135,6 +2145,7 @@ cellspe_service* cellspe_service_create(const cellspe_service_config* cfg)
     sv->budget = b;
     int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 8;
     sv->priority_samples = !cfg || cfg->priority_samples == 0 ? (1LL << 24) : cfg->priority_samples;
+    sv->large_samples = cfg ? cfg->large_samples : 0;
     for (int i = 0; i < n; i++) sv->workers.emplace_back(service_worker, sv);
     return sv;
 }
@@ -2149,6 +2160,7 @@ int cellspe_service_submit(cellspe_service* sv, const cellspe_fx_params* p, cons
     j->poly = delay_poly;
     j->vis = vis;
     j->footprint = fx_bytes(p, delay_poly != nullptr);
+    j->large = sv->large_samples > 0 && (long long)p->n_inputs * p->fft_points * p->n_segments >= sv->large_samples;
     if (j->footprint > sv->budget)
         return set_err(CELLSPE_ERR_NOMEM, "service_submit: job footprint exceeds the service HBM budget");
     j->t_submit = std::chrono::steady_clock::now();

@@ -147,8 +147,12 @@ int cellspe_release_workspace(void);
  * cellspe_fx_correlate on the same job (same kernels, deterministic order).
  * Jobs of fewer than priority_samples samples (inputs x points x segments)
  * run on a high-priority stream, so the GPU schedules their thread blocks
- * ahead of the waiting blocks of larger jobs' kernels.  Workers use the F-stage
- * schedule that a direct call has timed (they time none themselves).
+ * ahead of the waiting blocks of larger jobs' kernels.  With large_samples > 0,
+ * jobs of at least that many samples run one at a time: a queued large job
+ * waits while another large job runs, and the jobs queued behind it are
+ * admitted past it (off by default: on the serving mix it did not lower the
+ * p99 latency).  Workers use the F-stage schedule that a direct call has timed (they
+ * time none themselves).
  * Buffers must stay valid until cellspe_service_wait returns for the job. */
 typedef struct cellspe_service cellspe_service;
 typedef struct {
@@ -156,6 +160,7 @@ typedef struct {
     int       max_streams;        /* concurrent jobs (0: 8)                    */
     int       reserved;
     long long priority_samples;   /* 0: 2^24; < 0: one priority for all jobs */
+    long long large_samples;      /* <= 0: no limit (large jobs may overlap)  */
 } cellspe_service_config;
 typedef struct {
     long long completed, failed, queued;

@@ -53,6 +53,35 @@ def test_service_mix_equals_solo(cg, priority_samples):
     assert 0 < st["p50_ms"] <= st["p99_ms"] and all(x > 0 for x in lat)
 
 
+def test_service_large_jobs_one_at_a_time(cg):
+    """Jobs of at least large_samples samples never overlap each other; smaller
+    jobs are admitted past a large job that waits.  Results are unchanged."""
+    jobs = _jobs()
+    solo = []
+    for S, N, K, mode, raw in jobs:
+        vis = np.zeros((N // 2, S * (S + 1) // 2), np.complex64)
+        cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=mode), raw, vis)
+        solo.append(vis)
+    for large, max_run in ((1, 1), (1 << 19, None)):
+        svc = cg.Service(max_streams=4, large_samples=large)
+        try:
+            outs, ids = [], []
+            for S, N, K, mode, raw in jobs:
+                vis = np.full((N // 2, S * (S + 1) // 2), np.nan, np.complex64)
+                outs.append(vis)
+                ids.append(svc.submit(cg.fx_params(S, N, K, raw.shape[1], x_mode=mode), raw, vis))
+            for i in ids:
+                svc.wait(i)
+            st = svc.stats()
+        finally:
+            svc.close()
+        for a, b in zip(outs, solo):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        assert st["completed"] == len(jobs) and st["failed"] == 0
+        if max_run is not None:
+            assert st["max_running"] == max_run
+
+
 def test_service_admission_by_footprint(cg):
     import synth
 
