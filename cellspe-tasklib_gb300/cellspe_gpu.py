@@ -394,7 +394,7 @@ def spectrometer_noalloc(params: SpecParams, raw, power, pcal_bins=None, pcal_to
 class Service:
     """cellspe_service_*: continuous-batching correlation service."""
 
-    def __init__(self, hbm_budget_bytes: int = 0, max_streams: int = 8, priority_samples: int = 0,
+    def __init__(self, hbm_budget_bytes: int = 0, max_streams: int = 0, priority_samples: int = 0,
                  large_samples: int = 0):
         cfg = ServiceConfig(hbm_budget_bytes, max_streams, 0, priority_samples, large_samples)
         self._h = lib().cellspe_service_create(ctypes.byref(cfg))

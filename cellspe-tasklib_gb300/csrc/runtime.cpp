@@ -2143,7 +2143,7 @@ cellspe_service* cellspe_service_create(const cellspe_service_config* cfg)
     auto* sv = new cellspe_service();
     long long b = (cfg && cfg->hbm_budget_bytes > 0) ? cfg->hbm_budget_bytes : (long long)(0.8 * (double)budget_bytes() / 0.9);
     sv->budget = b;
-    int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 8;
+    int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 2;
     sv->priority_samples = !cfg || cfg->priority_samples == 0 ? (1LL << 24) : cfg->priority_samples;
     sv->large_samples = cfg ? cfg->large_samples : 0;
     for (int i = 0; i < n; i++) sv->workers.emplace_back(service_worker, sv);

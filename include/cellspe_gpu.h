@@ -151,13 +151,15 @@ int cellspe_release_workspace(void);
  * jobs of at least that many samples run one at a time: a queued large job
  * waits while another large job runs, and the jobs queued behind it are
  * admitted past it (off by default: on the serving mix it did not lower the
- * p99 latency).  Workers use the F-stage schedule that a direct call has timed (they
+ * p99 latency).  Each large kernel fills the GPU on its own, so jobs that run
+ * side by side all finish late: two streams keep the p99 latency near the
+ * largest job's own run time while small jobs pass large ones.  Workers use the F-stage schedule that a direct call has timed (they
  * time none themselves).
  * Buffers must stay valid until cellspe_service_wait returns for the job. */
 typedef struct cellspe_service cellspe_service;
 typedef struct {
     long long hbm_budget_bytes;   /* 0: 80% of free device memory            */
-    int       max_streams;        /* concurrent jobs (0: 8)                    */
+    int       max_streams;        /* concurrent jobs (0: 2)                    */
     int       reserved;
     long long priority_samples;   /* 0: 2^24; < 0: one priority for all jobs */
     long long large_samples;      /* <= 0: no limit (large jobs may overlap)  */
