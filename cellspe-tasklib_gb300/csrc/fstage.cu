@@ -641,6 +641,230 @@ int launch_w2048(const CsFStageArgs& a, cudaStream_t st)
     return launch_w2048_choice<FMT, PHASE>(variant, a, tw, st);
 }
 
+
+// ---------------------------------------------------------------------------
+// N = 4096 ... 32768: M1 = M / 1024 warps per segment (M = N/2 complex points).
+// Decimation in time by M1: warp n1 transforms x_n1[m] = z[n1 + M1 m],
+// m < 1024, exactly as the 2048-point path does (lane l holds m = l + 32 j,
+// DFT-32 over j, twiddle W_1024^(l k1), padded per-warp transpose, DFT-32), so
+// lane l ends with Y_n1[l + 32 k2] in register k2.  The warps park Y_n1 in
+// shared memory (the warp's own transpose tile) and, after one CTA barrier,
+//     Z[k2 + 1024 k1] = sum_n1 W_M1^(n1 k1) (W_M^(n1 k2) Y_n1[k2]).
+// Each thread takes the mirrored columns k2 and 1024 - k2 (k2 = 1 ... 511;
+// thread 0 also columns 0 and 512): twiddled by powers of u = W_M^k2 (the
+// second column by conj(u)^n1, whose DFT comes out rotated by one since
+// W_M^(n1 (1024 - k2)) = W_M1^n1 conj(u)^n1), two M1-point DFTs, and the
+// real-FFT split pairs Z[k2 + 1024 k1] with Z[M - k2 - 1024 k1] =
+// Z[(1024 - k2) + 1024 (M1 - 1 - k1)], so the split needs no data exchange.
+// Channels then get the phasor exp(i (phase0 + c dphase)) and the optional
+// scale and are written segment-major ([S][K][C], coalesced along c) for
+// cs_spectra_transpose.  One segment per CTA; LSB-first input only.
+// ---------------------------------------------------------------------------
+constexpr int B_TILE = 32 * W_TP;               // float2 per warp: transpose tile, then Y_n1
+
+template <int M1>
+size_t wbig_smem()
+{
+    return (size_t)M1 * B_TILE * 8 + (size_t)(2048 * M1 / 64 + 2) * 16 + 16 * 8;
+}
+
+template <int M1, int FMT, bool PHASE>
+__global__ void __launch_bounds__(32 * M1) k_fx_fstage_wbig(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
+{
+    constexpr int M = 1024 * M1, N = 2 * M, NT = 32 * M1;
+    constexpr int RAWC = N / 64 + 2;             // 16-byte chunks of one segment (+ alignment slack)
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tiles = reinterpret_cast<float2*>(smem);
+    uint32_t* rw = reinterpret_cast<uint32_t*>(tiles + M1 * B_TILE);
+    float2* lut16 = reinterpret_cast<float2*>(rw + 4 * RAWC);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = blockIdx.x, s = blockIdx.y;
+    const int64_t sk = (int64_t)s * a.K + k;
+    const int64_t chunks = a.bytes_per_input >> 4;
+    const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
+
+    const int64_t start = a.start_sample + (int64_t)k * N + (a.shift ? __ldg(a.shift + sk) : 0);
+    {
+        const int64_t c0 = start >> 6;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rw);
+        for (int c = threadIdx.x; c < RAWC; c += NT) {
+            const int64_t ci = c0 + c;
+            const bool ok = ci >= 0 && ci < chunks;
+            cp_async16(dst + 16 * c, ok ? base + 16 * ci : a.raw, ok);
+        }
+        cp_async_commit();
+    }
+    if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(a.lut[threadIdx.x & 3], a.lut[threadIdx.x >> 2]);
+    // W_1024^(lane e): e < 8 by a balanced recurrence, then blocks of 8 by powers of W_1024^(8 lane)
+    float2 wp[8];
+    {
+        float sn, cs;
+        sincospif(-(float)lane / 512.0f, &sn, &cs);
+        wp[0] = make_float2(1.f, 0.f);
+        wp[1] = make_float2(cs, sn);
+#pragma unroll
+        for (int e = 2; e < 8; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], wp[1]) : cmul(wp[e / 2], wp[e / 2]);
+    }
+    const float2 w8 = cmul(wp[4], wp[4]);
+    cp_async_wait<0>();
+    __syncthreads();
+
+    // ---- warp n1: 1024-point transform of z[n1 + M1 m] ----
+    float2* tb = tiles + warp * B_TILE;
+    {
+        const int off = (int)(start & 63);
+        const int f0 = off + 2 * (warp + M1 * lane);            // sample offset of this lane's first pair
+        const int wb = f0 >> 4, sh = 2 * (f0 & 15);
+        float2 v[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {                           // pair j is 64 M1 samples = 4 M1 words further on
+            const uint32_t bits = __funnelshift_r(rw[wb + 4 * M1 * j], rw[wb + 4 * M1 * j + 1], sh);
+            v[j] = lut16[bits & 15u];
+        }
+        Dft<32>::run(v);
+        float2 q = make_float2(1.f, 0.f);
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                if (b == 0 && r == 0) continue;
+                v[8 * b + r] = cmul(v[8 * b + r], b ? cmul(q, wp[r]) : wp[r]);
+            }
+            q = b ? cmul(q, w8) : w8;
+        }
+#pragma unroll
+        for (int e = 0; e < 32; e++) tb[e * W_TP + lane] = v[e];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 32; e++) v[e] = tb[lane * W_TP + e];
+        __syncwarp();
+        Dft<32>::run(v);                                         // v[k2] = Y_n1[lane + 32 k2]
+#pragma unroll
+        for (int e = 0; e < 32; e++) tb[lane + 32 * e] = v[e];
+    }
+    __syncthreads();
+
+    // ---- mirrored column pairs: radix-M1 step, real-FFT split, phasor, write ----
+    float2 D = make_float2(1.f, 0.f);
+    float ph0 = 0.f, dph = 0.f;
+    if constexpr (PHASE) {
+        ph0 = __ldg(a.phase0 + sk);
+        dph = __ldg(a.dphase + sk);
+        float sn, cs;
+        sincosf(1024.f * dph, &sn, &cs);
+        D = make_float2(cs, sn);
+    }
+    const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
+    const int64_t obase = sk * M;
+    auto emit = [&](int c, float2 X) {
+        if (scl) X = cscale(X, __ldg(scl + c));
+        if constexpr (FMT == CS_SPECTRA_F32) reinterpret_cast<float2*>(a.out)[obase + c] = X;
+        else reinterpret_cast<__half2*>(a.out)[obase + c] = __floats2half2_rn(X.x, X.y);
+    };
+    auto phasor = [&](int c) -> float2 {
+        float sn, cs;
+        sincosf(ph0 + (float)c * dph, &sn, &cs);
+        return make_float2(cs, sn);
+    };
+    const float2 c2 = __ldg(tw + 1024);                          // W_N^1024 = W_(2 M1)
+#pragma unroll 1
+    for (int task = threadIdx.x; task < 512; task += NT) {
+        if (task == 0) {
+            // column 0 (u = 1) and column 512 (u = W_M^512), each paired with itself
+            float2 y0[M1], y5[M1];
+            const float2 u = __ldg(tw + 1024);
+            float2 p = make_float2(1.f, 0.f);
+#pragma unroll
+            for (int n1 = 0; n1 < M1; n1++) {
+                y0[n1] = tiles[n1 * B_TILE];
+                y5[n1] = cmul(tiles[n1 * B_TILE + 512], p);
+                p = cmul(p, u);
+            }
+            Dft<M1>::run(y0);
+            Dft<M1>::run(y5);
+            float2 w = make_float2(1.f, 0.f);                    // W_N^(1024 k1)
+#pragma unroll
+            for (int k1 = 0; k1 <= M1 / 2; k1++) {
+                float2 Xk, Xm;
+                r2c_pair(y0[k1], y0[(M1 - k1) % M1], w, Xk, Xm);
+                const int c = 1024 * k1;
+                if constexpr (PHASE) Xk = cmul(Xk, phasor(c)), Xm = cmul(Xm, phasor(M - c));
+                emit(c, Xk);
+                if (k1 > 0 && k1 < M1 / 2) emit(M - c, Xm);
+                w = cmul(w, c2);
+            }
+            w = __ldg(tw + 512);                                  // W_N^(512 + 1024 k1)
+#pragma unroll
+            for (int k1 = 0; k1 < M1 / 2; k1++) {
+                float2 Xk, Xm;
+                r2c_pair(y5[k1], y5[M1 - 1 - k1], w, Xk, Xm);
+                const int c = 512 + 1024 * k1;
+                if constexpr (PHASE) Xk = cmul(Xk, phasor(c)), Xm = cmul(Xm, phasor(M - c));
+                emit(c, Xk);
+                emit(M - c, Xm);
+                w = cmul(w, c2);
+            }
+            continue;
+        }
+        const int kA = task, kB = 1024 - task;
+        float2 ya[M1], yb[M1];
+        {
+            const float2 u = __ldg(tw + 2 * kA);                 // W_M^kA
+            float2 p = make_float2(1.f, 0.f);
+#pragma unroll
+            for (int n1 = 0; n1 < M1; n1++) {
+                ya[n1] = cmul(tiles[n1 * B_TILE + kA], p);
+                yb[n1] = cmul_conj(tiles[n1 * B_TILE + kB], p);
+                p = cmul(p, u);
+            }
+        }
+        Dft<M1>::run(ya);                                         // ya[k1] = Z[kA + 1024 k1]
+        Dft<M1>::run(yb);                                         // yb[(k1 + 1) % M1] = Z[kB + 1024 k1]
+        float2 w = __ldg(tw + kA);                                // W_N^(kA + 1024 k1)
+        float2 BA = make_float2(1.f, 0.f), BB = BA;
+        if constexpr (PHASE) {
+            BA = phasor(kA);                                      // channel kA + 1024 k1
+            BB = phasor(M - kA);                                  // channel M - kA - 1024 k1
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < M1; k1++) {
+            float2 Xk, Xm;
+            r2c_pair(ya[k1], yb[(M1 - k1) % M1], w, Xk, Xm);
+            const int c = kA + 1024 * k1;
+            if constexpr (PHASE) {
+                Xk = cmul(Xk, BA);
+                Xm = cmul(Xm, BB);
+                BA = cmul(BA, D);
+                BB = cmul_conj(BB, D);
+            }
+            emit(c, Xk);
+            emit(M - c, Xm);
+            w = cmul(w, c2);
+        }
+    }
+}
+
+template <int M1, int FMT, bool PHASE>
+int launch_wbig(const CsFStageArgs& a, cudaStream_t st)
+{
+    const float2* tw = cs_twiddles(2048 * M1);
+    if (!tw) return CS_ERR_ARG;
+    const size_t smem = wbig_smem<M1>();
+    auto kern = k_fx_fstage_wbig<M1, FMT, PHASE>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<dim3(a.K, a.S), 32 * M1, smem, st>>>(a, tw), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+template <int M1>
+int dispatch_wbig(const CsFStageArgs& a, cudaStream_t st)
+{
+    const bool ph = a.phase0 != nullptr;
+    if (a.format == CS_SPECTRA_F32)
+        return ph ? launch_wbig<M1, CS_SPECTRA_F32, true>(a, st) : launch_wbig<M1, CS_SPECTRA_F32, false>(a, st);
+    return ph ? launch_wbig<M1, CS_SPECTRA_F16, true>(a, st) : launch_wbig<M1, CS_SPECTRA_F16, false>(a, st);
+}
+
 }  // namespace
 
 void cs_fstage_allow_timing(bool allow) { t_w2048_timing_allowed = allow; }
@@ -712,6 +936,19 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
         if (a.format == CS_SPECTRA_F32)
             return ph ? launch_w2048<CS_SPECTRA_F32, true>(a, st) : launch_w2048<CS_SPECTRA_F32, false>(a, st);
         return ph ? launch_w2048<CS_SPECTRA_F16, true>(a, st) : launch_w2048<CS_SPECTRA_F16, false>(a, st);
+    }
+    // N = 4096 ... 32768, segment-major: the warp four-step (CELLSPE_FSTAGE_GENERIC=1
+    // selects the CTA-wide Stockham FFT instead)
+    if (a.seg_major && !a.msb_first && a.N >= 4096 && a.N <= 32768) {
+        const char* e = getenv("CELLSPE_FSTAGE_GENERIC");
+        if (!(e && e[0] == '1')) {
+            switch (a.N) {
+                case 4096: return dispatch_wbig<2>(a, st);
+                case 8192: return dispatch_wbig<4>(a, st);
+                case 16384: return dispatch_wbig<8>(a, st);
+                default: return dispatch_wbig<16>(a, st);
+            }
+        }
     }
     switch (a.N) {
         case 512: return dispatch_fstage<256>(a, st);

@@ -206,3 +206,43 @@ def test_fx_w2048_schedules_identical(cg, mode, K, monkeypatch):
         outs.append(vis)
     for o in outs[1:]:
         assert torch.equal(o, outs[0])
+
+
+@pytest.mark.parametrize("N,K", [(4096, 24), (8192, 16), (16384, 8), (32768, 8)])
+def test_fx_long_transforms_delay_model(cg, orc, N, K, monkeypatch):
+    """N = 4096 ... 32768 (the warp four-step F stage: N/2048 warps per segment,
+    each a 1024-point transform of every (N/2048)-th point, then radix-N/2048
+    columns and the real-FFT split in registers): FP32 path against the oracle's
+    FP32 path with the same delay model, and against the CTA-wide Stockham F
+    stage; the tensor-core path (K a multiple of 8) against the same job through
+    the Stockham F stage."""
+    import synth
+
+    S = 3
+    fs, lo = 32e6, 8.4e9
+    margin = 4096
+    raw = synth.stations_offset_binary(S, N * K + 2 * margin, rho=0.3, seed=N + 7)
+    rng = np.random.default_rng(N)
+    poly = np.zeros((S, 4))
+    poly[:, 0] = rng.uniform(-40e-6, 40e-6, S)
+    poly[:, 1] = rng.uniform(-3e-6, 3e-6, S)
+    kw = dict(vis_order=cg.VIS_BASELINE_MAJOR, start_sample=margin, fs_hz=fs, lo_hz=lo)
+    P = S * (S + 1) // 2
+    vis = np.zeros((P, N // 2), np.complex64)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], **kw), raw, vis, delay_poly=poly)
+    shift, ph0, dph = orc.delay_state_f64(poly, N, K, fs, lo)
+    c = np.arange(N // 2)
+    phasor = np.exp(1j * (ph0.astype(np.float32)[:, :, None].astype(np.float64) +
+                          c[None, None, :] * dph.astype(np.float32)[:, :, None].astype(np.float64))).astype(np.complex64)
+    ref = orc.fx_fp32(raw, S, N, K, start_sample=margin, shift=shift, phasor=phasor)
+    assert _rel(vis, ref) < TOL
+    tc = np.zeros_like(vis)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, **kw), raw, tc, delay_poly=poly)
+    monkeypatch.setenv("CELLSPE_FSTAGE_GENERIC", "1")
+    gen = np.zeros_like(vis)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], **kw), raw, gen, delay_poly=poly)
+    assert _rel(vis, gen) < 2e-6
+    gtc = np.zeros_like(vis)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, **kw), raw, gtc, delay_poly=poly)
+    assert _rel(tc, gtc) < 1e-3
+    assert _rel(tc, ref) < 1e-3
