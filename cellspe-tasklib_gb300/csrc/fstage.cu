@@ -658,14 +658,25 @@ int launch_w2048(const CsFStageArgs& a, cudaStream_t st)
 // Z[(1024 - k2) + 1024 (M1 - 1 - k1)], so the split needs no data exchange.
 // Channels then get the phasor exp(i (phase0 + c dphase)) and the optional
 // scale and are written segment-major ([S][K][C], coalesced along c) for
-// cs_spectra_transpose.  One segment per CTA; LSB-first input only.
+// cs_spectra_transpose.  LSB-first input only.  A CTA that fills an SM on its
+// own (16 warps, or 8 warps with the phasor's registers) takes SEGS = 4
+// consecutive segments and fetches the next one's raw words (cp.async) while
+// it transforms the current one; the other forms take one segment and leave
+// the overlap to the other CTAs on the SM.
 // ---------------------------------------------------------------------------
 constexpr int B_TILE = 32 * W_TP;               // float2 per warp: transpose tile, then Y_n1
 
-template <int M1>
+template <int M1, bool PHASE>
+constexpr int wbig_segs()
+{
+    return (M1 == 16 || (M1 == 8 && PHASE)) ? 4 : 1;
+}
+
+template <int M1, bool PHASE>
 size_t wbig_smem()
 {
-    return (size_t)M1 * B_TILE * 8 + (size_t)(2048 * M1 / 64 + 2) * 16 + 16 * 8;
+    constexpr int bufs = wbig_segs<M1, PHASE>() > 1 ? 2 : 1;
+    return (size_t)M1 * B_TILE * 8 + (size_t)bufs * (2048 * M1 / 64 + 2) * 16 + 16 * 8;
 }
 
 template <int M1, int FMT, bool PHASE>
@@ -673,27 +684,32 @@ __global__ void __launch_bounds__(32 * M1) k_fx_fstage_wbig(const __grid_constan
 {
     constexpr int M = 1024 * M1, N = 2 * M, NT = 32 * M1;
     constexpr int RAWC = N / 64 + 2;             // 16-byte chunks of one segment (+ alignment slack)
+    constexpr int SEGS = wbig_segs<M1, PHASE>(), BUFS = SEGS > 1 ? 2 : 1;
     extern __shared__ __align__(16) unsigned char smem[];
     float2* tiles = reinterpret_cast<float2*>(smem);
-    uint32_t* rw = reinterpret_cast<uint32_t*>(tiles + M1 * B_TILE);
-    float2* lut16 = reinterpret_cast<float2*>(rw + 4 * RAWC);
+    uint32_t* rw_all = reinterpret_cast<uint32_t*>(tiles + M1 * B_TILE);
+    float2* lut16 = reinterpret_cast<float2*>(rw_all + BUFS * 4 * RAWC);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int k = blockIdx.x, s = blockIdx.y;
-    const int64_t sk = (int64_t)s * a.K + k;
+    const int s = blockIdx.y, kbase = blockIdx.x * SEGS;
     const int64_t chunks = a.bytes_per_input >> 4;
     const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
 
-    const int64_t start = a.start_sample + (int64_t)k * N + (a.shift ? __ldg(a.shift + sk) : 0);
-    {
+    // raw words of segment kbase + i -> buffer i % BUFS (zero fill outside the
+    // input); returns the sample offset inside the staged words
+    auto prefetch = [&](int i) -> int {
+        const int k = kbase + i;
+        const int64_t start = a.start_sample + (int64_t)k * N + (a.shift ? __ldg(a.shift + (int64_t)s * a.K + k) : 0);
         const int64_t c0 = start >> 6;
-        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rw);
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rw_all + (i % BUFS) * 4 * RAWC);
         for (int c = threadIdx.x; c < RAWC; c += NT) {
             const int64_t ci = c0 + c;
             const bool ok = ci >= 0 && ci < chunks;
             cp_async16(dst + 16 * c, ok ? base + 16 * ci : a.raw, ok);
         }
         cp_async_commit();
-    }
+        return (int)(start & 63);
+    };
+    int off_next = prefetch(0);
     if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(a.lut[threadIdx.x & 3], a.lut[threadIdx.x >> 2]);
     // W_1024^(lane e): e < 8 by a balanced recurrence, then blocks of 8 by powers of W_1024^(8 lane)
     float2 wp[8];
@@ -706,13 +722,26 @@ __global__ void __launch_bounds__(32 * M1) k_fx_fstage_wbig(const __grid_constan
         for (int e = 2; e < 8; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], wp[1]) : cmul(wp[e / 2], wp[e / 2]);
     }
     const float2 w8 = cmul(wp[4], wp[4]);
-    cp_async_wait<0>();
-    __syncthreads();
+    float2* tb = tiles + warp * B_TILE;
+    const float2 c2 = __ldg(tw + 1024);                          // W_N^1024 = W_(2 M1)
+
+#pragma unroll 1
+    for (int i = 0; i < SEGS; i++) {
+    const int k = kbase + i;
+    if (k >= a.K) break;                                         // uniform over the CTA
+    const int64_t sk = (int64_t)s * a.K + k;
+    const int off = off_next;
+    if (i + 1 < SEGS && k + 1 < a.K) {
+        off_next = prefetch(i + 1);
+        cp_async_wait<1>();
+    } else {
+        cp_async_wait<0>();
+    }
+    __syncthreads();                 // raw words in; the previous segment's columns are read
+    const uint32_t* rw = rw_all + (i % BUFS) * 4 * RAWC;
 
     // ---- warp n1: 1024-point transform of z[n1 + M1 m] ----
-    float2* tb = tiles + warp * B_TILE;
     {
-        const int off = (int)(start & 63);
         const int f0 = off + 2 * (warp + M1 * lane);            // sample offset of this lane's first pair
         const int wb = f0 >> 4, sh = 2 * (f0 & 15);
         float2 v[32];
@@ -766,7 +795,6 @@ __global__ void __launch_bounds__(32 * M1) k_fx_fstage_wbig(const __grid_constan
         sincosf(ph0 + (float)c * dph, &sn, &cs);
         return make_float2(cs, sn);
     };
-    const float2 c2 = __ldg(tw + 1024);                          // W_N^1024 = W_(2 M1)
 #pragma unroll 1
     for (int task = threadIdx.x; task < 512; task += NT) {
         if (task == 0) {
@@ -842,6 +870,7 @@ __global__ void __launch_bounds__(32 * M1) k_fx_fstage_wbig(const __grid_constan
             w = cmul(w, c2);
         }
     }
+    }
 }
 
 template <int M1, int FMT, bool PHASE>
@@ -849,10 +878,11 @@ int launch_wbig(const CsFStageArgs& a, cudaStream_t st)
 {
     const float2* tw = cs_twiddles(2048 * M1);
     if (!tw) return CS_ERR_ARG;
-    const size_t smem = wbig_smem<M1>();
+    constexpr int SEGS = wbig_segs<M1, PHASE>();
+    const size_t smem = wbig_smem<M1, PHASE>();
     auto kern = k_fx_fstage_wbig<M1, FMT, PHASE>;
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<dim3(a.K, a.S), 32 * M1, smem, st>>>(a, tw), cs_count_launches(1);
+    kern<<<dim3((a.K + SEGS - 1) / SEGS, a.S), 32 * M1, smem, st>>>(a, tw), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
