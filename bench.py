@@ -327,6 +327,8 @@ def main():
                     help="length of the Poisson arrival window of the serving measurement (0 skips it)")
     ap.add_argument("--segments", type=int, default=K,
                     help="spectra per integration (smaller values make a profiling-sized case)")
+    ap.add_argument("--inputs", type=int, default=S,
+                    help="inputs (smaller values make a profiling-sized case)")
     ap.add_argument("--fft-points", type=int, default=N,
                     help="FFT length (smaller values make a profiling-sized case with fewer channels)")
     args = ap.parse_args()
@@ -355,13 +357,14 @@ def main():
         torch.cuda.synchronize()
 
     x_mode = cg.X_TC_FP16 if args.mode == "tc" else cg.X_FP32
-    K_run = args.segments
+    S_run, K_run = args.inputs, args.segments
+    P_run = S_run * (S_run + 1) // 2
     N_run = args.fft_points
     C_run = N_run // 2
     T_run = N_run * K_run
-    raw = synth.device_stations(S, T_run, RHO, seed=replicas.job_seed(rank))
-    vis = torch.empty((C_run, P), dtype=torch.complex64, device="cuda")
-    params = cg.fx_params(S, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+    raw = synth.device_stations(S_run, T_run, RHO, seed=replicas.job_seed(rank))
+    vis = torch.empty((C_run, P_run), dtype=torch.complex64, device="cuda")
+    params = cg.fx_params(S_run, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
     clk = ClockSampler(local).__enter__()             # running before the timed region
     for _ in range(args.warmup):
         cg.fx_correlate(params, raw, vis)
@@ -384,18 +387,18 @@ def main():
     launches = cg.kernel_launches() - l0
     ms = replicas.max_over_ranks(e0.elapsed_time(e1), dist, device="cuda")
     ms_step = ms / args.steps
-    value = replicas.aggregate_gsamples(world, S * T_run, ms_step)
+    value = replicas.aggregate_gsamples(world, S_run * T_run, ms_step)
     stage_ms = stage_sum / args.steps
 
     # ---- end to end through the C ABI with host buffers --------------------
-    raw_h = np.empty((S, T_run // 4), np.uint8)
+    raw_h = np.empty((S_run, T_run // 4), np.uint8)
     raw_h[:] = raw.cpu().numpy()
     e2e_ms, e2e_value = None, None
     if not args.no_e2e:
         pin_raw = torch.from_numpy(raw_h).pin_memory()
-        pin_vis = torch.empty((C_run, P), dtype=torch.complex64).pin_memory()
+        pin_vis = torch.empty((C_run, P_run), dtype=torch.complex64).pin_memory()
         raw_np, vis_np = pin_raw.numpy(), pin_vis.numpy()
-        hparams = cg.fx_params(S, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
+        hparams = cg.fx_params(S_run, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
         cg.fx_correlate(hparams, raw_np, vis_np)
         barrier()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -406,7 +409,7 @@ def main():
         f1.record()
         f1.synchronize()
         e2e_ms = replicas.max_over_ranks(f0.elapsed_time(f1) / args.e2e_steps, dist, device="cuda")
-        e2e_value = replicas.aggregate_gsamples(world, S * T_run, e2e_ms)
+        e2e_value = replicas.aggregate_gsamples(world, S_run * T_run, e2e_ms)
 
     # ---- roofline of the dominant kernel -----------------------------------
     # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) measured by
@@ -420,8 +423,8 @@ def main():
     X_TRAFFIC_PER_CHANNEL = 2049.0 * K_run + 1.0175e6
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
-    f_bytes = S * K_run * (N_run // 4 + C_run * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
-    x_flops = 8.0 * P * C_run * K_run                                              # 8 real flops per CMAC, triangle
+    f_bytes = S_run * K_run * (N_run // 4 + C_run * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
+    x_flops = 8.0 * P_run * C_run * K_run                                              # 8 real flops per CMAC, triangle
     stages = {"f_stage_ms": f_ms, "x_stage_ms": x_ms, "output_ms": stage_ms[3],
               "f_stage_gbs": f_bytes / (f_ms * 1e-3) / 1e9,
               "x_stage_tflops": x_flops / (x_ms * 1e-3) / 1e12}
@@ -441,10 +444,11 @@ def main():
     else:
         pk = peaks["hbm_gbs"]
         tc_f = x_mode == cg.X_TC_FP16 and N_run == 2048 and os.environ.get("CELLSPE_FSTAGE_TC") == "1"
-        fk = "k_fx_fstage_tc" if tc_f else ("k_fx_fstage_w2048" if N_run == 2048 else "k_fx_fstage")
+        fk = "k_fx_fstage_tc" if tc_f else ("k_fx_fstage_w2048" if N_run == 2048 else
+                                            "k_fx_fstage_wbig" if N_run >= 4096 else "k_fx_fstage")
         roof = {"bound": "hbm", "kernel": fk, "achieved": stages["f_stage_gbs"], "peak": pk,
                 "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
-                "traffic": (F_TRAFFIC_PER_SEGMENT * S * K_run
+                "traffic": (F_TRAFFIC_PER_SEGMENT * S_run * K_run
                             if F_TRAFFIC_PER_SEGMENT and fk == "k_fx_fstage_w2048" else None),
                 "note": "F stage is bound by instruction issue and the shared-memory pipe (ncu), not HBM"}
 
@@ -452,7 +456,7 @@ def main():
     if args.serve_seconds > 0:
         serving = run_serving(cg, torch, args.serve_seconds, 200.0, x_mode)
     configs = None
-    if not args.no_configs and N_run == N:
+    if not args.no_configs and N_run == N and S_run == S:
         configs = run_configs(cg, torch, x_mode, with_cpu=(rank == 0 and not args.no_cpu))
 
     cpu = None
@@ -462,9 +466,9 @@ def main():
         v, dt = cpu_baseline(raw_h, kb, nthreads)
         v1, dt1 = cpu_baseline(raw_h, max(1, kb // 16), 1)
         cpu = {"value": v, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
-               "sample": f"{S} inputs x {kb} segments x {N_run} samples, {dt:.1f} s",
+               "sample": f"{S_run} inputs x {kb} segments x {N_run} samples, {dt:.1f} s",
                "value_1core": v1,
-               "sample_1core": f"{S} inputs x {max(1, kb // 16)} segments, {dt1:.1f} s"}
+               "sample_1core": f"{S_run} inputs x {max(1, kb // 16)} segments, {dt1:.1f} s"}
 
     if rank == 0:
         line = {
@@ -473,13 +477,14 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f16-tc/f32-acc" if x_mode == cg.X_TC_FP16 else "f32",
             "data": "synthetic (seeded 2-bit offset binary, rho=0.02, generated on device)",
-            "config": {"workload": f"256-station dual-pol FX: S=512, N={N_run}, C={C_run}, K={K_run}",
-                       "inputs": S, "fft_points": N_run, "channels": C_run, "segments": K_run, "products": P,
+            "config": {"workload": (f"256-station dual-pol FX: S=512, N={N_run}, C={C_run}, K={K_run}" if S_run == S
+                                    else f"FX: S={S_run}, N={N_run}, C={C_run}, K={K_run}"),
+                       "inputs": S_run, "fft_points": N_run, "channels": C_run, "segments": K_run, "products": P_run,
                        "x_mode": args.mode, "vis_order": "channel-major [C][P]",
                        "l2": "inputs larger than L2 (1.07 GB raw, spectra 8.6/17 GB, vis 1.07 GB)",
                        "parallelism": f"replicas x{world} (one job per GPU)"},
-            "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(S * T_run // 4),
-                    "d2h_bytes_per_step": int(C_run * P * 8), "ms_per_step": e2e_ms},
+            "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(S_run * T_run // 4),
+                    "d2h_bytes_per_step": int(C_run * P_run * 8), "ms_per_step": e2e_ms},
             "gpu_launches": int(launches),
             "roofline": roof,
             "stages": stages,
