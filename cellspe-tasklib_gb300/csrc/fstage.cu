@@ -895,6 +895,216 @@ int dispatch_wbig(const CsFStageArgs& a, cudaStream_t st)
     return ph ? launch_wbig<M1, CS_SPECTRA_F16, true>(a, st) : launch_wbig<M1, CS_SPECTRA_F16, false>(a, st);
 }
 
+
+// ---------------------------------------------------------------------------
+// N = 512: one half-warp per segment.  The 256-point complex FFT of
+// z[n] = x[2n] + i x[2n+1] runs as a 16 x 16 four-step held in registers:
+// lane l of the half-warp keeps n = l + 16 j (j < 16), DFT-16 over j, twiddle
+// W_256^(l k1), a padded 16 x 17 transpose, DFT-16, after which lane l holds
+// Z[l + 16 k2].  The real-FFT split pairs Z[k] with Z[256 - k], which lives in
+// lane (16 - l) mod 16 of the same half-warp, register 15 - k2 (lane 0: its
+// own register (16 - k2) mod 16): a 16-wide shuffle.  A CTA of 8 warps
+// stages 64 segments of one input (each half-warp four, the next one's raw
+// words fetched with cp.async during the current transform) and writes them
+// corner-turned: 128-byte runs per (channel, plane) row in FP16, 512 in FP32.
+// The two half-warps of a warp fill staging columns 16 apart, so their
+// stores fall in disjoint banks.  LSB-first input only.
+// ---------------------------------------------------------------------------
+constexpr int H_G = 64, H_TP = 17, H_RAWC = 512 / 64 + 2, H_RAWW = 4 * H_RAWC;
+
+template <int FMT>
+size_t w512_smem()
+{
+    const size_t elem = (FMT == CS_SPECTRA_F32) ? 8 : 4;
+    return (size_t)16 * 16 * H_TP * 8 + (size_t)16 * 2 * H_RAWW * 4 + 16 * 8 + (size_t)256 * (H_G + 1) * elem;
+}
+
+template <int FMT, bool PHASE>
+__global__ void __launch_bounds__(256, FMT == CS_SPECTRA_F32 ? 1 : 2) k_fx_fstage_w512(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
+{
+    constexpr int M = 256, N = 512, NT = 256, G = H_G;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tb_all = reinterpret_cast<float2*>(smem);
+    uint32_t* rb_all = reinterpret_cast<uint32_t*>(tb_all + 16 * 16 * H_TP);
+    float2* lut16 = reinterpret_cast<float2*>(rb_all + 16 * 2 * H_RAWW);
+    unsigned char* stage = reinterpret_cast<unsigned char*>(lut16 + 16);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int hw = lane >> 4, hl = lane & 15, h = 2 * warp + hw;
+    float2* tb = tb_all + h * 16 * H_TP;
+    uint32_t* rb = rb_all + h * 2 * H_RAWW;
+    const int s = blockIdx.y, k0 = blockIdx.x * G;
+    const int64_t chunks = a.bytes_per_input >> 4;
+    const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
+    // staging column of round r: warp + 8 r', half 0 taking r' = 0, 1, 4, 5 and half 1 r' + 2
+    auto slot = [&](int r) { return warp + 8 * ((r & 1) + 4 * (r >> 1) + 2 * hw); };
+
+    auto prefetch = [&](int r) -> int {
+        const int k = k0 + slot(r);
+        const bool kv = k < a.K;
+        const int64_t start = a.start_sample + (int64_t)k * N + ((a.shift && kv) ? __ldg(a.shift + (int64_t)s * a.K + k) : 0);
+        const int64_t c0 = start >> 6;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rb + (r & 1) * H_RAWW);
+        if (hl < H_RAWC) {
+            const int64_t ci = c0 + hl;
+            const bool ok = kv && ci >= 0 && ci < chunks;
+            cp_async16(dst + 16 * hl, ok ? base + 16 * ci : a.raw, ok);
+        }
+        cp_async_commit();
+        return (int)(start & 63);
+    };
+    int off_next = prefetch(0);
+
+    if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(a.lut[threadIdx.x & 3], a.lut[threadIdx.x >> 2]);
+    float2 w1, whalf;
+    {
+        float sn, cs;
+        sincospif(-(float)hl / 128.0f, &sn, &cs);
+        w1 = make_float2(cs, sn);                                // W_256^hl
+        sincospif(-(float)hl / 256.0f, &sn, &cs);
+        whalf = make_float2(0.5f * cs, 0.5f * sn);               // W_512^hl / 2
+    }
+    float2 wp[16];
+    wp[0] = make_float2(1.f, 0.f);
+    wp[1] = w1;
+#pragma unroll
+    for (int e = 2; e < 16; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], w1) : cmul(wp[e / 2], wp[e / 2]);
+    __syncthreads();
+    const int src = (16 - hl) & 15;
+
+#pragma unroll 1
+    for (int r = 0; r < 4; r++) {
+        const int ls = slot(r), k = k0 + ls;
+        const int off = off_next;
+        if (r + 1 < 4) {
+            off_next = prefetch(r + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        const uint32_t* rw = rb + (r & 1) * H_RAWW;
+        const int f0 = off + 2 * hl;
+        const int wb = f0 >> 4, sh = 2 * (f0 & 15);
+        float2 v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {                           // pair j is 32 samples = 2 words further on
+            const uint32_t bits = __funnelshift_r(rw[wb + 2 * j], rw[wb + 2 * j + 1], sh);
+            v[j] = lut16[bits & 15u];
+        }
+        Dft<16>::run(v);
+#pragma unroll
+        for (int e = 1; e < 16; e++) v[e] = cmul(v[e], wp[e]);
+#pragma unroll
+        for (int e = 0; e < 16; e++) tb[e * H_TP + hl] = v[e];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < 16; e++) v[e] = tb[hl * H_TP + e];
+        __syncwarp();
+        Dft<16>::run(v);                                         // v[k2] = Z[hl + 16 k2]
+
+        // real-FFT split over the pairs (k, 256 - k), as in the 2048-point path
+        const bool kv = k < a.K;
+        const int64_t sk = (int64_t)s * a.K + (kv ? k : 0);
+        float2 B = make_float2(1.f, 0.f), D = B, B2 = B;
+        if constexpr (PHASE) {
+            const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);
+            float sn, cs;
+            sincosf(ph0 + (float)hl * dph, &sn, &cs);
+            B = make_float2(cs, sn);
+            sincosf(ph0 + (float)(M - hl) * dph, &sn, &cs);
+            B2 = make_float2(cs, sn);
+            sincosf(16.f * dph, &sn, &cs);
+            D = make_float2(cs, sn);
+        }
+        const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
+        auto put = [&](int c, float2 X) {
+            if (scl) X = cscale(X, __ldg(scl + c));
+            if constexpr (FMT == CS_SPECTRA_F32)
+                reinterpret_cast<float2*>(stage)[c * (G + 1) + ls] = X;
+            else
+                reinterpret_cast<__half2*>(stage)[c * (G + 1) + ls] = __floats2half2_rn(X.x, X.y);
+        };
+#pragma unroll
+        for (int k2 = 0; k2 <= 8; k2++) {
+            if (k2 == 8 && hl != 0) break;
+            float2 zb;
+            if (k2 < 8) {
+                zb.x = __shfl_sync(0xffffffffu, v[15 - k2].x, src, 16);
+                zb.y = __shfl_sync(0xffffffffu, v[15 - k2].y, src, 16);
+            }
+            if (hl == 0) zb = v[(16 - k2) & 15];
+            const float2 za = v[k2];
+            const float2 sm = make_float2(za.x + zb.x, za.y - zb.y);
+            const float2 df = make_float2(za.x - zb.x, za.y + zb.y);
+            const float2 t = cmul(cmul(whalf, w32(k2)), df);
+            float2 X1 = make_float2(fmaf(0.5f, sm.x, t.y), fmaf(0.5f, sm.y, -t.x));
+            float2 X2 = make_float2(fmaf(0.5f, sm.x, -t.y), -fmaf(0.5f, sm.y, t.x));
+            const int c1 = hl + 16 * k2, c2 = M - c1;
+            if constexpr (PHASE) {
+                X1 = cmul(X1, B);
+                X2 = cmul(X2, B2);
+                B = cmul(B, D);
+                B2 = cmul_conj(B2, D);
+            }
+            put(c1, X1);
+            if (k2 < 8 && c1 != 0) put(c2, X2);
+        }
+    }
+    __syncthreads();
+
+    // corner-turned write-out of the 64 staged segments
+    const int nvalid = max(0, min(G, a.K - k0));
+    const int S = out_rows(a), KP = out_pitch(a);
+    if constexpr (FMT == CS_SPECTRA_F32) {
+        const float2* st = reinterpret_cast<const float2*>(stage);
+        float2* out = reinterpret_cast<float2*>(a.out);
+        if (nvalid == G && KP % 2 == 0) {
+            for (int idx = threadIdx.x; idx < M * (G / 2); idx += NT) {
+                const int c = idx / (G / 2), l = 2 * (idx % (G / 2));
+                const float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
+                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * KP + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < M * G; idx += NT) {
+                const int c = idx / G, l = idx % G;
+                if (l < nvalid) out[((int64_t)c * S + s) * KP + k0 + l] = st[c * (G + 1) + l];
+            }
+        }
+    } else {
+        const __half2* st = reinterpret_cast<const __half2*>(stage);
+        __half* out = reinterpret_cast<__half*>(a.out);
+        if (nvalid == G && KP % 8 == 0) {
+            constexpr int P8 = G / 8;
+            for (int idx = threadIdx.x; idx < M * 2 * P8; idx += NT) {
+                const int piece = idx % P8, plane = (idx / P8) & 1, c = idx / (2 * P8);
+                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + 8 * piece);
+                const uint32_t sel = plane ? 0x7632u : 0x5410u;
+                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * KP + k0 + 8 * piece) =
+                    make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
+                               __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < M * 2 * G; idx += NT) {
+                const int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
+                if (l < nvalid) {
+                    const __half2 x = st[c * (G + 1) + l];
+                    out[(((int64_t)c * 2 + plane) * S + s) * KP + k0 + l] = plane ? __high2half(x) : __low2half(x);
+                }
+            }
+        }
+    }
+}
+
+template <int FMT, bool PHASE>
+int launch_w512(const CsFStageArgs& a, cudaStream_t st)
+{
+    const size_t smem = w512_smem<FMT>();
+    auto kern = k_fx_fstage_w512<FMT, PHASE>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<dim3((a.K + H_G - 1) / H_G, a.S), 256, smem, st>>>(a, nullptr), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
 }  // namespace
 
 void cs_fstage_allow_timing(bool allow) { t_w2048_timing_allowed = allow; }
@@ -967,11 +1177,18 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
             return ph ? launch_w2048<CS_SPECTRA_F32, true>(a, st) : launch_w2048<CS_SPECTRA_F32, false>(a, st);
         return ph ? launch_w2048<CS_SPECTRA_F16, true>(a, st) : launch_w2048<CS_SPECTRA_F16, false>(a, st);
     }
-    // N = 4096 ... 32768, segment-major: the warp four-step (CELLSPE_FSTAGE_GENERIC=1
-    // selects the CTA-wide Stockham FFT instead)
+    // N = 512 (channel-major) and N = 4096 ... 32768 (segment-major): the warp
+    // four-steps (CELLSPE_FSTAGE_GENERIC=1 selects the CTA-wide Stockham FFT)
+    const char* gen = getenv("CELLSPE_FSTAGE_GENERIC");
+    const bool generic = gen && gen[0] == '1';
+    if (a.N == 512 && !a.seg_major && !a.msb_first && !generic) {
+        const bool ph = a.phase0 != nullptr;
+        if (a.format == CS_SPECTRA_F32)
+            return ph ? launch_w512<CS_SPECTRA_F32, true>(a, st) : launch_w512<CS_SPECTRA_F32, false>(a, st);
+        return ph ? launch_w512<CS_SPECTRA_F16, true>(a, st) : launch_w512<CS_SPECTRA_F16, false>(a, st);
+    }
     if (a.seg_major && !a.msb_first && a.N >= 4096 && a.N <= 32768) {
-        const char* e = getenv("CELLSPE_FSTAGE_GENERIC");
-        if (!(e && e[0] == '1')) {
+        if (!generic) {
             switch (a.N) {
                 case 4096: return dispatch_wbig<2>(a, st);
                 case 8192: return dispatch_wbig<4>(a, st);

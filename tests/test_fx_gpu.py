@@ -208,14 +208,15 @@ def test_fx_w2048_schedules_identical(cg, mode, K, monkeypatch):
         assert torch.equal(o, outs[0])
 
 
-@pytest.mark.parametrize("N,K", [(4096, 24), (8192, 16), (16384, 8), (32768, 8)])
-def test_fx_long_transforms_delay_model(cg, orc, N, K, monkeypatch):
-    """N = 4096 ... 32768 (the warp four-step F stage: N/2048 warps per segment,
-    each a 1024-point transform of every (N/2048)-th point, then radix-N/2048
-    columns and the real-FFT split in registers): FP32 path against the oracle's
-    FP32 path with the same delay model, and against the CTA-wide Stockham F
-    stage; the tensor-core path (K a multiple of 8) against the same job through
-    the Stockham F stage."""
+@pytest.mark.parametrize("N,K", [(512, 40), (512, 128), (4096, 24), (8192, 16), (16384, 8), (32768, 8)])
+def test_fx_warp_fstages_delay_model(cg, orc, N, K, monkeypatch):
+    """The warp four-step F stages other than N = 2048: N = 512 (a half-warp per
+    segment, 64-segment tiles: K = 40 a partial tile, K = 128 two full ones) and
+    N = 4096 ... 32768 (N/2048 warps per segment, each a 1024-point transform of
+    every (N/2048)-th point, then radix-N/2048 columns and the real-FFT split in
+    registers).  FP32 path against the oracle's FP32 path with the same delay
+    model and against the CTA-wide Stockham F stage; the tensor-core path (K a
+    multiple of 8) against the same job through the Stockham F stage."""
     import synth
 
     S = 3

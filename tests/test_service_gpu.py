@@ -111,3 +111,27 @@ def ctypes_byref(x):
     import ctypes
 
     return ctypes.byref(x)
+
+
+def test_service_failed_job_reports_worker_error(cg):
+    """A job that the worker rejects (here N = 3000, not a power of two) fails
+    alone: wait() raises with the worker's message, the next job still runs."""
+    import synth
+
+    S, N, K = 4, 2048, 8
+    raw = synth.stations_offset_binary(S, N * K, rho=0.1, seed=8)
+    svc = cg.Service()
+    try:
+        bad = svc.submit(cg.fx_params(S, 3000, 4, raw.shape[1]), raw, np.zeros((1500, 10), np.complex64))
+        out = np.zeros((N // 2, S * (S + 1) // 2), np.complex64)
+        good = svc.submit(cg.fx_params(S, N, K, raw.shape[1]), raw, out)
+        with pytest.raises(cg.CellspeError) as e:
+            svc.wait(bad)
+        assert e.value.code == cg.ERR_ARG and "power of two" in str(e.value)
+        svc.wait(good)
+        st = svc.stats()
+    finally:
+        svc.close()
+    ref = np.zeros_like(out)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1]), raw, ref)
+    assert np.array_equal(out, ref) and st["failed"] == 1 and st["completed"] == 1
