@@ -910,6 +910,54 @@ int dispatch_wbig(const CsFStageArgs& a, cudaStream_t st)
 // The two half-warps of a warp fill staging columns 16 apart, so their
 // stores fall in disjoint banks.  LSB-first input only.
 // ---------------------------------------------------------------------------
+// Corner-turned write-out of a staging tile [M channels][G + 1] (G segments of
+// input s from segment k0; FP32 float2 or FP16 half2 Re|Im) into the channel-
+// major layout: F32 float2 rows (c, s), F16 half rows (c, plane, s), pitch KP.
+template <int FMT, int M, int G, int NT>
+CS_DEV void stage_writeout(const CsFStageArgs& a, const unsigned char* stage, int s, int k0)
+{
+    const int nvalid = max(0, min(G, a.K - k0));
+    const int S = out_rows(a), KP = out_pitch(a);
+    if constexpr (FMT == CS_SPECTRA_F32) {
+        const float2* st = reinterpret_cast<const float2*>(stage);
+        float2* out = reinterpret_cast<float2*>(a.out);
+        if (nvalid == G && KP % 2 == 0) {
+            for (int idx = threadIdx.x; idx < M * (G / 2); idx += NT) {
+                const int c = idx / (G / 2), l = 2 * (idx % (G / 2));
+                const float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
+                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * KP + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < M * G; idx += NT) {
+                const int c = idx / G, l = idx % G;
+                if (l < nvalid) out[((int64_t)c * S + s) * KP + k0 + l] = st[c * (G + 1) + l];
+            }
+        }
+    } else {
+        const __half2* st = reinterpret_cast<const __half2*>(stage);
+        __half* out = reinterpret_cast<__half*>(a.out);
+        if (nvalid == G && KP % 8 == 0) {
+            constexpr int P8 = G / 8;
+            for (int idx = threadIdx.x; idx < M * 2 * P8; idx += NT) {
+                const int piece = idx % P8, plane = (idx / P8) & 1, c = idx / (2 * P8);
+                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + 8 * piece);
+                const uint32_t sel = plane ? 0x7632u : 0x5410u;
+                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * KP + k0 + 8 * piece) =
+                    make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
+                               __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < M * 2 * G; idx += NT) {
+                const int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
+                if (l < nvalid) {
+                    const __half2 x = st[c * (G + 1) + l];
+                    out[(((int64_t)c * 2 + plane) * S + s) * KP + k0 + l] = plane ? __high2half(x) : __low2half(x);
+                }
+            }
+        }
+    }
+}
+
 constexpr int H_G = 64, H_TP = 17, H_RAWC = 512 / 64 + 2, H_RAWW = 4 * H_RAWC;
 
 template <int FMT>
@@ -1051,48 +1099,7 @@ __global__ void __launch_bounds__(256, FMT == CS_SPECTRA_F32 ? 1 : 2) k_fx_fstag
         }
     }
     __syncthreads();
-
-    // corner-turned write-out of the 64 staged segments
-    const int nvalid = max(0, min(G, a.K - k0));
-    const int S = out_rows(a), KP = out_pitch(a);
-    if constexpr (FMT == CS_SPECTRA_F32) {
-        const float2* st = reinterpret_cast<const float2*>(stage);
-        float2* out = reinterpret_cast<float2*>(a.out);
-        if (nvalid == G && KP % 2 == 0) {
-            for (int idx = threadIdx.x; idx < M * (G / 2); idx += NT) {
-                const int c = idx / (G / 2), l = 2 * (idx % (G / 2));
-                const float2 x0 = st[c * (G + 1) + l], x1 = st[c * (G + 1) + l + 1];
-                *reinterpret_cast<float4*>(out + ((int64_t)c * S + s) * KP + k0 + l) = make_float4(x0.x, x0.y, x1.x, x1.y);
-            }
-        } else {
-            for (int idx = threadIdx.x; idx < M * G; idx += NT) {
-                const int c = idx / G, l = idx % G;
-                if (l < nvalid) out[((int64_t)c * S + s) * KP + k0 + l] = st[c * (G + 1) + l];
-            }
-        }
-    } else {
-        const __half2* st = reinterpret_cast<const __half2*>(stage);
-        __half* out = reinterpret_cast<__half*>(a.out);
-        if (nvalid == G && KP % 8 == 0) {
-            constexpr int P8 = G / 8;
-            for (int idx = threadIdx.x; idx < M * 2 * P8; idx += NT) {
-                const int piece = idx % P8, plane = (idx / P8) & 1, c = idx / (2 * P8);
-                const uint32_t* w = reinterpret_cast<const uint32_t*>(st + c * (G + 1) + 8 * piece);
-                const uint32_t sel = plane ? 0x7632u : 0x5410u;
-                *reinterpret_cast<uint4*>(out + (((int64_t)c * 2 + plane) * S + s) * KP + k0 + 8 * piece) =
-                    make_uint4(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel),
-                               __byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel));
-            }
-        } else {
-            for (int idx = threadIdx.x; idx < M * 2 * G; idx += NT) {
-                const int l = idx % G, plane = (idx / G) & 1, c = idx / (2 * G);
-                if (l < nvalid) {
-                    const __half2 x = st[c * (G + 1) + l];
-                    out[(((int64_t)c * 2 + plane) * S + s) * KP + k0 + l] = plane ? __high2half(x) : __low2half(x);
-                }
-            }
-        }
-    }
+    stage_writeout<FMT, M, G, NT>(a, stage, s, k0);
 }
 
 template <int FMT, bool PHASE>
@@ -1102,6 +1109,215 @@ int launch_w512(const CsFStageArgs& a, cudaStream_t st)
     auto kern = k_fx_fstage_w512<FMT, PHASE>;
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<dim3((a.K + H_G - 1) / H_G, a.S), 256, smem, st>>>(a, nullptr), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
+// N = 1024: one half-warp per segment, 32 points per lane.  The 512-point
+// complex FFT is a 16 x 32 four-step: lane l keeps n = l + 16 j (j < 32),
+// DFT-32 over j, twiddle W_512^(l k1), a padded 16 x 33 transpose after which
+// lane l holds the 16 values of columns k1 = l and k1 = l + 16, and two
+// DFT-16s give A[k2] = Z[l + 32 k2] and B[k2] = Z[l + 16 + 32 k2].  The split
+// partner of Z[l + 32 k2] is Z[(32 - l) + 32 (15 - k2)], i.e. B[15 - k2] of
+// lane 16 - l (lane 0: its own A[(16 - k2) mod 16]); that of Z[l + 16 + 32 k2]
+// is A[15 - k2] of lane 16 - l (lane 0: its own B[15 - k2]).  CTA tiles of 64
+// segments (FP16) or 32 (FP32), staged as in the 512-point form.
+// ---------------------------------------------------------------------------
+constexpr int Q_TP = 33, Q_RAWC = 1024 / 64 + 2, Q_RAWW = 4 * Q_RAWC;
+
+template <int FMT>
+constexpr int w1024_g() { return FMT == CS_SPECTRA_F32 ? 32 : 64; }
+
+template <int FMT>
+size_t w1024_smem()
+{
+    const size_t elem = (FMT == CS_SPECTRA_F32) ? 8 : 4;
+    return (size_t)16 * 16 * Q_TP * 8 + (size_t)16 * 2 * Q_RAWW * 4 + 16 * 8 + (size_t)512 * (w1024_g<FMT>() + 1) * elem;
+}
+
+template <int FMT, bool PHASE>
+__global__ void __launch_bounds__(256, 1) k_fx_fstage_w1024(const __grid_constant__ CsFStageArgs a, const float2* __restrict__ tw)
+{
+    constexpr int M = 512, N = 1024, NT = 256, G = w1024_g<FMT>(), ROUNDS = G / 16;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tb_all = reinterpret_cast<float2*>(smem);
+    uint32_t* rb_all = reinterpret_cast<uint32_t*>(tb_all + 16 * 16 * Q_TP);
+    float2* lut16 = reinterpret_cast<float2*>(rb_all + 16 * 2 * Q_RAWW);
+    unsigned char* stage = reinterpret_cast<unsigned char*>(lut16 + 16);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int hw = lane >> 4, hl = lane & 15, h = 2 * warp + hw;
+    float2* tb = tb_all + h * 16 * Q_TP;
+    uint32_t* rb = rb_all + h * 2 * Q_RAWW;
+    const int s = blockIdx.y, k0 = blockIdx.x * G;
+    const int64_t chunks = a.bytes_per_input >> 4;
+    const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
+    // staging column of round r: the two half-warps of a warp 16 columns apart
+    auto slot = [&](int r) {
+        if constexpr (ROUNDS == 4) return warp + 8 * ((r & 1) + 4 * (r >> 1) + 2 * hw);
+        else return warp + 8 * (r + 2 * hw);
+    };
+
+    auto prefetch = [&](int r) -> int {
+        const int k = k0 + slot(r);
+        const bool kv = k < a.K;
+        const int64_t start = a.start_sample + (int64_t)k * N + ((a.shift && kv) ? __ldg(a.shift + (int64_t)s * a.K + k) : 0);
+        const int64_t c0 = start >> 6;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rb + (r & 1) * Q_RAWW);
+        for (int c = hl; c < Q_RAWC; c += 16) {
+            const int64_t ci = c0 + c;
+            const bool ok = kv && ci >= 0 && ci < chunks;
+            cp_async16(dst + 16 * c, ok ? base + 16 * ci : a.raw, ok);
+        }
+        cp_async_commit();
+        return (int)(start & 63);
+    };
+    int off_next = prefetch(0);
+
+    if (threadIdx.x < 16) lut16[threadIdx.x] = make_float2(a.lut[threadIdx.x & 3], a.lut[threadIdx.x >> 2]);
+    // W_512^(hl e), e < 32: e < 8 by a balanced recurrence, blocks of 8 by powers of W_512^(8 hl)
+    float2 wp[8], whA, whB;
+    {
+        float sn, cs;
+        sincospif(-(float)hl / 256.0f, &sn, &cs);
+        wp[0] = make_float2(1.f, 0.f);
+        wp[1] = make_float2(cs, sn);
+#pragma unroll
+        for (int e = 2; e < 8; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], wp[1]) : cmul(wp[e / 2], wp[e / 2]);
+        sincospif(-(float)hl / 512.0f, &sn, &cs);
+        whA = make_float2(0.5f * cs, 0.5f * sn);                 // W_1024^hl / 2
+        sincospif(-(float)(hl + 16) / 512.0f, &sn, &cs);
+        whB = make_float2(0.5f * cs, 0.5f * sn);                 // W_1024^(hl + 16) / 2
+    }
+    const float2 w8 = cmul(wp[4], wp[4]);
+    __syncthreads();
+    const int src = (16 - hl) & 15;
+
+#pragma unroll 1
+    for (int r = 0; r < ROUNDS; r++) {
+        const int ls = slot(r), k = k0 + ls;
+        const int off = off_next;
+        if (r + 1 < ROUNDS) {
+            off_next = prefetch(r + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        const uint32_t* rw = rb + (r & 1) * Q_RAWW;
+        const int f0 = off + 2 * hl;
+        const int wb = f0 >> 4, sh = 2 * (f0 & 15);
+        float2 v[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {                           // pair j is 32 samples = 2 words further on
+            const uint32_t bits = __funnelshift_r(rw[wb + 2 * j], rw[wb + 2 * j + 1], sh);
+            v[j] = lut16[bits & 15u];
+        }
+        Dft<32>::run(v);
+        {
+            float2 q = make_float2(1.f, 0.f);
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    if (b == 0 && e == 0) continue;
+                    v[8 * b + e] = cmul(v[8 * b + e], b ? cmul(q, wp[e]) : wp[e]);
+                }
+                q = b ? cmul(q, w8) : w8;
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 32; e++) tb[hl * Q_TP + e] = v[e];
+        __syncwarp();
+#pragma unroll
+        for (int l = 0; l < 16; l++) {
+            v[l] = tb[l * Q_TP + hl];
+            v[16 + l] = tb[l * Q_TP + hl + 16];
+        }
+        __syncwarp();
+        Dft<16>::run(v);                                         // v[k2] = Z[hl + 32 k2]
+        Dft<16>::run(v + 16);                                    // v[16 + k2] = Z[hl + 16 + 32 k2]
+
+        const bool kv = k < a.K;
+        const int64_t sk = (int64_t)s * a.K + (kv ? k : 0);
+        float2 A1 = make_float2(1.f, 0.f), A2 = A1, B1 = A1, B2 = A1, D = A1;
+        if constexpr (PHASE) {
+            const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);
+            float sn, cs;
+            sincosf(ph0 + (float)hl * dph, &sn, &cs);            A1 = make_float2(cs, sn);
+            sincosf(ph0 + (float)(M - hl) * dph, &sn, &cs);      A2 = make_float2(cs, sn);
+            sincosf(ph0 + (float)(hl + 16) * dph, &sn, &cs);     B1 = make_float2(cs, sn);
+            sincosf(ph0 + (float)(M - hl - 16) * dph, &sn, &cs); B2 = make_float2(cs, sn);
+            sincosf(32.f * dph, &sn, &cs);                       D = make_float2(cs, sn);
+        }
+        const float* scl = a.scale ? a.scale + (int64_t)s * M : nullptr;
+        auto put = [&](int c, float2 X) {
+            if (scl) X = cscale(X, __ldg(scl + c));
+            if constexpr (FMT == CS_SPECTRA_F32)
+                reinterpret_cast<float2*>(stage)[c * (G + 1) + ls] = X;
+            else
+                reinterpret_cast<__half2*>(stage)[c * (G + 1) + ls] = __floats2half2_rn(X.x, X.y);
+        };
+        // X[k] = s/2 - i t, X[M - k] = conj(s/2 + i t), s = Z[k] + conj(Z[M-k]), t = (W_N^k / 2)(Z[k] - conj(Z[M-k]))
+        auto split = [&](float2 za, float2 zb, float2 wh, float2& X1, float2& X2) {
+            const float2 sm = make_float2(za.x + zb.x, za.y - zb.y);
+            const float2 df = make_float2(za.x - zb.x, za.y + zb.y);
+            const float2 t = cmul(wh, df);
+            X1 = make_float2(fmaf(0.5f, sm.x, t.y), fmaf(0.5f, sm.y, -t.x));
+            X2 = make_float2(fmaf(0.5f, sm.x, -t.y), -fmaf(0.5f, sm.y, t.x));
+        };
+#pragma unroll
+        for (int k2 = 0; k2 <= 8; k2++) {
+            if (k2 == 8 && hl != 0) break;
+            float2 pa, pb;                                        // partners of Z[hl + 32 k2] and Z[hl + 16 + 32 k2]
+            if (k2 < 8) {
+                pa.x = __shfl_sync(0xffffffffu, v[16 + 15 - k2].x, src, 16);
+                pa.y = __shfl_sync(0xffffffffu, v[16 + 15 - k2].y, src, 16);
+                pb.x = __shfl_sync(0xffffffffu, v[15 - k2].x, src, 16);
+                pb.y = __shfl_sync(0xffffffffu, v[15 - k2].y, src, 16);
+            }
+            if (hl == 0) {
+                pa = v[(16 - k2) & 15];
+                pb = v[16 + 15 - k2];
+            }
+            const float2 w32k = w32(k2);
+            float2 X1, X2;
+            split(v[k2], pa, cmul(whA, w32k), X1, X2);
+            const int cA = hl + 32 * k2;
+            if constexpr (PHASE) {
+                X1 = cmul(X1, A1);
+                X2 = cmul(X2, A2);
+                A1 = cmul(A1, D);
+                A2 = cmul_conj(A2, D);
+            }
+            put(cA, X1);
+            if (k2 < 8 && cA != 0) put(M - cA, X2);
+            if (k2 < 8) {
+                split(v[16 + k2], pb, cmul(whB, w32k), X1, X2);
+                const int cB = hl + 16 + 32 * k2;
+                if constexpr (PHASE) {
+                    X1 = cmul(X1, B1);
+                    X2 = cmul(X2, B2);
+                    B1 = cmul(B1, D);
+                    B2 = cmul_conj(B2, D);
+                }
+                put(cB, X1);
+                put(M - cB, X2);
+            }
+        }
+    }
+    __syncthreads();
+    stage_writeout<FMT, M, G, NT>(a, stage, s, k0);
+}
+
+template <int FMT, bool PHASE>
+int launch_w1024(const CsFStageArgs& a, cudaStream_t st)
+{
+    const size_t smem = w1024_smem<FMT>();
+    auto kern = k_fx_fstage_w1024<FMT, PHASE>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    constexpr int G = w1024_g<FMT>();
+    kern<<<dim3((a.K + G - 1) / G, a.S), 256, smem, st>>>(a, nullptr), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
@@ -1177,8 +1393,8 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
             return ph ? launch_w2048<CS_SPECTRA_F32, true>(a, st) : launch_w2048<CS_SPECTRA_F32, false>(a, st);
         return ph ? launch_w2048<CS_SPECTRA_F16, true>(a, st) : launch_w2048<CS_SPECTRA_F16, false>(a, st);
     }
-    // N = 512 (channel-major) and N = 4096 ... 32768 (segment-major): the warp
-    // four-steps (CELLSPE_FSTAGE_GENERIC=1 selects the CTA-wide Stockham FFT)
+    // N = 512, 1024 (channel-major) and N = 4096 ... 32768 (segment-major): the
+    // warp four-steps (CELLSPE_FSTAGE_GENERIC=1 selects the CTA-wide Stockham FFT)
     const char* gen = getenv("CELLSPE_FSTAGE_GENERIC");
     const bool generic = gen && gen[0] == '1';
     if (a.N == 512 && !a.seg_major && !a.msb_first && !generic) {
@@ -1186,6 +1402,12 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
         if (a.format == CS_SPECTRA_F32)
             return ph ? launch_w512<CS_SPECTRA_F32, true>(a, st) : launch_w512<CS_SPECTRA_F32, false>(a, st);
         return ph ? launch_w512<CS_SPECTRA_F16, true>(a, st) : launch_w512<CS_SPECTRA_F16, false>(a, st);
+    }
+    if (a.N == 1024 && !a.seg_major && !a.msb_first && !generic) {
+        const bool ph = a.phase0 != nullptr;
+        if (a.format == CS_SPECTRA_F32)
+            return ph ? launch_w1024<CS_SPECTRA_F32, true>(a, st) : launch_w1024<CS_SPECTRA_F32, false>(a, st);
+        return ph ? launch_w1024<CS_SPECTRA_F16, true>(a, st) : launch_w1024<CS_SPECTRA_F16, false>(a, st);
     }
     if (a.seg_major && !a.msb_first && a.N >= 4096 && a.N <= 32768) {
         if (!generic) {

@@ -208,10 +208,12 @@ def test_fx_w2048_schedules_identical(cg, mode, K, monkeypatch):
         assert torch.equal(o, outs[0])
 
 
-@pytest.mark.parametrize("N,K", [(512, 40), (512, 128), (4096, 24), (8192, 16), (16384, 8), (32768, 8)])
+@pytest.mark.parametrize("N,K", [(512, 40), (512, 128), (1024, 40), (1024, 128), (4096, 24), (8192, 16), (16384, 8),
+                                 (32768, 8)])
 def test_fx_warp_fstages_delay_model(cg, orc, N, K, monkeypatch):
-    """The warp four-step F stages other than N = 2048: N = 512 (a half-warp per
-    segment, 64-segment tiles: K = 40 a partial tile, K = 128 two full ones) and
+    """The warp four-step F stages other than N = 2048: N = 512 and 1024 (a
+    half-warp per segment, 16 or 32 points per lane; 64-segment tiles in FP16, 32
+    in FP32 at N = 1024: K = 40 a partial tile, K = 128 full ones) and
     N = 4096 ... 32768 (N/2048 warps per segment, each a 1024-point transform of
     every (N/2048)-th point, then radix-N/2048 columns and the real-FFT split in
     registers).  FP32 path against the oracle's FP32 path with the same delay
