@@ -314,7 +314,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="tc", choices=["tc", "fp32"])
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10,
+                    help="timed end-to-end calls (their mean: single calls over the CPU-GPU link vary by a few ms)")
     ap.add_argument("--cpu-segments", type=int, default=64,
                     help="segments per step of the reference arm (--impl reference)")
     ap.add_argument("--cpu-baseline-segments", type=int, default=1024,
@@ -399,7 +400,8 @@ def main():
         pin_vis = torch.empty((C_run, P_run), dtype=torch.complex64).pin_memory()
         raw_np, vis_np = pin_raw.numpy(), pin_vis.numpy()
         hparams = cg.fx_params(S_run, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
-        cg.fx_correlate(hparams, raw_np, vis_np)
+        for _ in range(max(1, args.warmup)):         # the first call sizes the workspace
+            cg.fx_correlate(hparams, raw_np, vis_np)
         barrier()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record()
