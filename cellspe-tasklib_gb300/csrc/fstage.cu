@@ -1,6 +1,17 @@
 // K-a + K-b + K-c fused: the FX F stage.
 //
-// One CTA takes G consecutive segments of one input.  For each segment a
+// Every kernel here decodes the 2-bit samples, transforms each segment (the
+// N-point real FFT as an M = N/2-point complex FFT of z[n] = x[2n] + i x[2n+1]
+// and a split), applies the channel phasor and scale, and writes FP32 or FP16
+// spectra for the X stage.  Which kernel runs (cs_fx_fstage):
+//   N = 512      k_fx_fstage_w512    a half-warp per segment, 16 points per lane
+//   N = 1024     k_fx_fstage_w1024   a half-warp per segment, 32 points per lane
+//   N = 2048     k_fx_fstage_w2048   a warp per segment (five CTA schedules, timed)
+//   N >= 4096    k_fx_fstage_wbig    N/2048 warps per segment, segment-major out
+//                                    (cs_spectra_transpose makes the X-stage rows)
+//   MSB-first input, or CELLSPE_FSTAGE_GENERIC=1: k_fx_fstage, described next.
+//
+// k_fx_fstage: one CTA takes G consecutive segments of one input.  For each segment a
 // group of M/16 threads (M = N/2) decodes the 2-bit samples straight into
 // registers (LUT), runs the M-point complex FFT of z[n] = x[2n] + i x[2n+1]
 // in shared memory, splits it into the N/2 channels of the real FFT (the
