@@ -9,39 +9,55 @@
 //   (DataUnpackers.cpp:244-288, intended behaviour; the reference masks
 //   0xC0 for every sample, an out-of-range read for samples 1..3).
 //
-// Each thread reads one 16-byte vector (64 fields) and writes whole float4
-// runs per channel, so loads and stores are 128-bit and coalesced.
+// A warp takes 512 raw bytes (32 16-byte vectors, one coalesced load each),
+// parks them in shared memory and writes every channel's float4 runs so that
+// one store instruction covers 512 contiguous output bytes: the bytes holding
+// sample times 4q..4q+3 of all channels (nchan bytes) feed run q, lane q mod 32.
+// Levels come from register selects on the code's two bits, not from an
+// indexed table load.
 #include "common.cuh"
 #include "kernels.h"
 
 struct Lut4 { float v[4]; };
 
 template <int NCH, bool MSB>
-__global__ void __launch_bounds__(256) k_unpack2bit(const uint4* __restrict__ raw, int64_t nvec,
+__global__ void __launch_bounds__(256) k_unpack2bit(const uint4* __restrict__ raw, int64_t nblk,
                                                     float* __restrict__ out, int64_t nsamp, Lut4 lut)
 {
     constexpr int TPV = 64 / NCH;   // sample times per 16-byte vector
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nvec) return;
-    uint4 q = __ldg(raw + i);
-    uint32_t w[4] = {q.x, q.y, q.z, q.w};
-    int64_t t0 = i * TPV;
+    constexpr int NQ = 16 / NCH;    // float4 runs per channel and lane
+    __shared__ uint4 stage[8][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t blk = (int64_t)blockIdx.x * 8 + wid;   // warp block: 512 bytes, 32 * TPV sample times
+    if (blk >= nblk) return;                              // whole warps leave together
+    const float L0 = lut.v[0], L1 = lut.v[1], L2 = lut.v[2], L3 = lut.v[3];
+    const uint4 v = __ldg(raw + blk * 32 + lane);
+    if constexpr (NCH < 16) {
+        stage[wid][lane] = v;
+        __syncwarp();
+    }
+    const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage[wid]);
+    float* o = out + blk * 32 * TPV;
 #pragma unroll
-    for (int c = 0; c < NCH; c++) {
-        float vals[TPV];
+    for (int j = 0; j < NQ; j++) {
+        const int q = j * 32 + lane;                      // run: sample times 4q..4q+3 of the block
+        uint32_t w[4] = {0u, 0u, 0u, 0u};
+        if constexpr (NCH == 16) { w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w; }
+        else if constexpr (NCH == 8) { uint2 x = reinterpret_cast<const uint2*>(sb)[q]; w[0] = x.x; w[1] = x.y; }
+        else if constexpr (NCH == 4) w[0] = reinterpret_cast<const uint32_t*>(sb)[q];
+        else if constexpr (NCH == 2) w[0] = reinterpret_cast<const uint16_t*>(sb)[q];
+        else w[0] = sb[q];
 #pragma unroll
-        for (int t = 0; t < TPV; t++) {
-            int f = t * NCH + c;              // field index inside the vector
-            vals[t] = lut.v[code2(w[f >> 4], f & 15, MSB)];
-        }
-        float* o = out + (int64_t)c * nsamp + t0;
-        if constexpr (TPV % 4 == 0) {
+        for (int c = 0; c < NCH; c++) {
+            float r[4];
 #pragma unroll
-            for (int t = 0; t < TPV; t += 4)
-                *reinterpret_cast<float4*>(o + t) = make_float4(vals[t], vals[t + 1], vals[t + 2], vals[t + 3]);
-        } else {
-#pragma unroll
-            for (int t = 0; t < TPV; t++) o[t] = vals[t];
+            for (int u = 0; u < 4; u++) {
+                const int f = u * NCH + c;                // field index inside the nchan-byte chunk
+                const uint32_t code = code2(w[f >> 4], f & 15, MSB);
+                const float lo = (code & 1u) ? L1 : L0, hi = (code & 1u) ? L3 : L2;
+                r[u] = (code & 2u) ? hi : lo;
+            }
+            *reinterpret_cast<float4*>(o + (int64_t)c * nsamp + 4 * q) = make_float4(r[0], r[1], r[2], r[3]);
         }
     }
 }
@@ -63,11 +79,11 @@ __global__ void k_unpack2bit_scalar(const uint8_t* __restrict__ raw, int64_t t_b
 }
 
 template <int NCH, bool MSB>
-static void launch_vec(const void* raw, int64_t nvec, float* out, int64_t nsamp, Lut4 lut, cudaStream_t st)
+static void launch_vec(const void* raw, int64_t nblk, float* out, int64_t nsamp, Lut4 lut, cudaStream_t st)
 {
-    if (nvec <= 0) return;
-    int64_t blocks = (nvec + 255) / 256;
-    k_unpack2bit<NCH, MSB><<<(unsigned)blocks, 256, 0, st>>>((const uint4*)raw, nvec, out, nsamp, lut), cs_count_launches(1);
+    if (nblk <= 0) return;
+    int64_t blocks = (nblk + 7) / 8;
+    k_unpack2bit<NCH, MSB><<<(unsigned)blocks, 256, 0, st>>>((const uint4*)raw, nblk, out, nsamp, lut), cs_count_launches(1);
 }
 
 int cs_unpack2bit(const void* raw, int64_t nsamp, int nchan, int msb_first, const float lut4[4],
@@ -80,18 +96,18 @@ int cs_unpack2bit(const void* raw, int64_t nsamp, int nchan, int msb_first, cons
     const int tpv = 64 / nchan;
     bool aligned = ((uintptr_t)raw % 16 == 0) && ((uintptr_t)out % 16 == 0) &&
                    (nsamp % 4 == 0 || tpv < 4);
-    int64_t nvec = aligned ? nsamp / tpv : 0;
-    if (nvec > 0) {
-        if (msb_first) launch_vec<1, true>(raw, nvec, out, nsamp, lut, st);
+    int64_t nblk = aligned ? nsamp / tpv / 32 : 0;   // whole 512-byte warp blocks
+    if (nblk > 0) {
+        if (msb_first) launch_vec<1, true>(raw, nblk, out, nsamp, lut, st);
         else switch (nchan) {
-            case 1: launch_vec<1, false>(raw, nvec, out, nsamp, lut, st); break;
-            case 2: launch_vec<2, false>(raw, nvec, out, nsamp, lut, st); break;
-            case 4: launch_vec<4, false>(raw, nvec, out, nsamp, lut, st); break;
-            case 8: launch_vec<8, false>(raw, nvec, out, nsamp, lut, st); break;
-            default: launch_vec<16, false>(raw, nvec, out, nsamp, lut, st); break;
+            case 1: launch_vec<1, false>(raw, nblk, out, nsamp, lut, st); break;
+            case 2: launch_vec<2, false>(raw, nblk, out, nsamp, lut, st); break;
+            case 4: launch_vec<4, false>(raw, nblk, out, nsamp, lut, st); break;
+            case 8: launch_vec<8, false>(raw, nblk, out, nsamp, lut, st); break;
+            default: launch_vec<16, false>(raw, nblk, out, nsamp, lut, st); break;
         }
     }
-    int64_t t_begin = nvec * tpv;
+    int64_t t_begin = nblk * 32 * tpv;
     int64_t rem = (nsamp - t_begin) * nchan;
     if (rem > 0) {
         int64_t blocks = (rem + 255) / 256;
