@@ -139,15 +139,35 @@ __global__ void __launch_bounds__(256) k_cornerturn(const uint32_t* __restrict__
         uint4 q = __ldg(src + i);
         w[4 * i] = q.x; w[4 * i + 1] = q.y; w[4 * i + 2] = q.z; w[4 * i + 3] = q.w;
     }
+    if constexpr (NCH == 16) {
+        // Word t holds channel c at bits 2c; plane word c wants time t at bits 2t: a
+        // 16 x 16 transpose of 2-bit fields, done as four stages of masked swaps of
+        // 8-, 4-, 2- and 1-field blocks between words r and r + j.
 #pragma unroll
-    for (int c = 0; c < NCH; c++) {
-        uint32_t o = 0;
+        for (int s = 0; s < 4; s++) {
+            const int j = 8 >> s;
+            const uint32_t m = s == 0 ? 0x0000FFFFu : s == 1 ? 0x00FF00FFu : s == 2 ? 0x0F0F0F0Fu : 0x33333333u;
 #pragma unroll
-        for (int t = 0; t < 16; t++) {
-            int f = t * NCH + c;
-            o |= ((w[f >> 4] >> (2 * (f & 15))) & 3u) << (2 * t);
+            for (int r = 0; r < 16; r++) {
+                if (r & j) continue;
+                const uint32_t t = ((w[r] >> (2 * j)) ^ w[r + j]) & m;
+                w[r + j] ^= t;
+                w[r] ^= t << (2 * j);
+            }
         }
-        planes[(int64_t)c * plane_words + g] = o;
+#pragma unroll
+        for (int c = 0; c < 16; c++) planes[(int64_t)c * plane_words + g] = w[c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < NCH; c++) {
+            uint32_t o = 0;
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                int f = t * NCH + c;
+                o |= ((w[f >> 4] >> (2 * (f & 15))) & 3u) << (2 * t);
+            }
+            planes[(int64_t)c * plane_words + g] = o;
+        }
     }
 }
 

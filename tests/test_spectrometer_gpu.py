@@ -145,3 +145,28 @@ def test_spectrometer_config2_shape(cg, orc):
         ref, ref_b = orc.spectrometer(planes[c], N, 2, 2, K, 32, 32, 0.0, fs)
         assert np.linalg.norm(power[c] - ref) / np.linalg.norm(ref) < TOL
         assert np.linalg.norm(bins[c] - ref_b) / np.linalg.norm(ref_b) < TOL
+
+
+def test_spectrometer_interleaved_equals_planes_full_size(cg):
+    """The Mark5B spectrometer input at full size (16 subbands x 2^25 samples, 128 MiB in
+    device memory, N = 65536, overlap 2, cosine^2): the interleaved layout, which goes
+    through the on-device corner turn, gives the same spectra bit for bit as the
+    per-subband 2-bit planes built here from the same words with torch bit operations."""
+    import torch
+
+    nsub, N, T = 16, 65536, 1 << 25
+    K = T // N
+    g = torch.Generator(device="cuda").manual_seed(25)
+    raw = torch.randint(0, 256, (T * nsub // 4,), dtype=torch.uint8, device="cuda", generator=g)
+    words = raw.view(torch.int32).to(torch.int64)                # one 32-bit word per sample time
+    shifts = torch.arange(0, 8, 2, device="cuda", dtype=torch.int64)
+    planes = torch.cat([(((words >> (2 * c)) & 3).view(-1, 4) << shifts).sum(dim=1).to(torch.uint8)
+                        for c in range(nsub)])
+    del words
+    a = torch.zeros((nsub, 1, N // 2 + 1), dtype=torch.float32, device="cuda")
+    b = torch.zeros_like(a)
+    cg.spectrometer(cg.spec_params(N, 2, 2, K, 1, nsub, raw.numel()), raw, a)
+    cg.spectrometer(cg.spec_params(N, 2, 2, K, 1, nsub, planes.numel(), layout=cg.SPEC_PLANES), planes, b)
+    torch.cuda.synchronize()
+    assert torch.isfinite(a).all() and float(a.abs().max()) > 0
+    assert torch.equal(a, b)
