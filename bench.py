@@ -13,6 +13,10 @@ X stage through the engine's C ABI.
           input to the GPU and the visibilities back.
 * roofline: the dominant kernel's algorithmic rate, from CUDA events the
           library records on its own stream around each stage.
+* error : after the timed regions, the timed job's visibilities against the
+          FP64 oracle on a seeded subset of inputs x channels with the full K
+          (amplitude and phase error; the oracle is only the checker), and the
+          tensor-core path against the FP32 path over every product.
 * cpu_baseline: the FX path of the CPU oracle (restated genericAddProduct_32fc_conj
           X stage, radix-2 FFT standing in for the absent FFTW) on a bounded
           sample of the same inputs, all host threads.
@@ -175,21 +179,62 @@ def _time_calls(torch, fn, steps: int, warmup: int) -> float:
     return e0.elapsed_time(e1) / steps
 
 
-def run_configs(cg, torch, x_mode: int, with_cpu: bool):
+def vis_error(torch, raw, vis, Sx: int, Nx: int, Kx: int, n_inputs: int, n_chans: int, seed: int,
+              start_sample: int = 0, delay=None):
+    """Amplitude and phase error of channel-major visibilities [C][P] against the
+    FP64 oracle on a seeded subset of inputs x channels with the full K (the
+    accuracy check after the timed region; the oracle is the checker here).
+    delay = (shift, phase0, dphase) from the FP64 delay model, or None."""
+    import oracle
+
+    rng = np.random.default_rng(seed)
+    inputs = sorted(int(i) for i in rng.choice(Sx, size=n_inputs, replace=False))
+    chans = sorted(int(c) for c in rng.choice(Nx // 2, size=n_chans, replace=False))
+    sh, p0, dp = (None, None, None) if delay is None else (d[inputs] for d in delay)
+    t0 = time.perf_counter()
+    ref, autos = oracle.fx_vis_subset_f64(raw[inputs].cpu().numpy(), Nx, Kx, chans, start_sample, sh, p0, dp)
+    n = len(inputs)
+    pidx = [inputs[a] * (inputs[a] + 1) // 2 + inputs[b] for a in range(n) for b in range(a + 1)]
+    sel = vis[torch.as_tensor(chans, device=vis.device)][:, torch.as_tensor(pidx, device=vis.device)].cpu().numpy()
+    got = np.zeros((n, n, len(chans)), np.complex128)
+    q = 0
+    for a in range(n):
+        for b in range(a + 1):
+            got[a, b] = sel[:, q]
+            q += 1
+    err = oracle.vis_errors(got, ref, autos, Kx)
+    err.update({"subset": f"{n} inputs ({n * (n + 1) // 2} products) x {len(chans)} channels, full K={Kx}",
+                "reference": "FP64 oracle", "oracle_s": round(time.perf_counter() - t0, 1)})
+    return err
+
+
+def rel_all(torch, v, ref) -> float:
+    """Max over products (columns of [C][P]) of ||v - ref|| / ||ref|| over channels."""
+    num = torch.linalg.vector_norm(v - ref, dim=0)
+    den = torch.linalg.vector_norm(ref, dim=0)
+    return float((num / den).max())
+
+
+def run_configs(cg, torch, x_mode: int, with_cpu: bool, raw, vis_main):
     """The other benchmark configurations, measured beside the headline: the FP32
-    path on the headline job, the Mark5B spectrometer (payload and framed
-    recordings) and the 16-station delay-tracked job, each with its CPU rate."""
+    path on the headline job (same input; its error, and the tensor-core path's
+    error against it), the Mark5B spectrometer (payload and framed recordings)
+    and the 16-station delay-tracked job, each with its CPU rate and error."""
     out = {}
     # -- FP32 CUDA-core path on the headline job (tensor-core vs FP32 ratio)
     T = N * K
     g = torch.Generator(device="cuda").manual_seed(4)
-    raw = torch.randint(0, 256, (S, T // 4), dtype=torch.uint8, device="cuda", generator=g)
     vis = torch.empty((C, P), dtype=torch.complex64, device="cuda")
     p32 = cg.fx_params(S, N, K, T // 4, x_mode=cg.X_FP32, vis_order=cg.VIS_CHANNEL_MAJOR)
     ms = _time_calls(torch, lambda: cg.fx_correlate(p32, raw, vis), steps=3, warmup=1)
     out["fp32_path"] = {"value": S * T / (ms * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms,
-                        "workload": "same as the headline, x_mode = FP32 CUDA cores"}
-    del raw, vis
+                        "workload": "same job and input as the headline, x_mode = FP32 CUDA cores",
+                        "error": vis_error(torch, raw, vis, S, N, K, 16, 32, seed=K)}
+    if x_mode == cg.X_TC_FP16:
+        out["tc_vs_fp32_max_rel"] = rel_all(torch, vis_main, vis)
+    del vis
+
+    import synth
 
     # -- Mark5B spectrometer: 16 subbands x 2^25 samples, N = 65536, overlap 2, cosine^2, PCal
     nsub, nsamp, NS, fs = 16, 1 << 25, 65536, 32e6
@@ -219,8 +264,6 @@ def run_configs(cg, torch, x_mode: int, with_cpu: bool):
     del framed
     # the same samples as a VDIF recording: 32-byte headers per 8000-byte payload
     # (1024 Mbps, 16000 frames per second), every frame validated on the device
-    import synth
-
     nfv = -(-payload.numel() // 8000)
     mbps = int(fs * 2 * nsub / 1e6)
     hdr = synth.vdif_frames(np.zeros(nfv * 8000, np.uint8), 8000, nsub, mbps).reshape(nfv, 8032)[:, :32]
@@ -251,25 +294,35 @@ def run_configs(cg, torch, x_mode: int, with_cpu: bool):
     # -- 16-station dual-pol (32 inputs), N = 8192, K = 4096, cubic delay model, one subband
     S3, N3, K3 = 32, 8192, 4096
     T3 = N3 * K3
+    fs3, lo3, rho3 = 32e6, 8.4e9, 0.3
     margin = 1 << 17
-    raw3 = torch.randint(0, 256, (S3, (T3 + 2 * margin) // 4), dtype=torch.uint8, device="cuda", generator=g)
     rng = np.random.default_rng(3)
     poly = np.zeros((S3, 4))
     poly[:, 0] = rng.uniform(-2e-3, 2e-3, S3)
     poly[:, 1] = rng.uniform(-3e-6, 3e-6, S3)
     poly[:, 2] = rng.uniform(-1e-9, 1e-9, S3)
     poly[:, 3] = rng.uniform(-1e-12, 1e-12, S3)
+    raw3 = synth.device_delayed_stations(S3, N3, K3, poly, fs3, lo3, rho3, seed=33, margin=margin)
     dpoly = torch.from_numpy(poly).cuda()
     vis3 = torch.empty((N3 // 2, S3 * (S3 + 1) // 2), dtype=torch.complex64, device="cuda")
-    r3 = {"workload": "32 inputs, N=8192 (4096 channels), K=4096, cubic delay per input (a0 within +-2 ms), "
-                      "fs 32 MS/s, LO 8.4 GHz, one of 8 subbands"}
+    r3 = {"workload": "32 inputs, N=8192 (4096 channels), K=4096, cubic delay per input (a0 within +-2 ms, "
+                      "a1 within +-3 us/s), fs 32 MS/s, LO 8.4 GHz, one of 8 subbands; a sky signal (rho 0.3) "
+                      "delayed by the same model, so delay-corrected cross products are coherent"}
+    import oracle
+
+    delay = oracle.delay_state_f64(poly, N3, K3, fs3, lo3)
+    outs = {}
     for name, mode in (("tc", cg.X_TC_FP16), ("fp32", cg.X_FP32)):
         p3 = cg.fx_params(S3, N3, K3, raw3.shape[1], x_mode=mode, vis_order=cg.VIS_CHANNEL_MAJOR,
-                          start_sample=margin, fs_hz=32e6, lo_hz=8.4e9)
+                          start_sample=margin, fs_hz=fs3, lo_hz=lo3)
         ms3 = _time_calls(torch, lambda: cg.fx_correlate(p3, raw3, vis3, delay_poly=dpoly), steps=3, warmup=1)
-        r3[name] = {"value": S3 * T3 / (ms3 * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms3}
+        r3[name] = {"value": S3 * T3 / (ms3 * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms3,
+                    "error": vis_error(torch, raw3, vis3, S3, N3, K3, 8, 32, seed=16, start_sample=margin,
+                                       delay=delay)}
+        outs[name] = vis3.clone()
+    r3["tc_vs_fp32_max_rel"] = rel_all(torch, outs["tc"], outs["fp32"])
     out["fx_16station_delay"] = r3
-    del raw3, vis3
+    del raw3, vis3, outs
     torch.cuda.empty_cache()
     return out
 
@@ -322,6 +375,7 @@ def main():
                     help="segments of this arm's cpu_baseline sample (~11 s on 16 cores; 1 core: 1/16 of it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-error", action="store_true", help="skip the FP64 accuracy check of the timed job")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the FP32-path, spectrometer and delay-tracked measurements")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
@@ -454,12 +508,34 @@ def main():
                             if F_TRAFFIC_PER_SEGMENT and fk == "k_fx_fstage_w2048" else None),
                 "note": "F stage is bound by instruction issue and the shared-memory pipe (ncu), not HBM"}
 
+    # ---- accuracy of the timed job (after the timed regions) ----------------
+    # FP64 oracle on a seeded subset (16 inputs x 32 channels, full K) of this
+    # very run's visibilities; at rho = 0.02 the cross products sit below the
+    # 3-sigma noise floor, so the phase bar is also checked on the same shape at
+    # rho = 0.3 with K = 1024, where they rise above it.
+    error = None
+    if not args.no_error:
+        error = vis_error(torch, raw, vis, S_run, N_run, K_run, min(16, S_run), min(32, C_run), seed=K_run)
+        if S_run == S and N_run == N:
+            k_ph = min(K_run, 1024)
+            raw_ph = synth.device_stations(S_run, N_run * k_ph, 0.3, seed=40 + rank)
+            vis_ph = torch.empty((C_run, P_run), dtype=torch.complex64, device="cuda")
+            cg.fx_correlate(cg.fx_params(S_run, N_run, k_ph, raw_ph.shape[1], x_mode=x_mode,
+                                         vis_order=cg.VIS_CHANNEL_MAJOR), raw_ph, vis_ph)
+            ph = vis_error(torch, raw_ph, vis_ph, S_run, N_run, k_ph, 16, 32, seed=k_ph)
+            error["phase_check_rho0.3"] = {k: ph[k] for k in ("max_rel_amp", "max_phase_deg", "phase_cells",
+                                                               "cross_products_above_floor", "cross_products")}
+            error["phase_check_rho0.3"]["job"] = f"S={S_run}, N={N_run}, K={k_ph}, rho=0.3"
+            del raw_ph, vis_ph
+        error["bars"] = ("tensor-core: <= 1e-3 relative amplitude per product, <= 0.05 deg above the noise floor; "
+                         "FP32: <= 1e-5")
+
     serving = None
     if args.serve_seconds > 0:
         serving = run_serving(cg, torch, args.serve_seconds, 200.0, x_mode)
     configs = None
     if not args.no_configs and N_run == N and S_run == S:
-        configs = run_configs(cg, torch, x_mode, with_cpu=(rank == 0 and not args.no_cpu))
+        configs = run_configs(cg, torch, x_mode, (rank == 0 and not args.no_cpu), raw, vis)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -489,6 +565,7 @@ def main():
                     "d2h_bytes_per_step": int(C_run * P_run * 8), "ms_per_step": e2e_ms},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "error": error,
             "stages": stages,
             "clocks": clk.summary(),
             "serving": serving,

@@ -3,12 +3,16 @@
 Every .cu / .cpp under csrc/ is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` and linked
 into ``libcellspe_gpu.so`` next to this file (static CUDA runtime, C ABI of
-include/*.h).  Objects go to _build/ (git-ignored).  Rebuilds only what
-changed (by mtime against the sources and headers).
+include/*.h).  Objects go to _build/<host machine>/ (git-ignored), so objects
+of another host architecture are never linked; the library and the programs
+are relinked when the stamp of this host's last link is missing or older
+than an object.  Rebuilds only what changed (by mtime against the sources
+and headers).
 """
 from __future__ import annotations
 
 import os
+import platform
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -17,8 +21,9 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
-OUT = PKG / "_build"
+OUT = PKG / "_build" / platform.machine()
 LIB = PKG / "libcellspe_gpu.so"
+STAMP = OUT / "linked.stamp"            # this host's last link of LIB and the programs
 APPS = sorted((CSRC / "apps").glob("*.cpp"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -52,14 +57,16 @@ def _compile(src: Path, verbose_ptxas: bool) -> Path:
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
-    OUT.mkdir(exist_ok=True)
+    OUT.mkdir(parents=True, exist_ok=True)
     srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     deps = _headers()
     todo = [s for s in srcs if force or verbose_ptxas or _stale(OUT / (s.name + ".o"), s, deps)]
     with ThreadPoolExecutor(max_workers=max(2, min(len(todo) or 1, os.cpu_count() or 4))) as ex:
         list(ex.map(lambda s: _compile(s, verbose_ptxas), todo))
     objs = [OUT / (s.name + ".o") for s in srcs]
-    if force or todo or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
+    relink = (force or bool(todo) or not LIB.exists() or not STAMP.exists()
+              or any(o.stat().st_mtime > STAMP.stat().st_mtime for o in objs))
+    if relink:
         cmd = [NVCC, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -67,13 +74,15 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
             raise RuntimeError("link failed")
     for src in APPS:                 # entry-point programs linked against the library
         exe = PKG / src.stem
-        if force or not exe.exists() or exe.stat().st_mtime < max(src.stat().st_mtime, LIB.stat().st_mtime):
+        if relink or not exe.exists() or exe.stat().st_mtime < max(src.stat().st_mtime, LIB.stat().st_mtime):
             cmd = ["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
                    "-L", str(PKG), "-lcellspe_gpu", "-Wl,-rpath,$ORIGIN", "-lpthread"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 sys.stderr.write(r.stdout + r.stderr)
                 raise RuntimeError(f"link failed for {src.name}")
+    if relink:
+        STAMP.touch()
     return LIB
 
 

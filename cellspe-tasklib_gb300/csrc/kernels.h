@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/cellspe_gpu.h"
+
 #define CS_ERR_ARG 10001      // invalid argument (size, alignment, null)
 #define CS_ERR_UNSUPPORTED 10002
 
@@ -206,3 +208,11 @@ int cs_sincos(const float* arg, float2* cossin, int64_t n, int normalized, cudaS
 int cs_sincos_generator(float start, float inc, float2* cossin, int64_t n, cudaStream_t st);
 int cs_autocorr_acc(const float2* x, float2* acc, int64_t n, cudaStream_t st);
 int cs_reciprocal(const float* in, float* out, int64_t n, cudaStream_t st);
+
+// runtime.cpp: checks shared by entry points defined in other files ---------
+// The four levels that `format` (CELLSPE_LEVELS_*) or `custom` names; false
+// for an unknown table.
+bool cs_pick_levels(int format, const float* custom, float out[4]);
+// The argument checks every spectrometer entry point runs; 0 or a
+// CELLSPE_ERR_* code with the error text set ("who" names the caller).
+int cs_spec_check(const cellspe_spec_params* p, const char* who);

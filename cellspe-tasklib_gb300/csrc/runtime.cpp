@@ -994,6 +994,9 @@ int spec_check(const cellspe_spec_params* p, const char* who)
         return set_err(CELLSPE_ERR_ARG, w + ": fft_points must be a power of two in [1024, 65536]");
     if (p->overlap < 1 || p->ffts_per_spectrum < 1 || p->n_spectra < 1 || p->fft_points % (16 * p->overlap))
         return set_err(CELLSPE_ERR_ARG, w + ": bad overlap, ffts_per_spectrum or n_spectra");
+    // the phase-cal rotator is exp(-2 pi i offset n / fs): no rotator without a sample rate
+    if (p->pcal_tonebins > 0 && !(p->sample_rate_hz > 0))
+        return set_err(CELLSPE_ERR_ARG, w + ": phase-cal needs sample_rate_hz > 0");
     if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED) {
         if (nsub == 1) return set_err(CELLSPE_ERR_ARG, w + ": framed Mark5B input needs 4, 8 or 16 subbands");
         if (p->raw_bytes < 2 * M5B_FRAME) return set_err(CELLSPE_ERR_ARG, w + ": framed input shorter than two frames");
@@ -1617,6 +1620,8 @@ void worker_main(Slot* s)
 }  // namespace
 
 int cs_set_error(int code, const char* msg) { return set_err(code, msg ? msg : ""); }
+bool cs_pick_levels(int format, const float* custom, float out[4]) { return pick_levels(format, custom, out); }
+int cs_spec_check(const cellspe_spec_params* p, const char* who) { return spec_check(p, who); }
 
 // ===========================================================================
 // exported: task runtime

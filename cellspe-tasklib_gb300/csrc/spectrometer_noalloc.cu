@@ -69,15 +69,15 @@ int setup_device(int dev, NoallocPtrs* out)
     return 0;
 }
 
-// Same values as the host-built tables of the allocating path (FP64, rounded
-// to FP32).
+// The host-built tables of the allocating path, by the same FP64 formulas
+// rounded to FP32 (the device's FP64 cos/sin may differ from the host's in
+// the last bit of a double, which can move a rounded entry by one FP32 ulp).
 __global__ void k_fill_tables(float2* tw, float* win, int n, int window, float2* rot, int rotlen, double dphi)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        double sn, cs;
-        sincospi(-2.0 * (double)i / (double)n, &sn, &cs);
-        tw[i] = make_float2((float)cs, (float)sn);
+        const double a = -2.0 * M_PI * (double)i / (double)n;
+        tw[i] = make_float2((float)cos(a), (float)sin(a));
         float w = 1.f;
         if (window != 0) {
             double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
@@ -89,40 +89,28 @@ __global__ void k_fill_tables(float2* tw, float* win, int n, int window, float2*
     if (i < rotlen) rot[i] = make_float2((float)cos(dphi * (double)i), (float)sin(dphi * (double)i));
 }
 
-bool pow2i(long long n) { return n > 0 && (n & (n - 1)) == 0; }
-
 }  // namespace
 
 extern "C" int cellspe_spectrometer_noalloc(const cellspe_spec_params* p, const void* raw, float* power,
                                             void* pcal_bins, void* pcal_tones, void* stream)
 {
     if (!p || !raw || !power) return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: null argument");
+    // the checks cellspe_spectrometer runs, then the limits of this entry point
+    if (int rc = cs_spec_check(p, "spectrometer_noalloc")) return rc;
     if (p->memory != CELLSPE_MEM_DEVICE)
         return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: device memory only (memory = CELLSPE_MEM_DEVICE)");
     const int nsub = p->n_subbands;
-    if (!(nsub == 1 || nsub == 4 || nsub == 8 || nsub == 16))
-        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: n_subbands must be 1, 4, 8 or 16");
     if (p->input_layout == CELLSPE_SPEC_MARK5B_FRAMED || p->input_layout == CELLSPE_SPEC_VDIF_FRAMED)
         return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: framed input needs deframing scratch");
     if (nsub > 1 && p->input_layout != CELLSPE_SPEC_PLANES)
         return cs_set_error(CELLSPE_ERR_ARG,
                             "spectrometer_noalloc: needs CELLSPE_SPEC_PLANES input (the corner turn needs a raw-sized buffer)");
     const int N = p->fft_points;
-    if (!pow2i(N) || N < 1024 || N > CS_NOALLOC_MAX_N)
-        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: fft_points must be a power of two in [1024, 65536]");
-    if (p->overlap < 1 || p->ffts_per_spectrum < 1 || p->n_spectra < 1 || p->raw_bytes <= 0 ||
-        p->raw_bytes % (16 * nsub))
-        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: bad sizes");
     if (p->pcal_tonebins > 0 && (!pcal_bins || p->pcal_rotatorlen <= 0 || p->pcal_rotatorlen > CS_NOALLOC_MAX_N))
         return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: phase-cal needs pcal_bins and rotatorlen <= 65536");
-    static const float mk5b[4] = {-3.3359f, 1.0f, -1.0f, 3.3359f};
-    static const float twob[4] = {1.0f, -1.0f, 3.3359f, -3.3359f};
-    static const float offb[4] = {-3.336f, -1.0f, 1.0f, 3.336f};
-    const float* lut = p->custom_levels ? p->custom_levels
-                       : (p->levels & 0xff) == CELLSPE_LEVELS_MARK5B ? mk5b
-                       : (p->levels & 0xff) == CELLSPE_LEVELS_TWOBIT ? twob
-                       : (p->levels & 0xff) == CELLSPE_LEVELS_OFFSET_BINARY ? offb : nullptr;
-    if (!lut) return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: unknown level table");
+    float lut[4];
+    if (!cs_pick_levels(p->levels, p->custom_levels, lut))
+        return cs_set_error(CELLSPE_ERR_ARG, "spectrometer_noalloc: unknown level table");
 
     // Chunking: the default number of FFTs per partial, grown until the
     // partials (plus phase-cal partials) fit the static scratch.
@@ -166,7 +154,7 @@ extern "C" int cellspe_spectrometer_noalloc(const cellspe_spec_params* p, const 
     cudaStream_t st = (cudaStream_t)stream;
     const int rotlen = p->pcal_tonebins > 0 ? p->pcal_rotatorlen : 0;
     const int nfill = N > rotlen ? N : rotlen;
-    const double dphi = 2.0 * M_PI * (p->sample_rate_hz > 0 ? -p->pcal_offset_hz / p->sample_rate_hz : 0.0);
+    const double dphi = rotlen > 0 ? 2.0 * M_PI * (-p->pcal_offset_hz / p->sample_rate_hz) : 0.0;   // fs > 0 checked
     k_fill_tables<<<(nfill + 255) / 256, 256, 0, st>>>(ptrs.tw, ptrs.win, N, p->window, ptrs.rot, rotlen, dphi),
         cs_count_launches(1);
     cudaError_t e = cudaGetLastError();

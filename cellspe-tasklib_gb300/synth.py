@@ -14,6 +14,9 @@ it.  These generators produce the inputs of the benchmark configurations:
 * ``device_stations`` -- the same statistics as stations_offset_binary,
   generated on the GPU with torch (for the 512-input configuration whose
   4.3 G samples would take minutes on the host).
+* ``device_delayed_stations`` -- a sky signal seen through per-input cubic
+  geometric delays with fringe rotation (the 16-station configuration), so
+  that delay-corrected visibilities are coherent.
 * ``mark5b_frames`` / ``mark5b_fill`` -- a payload byte stream wrapped into
   Mark5B frames (16-byte header + 10000-byte payload) and fill-pattern
   (0x11223344) zones written over parts of payloads, the way a recorder marks
@@ -115,6 +118,76 @@ def device_stations(S: int, T: int, rho: float, seed: int, device="cuda", chunk:
             packed = (codes << shifts).sum(dim=-1, dtype=torch.uint8)
             out[s0:s1, t0 // 4 : (t0 + chunk) // 4] = packed
     return out
+
+
+def geometric_delay_state(poly, N: int, K: int, fs_hz: float, lo_hz: float):
+    """Per (input, segment) delay seen by the sky signal, in FP64.
+
+    tau(t) = sum_m poly[s, m] t^m at the segment centre t = (k N + N/2) / fs:
+    integer sample shift round(tau fs), fringe phase 2 pi (lo tau mod 1) and
+    the per-channel phase step 2 pi (fs / N) (tau - shift / fs) -- the delay
+    model the engine's header (cellspe_fx_correlate) defines.
+    """
+    poly = np.asarray(poly, np.float64)
+    t = (np.arange(K, dtype=np.float64) * N + N / 2) / fs_hz
+    tau = np.zeros((poly.shape[0], K))
+    for m in range(poly.shape[1] - 1, -1, -1):
+        tau = tau * t[None, :] + poly[:, m:m + 1]
+    shift = np.rint(tau * fs_hz).astype(np.int64)
+    cyc = lo_hz * tau
+    phase0 = 2 * np.pi * (cyc - np.floor(cyc))
+    dphase = 2 * np.pi * (fs_hz / N) * (tau - shift / fs_hz)
+    return shift, phase0, dphase
+
+
+def device_delayed_stations(S: int, N: int, K: int, poly, fs_hz: float, lo_hz: float, rho: float, seed: int,
+                            margin: int, device="cuda", chunk: int = 128):
+    """A common sky signal seen by S inputs through a delay model (torch uint8 [S][(N K + 2 margin) / 4]).
+
+    Each N-sample segment k is synthesised in the frequency domain: channel c
+    of input s carries sqrt(rho) S_k(c) exp(-i (phase0 + c dphase)) +
+    sqrt(1 - rho) n_{s,k}(c) (complex N(0,1) spectra, the sky at RF lo + c fs/N
+    delayed by tau_s(t_k)), is brought to the time domain by an inverse real
+    FFT, quantised to offset-binary 2-bit codes at +-0.98 sigma and written at
+    sample margin + k N + shift[s, k], where the delay model's segment k
+    starts.  The engine's delay correction therefore makes the inputs coherent
+    again (|V_ij| ~ 0.88 rho per sample); samples no segment covers are noise.
+    """
+    import torch
+
+    shift, phase0, dphase = geometric_delay_state(poly, N, K, fs_hz, lo_hz)
+    lo_s, hi_s = int(shift.min()), int(shift.max())
+    assert margin + lo_s >= 0 and margin + hi_s + N * K <= N * K + 2 * margin, "margin too small for the delays"
+    Tt = N * K + 2 * margin
+    assert Tt % 4 == 0
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    thr = torch.tensor([-THRESH, 0.0, THRESH], device=device)
+    codes = torch.bucketize(torch.randn((S, Tt), generator=g, device=device), thr, right=True).to(torch.uint8)
+    C = N // 2 + 1
+    c = torch.arange(C, dtype=torch.float64, device=device)
+    a, b = float(np.sqrt(rho)), float(np.sqrt(1.0 - rho))
+    sh_d = torch.from_numpy(shift).to(device)
+    p0_d = torch.from_numpy(phase0).to(device)
+    dp_d = torch.from_numpy(dphase).to(device)
+    n_idx = torch.arange(N, dtype=torch.int64, device=device)
+    for k0 in range(0, K, chunk):
+        k1 = min(K, k0 + chunk)
+        kc = k1 - k0
+        sky = torch.complex(torch.randn((kc, C), generator=g, device=device),
+                            torch.randn((kc, C), generator=g, device=device)) * (0.5 ** 0.5)
+        noise = torch.complex(torch.randn((S, kc, C), generator=g, device=device),
+                              torch.randn((S, kc, C), generator=g, device=device)) * (0.5 ** 0.5)
+        ph = p0_d[:, k0:k1, None] + c[None, None, :] * dp_d[:, k0:k1, None]          # FP64 phases
+        rot = torch.polar(torch.ones_like(ph), -ph).to(torch.complex64)
+        Y = a * sky[None] * rot + b * noise
+        x = torch.fft.irfft(Y, n=N, dim=-1) * float(np.sqrt(N))                      # ~N(0,1) per sample
+        q = torch.bucketize(x, thr, right=True).to(torch.uint8)
+        start = margin + (torch.arange(k0, k1, device=device) * N)[None, :] + sh_d[:, k0:k1]   # [S][kc]
+        idx = (start[:, :, None] + n_idx[None, None, :]).reshape(S, -1)
+        codes.scatter_(1, idx, q.reshape(S, -1))
+    shifts = torch.tensor([0, 2, 4, 6], dtype=torch.uint8, device=device)
+    return (codes.view(S, -1, 4) << shifts).sum(dim=-1, dtype=torch.uint8)
 
 
 MARK5B_FRAME = 10016

@@ -45,13 +45,13 @@ def _ptr(a: np.ndarray):
     return ctypes.c_void_p(a.ctypes.data)
 
 
-def build(with_ref: bool | None = None) -> None:
-    """Compile liboracle.so (always) and oracle/_ref (when the reference tree exists)."""
+def build(ref_tree: str | None = None) -> None:
+    """Compile liboracle.so (always) and oracle/_ref from the reference tree
+    ``ref_tree`` (else the CELLSPE_REFERENCE_TREE environment variable) when
+    one is given and exists; without one only the restatement is built."""
     subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
-    ref_tree = os.environ.get("CELLSPE_REFERENCE_TREE", "/root/reference")
-    if with_ref is None:
-        with_ref = Path(ref_tree).is_dir()
-    if with_ref:
+    ref_tree = ref_tree or os.environ.get("CELLSPE_REFERENCE_TREE")
+    if ref_tree and Path(ref_tree).is_dir():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref_tree}"], check=True)
 
 
@@ -60,7 +60,7 @@ def lib() -> ctypes.CDLL:
     if _lib is None:
         so = HERE / "liboracle.so"
         if not so.exists():
-            build(with_ref=False)
+            build()
         _lib = ctypes.CDLL(str(so))
         V, I, L = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
         _lib.orc_unpack2bit.argtypes = [V, L, I, I, V, V]
@@ -357,3 +357,75 @@ def delay_state_f64(poly: np.ndarray, N: int, K: int, fs_hz: float, lo_hz: float
 
 def tri_index(i: int, j: int) -> int:
     return i * (i + 1) // 2 + j
+
+
+def _decode_rows(raw_row: np.ndarray, first: np.ndarray, N: int, lut64: np.ndarray, msb_first: bool):
+    """Samples [len(first)][N] of one input whose segments start at sample first[k]."""
+    f = first[:, None] + np.arange(N, dtype=np.int64)[None, :]
+    b = raw_row[f >> 2]
+    sh = (6 - 2 * (f & 3)) if msb_first else (2 * (f & 3))
+    return lut64[(b >> sh.astype(np.uint8)) & 3]
+
+
+def fx_vis_subset_f64(raw_rows, N: int, K: int, channels, start_sample: int = 0, shift=None, phase0=None,
+                      dphase=None, lut=OFFSET_BINARY_LUT, msb_first: bool = False, chunk: int = 256):
+    """FP64 visibilities of a subset of inputs and channels, streamed over segments.
+
+    raw_rows: uint8 [n][bytes] -- the raw bytes of the chosen inputs (row a of
+    the result's inputs is raw_rows[a]); shift / phase0 / dphase: [n][K] rows
+    of the delay state of those inputs (or None).  Spectra are an exact DFT at
+    the chosen channels, X[c] = sum_t x[t] exp(-2 pi i c t / N) with the
+    argument reduced in integers, multiplied by exp(i (phase0 + c dphase)) as
+    the engine's model defines (fx_spectra_f64), and accumulated as
+    V[a][b][c] = sum_k X_a[k][c] conj(X_b[k][c]) for b <= a.  Memory stays at
+    one chunk of segments, so K = 4096 at N = 8192 is a few seconds per input.
+    Returns (V [n][n][len(channels)] complex128 with the lower triangle and the
+    diagonal filled, autos [n][len(channels)] float64).
+    """
+    raw_rows = np.ascontiguousarray(raw_rows, np.uint8)
+    n = raw_rows.shape[0]
+    ch = np.asarray(channels, np.int64)
+    t = np.arange(N, dtype=np.int64)
+    W = np.exp(-2j * np.pi * ((t[:, None] * ch[None, :]) % N) / N)           # [N][nc]
+    lut64 = np.asarray(lut, np.float32).astype(np.float64)
+    V = np.zeros((n, n, ch.size), np.complex128)
+    for k0 in range(0, K, chunk):
+        k1 = min(K, k0 + chunk)
+        ks = np.arange(k0, k1, dtype=np.int64)
+        X = np.empty((n, k1 - k0, ch.size), np.complex128)
+        for a in range(n):
+            first = start_sample + ks * N + (0 if shift is None else np.asarray(shift[a][k0:k1], np.int64))
+            X[a] = _decode_rows(raw_rows[a], first, N, lut64, msb_first) @ W
+            if phase0 is not None:
+                p0 = np.asarray(phase0[a][k0:k1], np.float64)[:, None]
+                dp = np.asarray(dphase[a][k0:k1], np.float64)[:, None]
+                X[a] *= np.exp(1j * (p0 + ch[None, :].astype(np.float64) * dp))
+        for a in range(n):
+            V[a, : a + 1] += np.einsum("kc,bkc->bc", X[a], np.conj(X[: a + 1]))
+    autos = np.stack([V[a, a].real for a in range(n)])
+    return V, autos
+
+
+def vis_errors(got, ref, autos, K: int):
+    """Errors of visibilities against an FP64 reference, the engine's bars.
+
+    got, ref: [n][n][nc] (lower triangle + diagonal used); autos: [n][nc].
+    * amplitude: max over products of ||got - ref||_2 / ||ref||_2 over channels;
+    * phase: max |arg(got conj(ref))| in degrees over (product, channel) whose
+      |ref| is above the thermal-noise floor 3 sqrt(V_aa V_bb / K);
+    * the number of cross products (b < a) with at least one channel above it.
+    """
+    n = ref.shape[0]
+    amp, ph, cross_cov, cells = 0.0, 0.0, 0, 0
+    for a in range(n):
+        for b in range(a + 1):
+            r, g = ref[a, b], got[a, b]
+            amp = max(amp, float(np.linalg.norm(g - r) / np.linalg.norm(r)))
+            floor = 3 * np.sqrt(autos[a] * autos[b] / K)
+            m = np.abs(r) > floor
+            if m.any():
+                ph = max(ph, float(np.degrees(np.abs(np.angle(g[m] * np.conj(r[m])))).max()))
+                cells += int(m.sum())
+                cross_cov += int(a != b)
+    return {"max_rel_amp": amp, "max_phase_deg": ph, "phase_cells": cells, "cross_products_above_floor": cross_cov,
+            "products": n * (n + 1) // 2, "cross_products": n * (n - 1) // 2}

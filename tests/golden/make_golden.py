@@ -21,9 +21,9 @@ oracle/_ref/, and this script calls them on the reference's own test inputs:
   indices (0..3 = VDIF lut entry, 4 = blanked 0.0).
 * minitest-cell.cpp:131-138 -- the MAC validation ramp
   (in1 = 0.5i - 0.5i*j, in2 = 0.15 i^2 - 0.25j, acc = 1 + 1.5j), run through
-  genericAddProduct_32fc and genericAddProduct_32fc_conj.
+  genericAddProduct_32fc, genericAddProduct_32fc_conj and genericMul_32fc.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py <reference tree>
 """
 import ctypes
 import sys
@@ -141,7 +141,10 @@ def vdif_cases():
 
 
 def main():
-    oracle.build(with_ref=True)
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference tree>")
+    oracle.build(sys.argv[1])
+    assert oracle.have_ref(), "oracle/_ref was not built"
     m5 = oracle.ref_mark5()
     out = {}
     for fmt, nch in [("Mark5B-512-16-2", 16), ("Mark5B-256-8-2", 8), ("Mark5B-128-4-2", 4)]:
@@ -169,7 +172,9 @@ def main():
     gen.ref_addproduct_32fc(a.ctypes.data, b.ctypes.data, acc.ctypes.data, n)
     accc = acc0.copy()
     gen.ref_addproduct_32fc_conj(a.ctypes.data, b.ctypes.data, accc.ctypes.data, n)
-    np.savez_compressed(HERE / "generic_mac.npz", a=a, b=b, acc0=acc0, mac=acc, mac_conj=accc)
+    mul = np.zeros(n, np.complex64)
+    gen.ref_mul_32fc(a.ctypes.data, b.ctypes.data, mul.ctypes.data, n)
+    np.savez_compressed(HERE / "generic_mac.npz", a=a, b=b, acc0=acc0, mac=acc, mac_conj=accc, mul=mul)
     print("golden vectors written to", HERE)
 
 

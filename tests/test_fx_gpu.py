@@ -120,16 +120,18 @@ def test_xf_lags_match_backward_fft(cg, orc):
     import synth
 
     S, N, K = 2, 1024, 512
-    raw = synth.stations_offset_binary(S, N * K, rho=0.2, lags=[0, 5], seed=21)
+    raw = synth.stations_offset_binary(S, N * K, rho=0.2, lags=[0, 6], seed=21)
     vis = np.zeros((3, N // 2), np.complex64)
     cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], vis_order=cg.VIS_BASELINE_MAJOR), raw, vis)
     lags = np.zeros_like(vis)
     cg.vis_lags(vis, lags, scale=1.0 / K)
     ref = np.fft.ifft(vis.astype(np.complex128), axis=1) * (N // 2) / K
     assert np.linalg.norm(lags - ref) / np.linalg.norm(ref) < 1e-5
-    # the 5-sample lag of station 1 appears at channel-lag index 5 (x_1(t) = c(t-5))
+    # x_1(t) = c(t - 6): V_10(k) = |C|^2 exp(-2 pi i k 6 / N) over the N/2 channels,
+    # whose backward transform peaks at lag index 6 / 2 = 3 (two samples per index)
     cross = lags[orc.tri_index(1, 0)]
-    assert int(np.argmax(np.abs(cross))) in (5 // 2, 5 // 2 + 1, (N // 2) - 5 // 2)
+    assert int(np.argmax(np.abs(cross))) == 3
+    assert np.abs(cross[3]) > 5 * np.abs(np.delete(cross, 3)).max()
 
 
 @pytest.mark.parametrize("mode", ["tc", "fp32"])

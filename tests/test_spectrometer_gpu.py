@@ -170,3 +170,49 @@ def test_spectrometer_interleaved_equals_planes_full_size(cg):
     torch.cuda.synchronize()
     assert torch.isfinite(a).all() and float(a.abs().max()) > 0
     assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("slope_deg", [5.0, 0.0])
+def test_pcal_unit_test_recipe_through_the_gpu(cg, slope_deg):
+    """The reference's phase-cal known answer (PCal.cpp:879-951) through
+    cellspe_spectrometer's phase-cal fold and tone transform: tones at
+    t * 1 MHz in a 16 MHz band (fs = 32 MS/s, offset 0, 32 bins, 16 tones) with
+    phase t * slope, data[n] = sum_t sin(pi n t spacing / bw + t slope); the
+    extracted tone t must read -90 deg + t slope within 0.1 deg.
+
+    The engine's input is 2-bit; the recipe's data is real-valued.  The fold
+    and the tone transform are linear in the samples, so the data go in as a
+    16-bit integer (2000 x data + 32768) split into eight base-4 digit planes,
+    each run as a 2-bit recording whose custom level table is that digit's
+    weight {0, 1, 2, 3} x 4^b; the eight tone sets add up to the tones of the
+    16-bit samples (rounding at 1/4000 of a tone amplitude; the constant
+    offset lands on the DC tone only, which has no phase and is not checked,
+    as in the reference)."""
+    import synth
+
+    fs, bw, spacing = 32e6, 16e6, 1e6
+    tb, ntones = 32, 16
+    N, K = 4096, 32
+    n = np.arange(N * K, dtype=np.float64)
+    data = np.zeros(n.size)
+    for t in range(ntones):
+        data += np.sin(np.pi * n * (t * spacing) / bw + t * np.pi * slope_deg / 180)
+    v = (np.rint(data * 2000.0) + 32768).astype(np.int64)
+    assert v.min() >= 0 and v.max() < 65536
+    tones = np.zeros(ntones, np.complex128)
+    for b in range(8):
+        digits = ((v >> (2 * b)) & 3).astype(np.uint8)
+        raw = synth.pack2bit(digits)
+        levels = (np.arange(4) * float(4 ** b)).astype(np.float32)
+        p = cg.spec_params(N, 1, 0, K, 1, 1, raw.size, layout=cg.SPEC_PLANES, tonebins=tb, rotatorlen=tb,
+                           ntones=ntones, offset_hz=0.0, fs_hz=fs)
+        p.custom_levels = levels.ctypes.data
+        power = np.zeros((1, 1, N // 2 + 1), np.float32)
+        bins = np.zeros((1, 1, tb), np.complex64)
+        tn = np.zeros((1, 1, ntones), np.complex64)
+        cg.spectrometer(p, raw, power, bins, tn)
+        tones += tn[0, 0]
+    phase = np.degrees(np.angle(tones[1:]))
+    expect = -90.0 + slope_deg * np.arange(1, ntones)
+    err = np.abs((phase - expect + 180) % 360 - 180)
+    assert err.max() < 0.1, err

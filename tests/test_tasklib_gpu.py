@@ -184,3 +184,151 @@ def test_unpack_task_per_channel_outputs(cg, orc, rt):
     assert rt.celldsp_executeTask(ctypes.byref(t)) == 0
     ref = orc.unpack2bit(raw, 256, 8, orc.MARK5B_LUT)
     assert all(np.array_equal(outs[c], ref[c]) for c in range(8))
+
+
+def test_mulc_addc_tasks(cg, rt):
+    """CELLDSP_TASK_MULC / ADDC (cellspe-tasklib-dsp.h:30-31: out = in1 * in2,
+    out = in1 + in2).  The reference's SPU loop accepts both without computing
+    (cellspe-tasklib.cpp:502-505); the product is the generic genericMul_32fc
+    (architecture.h:270-278), compiled from the reference for the golden
+    vector, and matches it bit for bit; the sum is one correctly rounded FP32
+    add per component."""
+    g = np.load(GOLD / "generic_mac.npz")
+    a, b = g["a"].copy(), g["b"].copy()
+    out = np.full_like(a, np.nan)
+    t = cg.new_task(cg.TASK_MULC)
+    cg.add_in(t, a); cg.add_in(t, b); cg.add_out(t, out)
+    assert rt.celldsp_executeTask(ctypes.byref(t)) == 0 and t.completed_flag == cg.TASK_OK
+    assert np.array_equal(out.view(np.uint32), g["mul"].view(np.uint32))
+    out = np.full_like(a, np.nan)
+    t = cg.new_task(cg.TASK_ADDC)
+    cg.add_in(t, a); cg.add_in(t, b); cg.add_out(t, out)
+    assert rt.celldsp_executeTask(ctypes.byref(t)) == 0 and t.completed_flag == cg.TASK_OK
+    ref = (a.view(np.float32) + b.view(np.float32)).view(np.complex64)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def _difx_expect(x, mult, nch, band_off_pts, auto0):
+    X = np.concatenate([np.fft.fft(x.astype(np.complex128)), np.zeros(band_off_pts + nch, np.complex128)])
+    band = X[band_off_pts:band_off_pts + nch] * mult[:nch]
+    return band, auto0 + np.abs(band) ** 2
+
+
+def test_difx_process_upper_sideband(cg, rt):
+    """exec_difxprocess with useUpperOrLower = 1 (cellspe-tasklib-dsp.cpp:663-668):
+    the band starts outputvector_lengths[0] bytes into the FFT output.  As a
+    task whose output 0 holds numchannels points that is the upper half of the
+    FFT, X[nch .. 2 nch); through speDIFX_process, whose output 0 holds
+    numchannels + 4 points (:334-338), the reference's window runs 4 points
+    past the FFT, which read as zeros here."""
+    rng = np.random.default_rng(3)
+    nch = 64
+    nfft = 2 * nch
+    x = (rng.standard_normal(nfft) + 1j * rng.standard_normal(nfft)).astype(np.complex64)
+    mult = np.exp(1j * rng.uniform(0, 6.28, nch + 4)).astype(np.complex64)
+    # the task form: output 0 of numchannels points -> the upper half
+    fftout = np.zeros(nch, np.complex64)
+    conj = np.zeros(nch, np.complex64)
+    auto = np.full(nch, 0.25, np.complex64)
+    t = cg.new_task(cg.TASK_DIFXPROCESS)
+    cg.add_in(t, x); cg.add_in(t, mult[:nch].copy())
+    cg.add_out(t, fftout); cg.add_out(t, conj); cg.add_out(t, auto)
+    t.subcontext[0] = nfft
+    t.subcontext[2] = 1            # useUpperOrLower
+    t.subcontext[3] = nfft         # twicenumchannels
+    t.subcontext[4] = nch          # numchannels
+    assert rt.celldsp_executeTask(ctypes.byref(t)) == 0 and t.completed_flag == cg.TASK_OK
+    band, acc = _difx_expect(x, mult, nch, nch, 0.25)
+    assert np.linalg.norm(fftout - band) / np.linalg.norm(band) < 1e-5
+    assert np.allclose(auto.real, acc, rtol=1e-5)
+    # the wrapper form: window at (nch + 4) points
+    fftout = np.zeros(nch + 4, np.complex64)
+    conj = np.zeros(nch + 4, np.complex64)
+    auto = np.full(nch + 4, 0.5, np.complex64)
+    assert rt.speDIFX_process(x.ctypes.data, mult.ctypes.data, fftout.ctypes.data, conj.ctypes.data,
+                              auto.ctypes.data, nfft, nfft, 1) == 0
+    band, acc = _difx_expect(x, mult, nch, nch + 4, 0.5)
+    assert np.linalg.norm(fftout[:nch] - band) / np.linalg.norm(band) < 1e-5
+    assert np.allclose(auto[:nch].real, acc, rtol=1e-5)
+
+
+def test_rfft_task(cg, rt):
+    """CELLDSP_TASK_RFFT: rows of N reals -> N/2+1 bins each (genericFFTexec_R,
+    architecture.h:563-600: FFTW r2c, forward, unscaled)."""
+    rng = np.random.default_rng(4)
+    for n, rows in ((64, 3), (4096, 5)):
+        x = rng.standard_normal((rows, n)).astype(np.float32)
+        out = np.zeros((rows, n // 2 + 1), np.complex64)
+        t = cg.new_task(cg.TASK_RFFT)
+        cg.add_in(t, x); cg.add_out(t, out)
+        t.subcontext[0] = n
+        assert rt.celldsp_executeTask(ctypes.byref(t)) == 0 and t.completed_flag == cg.TASK_OK
+        ref = np.fft.rfft(x.astype(np.float64), axis=1)
+        assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-5
+
+
+def test_xmac_task(cg, rt):
+    """CELLDSP_TASK_XMAC: V_ij = sum_k X_i conj(X_j) over precomputed spectra
+    (genericAddProduct_32fc_conj, architecture.h:427-433, for every product),
+    then once more with accumulate set (read-modify-write output)."""
+    rng = np.random.default_rng(5)
+    S, C, K = 6, 4, 40
+    spec = (rng.standard_normal((C, S, K)) + 1j * rng.standard_normal((C, S, K))).astype(np.complex64)
+    P = S * (S + 1) // 2
+    vis = np.zeros((C, P), np.complex64)
+    prm = cg.XmacParams(S, C, K, 0)
+    t = cg.new_task(cg.TASK_XMAC)
+    cg.add_in_struct(t, prm); cg.add_in(t, spec); cg.add_out(t, vis)
+    assert rt.celldsp_executeTask(ctypes.byref(t)) == 0 and t.completed_flag == cg.TASK_OK
+    X = spec.astype(np.complex128)
+    ii, jj = np.tril_indices(S)
+    order = np.argsort(ii * (ii + 1) // 2 + jj)
+    ref = np.einsum("csk,ctk->cst", X, np.conj(X))[:, ii[order], jj[order]]
+    assert np.linalg.norm(vis - ref) / np.linalg.norm(ref) < 1e-5
+    prm2 = cg.XmacParams(S, C, K, 1)
+    t = cg.new_task(cg.TASK_XMAC)
+    cg.add_in_struct(t, prm2); cg.add_in(t, spec); cg.add_out(t, vis)
+    assert rt.celldsp_executeTask(ctypes.byref(t)) == 0
+    assert np.linalg.norm(vis - 2 * ref) / np.linalg.norm(2 * ref) < 1e-5
+
+
+def test_continuable_tasks(cg, rt):
+    """celldsp_startContinuableTask / continueTask / stopContinuableTask
+    (cellspe-tasklib.cpp:364-412): the first task reserves a slot and runs
+    there, later tasks run on the same slot, stop frees it and sets -1.  A
+    failing first task frees the slot again and returns 1 (!vecNoErr)."""
+    n = 512
+    init = cg.new_task(cg.TASK_FFT_INIT)
+    init.subcontext[0] = n
+    spe = ctypes.c_int(-1)
+    assert rt.celldsp_startContinuableTask(ctypes.byref(init), ctypes.byref(spe)) == 0
+    assert 0 <= spe.value < cg.MAX_SLOTS
+    rng = np.random.default_rng(6)
+    for _ in range(3):
+        x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+        out = np.zeros_like(x)
+        t = cg.new_task(cg.TASK_FFT_EXEC)
+        cg.add_in(t, x); cg.add_out(t, out)
+        t.subcontext[0] = n
+        assert rt.celldsp_continueTask(ctypes.byref(t), ctypes.byref(spe)) == 0
+        ref = np.fft.fft(x.astype(np.complex128))
+        assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-5
+    # an FFT_EXEC of another length than the slot was prepared for fails
+    bad = cg.new_task(cg.TASK_FFT_EXEC)
+    xb = np.zeros(256, np.complex64)
+    cg.add_in(bad, xb); cg.add_out(bad, xb)
+    bad.subcontext[0] = 256
+    assert rt.celldsp_continueTask(ctypes.byref(bad), ctypes.byref(spe)) == 1
+    assert rt.celldsp_stopContinuableTask(ctypes.byref(spe)) == 0 and spe.value == -1
+    # a first task that fails leaves no slot reserved
+    before = [rt.celldsp_getFreeSPE() for _ in range(cg.MAX_SLOTS)]
+    for s in before:
+        rt.celldsp_setFreeSPE(s)
+    init_bad = cg.new_task(cg.TASK_FFT_INIT)
+    init_bad.subcontext[0] = 3                           # not a power of two
+    spe2 = ctypes.c_int(-1)
+    assert rt.celldsp_startContinuableTask(ctypes.byref(init_bad), ctypes.byref(spe2)) == 1
+    after = [rt.celldsp_getFreeSPE() for _ in range(cg.MAX_SLOTS)]
+    assert sorted(after) == list(range(cg.MAX_SLOTS))
+    for s in after:
+        rt.celldsp_setFreeSPE(s)
