@@ -7,7 +7,9 @@ include/*.h).  Objects go to _build/<host machine>/ (git-ignored), so objects
 of another host architecture are never linked; the library and the programs
 are relinked when the stamp of this host's last link is missing or older
 than an object.  Rebuilds only what changed (by mtime against the sources
-and headers).
+and headers).  The swspectrometer plug-in (taskcore/: TaskCoreCUDA and its
+in-memory dispatcher) is host C++ over that library's C ABI, built with g++
+into libcellspe_taskcore.so.
 """
 from __future__ import annotations
 
@@ -25,6 +27,8 @@ OUT = PKG / "_build" / platform.machine()
 LIB = PKG / "libcellspe_gpu.so"
 STAMP = OUT / "linked.stamp"            # this host's last link of LIB and the programs
 APPS = sorted((CSRC / "apps").glob("*.cpp"))
+TASKCORE = PKG / "taskcore"
+TASKCORE_LIB = PKG / "libcellspe_taskcore.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"),
@@ -81,6 +85,18 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
             if r.returncode != 0:
                 sys.stderr.write(r.stdout + r.stderr)
                 raise RuntimeError(f"link failed for {src.name}")
+    # the swspectrometer plug-in (TaskCoreCUDA) and its in-memory dispatcher,
+    # compiled against the stand-in spectrometer headers
+    tc_srcs = sorted(TASKCORE.glob("*.cpp"))
+    tc_deps = tc_srcs + list(TASKCORE.glob("*.h")) + list((TASKCORE / "compat").glob("*.h")) + [LIB]
+    if relink or not TASKCORE_LIB.exists() or TASKCORE_LIB.stat().st_mtime < max(d.stat().st_mtime for d in tc_deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", str(TASKCORE / "compat"),
+               "-I", str(TASKCORE), "-I", str(ROOT / "include"), *map(str, tc_srcs), "-o", str(TASKCORE_LIB),
+               "-L", str(PKG), "-lcellspe_gpu", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("build failed for libcellspe_taskcore.so")
     if relink:
         STAMP.touch()
     return LIB

@@ -137,6 +137,55 @@ def declared_functions() -> list[str]:
     return sorted(set(names))
 
 
+TASKCORE_LIB_PATH = PKG / "libcellspe_taskcore.so"
+_taskcore = None
+
+
+class TaskcoreConfig(ctypes.Structure):
+    """cellspe_taskcore_config (taskcore/cellspe_taskcore.h)."""
+    _fields_ = [("num_cores", ctypes.c_int), ("fft_points", ctypes.c_int), ("integ_seconds", ctypes.c_double),
+                ("overlap", ctypes.c_int), ("window", ctypes.c_int), ("source_channels", ctypes.c_int),
+                ("channel1", ctypes.c_int), ("channel2", ctypes.c_int), ("channelorder_increasing", ctypes.c_int),
+                ("sourceformat", ctypes.c_int), ("samplingfreq", ctypes.c_double), ("extract_pcal", ctypes.c_int),
+                ("pcal_offset_hz", ctypes.c_double), ("pcal_harmonics_hz", ctypes.c_double),
+                ("num_sources", ctypes.c_int), ("calc_xpol", ctypes.c_int), ("max_rawbuf_bytes", ctypes.c_longlong)]
+
+
+def taskcore_lib() -> ctypes.CDLL:
+    """libcellspe_taskcore.so: the TaskCoreCUDA plug-in and its in-memory dispatcher."""
+    global _taskcore
+    if _taskcore is None:
+        if not TASKCORE_LIB_PATH.exists():
+            raise CellspeError(ERR_CUDA, f"{TASKCORE_LIB_PATH.name} is not built; run __graft_entry__.build()")
+        L = ctypes.CDLL(str(TASKCORE_LIB_PATH))
+        V, LLP = ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)
+        L.cellspe_taskcore_spectrometer.argtypes = [V, V, V, ctypes.c_longlong, ctypes.POINTER(V), LLP, LLP, LLP]
+        L.cellspe_taskcore_spectrometer.restype = ctypes.c_int
+        L.cellspe_taskcore_last_error.restype = ctypes.c_char_p
+        _taskcore = L
+    return _taskcore
+
+
+def taskcore_spectrometer(cfg: TaskcoreConfig, src0: np.ndarray, src1=None, sink_bytes=(0, 0, 0, 0, 0)):
+    """Runs cellspe_taskcore_spectrometer on host recordings; returns (sinks as uint8 arrays, spectra count)."""
+    L = taskcore_lib()
+    src0 = np.ascontiguousarray(src0, np.uint8)
+    if src1 is not None:
+        src1 = np.ascontiguousarray(src1, np.uint8)
+        assert src1.size == src0.size
+    sinks = [np.zeros(max(int(n), 1), np.uint8) for n in sink_bytes]
+    ptrs = (ctypes.c_void_p * 5)(*[s.ctypes.data if n else None for s, n in zip(sinks, sink_bytes)])
+    caps = (ctypes.c_longlong * 5)(*[int(n) for n in sink_bytes])
+    used = (ctypes.c_longlong * 5)()
+    nspec = ctypes.c_longlong()
+    rc = L.cellspe_taskcore_spectrometer(ctypes.byref(cfg), src0.ctypes.data,
+                                         src1.ctypes.data if src1 is not None else None, src0.size, ptrs, caps,
+                                         used, ctypes.byref(nspec))
+    if rc != 0:
+        raise CellspeError(ERR_CUDA, L.cellspe_taskcore_last_error().decode())
+    return [s[: used[i]] for i, s in enumerate(sinks)], nspec.value
+
+
 def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
@@ -170,6 +219,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_spectrometer": ([V, V, V, V, V], I),
             "cellspe_spectrometer_workspace_bytes": ([V], LL),
             "cellspe_spectrometer_noalloc": ([V, V, V, V, V, V], I),
+            "cellspe_accumulate_f32": ([V, V, LL, I], I),
             "cellspe_mark5b_decode": ([V, LL, I, LL, V, I, V], I),
             "cellspe_spectrometer_xpol": ([V, V, V, I, I, V, V, V], I),
             "cellspe_mark5b_deframe": ([V, LL, I, LL, V, V, I, V], I),

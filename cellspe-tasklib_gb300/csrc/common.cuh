@@ -13,6 +13,30 @@
 
 #define CS_DEV __device__ __forceinline__
 
+// Window weight of sample i of an n-point FFT for the spectrometer's window
+// types, which are the reference's WindowFunctionType (spectrometer
+// Settings.h: 0 None, 1 Cosine, 2 Cosine2, 3 Hamming, 4 Hann, 5 Blackman), in
+// FP64 (callers round to FP32).  Cosine and Cosine2 are
+// TaskCoreIPP::generate_windowfunction's own loops (TaskCoreIPP.cpp:569-605,
+// i and n rounded to FP32 in the argument); Hamming, Hann and Blackman are the
+// IPP windows it calls (ippsWinHamming_32f_I, ippsWinHann_32f_I,
+// ippsWinBlackman_32f_I with alpha 0.5), from IPP's published definitions
+// with x = 2 pi i / (n - 1): 0.54 - 0.46 cos x; 0.5 - 0.5 cos x;
+// (alpha + 1)/2 - 0.5 cos x - (alpha/2) cos 2x.  Any other type is 1.0.
+__host__ __device__ inline double cs_window_value(int type, int i, int n)
+{
+    if (type == 1 || type == 2) {
+        const double arg = 3.14159265358979323846 * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
+        const double c = cos(arg);
+        return type == 1 ? (double)(float)c : c * c;
+    }
+    const double x = 2.0 * 3.14159265358979323846 * (double)i / (double)(n - 1);
+    if (type == 3) return 0.54 - 0.46 * cos(x);
+    if (type == 4) return 0.5 - 0.5 * cos(x);
+    if (type == 5) return 0.75 - 0.5 * cos(x) - 0.25 * cos(2.0 * x);
+    return 1.0;
+}
+
 CS_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 CS_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 CS_DEV float2 cmul(float2 a, float2 b)

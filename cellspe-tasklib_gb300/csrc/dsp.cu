@@ -7,6 +7,8 @@
 //   SINCOS_NORM  {cos 2 pi x, sin 2 pi x}   exec_sincosnormalized (:874-977)
 //   SINCOS_GENERTR {cos, sin}(start + n*inc) exec_sincos_generator (:725-804)
 //   autocorrelation accumulate acc.re += |x|^2  do_complex_autocorrelation (:431-449)
+//   FADD     acc += x (floats)   ippsAdd_32f_I of TaskCoreIPP::combineResults
+//                                 (spectrometer/src/IA-32/TaskCoreIPP.cpp:311-349)
 // Each MAC/MUL keeps the reference's operand order and rounds every product
 // and sum separately (__fmul_rn/__fadd_rn stop the compiler from fusing them
 // into FMAs), so the FP32 results are bit-identical to the scalar generic
@@ -70,6 +72,12 @@ __global__ void k_autocorr(const float2* __restrict__ x, float2* __restrict__ ac
     acc[i] = a;
 }
 
+__global__ void k_fadd(const float* __restrict__ x, float* __restrict__ acc, int64_t n)
+{
+    int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x;
+    if (i < n) acc[i] = __fadd_rn(acc[i], x[i]);
+}
+
 __global__ void k_recip(const float* __restrict__ in, float* __restrict__ out, int64_t n)
 {
     int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x;
@@ -119,6 +127,13 @@ int cs_autocorr_acc(const float2* x, float2* acc, int64_t n, cudaStream_t st)
 {
     if (n <= 0) return n == 0 ? 0 : CS_ERR_ARG;
     k_autocorr<<<nblk(n), NT, 0, st>>>(x, acc, n), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+int cs_fadd(const float* x, float* acc, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return n == 0 ? 0 : CS_ERR_ARG;
+    k_fadd<<<nblk(n), NT, 0, st>>>(x, acc, n), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 

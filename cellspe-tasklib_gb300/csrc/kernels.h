@@ -208,6 +208,7 @@ int cs_sincos(const float* arg, float2* cossin, int64_t n, int normalized, cudaS
 int cs_sincos_generator(float start, float inc, float2* cossin, int64_t n, cudaStream_t st);
 int cs_autocorr_acc(const float2* x, float2* acc, int64_t n, cudaStream_t st);
 int cs_reciprocal(const float* in, float* out, int64_t n, cudaStream_t st);
+int cs_fadd(const float* x, float* acc, int64_t n, cudaStream_t st);      // acc += x
 
 // runtime.cpp: checks shared by entry points defined in other files ---------
 // The four levels that `format` (CELLSPE_LEVELS_*) or `custom` names; false

@@ -994,6 +994,8 @@ int spec_check(const cellspe_spec_params* p, const char* who)
         return set_err(CELLSPE_ERR_ARG, w + ": fft_points must be a power of two in [1024, 65536]");
     if (p->overlap < 1 || p->ffts_per_spectrum < 1 || p->n_spectra < 1 || p->fft_points % (16 * p->overlap))
         return set_err(CELLSPE_ERR_ARG, w + ": bad overlap, ffts_per_spectrum or n_spectra");
+    if (p->window < 0 || p->window > 5)
+        return set_err(CELLSPE_ERR_ARG, w + ": window must be 0 (none) .. 5 (Blackman)");
     // the phase-cal rotator is exp(-2 pi i offset n / fs): no rotator without a sample rate
     if (p->pcal_tonebins > 0 && !(p->sample_rate_hz > 0))
         return set_err(CELLSPE_ERR_ARG, w + ": phase-cal needs sample_rate_hz > 0");
@@ -2077,6 +2079,22 @@ int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memo
 {
     DIRECT_PROLOGUE
     return op_fft(*ws, memory == CELLSPE_MEM_HOST, in, out, n, batch, true);
+}
+
+int cellspe_accumulate_f32(float* acc, const float* add, long long n, int memory)
+{
+    DIRECT_PROLOGUE
+    if (!acc || !add || n < 0) return set_err(CELLSPE_ERR_ARG, "accumulate_f32: bad arguments");
+    if (n == 0) return 0;
+    const bool host = memory == CELLSPE_MEM_HOST;
+    Job j(*ws, host);
+    const float* d_add = (const float*)j.in(add, (size_t)n * 4);
+    float* d_acc = (float*)j.out(acc, (size_t)n * 4, true);
+    if (!j.err) {
+        int rc = map_rc(cs_fadd(d_add, d_acc, n, ws->stream), "accumulate_f32");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
 }
 
 int cellspe_vis_lags(const void* vis, void* lags, long long n_products, int n_channels, double scale, int memory)

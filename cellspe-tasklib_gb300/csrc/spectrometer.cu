@@ -55,12 +55,7 @@ const float* window_table(int type, int n)
     auto it = g_win.find(key);
     if (it != g_win.end()) return it->second;
     std::vector<float> h(n);
-    for (int i = 0; i < n; i++) {
-        if (type == 0) { h[i] = 1.f; continue; }
-        double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
-        double c = std::cos(arg);
-        h[i] = (type == 1) ? (float)c : (float)(c * c);
-    }
+    for (int i = 0; i < n; i++) h[i] = (float)cs_window_value(type, i, n);
     float* d = nullptr;
     if (cudaMalloc(&d, sizeof(float) * n) != cudaSuccess) return nullptr;
     cudaMemcpy(d, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice);

@@ -78,13 +78,7 @@ __global__ void k_fill_tables(float2* tw, float* win, int n, int window, float2*
     if (i < n) {
         const double a = -2.0 * M_PI * (double)i / (double)n;
         tw[i] = make_float2((float)cos(a), (float)sin(a));
-        float w = 1.f;
-        if (window != 0) {
-            double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
-            double c = cos(arg);
-            w = (window == 1) ? (float)c : (float)(c * c);
-        }
-        win[i] = w;
+        win[i] = (float)cs_window_value(window, i, n);
     }
     if (i < rotlen) rot[i] = make_float2((float)cos(dphi * (double)i), (float)sin(dphi * (double)i));
 }

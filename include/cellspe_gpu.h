@@ -90,6 +90,14 @@ int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memo
  * vis, lags: complex64 [P][C] (baseline-major), C a power of two <= 16384. */
 int cellspe_vis_lags(const void* vis, void* lags, long long n_products, int n_channels, double scale, int memory);
 
+/* ---- Spectrum accumulation ---------------------------------------------------
+ * acc[i] += add[i] for n floats on the GPU: the ippsAdd_32f_I / ippsAdd_32fc_I
+ * summation of TaskCoreIPP::combineResults (spectrometer/src/IA-32/
+ * TaskCoreIPP.cpp:311-349), used by the TaskCoreCUDA plug-in to add a core's
+ * sub-spectra into the dispatcher's common spectra.  Both pointers in the
+ * memory space `memory` names. */
+int cellspe_accumulate_f32(float* acc, const float* add, long long n, int memory);
+
 /* ---- K-d: X stage on precomputed spectra ----------------------------------
  * spectra complex64 [C][S][K] (FP32 mode) -> vis complex64 [C][P] (channel-major),
  * V_ij = sum_k X_i conj(X_j), j <= i, p = i(i+1)/2 + j.
@@ -196,7 +204,8 @@ void cellspe_service_destroy(cellspe_service* s);
 typedef struct {
     int    fft_points;        /* N: 1024 .. 65536                                  */
     int    overlap;           /* fft_overlap_factor                                */
-    int    window;            /* 0 none, 1 cosine, 2 cosine^2                       */
+    int    window;            /* WindowFunctionType: 0 none, 1 cosine, 2 cosine^2,
+                               * 3 Hamming, 4 Hann, 5 Blackman (alpha 0.5)          */
     int    ffts_per_spectrum; /* K non-overlapped FFTs per spectrum                 */
     int    n_spectra;
     int    n_subbands;        /* 1, 4, 8 or 16                                      */

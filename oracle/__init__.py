@@ -53,6 +53,16 @@ def build(ref_tree: str | None = None) -> None:
     ref_tree = ref_tree or os.environ.get("CELLSPE_REFERENCE_TREE")
     if ref_tree and Path(ref_tree).is_dir():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref_tree}"], check=True)
+        (REF_DIR / "reference_tree.txt").write_text(str(Path(ref_tree).resolve()))
+
+
+def reference_tree() -> Path | None:
+    """The reference tree oracle/_ref was built from (None where it was not built)."""
+    f = REF_DIR / "reference_tree.txt"
+    if not f.exists():
+        return None
+    p = Path(f.read_text().strip())
+    return p if p.is_dir() else None
 
 
 def lib() -> ctypes.CDLL:

@@ -372,13 +372,24 @@ int orc_spec_overlapped_ffts(const orc_spec_cfg* cfg)
     return cfg->overlap * cfg->ffts_per_spectrum - (cfg->overlap - 1);
 }
 
+/* TaskCoreIPP::generate_windowfunction (TaskCoreIPP.cpp:569-605): None,
+ * Cosine, Cosine2 as its loops; Hamming, Hann and Blackman (alpha 0.5) are
+ * IPP's ippsWin*_32f_I, restated from IPP's published definitions with
+ * x = 2 pi i / (n - 1) (IPP is absent: these three are not pinned). */
 void orc_spec_window(int type, int n, float* w)
 {
     for (int i = 0; i < n; i++) {
-        if (type == 0) { w[i] = 1.0f; continue; }
-        double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
-        double c = cos(arg);
-        w[i] = (type == 1) ? (float)c : (float)(c * c);
+        if (type == 1 || type == 2) {
+            double arg = M_PI * ((double)(float)i - 0.5 * (double)(float)n + 0.5) / (double)(float)n;
+            double c = cos(arg);
+            w[i] = (type == 1) ? (float)c : (float)(c * c);
+            continue;
+        }
+        double x = 2.0 * M_PI * (double)i / (double)(n - 1);
+        if (type == 3) w[i] = (float)(0.54 - 0.46 * cos(x));
+        else if (type == 4) w[i] = (float)(0.5 - 0.5 * cos(x));
+        else if (type == 5) w[i] = (float)(0.75 - 0.5 * cos(x) - 0.25 * cos(2.0 * x));
+        else w[i] = 1.0f;
     }
 }
 
