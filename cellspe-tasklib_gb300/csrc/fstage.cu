@@ -1398,6 +1398,10 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
         const char* e = getenv("CELLSPE_FSTAGE_TC");
         if (e && e[0] == '1') return cs_fx_fstage_tc(a, st);
     }
+    if (a.kblock && cs_fstage_tc32_supported(a)) {
+        const char* e = getenv("CELLSPE_FSTAGE_TC32");
+        if (e && e[0] == '1') return cs_fx_fstage_tc32(a, st);
+    }
     if (a.N == 2048 && !a.msb_first) {
         const bool ph = a.phase0 != nullptr;
         if (a.format == CS_SPECTRA_F32)

@@ -1,0 +1,611 @@
+// K-b/K-c on the tensor cores, 32-segment units: the FX F stage for N = 2048
+// with FP16 spectra written k-blocked (__half [C][S_out][kp/32][2][32], the
+// layout the tcgen05 X stage reads), for K and kp multiples of 32.
+//
+// The real 2048-point DFT X[c] = sum_n x[n] W_2048^(n c), c < 1024, as a
+// four-step transform with both passes on the tensor cores (FP16 operands,
+// FP32 accumulators in TMEM).  With n = n2 + 32 n1 (n1 < 64, n2 < 32) and
+// c = k1 + 64 k2:
+//     Y[k1][n2] = sum_n1 x[n2 + 32 n1] W_64^(n1 k1)        pass 1
+//     Z[k1][n2] = Y[k1][n2] W_2048^(n2 k1)                 CUDA cores
+//     X[k1 + 64 k2] = sum_n2 Z[k1][n2] W_32^(n2 k2)        pass 2
+// The input is real, so X[2048 - c] = conj(X[c]) and only k1 = 0..32 is
+// needed: pass 2 runs for k1 < 32 over all 32 k2 and gives the channels with
+// c mod 64 < 32 directly (k2 < 16) and those with c mod 64 > 32 as conj(X) of
+// the mirror bin (k2 >= 16); the 16 channels with c mod 64 = 32 come from the
+// k1 = 32 row (real Y) through one more pass-2 product per unit.  Per segment
+// the CUDA cores twiddle 1024 values instead of 2048.
+//
+// Work unit = 32 consecutive segments of one input, in 8 quads of 4
+// segments.  Per quad:
+//  * decode: 2-bit samples -> B1 (FP16, MN-major: K = n1, N = (segment, n2))
+//  * pass 1: D1 = A1 B1, A1 the constant DFT-64 rows (TMEM lane quarter q
+//    holds Re rows 32q..32q+7 and Im rows 32q+8..32q+15 of k1 = 8q..8q+7, and
+//    quarter 0 the k1 = 32 row in lanes 16..23), 128 x 128 x 64
+//  * epilogue 1: Z = Y W -> A2 (FP16, K-major rows (segment, k1), K = Re | Im
+//    of n2); the k1 = 32 values -> A2' (row = segment of the unit)
+//  * pass 2: D2 = A2 B2, B2 the constant DFT-32 as a real 64 x 64 operand
+//  * epilogue 2: delay / fringe phasor, channel scale, FP16 -> staging
+//    [segment][channel] (Re, Im) words
+// and per unit pass 2' (D2' = A2' B2) and its epilogue for the k1 = 32
+// channels, then the write-out: each (channel, input, 32-segment block) is one
+// 128-byte run (32 Re halves, 32 Im halves), written by the workers from the
+// staging with 16-byte stores, 4 lanes per 64-byte half-run.
+//
+// Warps 0..7 are the workers (decode, both epilogues, write-out); warp 8 owns
+// TMEM and one of its threads issues the MMAs.  D1 and D2 are double-buffered
+// in TMEM, so pass 1 of quad j+1 overlaps epilogue 2 of quad j and pass 2 of
+// quad j overlaps the decode of quad j+1.  Every mbarrier wait is bounded
+// (~2 s): on timeout the threads record an error code, leave their loops
+// together (worker votes), drain the tensor pipe and free TMEM.
+#include "common.cuh"
+#include "kernels.h"
+#include "tcgen05.cuh"
+
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
+namespace {
+
+constexpr int FN = 2048, FC = 1024;
+constexpr int QS = 4;                                 // segments per quad
+constexpr int US = 32;                                // segments per unit
+constexpr int QUADS = US / QS;
+constexpr int WORKERS = 256, THREADS = WORKERS + 32;  // + MMA warp (8)
+constexpr int RAWC = 34;                              // 16-byte raw chunks per segment (2048 samples + slack)
+// constant operands (pre-swizzled on the host)
+constexpr int OFF_A1 = 0;                             // DFT-64: 128 rows x 128 B, K-major, 128-byte swizzle
+constexpr int OFF_B2 = 16384;                         // DFT-32: 64 rows x 128 B
+constexpr int CONST_BYTES = 24576;
+constexpr int OFF_B1 = CONST_BYTES;                   // samples: 2 buffers x 2 atoms x (64 rows x 128 B)
+constexpr int B1_BYTES = 16384;
+constexpr int OFF_A2 = OFF_B1 + 2 * B1_BYTES;         // Z of the quad: 128 rows x 128 B
+constexpr int OFF_A2P = OFF_A2 + 16384;               // Z of the k1 = 32 row: row = segment of the unit
+constexpr int STG_PITCH = FC + 1;                     // words per staging row (one row per segment)
+constexpr int OFF_STG = OFF_A2P + 16384;              // staging: [US][STG_PITCH] half2 (Re, Im)
+constexpr int STG_BYTES = US * STG_PITCH * 4;
+constexpr int OFF_RAW = OFF_STG + STG_BYTES;          // 2 x QS x RAWC x 16
+constexpr int RAW_BYTES = QS * RAWC * 16;
+constexpr int OFF_OFFS = OFF_RAW + 2 * RAW_BYTES;     // sample offsets: 2 x QS ints
+constexpr int OFF_LUT = OFF_OFFS + 32;                // 16 half2 pair levels
+constexpr int OFF_BAR = OFF_LUT + 64;                 // mbarriers
+constexpr int NBAR = 12;
+constexpr int OFF_SLOT = OFF_BAR + 8 * NBAR;
+constexpr int SMEM_USED = OFF_SLOT + 16;
+constexpr int SMEM_BYTES = SMEM_USED + 1024;          // + alignment of the base to 1024 B
+constexpr uint32_t TMEM_COLS = 512;                   // D1: 0, 128; D2: 256, 320; D2': 384
+constexpr uint32_t COL_D1 = 0, COL_D2 = 256, COL_D2P = 384;
+constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s
+
+// barriers
+constexpr int B_B1FULL0 = 0, B_D1FULL = 2, B_EPI1 = 3, B_D2FULL = 4, B_EPI2_0 = 5, B_D2PFULL = 7, B_EPI2P = 8,
+              B_DRAIN = 9;
+// error codes
+constexpr unsigned E_MMA_WAIT = 1, E_WORKER_WAIT = 2;
+
+__device__ unsigned g_fst32_error;
+
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(OFF_B1 % 1024 == 0 && OFF_A2 % 1024 == 0 && OFF_A2P % 1024 == 0, "swizzle atoms need 1024-B alignment");
+
+CS_DEV void cp_async16(uint32_t dst, const void* src, bool valid)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+CS_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+CS_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+CS_DEV void worker_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+// all 256 workers agree on `ok` (and synchronise)
+CS_DEV bool worker_vote(bool ok)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, 1, 256, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(ok ? 1u : 0u)
+        : "memory");
+    return r != 0;
+}
+
+// After tcgen05.wait::ld: ties the loaded registers to that point.
+CS_DEV void pin16(uint32_t (&r)[16])
+{
+#pragma unroll
+    for (int i = 0; i < 16; i++) asm volatile("" : "+r"(r[i]));
+}
+
+// byte offset of element (row, k) of a 128-byte-swizzled K-major operand
+// (rows of 64 FP16, 8-row groups every 1024 B)
+CS_DEV uint32_t sw128(uint32_t row, uint32_t k)
+{
+    return row * 128 + ((((k >> 3) ^ row) & 7) << 4) + (k & 7) * 2;
+}
+
+CS_DEV uint32_t h2u(__half2 v) { return *reinterpret_cast<const uint32_t*>(&v); }
+
+struct Tc32Args {
+    CsFStageArgs f;
+    const uint4* consts;      // A1 + B2, CONST_BYTES, already swizzled
+    int units_k;              // 32-segment units per input = K / 32
+    int64_t units;            // S * units_k
+    int nkb;                  // kp / 32: 32-segment blocks per output row
+    int s_rows;               // S_out
+};
+
+template <bool PHASE>
+__global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_constant__ Tc32Args args)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = tc::smem_u32(sm);
+    const CsFStageArgs& a = args.f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x;
+    const uint32_t bar0 = sbase + OFF_BAR;
+    auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + OFF_SLOT);
+    int* offs = reinterpret_cast<int*>(sm + OFF_OFFS);
+    __half2* lut2 = reinterpret_cast<__half2*>(sm + OFF_LUT);
+
+    // constants into shared memory, A2' zeroed (its rows past the unit's 32
+    // segments are read by the MMA but never used), barriers, TMEM
+    for (int i = tid; i < CONST_BYTES / 16; i += THREADS)
+        reinterpret_cast<uint4*>(sm)[i] = __ldg(args.consts + i);
+    for (int i = tid; i < 16384 / 16; i += THREADS)
+        reinterpret_cast<uint4*>(sm + OFF_A2P)[i] = make_uint4(0, 0, 0, 0);
+    if (tid < 16) lut2[tid] = __floats2half2_rn(a.lut[tid & 3], a.lut[tid >> 2]);
+    if (tid == 0) {
+        tc::mbar_init(bar(B_B1FULL0), WORKERS);
+        tc::mbar_init(bar(B_B1FULL0 + 1), WORKERS);
+        tc::mbar_init(bar(B_D1FULL), 1);
+        tc::mbar_init(bar(B_EPI1), WORKERS);
+        tc::mbar_init(bar(B_D2FULL), 1);
+        tc::mbar_init(bar(B_EPI2_0), WORKERS);
+        tc::mbar_init(bar(B_EPI2_0 + 1), WORKERS);
+        tc::mbar_init(bar(B_D2PFULL), 1);
+        tc::mbar_init(bar(B_EPI2P), WORKERS);
+        tc::mbar_init(bar(B_DRAIN), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 8) tc::tmem_alloc(tc::smem_u32(slot), TMEM_COLS);
+    tc::fence_proxy_async();                       // constant operands -> tensor core
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *slot;
+
+    const int64_t units = args.units;
+    const int nunits = (blockIdx.x < units) ? (int)((units - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    const int nquads = nunits * QUADS;
+    const int K = a.K;
+
+    if (warp == 8) {
+        // ------------------------------ MMA issuer ------------------------------
+        if (lane == 0) {
+            const uint32_t id1 = tc::idesc_f16(128, 128, false, false, true);    // B1 MN-major
+            const uint32_t id2 = tc::idesc_f16(128, 64, false, false, false);
+            bool ok = true;
+            for (int j = 0; j < nquads && ok; j++) {
+                const int b = j & 1;
+                // B1 of quad j decoded (the workers arrive after epilogue 1 of
+                // quad j-1, which freed D1 buffer b of quad j-2)
+                ok = tc::mbar_wait(bar(B_B1FULL0 + b), (uint32_t)(j >> 1) & 1, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
+                if (!ok) break;
+                tc::fence_after();
+                const uint32_t b1 = sbase + OFF_B1 + (uint32_t)b * B1_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t da = tc::smem_desc(sbase + OFF_A1 + 32u * kk, 16, 1024, tc::SW128);
+                    // MN-major: 8-row K groups every 1024 B, 64-wide N atoms every 8192 B
+                    const uint64_t db = tc::smem_desc(b1 + 2048u * kk, 8192, 1024, tc::SW128);
+                    tc::mma_f16(tmem + COL_D1 + 128u * b, da, db, id1, kk ? 1u : 0u);
+                }
+                tc::commit(bar(B_D1FULL));
+                // A2 (and the quad's A2' rows) written by epilogue 1 of quad j
+                ok = tc::mbar_wait(bar(B_EPI1), (uint32_t)j & 1, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
+                // D2 buffer b free: epilogue 2 of quad j-2 done
+                if (ok && j >= 2)
+                    ok = tc::mbar_wait(bar(B_EPI2_0 + b), (uint32_t)((j - 2) >> 1) & 1, &g_fst32_error, E_MMA_WAIT,
+                                       WAIT_CYCLES);
+                if (!ok) break;
+                tc::fence_after();
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t da = tc::smem_desc(sbase + OFF_A2 + 32u * kk, 16, 1024, tc::SW128);
+                    const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
+                    tc::mma_f16(tmem + COL_D2 + 64u * b, da, db, id2, kk ? 1u : 0u);
+                }
+                tc::commit(bar(B_D2FULL));
+                if (j % QUADS == QUADS - 1) {
+                    // the unit's k1 = 32 rows are complete; D2' free once the
+                    // previous unit's epilogue 2' is done
+                    const int u = j / QUADS;
+                    if (u >= 1)
+                        ok = tc::mbar_wait(bar(B_EPI2P), (uint32_t)(u - 1) & 1, &g_fst32_error, E_MMA_WAIT,
+                                           WAIT_CYCLES);
+                    if (!ok) break;
+                    tc::fence_after();
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint64_t da = tc::smem_desc(sbase + OFF_A2P + 32u * kk, 16, 1024, tc::SW128);
+                        const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
+                        tc::mma_f16(tmem + COL_D2P, da, db, id2, kk ? 1u : 0u);
+                    }
+                    tc::commit(bar(B_D2PFULL));
+                }
+            }
+            // completes once every MMA issued above has finished
+            tc::commit(bar(B_DRAIN));
+            tc::mbar_wait(bar(B_DRAIN), 0, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------ workers ------------------------------
+        const int q = warp & 3, h = warp >> 2;        // TMEM lane quarter, half
+        const int64_t chunks = a.bytes_per_input >> 4;
+        const int k1 = 8 * q + (lane >> 2);           // epilogue 1: this thread's k1 (< 32)
+
+        // epilogue-1 twiddles W_2048^(n2 k1), n2 = 8 m + 2 (lane % 4) + e
+        float2 tw[4][2];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int n2 = 8 * m + 2 * (lane & 3) + e;
+                double sn, cs;
+                sincospi(-(double)((n2 * k1) & 2047) / 1024.0, &sn, &cs);
+                tw[m][e] = make_float2((float)cs, (float)sn);
+            }
+        // the k1 = 32 row (quarter 0): this thread's (m, e) and W_64^(n2)
+        const int m32 = (lane >> 2) & 3, e32 = lane >> 4;
+        const int n2_32 = 8 * m32 + 2 * (lane & 3) + e32;
+        float2 tw32;
+        {
+            double sn, cs;
+            sincospi(-(double)n2_32 / 32.0, &sn, &cs);
+            tw32 = make_float2((float)cs, (float)sn);
+        }
+
+        auto unit_of = [&](int u, int& s, int& kb) {
+            const int64_t uu = (int64_t)blockIdx.x + (int64_t)u * gridDim.x;
+            s = (int)(uu / args.units_k);
+            kb = (int)(uu % args.units_k);
+        };
+        // raw chunks of quad j -> raw buffer j & 1 (zero outside the input)
+        auto fetch = [&](int j) {
+            int s, kb;
+            unit_of(j / QUADS, s, kb);
+            const int kq = kb * US + (j % QUADS) * QS;
+            const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
+            const uint32_t dst0 = sbase + OFF_RAW + (uint32_t)(j & 1) * RAW_BYTES;
+            for (int i = tid; i < QS * RAWC; i += WORKERS) {
+                const int g = i / RAWC, c = i % RAWC, k = kq + g;
+                const int64_t start = a.start_sample + (int64_t)k * FN + (a.shift ? __ldg(a.shift + (int64_t)s * K + k) : 0);
+                const int64_t ci = (start >> 6) + c;
+                const bool ok = ci >= 0 && ci < chunks;
+                cp_async16(dst0 + 16u * i, ok ? base + 16 * ci : a.raw, ok);
+                if (c == 0) offs[(j & 1) * QS + g] = (int)(start & 63);
+            }
+            cp_async_commit();
+        };
+        // unpack quad j (raw buffer j & 1) -> B1 buffer j & 1:
+        // element (n1, 32 g + n2) = sample 32 n1 + n2 of segment g
+        auto decode = [&](int j) {
+            const uint32_t* rw0 = reinterpret_cast<const uint32_t*>(sm + OFF_RAW + (j & 1) * RAW_BYTES);
+            unsigned char* b1 = sm + OFF_B1 + (j & 1) * B1_BYTES;
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int idx = tid + WORKERS * r;
+                const int g = idx >> 7, wd = idx & 127;
+                const int off = offs[(j & 1) * QS + g];
+                const uint32_t* rw = rw0 + g * RAWC * 4 + (off >> 4) + wd;
+                const uint32_t bits = __funnelshift_r(rw[0], rw[1], 2 * (off & 15));
+                uint32_t hv[8];
+#pragma unroll
+                for (int p = 0; p < 8; p++) hv[p] = h2u(lut2[(bits >> (4 * p)) & 15u]);
+                const int n1 = wd >> 1;
+                const int chunk = 4 * (g & 1) + 2 * (wd & 1);
+                unsigned char* rowp = b1 + (g >> 1) * 8192 + n1 * 128;
+                *reinterpret_cast<uint4*>(rowp + (((chunk ^ n1) & 7) << 4)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                *reinterpret_cast<uint4*>(rowp + ((((chunk + 1) ^ n1) & 7) << 4)) = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+            }
+        };
+        uint32_t* stg = reinterpret_cast<uint32_t*>(sm + OFF_STG);
+        // one spectrum value of the segment (unit-relative `seg`) into the staging
+        auto stage = [&](int seg, int s, int c, float2 X, float2& B, const float2 D) {
+            if (PHASE) {
+                X = cmul(X, B);
+                B = cmul(B, D);
+            }
+            if (a.scale) X = cscale(X, __ldg(a.scale + (int64_t)s * FC + c));
+            stg[seg * STG_PITCH + c] = h2u(__floats2half2_rn(X.x, X.y));
+        };
+        auto phasor = [&](int s, int k, float cstart, float cstep, float2& B, float2& D) {
+            if (PHASE) {
+                const int64_t sk = (int64_t)s * K + k;
+                const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);
+                float sn, cs;
+                sincosf(ph0 + cstart * dph, &sn, &cs);
+                B = make_float2(cs, sn);
+                sincosf(cstep * dph, &sn, &cs);
+                D = make_float2(cs, sn);
+            } else {
+                B = D = make_float2(1.f, 0.f);
+            }
+        };
+
+        bool ok = true;
+        if (nquads > 0) {
+            fetch(0);
+            if (nquads > 1) fetch(1);
+            cp_async_wait_all();
+            worker_bar();
+            decode(0);
+            tc::fence_proxy_async();
+            tc::mbar_arrive(bar(B_B1FULL0));
+        }
+        for (int j = 0; j < nquads; j++) {
+            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
+            int s, kb;
+            unit_of(u, s, kb);
+
+            // ---- epilogue 1: Y -> Z = Y W_2048^(n2 k1) -> A2 (FP16) ----
+            ok = tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+            if (!worker_vote(ok)) { ok = false; break; }
+            tc::fence_after();
+            {
+                unsigned char* a2 = sm + OFF_A2;
+                const uint32_t d1 = tmem + COL_D1 + 128u * b;
+#pragma unroll
+                for (int gi = 0; gi < 2; gi++) {
+                    const int g = 2 * h + gi;                 // segment in the quad
+                    uint32_t r[16];
+                    tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16) + 32u * g, r);
+                    uint32_t r32[16];
+                    if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16) + 32u * g, r32);
+                    tc::tmem_ld_wait();
+                    pin16(r);
+                    const uint32_t row = 32 * g + k1;
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
+                        const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
+                        const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
+                        const uint32_t kpos = 8 * m + 2 * (lane & 3);
+                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, kpos)) = h2u(__floats2half2_rn(z0.x, z1.x));
+                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, 32 + kpos)) = h2u(__floats2half2_rn(z0.y, z1.y));
+                    }
+                    if (q == 0) {
+                        // lanes 16..23 hold copies of the real k1 = 32 row: thread
+                        // (lane) takes column 8 m32 + 2 (lane % 4) + e32 of its copy
+                        pin16(r32);
+                        float y = 0.f;                         // r32[4 m32 + e32] without local memory
+#pragma unroll
+                        for (int i = 0; i < 16; i++)
+                            if (i == 4 * m32 + e32) y = __uint_as_float(r32[i]);
+                        const __half zr = __float2half_rn(y * tw32.x), zi = __float2half_rn(y * tw32.y);
+                        unsigned char* a2p = sm + OFF_A2P;
+                        const uint32_t prow = QS * qd + g;     // segment of the unit
+                        *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = zr;
+                        *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = zi;
+                    }
+                }
+            }
+            tc::fence_before();
+            tc::fence_proxy_async();
+            tc::mbar_arrive(bar(B_EPI1));
+
+            // ---- decode quad j+1 while pass 2 of quad j runs ----
+            if (j + 1 < nquads) {
+                cp_async_wait_all();
+                worker_bar();                                   // every thread's copies have landed
+                decode(j + 1);
+                tc::fence_proxy_async();
+                tc::mbar_arrive(bar(B_B1FULL0 + ((j + 1) & 1)));
+            }
+            // raw buffer j & 1 (and its offsets) were read by decode(j) one
+            // iteration ago, behind at least one worker barrier
+            if (j + 2 < nquads) fetch(j + 2);
+
+            // ---- epilogue 2: X -> phasor, scale -> FP16 staging ----
+            ok = tc::mbar_wait(bar(B_D2FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+            if (!worker_vote(ok)) { ok = false; break; }
+            tc::fence_after();
+            {
+                // lane quarter q = segment q of the quad, lane = k1; half h: k2 in [16 h, 16 h + 16)
+                const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
+                uint32_t re[16], im[16];
+                tc::tmem_ld_32x32b_x16(d2 + 16u * h, re);
+                tc::tmem_ld_32x32b_x16(d2 + 32u + 16u * h, im);
+                tc::tmem_ld_wait();
+                pin16(re);
+                pin16(im);
+                const int kk1 = lane;                           // k1 of this TMEM lane
+                const int seg = QS * qd + q, k = kb * US + seg;
+                float2 B, D;
+                if (h == 0) {
+                    // c = k1 + 64 k2, k2 < 16
+                    phasor(s, k, (float)kk1, 64.f, B, D);
+#pragma unroll
+                    for (int i = 0; i < 16; i++)
+                        stage(seg, s, kk1 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
+                } else if (kk1 > 0) {
+                    // c = 2048 - k1 - 64 k2 (k2 = 16 + i) holds conj(X[k1 + 64 k2])
+                    phasor(s, k, (float)(FC - kk1), -64.f, B, D);
+#pragma unroll
+                    for (int i = 0; i < 16; i++)
+                        stage(seg, s, FC - kk1 - 64 * i,
+                              make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])), B, D);
+                }
+            }
+            tc::fence_before();
+            tc::mbar_arrive(bar(B_EPI2_0 + b));
+
+            if (qd == QUADS - 1) {
+                // ---- k1 = 32 channels (c = 32 + 64 k2) of the unit's 32 segments ----
+                ok = tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+                if (!worker_vote(ok)) { ok = false; break; }
+                tc::fence_after();
+                if (warp == 0) {
+                    uint32_t re[16], im[16];
+                    tc::tmem_ld_32x32b_x16(tmem + COL_D2P, re);
+                    tc::tmem_ld_32x32b_x16(tmem + COL_D2P + 32u, im);
+                    tc::tmem_ld_wait();
+                    pin16(re);
+                    pin16(im);
+                    const int seg = lane, k = kb * US + seg;
+                    float2 B, D;
+                    phasor(s, k, 32.f, 64.f, B, D);
+#pragma unroll
+                    for (int i = 0; i < 16; i++)
+                        stage(seg, s, 32 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
+                }
+                tc::fence_before();
+                tc::mbar_arrive(bar(B_EPI2P));
+                worker_bar();                                   // the unit's staging is complete
+
+                // ---- write-out: (channel, 8-segment group) tasks, 4 lanes per channel ----
+                __half* out = reinterpret_cast<__half*>(a.out);
+                const int64_t row0 = (int64_t)s * args.nkb + kb;       // run index of channel 0
+                const int64_t crow = (int64_t)args.s_rows * args.nkb;   // runs between channels
+#pragma unroll 4
+                for (int r = 0; r < (FC * 4) / WORKERS; r++) {
+                    const int task = r * WORKERS + tid;
+                    const int c = task >> 2, g4 = task & 3;
+                    uint32_t w[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) w[i] = stg[(8 * g4 + i) * STG_PITCH + c];
+                    __half* run = out + ((int64_t)c * crow + row0) * 64;
+                    *reinterpret_cast<uint4*>(run + 8 * g4) =
+                        make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
+                                   __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
+                    *reinterpret_cast<uint4*>(run + 32 + 8 * g4) =
+                        make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
+                                   __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
+                }
+                worker_bar();                                   // staging free for the next unit
+            }
+        }
+        cp_async_wait_all();
+        tc::fence_before();
+    }
+    __syncthreads();
+    if (warp == 8) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// A1 (DFT-64: per TMEM lane quarter q the Re rows 32q..32q+7 and Im rows
+// 32q+8..32q+15 of k1 = 8q..8q+7; rows 16..23 the real k1 = 32 row) and B2
+// (DFT-32 as a real 64 x 64 operand: rows k2 give Re X, rows 32 + k2 Im X) in
+// FP16, 128-byte-swizzled K-major, one copy per device.
+std::mutex g_const_mu;
+std::map<int, uint4*> g_consts;
+
+const uint4* tc32_constants()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_const_mu);
+    auto it = g_consts.find(dev);
+    if (it != g_consts.end()) return it->second;
+    std::vector<__half> h(CONST_BYTES / 2, __float2half(0.f));
+    auto put = [&](int base, int row, int k, double v) {
+        const uint32_t off = (uint32_t)row * 128 + ((((k >> 3) ^ row) & 7) << 4) + (k & 7) * 2;
+        h[(base + off) / 2] = __double2half(v);
+    };
+    for (int r = 0; r < 128; r++) {
+        const int q = r / 32, rr = r % 32;
+        for (int n1 = 0; n1 < 64; n1++) {
+            double v = 0.0;
+            if (rr < 16) {
+                const int k1 = 8 * q + rr % 8;
+                const double th = 2.0 * M_PI * (double)((n1 * k1) % 64) / 64.0;
+                v = rr < 8 ? std::cos(th) : -std::sin(th);
+            } else if (q == 0 && rr < 24) {
+                v = (n1 & 1) ? -1.0 : 1.0;             // W_64^(32 n1)
+            }
+            put(OFF_A1, r, n1, v);
+        }
+    }
+    for (int r = 0; r < 64; r++) {
+        const int k2 = r % 32, part = r / 32;
+        for (int kk = 0; kk < 64; kk++) {
+            const int plane = kk / 32, n2 = kk % 32;
+            const double th = 2.0 * M_PI * (double)((n2 * k2) % 32) / 32.0;
+            const double c = std::cos(th), sn = std::sin(th);
+            // Re X = sum Zr cos + Zi sin;  Im X = sum -Zr sin + Zi cos
+            const double v = part == 0 ? (plane == 0 ? c : sn) : (plane == 0 ? -sn : c);
+            put(OFF_B2, r, kk, v);
+        }
+    }
+    uint4* d = nullptr;
+    if (cudaMalloc(&d, CONST_BYTES) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), CONST_BYTES, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        return nullptr;
+    }
+    g_consts[dev] = d;
+    return d;
+}
+
+int g_sms32 = 0;
+
+}  // namespace
+
+bool cs_fstage_tc32_supported(const CsFStageArgs& a)
+{
+    const int kp = a.kp ? a.kp : a.K;
+    return a.N == FN && a.format == CS_SPECTRA_F16 && !a.msb_first && !a.seg_major && a.kblock && a.K % US == 0 &&
+           kp % US == 0;
+}
+
+int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st)
+{
+    if (!cs_fstage_tc32_supported(a)) return CS_ERR_UNSUPPORTED;
+    if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
+    if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
+    const uint4* consts = tc32_constants();
+    if (!consts) return (int)cudaErrorMemoryAllocation;
+    if (!g_sms32) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        g_sms32 = n > 0 ? n : 148;
+    }
+    void* errp = nullptr;
+    CS_CUDA_TRY(cudaGetSymbolAddress(&errp, g_fst32_error));
+    CS_CUDA_TRY(cudaMemsetAsync(errp, 0, sizeof(unsigned), st));
+    Tc32Args t{};
+    t.f = a;
+    t.consts = consts;
+    t.units_k = a.K / US;
+    t.units = (int64_t)a.S * t.units_k;
+    t.nkb = (a.kp ? a.kp : a.K) / US;
+    t.s_rows = a.S_out ? a.S_out : a.S;
+    const int grid = (int)std::min<int64_t>(t.units, g_sms32);
+    if (a.phase0) {
+        CS_CUDA_TRY(cudaFuncSetAttribute(k_fx_fstage_tc32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        k_fx_fstage_tc32<true><<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
+    } else {
+        CS_CUDA_TRY(cudaFuncSetAttribute(k_fx_fstage_tc32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        k_fx_fstage_tc32<false><<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
+    }
+    return (int)cudaGetLastError();
+}
+
+int cs_fstage_tc32_status(unsigned* code)
+{
+    return (int)cudaMemcpyFromSymbol(code, g_fst32_error, sizeof(unsigned));
+}

@@ -93,6 +93,13 @@ int cs_fx_fstage_tc(const CsFStageArgs& a, cudaStream_t st);
 // Error code of the last tensor-core F-stage launch (0 = ok; 1, 2 = a wait
 // timed out).  Call after the stream has synchronised.
 int cs_fstage_tc_status(unsigned* code);
+// fstage_tc32.cu: the N = 2048 tensor-core F stage with 32-segment units and
+// k-blocked FP16 output (kblock = 1, K and kp multiples of 32), real-input
+// symmetry halving the CUDA-core twiddle work.  cs_fx_fstage uses it for
+// those arguments unless CELLSPE_FSTAGE_TC32=0.
+bool cs_fstage_tc32_supported(const CsFStageArgs& a);
+int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st);
+int cs_fstage_tc32_status(unsigned* code);
 
 // xstage.cu -----------------------------------------------------------------
 // FP32 CUDA-core X stage: spectra float2 [C][S][kp] (K used) -> vis float2

@@ -603,9 +603,10 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     int rc = j.finish(sync);
     if (sync && !rc && p->x_mode != CELLSPE_X_FP32) {
         unsigned code = 0;
-        if (cs_fstage_tc_status(&code) != 0 || code != 0)
+        unsigned code32 = 0;
+        if (cs_fstage_tc_status(&code) != 0 || code != 0 || cs_fstage_tc32_status(&code32) != 0 || code32 != 0)
             rc = set_err(CELLSPE_ERR_CUDA, "F stage: tensor-core pipeline wait timed out (code " +
-                                               std::to_string(code) + ")");
+                                               std::to_string(code | code32) + ")");
         else if (cs_xmac_tc_status(&code) != 0 || code != 0)
             rc = set_err(CELLSPE_ERR_CUDA, "X stage: tensor-core pipeline wait timed out (code " +
                                                std::to_string(code) + ")");

@@ -169,3 +169,64 @@ def test_fx_tc_fstage_2048_delay_model(cg, orc, fstage_engine):
     pairs = [(i, j) for i in range(S) for j in range(i + 1)]
     # the random delays decorrelate the inputs: the phase bar covers the autos
     _tc_bars(orc, vis, X, pairs, K, cross_coverage=False)
+
+
+@pytest.fixture(params=["0", "1"], ids=["warp-fft", "tc32-fstage"])
+def fstage32(request, monkeypatch):
+    """N = 2048 k-blocked FP16 spectra from the warp FFT or the 32-segment
+    tensor-core F stage (real-input symmetry, k1 = 32 row via pass 2')."""
+    monkeypatch.setenv("CELLSPE_FSTAGE_TC32", request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("S,K,rho", [(24, 64, 0.5), (9, 96, 0.6), (40, 128, 0.4), (130, 32, 0.3)])
+def test_fx_tc32_fstage_vs_fp64(cg, orc, S, K, rho, fstage32):
+    """Every channel (the direct, mirrored and k1 = 32 families) of the
+    tensor-core F stage through the full FX path: all products of the first 8
+    inputs against the FP64 oracle, and the whole matrix against the FP32 path."""
+    import synth
+
+    N = 2048
+    raw = synth.stations_offset_binary(S, N * K, rho=rho, lags=np.arange(S) % 5, seed=S * 3 + K)
+    p = cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=cg.VIS_BASELINE_MAJOR)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis)
+    inputs = list(range(min(S, 8)))
+    X = orc.fx_spectra_f64(raw, S, N, K, inputs=inputs)
+    pairs = [(a, b) for a in range(len(inputs)) for b in range(a + 1)]
+    sel = [orc.tri_index(inputs[a], inputs[b]) for a, b in pairs]
+    _tc_bars(orc, vis, X, pairs, K, sel=sel, chans=slice(None))
+    v32 = np.zeros_like(vis)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_FP32, vis_order=cg.VIS_BASELINE_MAJOR),
+                    raw, v32)
+    rel = np.linalg.norm(vis - v32, axis=1) / np.linalg.norm(v32, axis=1)
+    assert rel.max() < 1e-3
+
+
+def test_fx_tc32_fstage_delay_model_and_scale(cg, orc, fstage32):
+    """Integer shifts at every sample alignment, the fringe / fractional-delay
+    phasor on all three channel families, and a per-(input, channel) scale."""
+    import synth
+
+    S, N, K = 5, 2048, 64
+    fs, lo = 32e6, 8.4e9
+    margin = 4096
+    raw = synth.stations_offset_binary(S, N * K + 2 * margin, rho=0.5, seed=23)
+    rng = np.random.default_rng(7)
+    poly = np.zeros((S, 4))
+    poly[:, 0] = rng.uniform(-40e-6, 40e-6, S)
+    poly[:, 1] = rng.uniform(-2e-3, 2e-3, S)
+    p = cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=cg.VIS_BASELINE_MAJOR,
+                     start_sample=margin, fs_hz=fs, lo_hz=lo)
+    vis = np.zeros((S * (S + 1) // 2, N // 2), np.complex64)
+    cg.fx_correlate(p, raw, vis, delay_poly=poly)
+    shift, ph0, dph = orc.delay_state_f64(poly, N, K, fs, lo)
+    X = orc.fx_spectra_f64(raw, S, N, K, margin, shift, ph0, dph)
+    pairs = [(i, j) for i in range(S) for j in range(i + 1)]
+    _tc_bars(orc, vis, X, pairs, K, cross_coverage=False)
+    scale = np.random.default_rng(3).uniform(0.01, 0.05, (S, N // 2)).astype(np.float32)
+    ps = cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=cg.VIS_BASELINE_MAJOR,
+                      start_sample=margin, fs_hz=fs, lo_hz=lo, channel_scale=scale)
+    vs = np.zeros_like(vis)
+    cg.fx_correlate(ps, raw, vs, delay_poly=poly)
+    assert np.linalg.norm(vs - vis) / np.linalg.norm(vis) < 1e-3
