@@ -83,3 +83,83 @@ def test_no_cpu_fallback_without_gpu():
     with pytest.raises(cg.CellspeError) as e:
         cg.unpack2bit(raw, 256, 1, out)
     assert e.value.code == cg.ERR_CUDA
+
+
+# A caller compiled against the reference's own declarations (cellspe-tasklib.h:
+# 122-133, cellspe-tasklib-dsp.h:79-94: C++ linkage, fc32 an unnamed-struct
+# typedef) links against the C++-mangled names; these are the declarations.
+CXX_CALLER = r'''
+#include <cstdio>
+#include <cstring>
+struct CellDSPTask_tt;
+typedef CellDSPTask_tt CellDSPTask_t;
+typedef struct { float re; float im; } fc32;
+typedef fc32 cf32;
+int celldsp_start(); int celldsp_stop(); int celldsp_getFreeSPE(); int celldsp_setFreeSPE(int targetSPE);
+int celldsp_startTask(int targetSPE, CellDSPTask_t* task); int celldsp_waitTask(int targetSPE);
+int celldsp_executeTask(CellDSPTask_t* task); int celldsp_startContinuableTask(CellDSPTask_t* task, int* speID);
+int celldsp_continueTask(CellDSPTask_t* task, int* speID); int celldsp_stopContinuableTask(int* speID);
+void celldsp_setBehaviour(unsigned int flags); unsigned int celldsp_getBehaviour();
+int speNOP(); int speRunAllCheck(); int speIOCheck(); int speIOSimulation();
+int speIOBench(void* buffer, unsigned int bufbytes, int spes);
+int speIOBenchStreamed(void* buffer, unsigned int bufbytes, int spes, int stream_length);
+int speAddProduct_32fc(fc32* src, fc32* src2, fc32* accumulator, int length);
+int speFFT_init(int fft_len, int* speID); int speFFT_exec(void* in, void* out, int fft_len, int* speID);
+int speFFT_destroy(int* speID); int speFFT_singleexec(void* in, void* out, int fft_len);
+int speDIFX_process(void*, void*, void*, void*, void*, int nfft, int twicenumchannels, int useUpperOrLower);
+int speSinCosGenerator(float startphase, float increment, fc32* cos_sin_out, int numiter);
+int speSinCosAccurate(float* argument, cf32* cos_sin_out, int argumentcount);
+int speSinCosAccurateNorm(float* normalizedargument, cf32* cos_sin_out, int argumentcount);
+volatile int use_all = 0;
+int main(int argc, char** argv) {
+  if (use_all) {   // referenced so that every name must resolve at link time
+    celldsp_getFreeSPE(); celldsp_setFreeSPE(0); celldsp_startTask(0, 0); celldsp_waitTask(0);
+    celldsp_executeTask(0); celldsp_startContinuableTask(0, 0); celldsp_continueTask(0, 0);
+    celldsp_stopContinuableTask(0); speRunAllCheck(); speIOCheck(); speIOSimulation(); speIOBench(0, 0, 0);
+    speIOBenchStreamed(0, 0, 0, 0); speFFT_init(0, 0); speFFT_exec(0, 0, 0, 0); speFFT_destroy(0);
+    speFFT_singleexec(0, 0, 0); speDIFX_process(0, 0, 0, 0, 0, 0, 0, 0); speSinCosGenerator(0, 0, 0, 0);
+    speSinCosAccurate(0, 0, 0); speSinCosAccurateNorm(0, 0, 0);
+  }
+  celldsp_setBehaviour(1u); unsigned b = celldsp_getBehaviour(); celldsp_setBehaviour(0u);
+  std::printf("behaviour %u\n", b);
+  if (argc > 1) {  // on a GPU: the MAC of minitest-cell.cpp:131-138 through the mangled names
+    const int n = 1024; static fc32 a[n], c[n], acc[n];
+    for (int i = 0; i < n; i++) { a[i].re = 0.5f * i; a[i].im = -0.5f * i; c[i].re = 0.15f * i * i; c[i].im = -0.25f;
+                                  acc[i].re = 1.0f; acc[i].im = 1.5f; }
+    if (celldsp_start() != 0 || speNOP() != 0) return 2;
+    int rc = speAddProduct_32fc(a, c, acc, n);
+    celldsp_stop();
+    FILE* f = std::fopen(argv[1], "wb"); std::fwrite(acc, sizeof acc, 1, f); std::fclose(f);
+    return rc;
+  }
+  return 0;
+}
+'''
+
+
+def build_cxx_caller(tmp_path):
+    import cellspe_gpu
+
+    src = tmp_path / "caller.cpp"
+    src.write_text(CXX_CALLER)
+    exe = tmp_path / "caller"
+    subprocess.run(["g++", "-std=c++17", str(src), "-o", str(exe), "-L", str(cellspe_gpu.PKG), "-lcellspe_gpu",
+                    f"-Wl,-rpath,{cellspe_gpu.PKG}"], check=True)
+    return exe
+
+
+def test_cxx_linkage_aliases_link_and_run(tmp_path):
+    """celldsp_* and spe* under their C++-mangled names, for callers already
+    compiled against the reference's headers."""
+    import cellspe_gpu
+
+    if not cellspe_gpu.LIB_PATH.exists():
+        import __graft_entry__
+
+        __graft_entry__.build()
+    exe = build_cxx_caller(tmp_path)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    assert out.startswith("behaviour ")          # (the runtime is not started: no GPU work here)
+    syms = subprocess.run(["nm", "-D", "--defined-only", str(cellspe_gpu.LIB_PATH)], capture_output=True, text=True,
+                          check=True).stdout
+    assert "_Z17celldsp_startTaskiP14CellDSPTask_tt" in syms and "_Z18speAddProduct_32fcP4fc32S0_S0_i" in syms

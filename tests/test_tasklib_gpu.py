@@ -332,3 +332,19 @@ def test_continuable_tasks(cg, rt):
     assert sorted(after) == list(range(cg.MAX_SLOTS))
     for s in after:
         rt.celldsp_setFreeSPE(s)
+
+
+def test_cxx_caller_through_mangled_names(tmp_path):
+    """A C++ caller built against the reference's declarations runs the
+    minitest-cell.cpp MAC through the mangled speAddProduct_32fc: bit for bit
+    the reference's genericAddProduct_32fc (golden vector)."""
+    import subprocess
+
+    from test_abi import build_cxx_caller
+
+    exe = build_cxx_caller(tmp_path)
+    out = tmp_path / "acc.bin"
+    subprocess.run([str(exe), str(out)], check=True)
+    acc = np.fromfile(out, np.complex64)
+    g = np.load(GOLD / "generic_mac.npz")
+    assert np.array_equal(acc.view(np.uint32), g["mac"].view(np.uint32))
