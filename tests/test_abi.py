@@ -122,14 +122,16 @@ int main(int argc, char** argv) {
   }
   celldsp_setBehaviour(1u); unsigned b = celldsp_getBehaviour(); celldsp_setBehaviour(0u);
   std::printf("behaviour %u\n", b);
-  if (argc > 1) {  // on a GPU: the MAC of minitest-cell.cpp:131-138 through the mangled names
+  if (argc > 2) {  // on a GPU: a MAC through the mangled names; in: a, b, acc; out: acc
     const int n = 1024; static fc32 a[n], c[n], acc[n];
-    for (int i = 0; i < n; i++) { a[i].re = 0.5f * i; a[i].im = -0.5f * i; c[i].re = 0.15f * i * i; c[i].im = -0.25f;
-                                  acc[i].re = 1.0f; acc[i].im = 1.5f; }
+    FILE* f = std::fopen(argv[1], "rb");
+    if (!f || std::fread(a, sizeof a, 1, f) != 1 || std::fread(c, sizeof c, 1, f) != 1 ||
+        std::fread(acc, sizeof acc, 1, f) != 1) return 3;
+    std::fclose(f);
     if (celldsp_start() != 0 || speNOP() != 0) return 2;
     int rc = speAddProduct_32fc(a, c, acc, n);
     celldsp_stop();
-    FILE* f = std::fopen(argv[1], "wb"); std::fwrite(acc, sizeof acc, 1, f); std::fclose(f);
+    f = std::fopen(argv[2], "wb"); std::fwrite(acc, sizeof acc, 1, f); std::fclose(f);
     return rc;
   }
   return 0;

@@ -343,8 +343,9 @@ def test_cxx_caller_through_mangled_names(tmp_path):
     from test_abi import build_cxx_caller
 
     exe = build_cxx_caller(tmp_path)
-    out = tmp_path / "acc.bin"
-    subprocess.run([str(exe), str(out)], check=True)
-    acc = np.fromfile(out, np.complex64)
     g = np.load(GOLD / "generic_mac.npz")
+    inp, out = tmp_path / "in.bin", tmp_path / "acc.bin"
+    np.concatenate([g["a"], g["b"], g["acc0"]]).astype(np.complex64).tofile(inp)
+    subprocess.run([str(exe), str(inp), str(out)], check=True)
+    acc = np.fromfile(out, np.complex64)
     assert np.array_equal(acc.view(np.uint32), g["mac"].view(np.uint32))
