@@ -33,9 +33,12 @@
 // staging with 16-byte stores, 4 lanes per 64-byte half-run.
 //
 // Warps 0..7 are the workers (decode, both epilogues, write-out); warp 8 owns
-// TMEM and one of its threads issues the MMAs.  D1 and D2 are double-buffered
-// in TMEM, so pass 1 of quad j+1 overlaps epilogue 2 of quad j and pass 2 of
-// quad j overlaps the decode of quad j+1.  Every mbarrier wait is bounded
+// TMEM and one of its threads issues the MMAs.  The workers' loop is skewed so
+// that they never wait on an MMA they just enabled: iteration j runs
+// epilogue 1 of quad j, the decode of quad j+1 and epilogue 2 of quad j-1, so
+// pass 2 of quad j runs during the decode and epilogue 2, and pass 1 of quad
+// j+1 during epilogue 2 (A2 and D2 double-buffered, D1 double-buffered in
+// TMEM).  Every mbarrier wait is bounded
 // (~2 s): on timeout the threads record an error code, leave their loops
 // together (worker votes), drain the tensor pipe and free TMEM.
 #include "common.cuh"
@@ -62,12 +65,18 @@ constexpr int RAWC = 34;                              // 16-byte raw chunks per 
 constexpr int OFF_A1 = 0;                             // DFT-64: 128 rows x 128 B, K-major, 128-byte swizzle
 constexpr int OFF_B2 = 16384;                         // DFT-32: 64 rows x 128 B
 constexpr int CONST_BYTES = 24576;
-constexpr int OFF_B1 = CONST_BYTES;                   // samples: 2 buffers x 2 atoms x (64 rows x 128 B)
+constexpr int OFF_B1 = CONST_BYTES;                   // samples of one quad: 2 atoms x (64 rows x 128 B)
 constexpr int B1_BYTES = 16384;
-constexpr int OFF_A2 = OFF_B1 + 2 * B1_BYTES;         // Z of the quad: 128 rows x 128 B
-constexpr int OFF_A2P = OFF_A2 + 16384;               // Z of the k1 = 32 row: row = segment of the unit
+constexpr int OFF_A2 = OFF_B1 + B1_BYTES;             // Z of a quad: 2 buffers x 128 rows x 128 B
+constexpr int A2_BYTES = 16384;
+// Z of the k1 = 32 row, row = segment of the unit: 2 regions of 32 rows
+// (units alternate).  Pass 2' reads a 128-row window from a region's start;
+// window rows 32..127 fall on the other region and the staging, and only
+// feed TMEM lanes 32..127 of D2', which are never read.
+constexpr int OFF_A2P = OFF_A2 + 2 * A2_BYTES;
+constexpr int A2P_REGION = 32 * 128;
 constexpr int STG_PITCH = FC + 1;                     // words per staging row (one row per segment)
-constexpr int OFF_STG = OFF_A2P + 16384;              // staging: [US][STG_PITCH] half2 (Re, Im)
+constexpr int OFF_STG = OFF_A2P + 2 * A2P_REGION;     // staging: [US][STG_PITCH] half2 (Re, Im)
 constexpr int STG_BYTES = US * STG_PITCH * 4;
 constexpr int OFF_RAW = OFF_STG + STG_BYTES;          // 2 x QS x RAWC x 16
 constexpr int RAW_BYTES = QS * RAWC * 16;
@@ -83,7 +92,7 @@ constexpr uint32_t COL_D1 = 0, COL_D2 = 256, COL_D2P = 384;
 constexpr long long WAIT_CYCLES = 4000000000LL;       // ~2 s
 
 // barriers
-constexpr int B_B1FULL0 = 0, B_D1FULL = 2, B_EPI1 = 3, B_D2FULL = 4, B_EPI2_0 = 5, B_D2PFULL = 7, B_EPI2P = 8,
+constexpr int B_B1FULL = 0, B_D1FULL = 1, B_EPI1 = 2, B_D2FULL0 = 3, B_EPI2_0 = 5, B_D2PFULL = 7, B_EPI2P = 8,
               B_DRAIN = 9;
 // error codes
 constexpr unsigned E_MMA_WAIT = 1, E_WORKER_WAIT = 2;
@@ -91,7 +100,9 @@ constexpr unsigned E_MMA_WAIT = 1, E_WORKER_WAIT = 2;
 __device__ unsigned g_fst32_error;
 
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
-static_assert(OFF_B1 % 1024 == 0 && OFF_A2 % 1024 == 0 && OFF_A2P % 1024 == 0, "swizzle atoms need 1024-B alignment");
+static_assert(OFF_B1 % 1024 == 0 && OFF_A2 % 1024 == 0 && OFF_A2P % 1024 == 0 && A2P_REGION % 1024 == 0,
+              "swizzle atoms need 1024-B alignment");
+static_assert(OFF_A2P + A2P_REGION + 16384 <= OFF_STG + US * STG_PITCH * 4, "pass-2' windows inside shared memory");
 
 CS_DEV void cp_async16(uint32_t dst, const void* src, bool valid)
 {
@@ -161,15 +172,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
     // segments are read by the MMA but never used), barriers, TMEM
     for (int i = tid; i < CONST_BYTES / 16; i += THREADS)
         reinterpret_cast<uint4*>(sm)[i] = __ldg(args.consts + i);
-    for (int i = tid; i < 16384 / 16; i += THREADS)
+    for (int i = tid; i < 2 * A2P_REGION / 16; i += THREADS)
         reinterpret_cast<uint4*>(sm + OFF_A2P)[i] = make_uint4(0, 0, 0, 0);
     if (tid < 16) lut2[tid] = __floats2half2_rn(a.lut[tid & 3], a.lut[tid >> 2]);
     if (tid == 0) {
-        tc::mbar_init(bar(B_B1FULL0), WORKERS);
-        tc::mbar_init(bar(B_B1FULL0 + 1), WORKERS);
+        tc::mbar_init(bar(B_B1FULL), WORKERS);
         tc::mbar_init(bar(B_D1FULL), 1);
         tc::mbar_init(bar(B_EPI1), WORKERS);
-        tc::mbar_init(bar(B_D2FULL), 1);
+        tc::mbar_init(bar(B_D2FULL0), 1);
+        tc::mbar_init(bar(B_D2FULL0 + 1), 1);
         tc::mbar_init(bar(B_EPI2_0), WORKERS);
         tc::mbar_init(bar(B_EPI2_0 + 1), WORKERS);
         tc::mbar_init(bar(B_D2PFULL), 1);
@@ -197,12 +208,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             bool ok = true;
             for (int j = 0; j < nquads && ok; j++) {
                 const int b = j & 1;
-                // B1 of quad j decoded (the workers arrive after epilogue 1 of
-                // quad j-1, which freed D1 buffer b of quad j-2)
-                ok = tc::mbar_wait(bar(B_B1FULL0 + b), (uint32_t)(j >> 1) & 1, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
+                // B1 holds quad j (decoded after epilogue 1 of quad j-1, which
+                // freed D1 buffer b of quad j-2)
+                ok = tc::mbar_wait(bar(B_B1FULL), (uint32_t)j & 1, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
                 if (!ok) break;
                 tc::fence_after();
-                const uint32_t b1 = sbase + OFF_B1 + (uint32_t)b * B1_BYTES;
+                const uint32_t b1 = sbase + OFF_B1;
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++) {
                     const uint64_t da = tc::smem_desc(sbase + OFF_A1 + 32u * kk, 16, 1024, tc::SW128);
@@ -211,7 +222,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                     tc::mma_f16(tmem + COL_D1 + 128u * b, da, db, id1, kk ? 1u : 0u);
                 }
                 tc::commit(bar(B_D1FULL));
-                // A2 (and the quad's A2' rows) written by epilogue 1 of quad j
+                // A2 buffer b (and the quad's A2' rows) written by epilogue 1 of quad j
                 ok = tc::mbar_wait(bar(B_EPI1), (uint32_t)j & 1, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
                 // D2 buffer b free: epilogue 2 of quad j-2 done
                 if (ok && j >= 2)
@@ -221,11 +232,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 tc::fence_after();
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++) {
-                    const uint64_t da = tc::smem_desc(sbase + OFF_A2 + 32u * kk, 16, 1024, tc::SW128);
+                    const uint64_t da = tc::smem_desc(sbase + OFF_A2 + (uint32_t)b * A2_BYTES + 32u * kk, 16, 1024, tc::SW128);
                     const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
                     tc::mma_f16(tmem + COL_D2 + 64u * b, da, db, id2, kk ? 1u : 0u);
                 }
-                tc::commit(bar(B_D2FULL));
+                tc::commit(bar(B_D2FULL0 + b));
                 if (j % QUADS == QUADS - 1) {
                     // the unit's k1 = 32 rows are complete; D2' free once the
                     // previous unit's epilogue 2' is done
@@ -237,7 +248,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                     tc::fence_after();
 #pragma unroll
                     for (int kk = 0; kk < 4; kk++) {
-                        const uint64_t da = tc::smem_desc(sbase + OFF_A2P + 32u * kk, 16, 1024, tc::SW128);
+                        const uint64_t da = tc::smem_desc(sbase + OFF_A2P + (uint32_t)(u & 1) * A2P_REGION + 32u * kk,
+                                                          16, 1024, tc::SW128);
                         const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
                         tc::mma_f16(tmem + COL_D2P, da, db, id2, kk ? 1u : 0u);
                     }
@@ -298,11 +310,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             }
             cp_async_commit();
         };
-        // unpack quad j (raw buffer j & 1) -> B1 buffer j & 1:
+        // unpack quad j (raw buffer j & 1) -> B1:
         // element (n1, 32 g + n2) = sample 32 n1 + n2 of segment g
         auto decode = [&](int j) {
             const uint32_t* rw0 = reinterpret_cast<const uint32_t*>(sm + OFF_RAW + (j & 1) * RAW_BYTES);
-            unsigned char* b1 = sm + OFF_B1 + (j & 1) * B1_BYTES;
+            unsigned char* b1 = sm + OFF_B1;
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const int idx = tid + WORKERS * r;
@@ -344,6 +356,115 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             }
         };
 
+        // ---- epilogue 1 of quad j: Y -> Z = Y W_2048^(n2 k1) -> A2 buffer j & 1 ----
+        auto epilogue1 = [&](int j) {
+            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
+            unsigned char* a2 = sm + OFF_A2 + b * A2_BYTES;
+            unsigned char* a2p = sm + OFF_A2P + (u & 1) * A2P_REGION;
+            const uint32_t d1 = tmem + COL_D1 + 128u * b;
+#pragma unroll
+            for (int gi = 0; gi < 2; gi++) {
+                const int g = 2 * h + gi;                 // segment in the quad
+                uint32_t r[16];
+                tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16) + 32u * g, r);
+                uint32_t r32[16];
+                if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16) + 32u * g, r32);
+                tc::tmem_ld_wait();
+                pin16(r);
+                const uint32_t row = 32 * g + k1;
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
+                    const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
+                    const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
+                    const uint32_t kpos = 8 * m + 2 * (lane & 3);
+                    *reinterpret_cast<uint32_t*>(a2 + sw128(row, kpos)) = h2u(__floats2half2_rn(z0.x, z1.x));
+                    *reinterpret_cast<uint32_t*>(a2 + sw128(row, 32 + kpos)) = h2u(__floats2half2_rn(z0.y, z1.y));
+                }
+                if (q == 0) {
+                    // lanes 16..23 hold copies of the real k1 = 32 row: thread
+                    // (lane) takes column 8 m32 + 2 (lane % 4) + e32 of its copy
+                    pin16(r32);
+                    float y = 0.f;                         // r32[4 m32 + e32] without local memory
+#pragma unroll
+                    for (int i = 0; i < 16; i++)
+                        if (i == 4 * m32 + e32) y = __uint_as_float(r32[i]);
+                    const __half zr = __float2half_rn(y * tw32.x), zi = __float2half_rn(y * tw32.y);
+                    const uint32_t prow = QS * qd + g;     // segment of the unit
+                    *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = zr;
+                    *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = zi;
+                }
+            }
+        };
+        // ---- epilogue 2 of quad j: X -> phasor, scale -> FP16 staging ----
+        auto epilogue2 = [&](int j, int s, int kb) {
+            // lane quarter q = segment q of the quad, lane = k1; half h: k2 in [16 h, 16 h + 16)
+            const int b = j & 1, qd = j % QUADS;
+            const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
+            uint32_t re[16], im[16];
+            tc::tmem_ld_32x32b_x16(d2 + 16u * h, re);
+            tc::tmem_ld_32x32b_x16(d2 + 32u + 16u * h, im);
+            tc::tmem_ld_wait();
+            pin16(re);
+            pin16(im);
+            const int kk1 = lane;                           // k1 of this TMEM lane
+            const int seg = QS * qd + q, k = kb * US + seg;
+            float2 B, D;
+            if (h == 0) {
+                // c = k1 + 64 k2, k2 < 16
+                phasor(s, k, (float)kk1, 64.f, B, D);
+#pragma unroll
+                for (int i = 0; i < 16; i++)
+                    stage(seg, s, kk1 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
+            } else if (kk1 > 0) {
+                // c = 2048 - k1 - 64 k2 (k2 = 16 + i) holds conj(X[k1 + 64 k2])
+                phasor(s, k, (float)(FC - kk1), -64.f, B, D);
+#pragma unroll
+                for (int i = 0; i < 16; i++)
+                    stage(seg, s, FC - kk1 - 64 * i, make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])), B, D);
+            }
+        };
+        // ---- the unit's k1 = 32 channels (c = 32 + 64 k2), then its write-out ----
+        auto unit_end = [&](int u, int s, int kb) {
+            if (warp == 0) {
+                uint32_t re[16], im[16];
+                tc::tmem_ld_32x32b_x16(tmem + COL_D2P, re);
+                tc::tmem_ld_32x32b_x16(tmem + COL_D2P + 32u, im);
+                tc::tmem_ld_wait();
+                pin16(re);
+                pin16(im);
+                const int seg = lane, k = kb * US + seg;
+                float2 B, D;
+                phasor(s, k, 32.f, 64.f, B, D);
+#pragma unroll
+                for (int i = 0; i < 16; i++)
+                    stage(seg, s, 32 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
+            }
+            tc::fence_before();
+            tc::mbar_arrive(bar(B_EPI2P));
+            worker_bar();                                   // the unit's staging is complete
+            // (channel, 8-segment group) tasks, 4 lanes per channel
+            __half* out = reinterpret_cast<__half*>(a.out);
+            const int64_t row0 = (int64_t)s * args.nkb + kb;       // run index of channel 0
+            const int64_t crow = (int64_t)args.s_rows * args.nkb;   // runs between channels
+#pragma unroll 4
+            for (int r = 0; r < (FC * 4) / WORKERS; r++) {
+                const int task = r * WORKERS + tid;
+                const int c = task >> 2, g4 = task & 3;
+                uint32_t w[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) w[i] = stg[(8 * g4 + i) * STG_PITCH + c];
+                __half* run = out + ((int64_t)c * crow + row0) * 64;
+                *reinterpret_cast<uint4*>(run + 8 * g4) =
+                    make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
+                               __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
+                *reinterpret_cast<uint4*>(run + 32 + 8 * g4) =
+                    make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
+                               __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
+            }
+            worker_bar();                                   // staging free for the next unit
+        };
+
         bool ok = true;
         if (nquads > 0) {
             fetch(0);
@@ -352,148 +473,47 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             worker_bar();
             decode(0);
             tc::fence_proxy_async();
-            tc::mbar_arrive(bar(B_B1FULL0));
+            tc::mbar_arrive(bar(B_B1FULL));
         }
-        for (int j = 0; j < nquads; j++) {
-            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
-            int s, kb;
-            unit_of(u, s, kb);
-
-            // ---- epilogue 1: Y -> Z = Y W_2048^(n2 k1) -> A2 (FP16) ----
-            ok = tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
-            if (!worker_vote(ok)) { ok = false; break; }
-            tc::fence_after();
-            {
-                unsigned char* a2 = sm + OFF_A2;
-                const uint32_t d1 = tmem + COL_D1 + 128u * b;
-#pragma unroll
-                for (int gi = 0; gi < 2; gi++) {
-                    const int g = 2 * h + gi;                 // segment in the quad
-                    uint32_t r[16];
-                    tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16) + 32u * g, r);
-                    uint32_t r32[16];
-                    if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16) + 32u * g, r32);
-                    tc::tmem_ld_wait();
-                    pin16(r);
-                    const uint32_t row = 32 * g + k1;
-#pragma unroll
-                    for (int m = 0; m < 4; m++) {
-                        const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
-                        const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
-                        const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
-                        const uint32_t kpos = 8 * m + 2 * (lane & 3);
-                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, kpos)) = h2u(__floats2half2_rn(z0.x, z1.x));
-                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, 32 + kpos)) = h2u(__floats2half2_rn(z0.y, z1.y));
-                    }
-                    if (q == 0) {
-                        // lanes 16..23 hold copies of the real k1 = 32 row: thread
-                        // (lane) takes column 8 m32 + 2 (lane % 4) + e32 of its copy
-                        pin16(r32);
-                        float y = 0.f;                         // r32[4 m32 + e32] without local memory
-#pragma unroll
-                        for (int i = 0; i < 16; i++)
-                            if (i == 4 * m32 + e32) y = __uint_as_float(r32[i]);
-                        const __half zr = __float2half_rn(y * tw32.x), zi = __float2half_rn(y * tw32.y);
-                        unsigned char* a2p = sm + OFF_A2P;
-                        const uint32_t prow = QS * qd + g;     // segment of the unit
-                        *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = zr;
-                        *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = zi;
-                    }
-                }
-            }
-            tc::fence_before();
-            tc::fence_proxy_async();
-            tc::mbar_arrive(bar(B_EPI1));
-
-            // ---- decode quad j+1 while pass 2 of quad j runs ----
-            if (j + 1 < nquads) {
-                cp_async_wait_all();
-                worker_bar();                                   // every thread's copies have landed
-                decode(j + 1);
-                tc::fence_proxy_async();
-                tc::mbar_arrive(bar(B_B1FULL0 + ((j + 1) & 1)));
-            }
-            // raw buffer j & 1 (and its offsets) were read by decode(j) one
-            // iteration ago, behind at least one worker barrier
-            if (j + 2 < nquads) fetch(j + 2);
-
-            // ---- epilogue 2: X -> phasor, scale -> FP16 staging ----
-            ok = tc::mbar_wait(bar(B_D2FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
-            if (!worker_vote(ok)) { ok = false; break; }
-            tc::fence_after();
-            {
-                // lane quarter q = segment q of the quad, lane = k1; half h: k2 in [16 h, 16 h + 16)
-                const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
-                uint32_t re[16], im[16];
-                tc::tmem_ld_32x32b_x16(d2 + 16u * h, re);
-                tc::tmem_ld_32x32b_x16(d2 + 32u + 16u * h, im);
-                tc::tmem_ld_wait();
-                pin16(re);
-                pin16(im);
-                const int kk1 = lane;                           // k1 of this TMEM lane
-                const int seg = QS * qd + q, k = kb * US + seg;
-                float2 B, D;
-                if (h == 0) {
-                    // c = k1 + 64 k2, k2 < 16
-                    phasor(s, k, (float)kk1, 64.f, B, D);
-#pragma unroll
-                    for (int i = 0; i < 16; i++)
-                        stage(seg, s, kk1 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
-                } else if (kk1 > 0) {
-                    // c = 2048 - k1 - 64 k2 (k2 = 16 + i) holds conj(X[k1 + 64 k2])
-                    phasor(s, k, (float)(FC - kk1), -64.f, B, D);
-#pragma unroll
-                    for (int i = 0; i < 16; i++)
-                        stage(seg, s, FC - kk1 - 64 * i,
-                              make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])), B, D);
-                }
-            }
-            tc::fence_before();
-            tc::mbar_arrive(bar(B_EPI2_0 + b));
-
-            if (qd == QUADS - 1) {
-                // ---- k1 = 32 channels (c = 32 + 64 k2) of the unit's 32 segments ----
-                ok = tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+        // iteration j: epilogue 1 (j), decode (j+1), epilogue 2 (j-1)
+        for (int j = 0; j <= nquads; j++) {
+            if (j < nquads) {
+                ok = tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
                 if (!worker_vote(ok)) { ok = false; break; }
                 tc::fence_after();
-                if (warp == 0) {
-                    uint32_t re[16], im[16];
-                    tc::tmem_ld_32x32b_x16(tmem + COL_D2P, re);
-                    tc::tmem_ld_32x32b_x16(tmem + COL_D2P + 32u, im);
-                    tc::tmem_ld_wait();
-                    pin16(re);
-                    pin16(im);
-                    const int seg = lane, k = kb * US + seg;
-                    float2 B, D;
-                    phasor(s, k, 32.f, 64.f, B, D);
-#pragma unroll
-                    for (int i = 0; i < 16; i++)
-                        stage(seg, s, 32 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
-                }
+                epilogue1(j);
                 tc::fence_before();
-                tc::mbar_arrive(bar(B_EPI2P));
-                worker_bar();                                   // the unit's staging is complete
-
-                // ---- write-out: (channel, 8-segment group) tasks, 4 lanes per channel ----
-                __half* out = reinterpret_cast<__half*>(a.out);
-                const int64_t row0 = (int64_t)s * args.nkb + kb;       // run index of channel 0
-                const int64_t crow = (int64_t)args.s_rows * args.nkb;   // runs between channels
-#pragma unroll 4
-                for (int r = 0; r < (FC * 4) / WORKERS; r++) {
-                    const int task = r * WORKERS + tid;
-                    const int c = task >> 2, g4 = task & 3;
-                    uint32_t w[8];
-#pragma unroll
-                    for (int i = 0; i < 8; i++) w[i] = stg[(8 * g4 + i) * STG_PITCH + c];
-                    __half* run = out + ((int64_t)c * crow + row0) * 64;
-                    *reinterpret_cast<uint4*>(run + 8 * g4) =
-                        make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
-                                   __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
-                    *reinterpret_cast<uint4*>(run + 32 + 8 * g4) =
-                        make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
-                                   __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
+                tc::fence_proxy_async();
+                tc::mbar_arrive(bar(B_EPI1));
+                // B1 is free: pass 1 of quad j has completed (D1FULL)
+                if (j + 1 < nquads) {
+                    cp_async_wait_all();
+                    worker_bar();                               // every thread's copies have landed
+                    decode(j + 1);
+                    tc::fence_proxy_async();
+                    tc::mbar_arrive(bar(B_B1FULL));
                 }
-                worker_bar();                                   // staging free for the next unit
+                // raw buffer j & 1 (and its offsets) were read by decode(j),
+                // behind the worker barrier above
+                if (j + 2 < nquads) fetch(j + 2);
+            }
+            if (j >= 1) {
+                const int jj = j - 1, u = jj / QUADS;
+                int s, kb;
+                unit_of(u, s, kb);
+                ok = tc::mbar_wait(bar(B_D2FULL0 + (jj & 1)), (uint32_t)(jj >> 1) & 1, &g_fst32_error, E_WORKER_WAIT,
+                                   WAIT_CYCLES);
+                if (!worker_vote(ok)) { ok = false; break; }
+                tc::fence_after();
+                epilogue2(jj, s, kb);
+                tc::fence_before();
+                tc::mbar_arrive(bar(B_EPI2_0 + (jj & 1)));
+                if (jj % QUADS == QUADS - 1) {
+                    ok = tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+                    if (!worker_vote(ok)) { ok = false; break; }
+                    tc::fence_after();
+                    unit_end(u, s, kb);
+                }
             }
         }
         cp_async_wait_all();
