@@ -209,6 +209,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_unpack2bit": ([V, LL, I, I, V, V, I], I),
             "cellspe_fft_c2c": ([V, V, I, LL, I], I),
             "cellspe_fft_r2c": ([V, V, I, LL, I], I),
+            "cellspe_fft_r2c_perm": ([V, V, I, LL, I], I),
             "cellspe_xmac": ([V, I, I, I, V, I, I], I),
             "cellspe_vis_lags": ([V, V, LL, I, D, I], I),
             "cellspe_xmac_f16": ([V, I, I, I, V, I, I], I),
@@ -315,6 +316,14 @@ def fft_c2c(x, out, n: int, batch: int):
 
 def fft_r2c(x, out, n: int, batch: int):
     _check(lib().cellspe_fft_r2c(_ptr(x)[0], _ptr(out)[0], n, batch, _mem(x, out)))
+    return out
+
+
+def fft_r2c_perm(x, out):
+    """cellspe_fft_r2c_perm: rows of n reals -> IPP Perm-packed rows of n floats."""
+    n = x.shape[-1]
+    batch = (x.size if isinstance(x, np.ndarray) else x.numel()) // n
+    _check(lib().cellspe_fft_r2c_perm(_ptr(x)[0], _ptr(out)[0], n, batch, _mem(x, out)))
     return out
 
 

@@ -48,6 +48,33 @@ const float2* cs_twiddles(int n)
     return d;
 }
 
+// IPP "Perm" packing of real-FFT bins (ippsDFTFwd_RToPerm_32f, read back by
+// TaskCoreIPP::doMaths, TaskCoreIPP.cpp:430, 438-439): each row of n floats is
+// [R0, R_{n/2}, Re 1, Im 1, ..., Re n/2-1, Im n/2-1], i.e. the n/2+1 complex
+// bins with the (zero) imaginary part of bin 0 replaced by the real Nyquist
+// bin and the Nyquist bin dropped.  bins [batch][n/2+1], out [batch][n].
+__global__ void k_perm_pack(const float2* __restrict__ bins, float* __restrict__ out, int n, int64_t batch)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;     // float2 slot of the output
+    const int half = n / 2;
+    if (i >= batch * half) return;
+    const int64_t row = i / half;
+    const int k = (int)(i - row * half);
+    const float2* b = bins + row * (half + 1);
+    float2 v = b[k];
+    if (k == 0) v.y = b[half].x;
+    reinterpret_cast<float2*>(out + row * n)[k] = v;
+}
+
+int cs_perm_pack(const float2* bins, float* out, int n, int64_t batch, cudaStream_t st)
+{
+    if (n < 2 || (n & 1) || batch < 0) return CS_ERR_ARG;
+    const int64_t total = batch * (n / 2);
+    if (total == 0) return 0;
+    k_perm_pack<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(bins, out, n, batch), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
 void cs_free_twiddles()
 {
     std::lock_guard<std::mutex> lk(g_tw_mu);

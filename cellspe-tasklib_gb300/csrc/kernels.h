@@ -34,6 +34,9 @@ int cs_cfft_batch(const float2* in, float2* out, int n, int64_t batch, cudaStrea
 int cs_cfft_inverse_batch(const float2* in, float2* out, int n, int64_t batch, float scale, cudaStream_t st);
 // Batched forward R2C FFT, n real points (64..32768) -> n/2+1 bins.
 int cs_rfft_batch(const float* in, float2* out, int n, int64_t batch, cudaStream_t st);
+// Real-FFT bins [batch][n/2+1] -> IPP Perm rows [batch][n] floats
+// ([R0, R_{n/2}, Re 1, Im 1, ...]).  bins and out must not overlap.
+int cs_perm_pack(const float2* bins, float* out, int n, int64_t batch, cudaStream_t st);
 
 // fstage.cu -----------------------------------------------------------------
 struct CsDelayState {       // per (input, segment)

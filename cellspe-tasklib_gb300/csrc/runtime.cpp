@@ -358,6 +358,24 @@ int op_fft(Workspace& ws, bool host, const void* in, void* out, int n, long long
     return j.finish();
 }
 
+// Real FFT with IPP Perm-packed rows: the bins go to workspace scratch, then
+// one packing pass writes [R0, R_{n/2}, Re 1, Im 1, ...] per row.
+int op_fft_perm(Workspace& ws, bool host, const float* in, float* out, int n, long long batch)
+{
+    if (!in || !out || batch < 0 || !pow2(n) || n < 32 || n > 32768)
+        return set_err(CELLSPE_ERR_ARG, "fft_r2c_perm: need n a power of two in [32, 32768]");
+    Job j(ws, host);
+    const void* d_in = j.in(in, (size_t)n * batch * 4);
+    void* bins = j.scratch((size_t)(n / 2 + 1) * batch * 8);
+    float* d_out = (float*)j.out(out, (size_t)n * batch * 4, false);
+    if (!j.err) {
+        int rc = map_rc(cs_rfft_batch((const float*)d_in, (float2*)bins, n, batch, ws.stream), "fft_r2c_perm");
+        if (!rc) rc = map_rc(cs_perm_pack((const float2*)bins, d_out, n, batch, ws.stream), "fft_r2c_perm pack");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
 int op_xmac(Workspace& ws, bool host, const void* spectra, int S, int C, int K, void* vis, int accumulate)
 {
     if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0) return set_err(CELLSPE_ERR_ARG, "xmac: bad arguments");
@@ -2080,6 +2098,12 @@ int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memo
 {
     DIRECT_PROLOGUE
     return op_fft(*ws, memory == CELLSPE_MEM_HOST, in, out, n, batch, true);
+}
+
+int cellspe_fft_r2c_perm(const float* in, float* out, int n, long long batch, int memory)
+{
+    DIRECT_PROLOGUE
+    return op_fft_perm(*ws, memory == CELLSPE_MEM_HOST, in, out, n, batch);
 }
 
 int cellspe_accumulate_f32(float* acc, const float* add, long long n, int memory)

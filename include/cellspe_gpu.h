@@ -81,6 +81,11 @@ int cellspe_unpack2bit(const void* raw, long long nsamp, int nchan, int format,
  * n/2+1 bins, n in [32, 32768], replaces genericFFTexec_R (architecture.h:563). */
 int cellspe_fft_c2c(const void* in, void* out, int n, long long batch, int memory);
 int cellspe_fft_r2c(const float* in, void* out, int n, long long batch, int memory);
+/* R2C with IPP "Perm" packing, the layout ippsDFTFwd_RToPerm_32f writes and
+ * TaskCoreIPP::doMaths reads (spectrometer/src/IA-32/TaskCoreIPP.cpp:116, 430,
+ * 438-439): n floats per row, [R0, R_{n/2}, Re X1, Im X1, ..., Re X_{n/2-1},
+ * Im X_{n/2-1}]; forward, unscaled; n a power of two in [32, 32768]. */
+int cellspe_fft_r2c_perm(const float* in, float* out, int n, long long batch, int memory);
 
 /* ---- XF lag products -------------------------------------------------------
  * lags[p][m] = scale * sum_c vis[p][c] exp(+2 pi i c m / C): the backward,

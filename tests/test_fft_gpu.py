@@ -55,3 +55,26 @@ def test_fft_large_batch_device(cg):
     ref = torch.fft.rfft(x.double(), dim=1)
     err = (torch.linalg.norm(out.to(torch.complex128) - ref) / torch.linalg.norm(ref)).item()
     assert err < TOL
+
+
+@pytest.mark.parametrize("n,batch", [(32, 3), (2048, 5), (32768, 2)])
+def test_fft_r2c_perm_packing(cg, n, batch):
+    """IPP Perm rows as TaskCoreIPP::doMaths reads them (TaskCoreIPP.cpp:438-439:
+    element 0 the DC bin, element 1 the Nyquist bin, then Re/Im pairs of bins
+    1..n/2-1), against an FP64 real FFT; host and device buffers."""
+    import torch
+
+    rng = np.random.default_rng(n + batch)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    out = np.zeros((batch, n), np.float32)
+    cg.fft_r2c_perm(x, out)
+    X = np.fft.rfft(x.astype(np.float64), axis=1)
+    ref = np.empty((batch, n))
+    ref[:, 0] = X[:, 0].real
+    ref[:, 1] = X[:, n // 2].real
+    ref[:, 2::2] = X[:, 1:n // 2].real
+    ref[:, 3::2] = X[:, 1:n // 2].imag
+    assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-5
+    xd, od = torch.from_numpy(x).cuda(), torch.zeros((batch, n), dtype=torch.float32, device="cuda")
+    cg.fft_r2c_perm(xd, od)
+    assert np.array_equal(od.cpu().numpy(), out)
