@@ -32,8 +32,8 @@
 // 128-byte run (32 Re halves, 32 Im halves), written by the workers from the
 // staging with 16-byte stores, 4 lanes per 64-byte half-run.
 //
-// Warps 0..7 are the workers (decode, both epilogues, write-out); warp 8 owns
-// TMEM and one of its threads issues the MMAs.  The workers' loop is skewed so
+// Warps 0..15 are the workers (decode, both epilogues, write-out); warp 16
+// owns TMEM and one of its threads issues the MMAs.  The workers' loop is skewed so
 // that they never wait on an MMA they just enabled: iteration j runs
 // epilogue 1 of quad j, the decode of quad j+1 and epilogue 2 of quad j-1, so
 // pass 2 of quad j runs during the decode and epilogue 2, and pass 1 of quad
@@ -59,7 +59,8 @@ constexpr int FN = 2048, FC = 1024;
 constexpr int QS = 4;                                 // segments per quad
 constexpr int US = 32;                                // segments per unit
 constexpr int QUADS = US / QS;
-constexpr int WORKERS = 256, THREADS = WORKERS + 32;  // + MMA warp (8)
+constexpr int WORKERS = 512, THREADS = WORKERS + 32;  // + the MMA warp
+constexpr int MMA_WARP = WORKERS / 32;
 constexpr int RAWC = 34;                              // 16-byte raw chunks per segment (2048 samples + slack)
 // constant operands (pre-swizzled on the host)
 constexpr int OFF_A1 = 0;                             // DFT-64: 128 rows x 128 B, K-major, 128-byte swizzle
@@ -112,15 +113,16 @@ CS_DEV void cp_async16(uint32_t dst, const void* src, bool valid)
 CS_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 CS_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-CS_DEV void worker_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-// all 256 workers agree on `ok` (and synchronise)
+static_assert(WORKERS == 512, "the named barriers below count 512 workers");
+CS_DEV void worker_bar() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
+// all workers agree on `ok` (and synchronise)
 CS_DEV bool worker_vote(bool ok)
 {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.and.pred q, 1, 256, p;\n\t"
+        "bar.red.and.pred q, 1, 512, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(r)
         : "r"(ok ? 1u : 0u)
@@ -174,7 +176,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
         reinterpret_cast<uint4*>(sm)[i] = __ldg(args.consts + i);
     for (int i = tid; i < 2 * A2P_REGION / 16; i += THREADS)
         reinterpret_cast<uint4*>(sm + OFF_A2P)[i] = make_uint4(0, 0, 0, 0);
-    if (tid < 16) lut2[tid] = __floats2half2_rn(a.lut[tid & 3], a.lut[tid >> 2]);
+    if (tid < 16) {
+        // the level table is in parameter space: read with constant indices only
+        const float l0 = a.lut[0], l1 = a.lut[1], l2 = a.lut[2], l3 = a.lut[3];
+        auto lv = [&](int c) { return c == 0 ? l0 : c == 1 ? l1 : c == 2 ? l2 : l3; };
+        lut2[tid] = __floats2half2_rn(lv(tid & 3), lv(tid >> 2));
+    }
     if (tid == 0) {
         tc::mbar_init(bar(B_B1FULL), WORKERS);
         tc::mbar_init(bar(B_D1FULL), 1);
@@ -188,7 +195,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
         tc::mbar_init(bar(B_DRAIN), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 8) tc::tmem_alloc(tc::smem_u32(slot), TMEM_COLS);
+    if (warp == MMA_WARP) tc::tmem_alloc(tc::smem_u32(slot), TMEM_COLS);
     tc::fence_proxy_async();                       // constant operands -> tensor core
     tc::fence_before();
     __syncthreads();
@@ -200,7 +207,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
     const int nquads = nunits * QUADS;
     const int K = a.K;
 
-    if (warp == 8) {
+    if (warp == MMA_WARP) {
         // ------------------------------ MMA issuer ------------------------------
         if (lane == 0) {
             const uint32_t id1 = tc::idesc_f16(128, 128, false, false, true);    // B1 MN-major
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
         __syncwarp();
     } else {
         // ------------------------------ workers ------------------------------
-        const int q = warp & 3, h = warp >> 2;        // TMEM lane quarter, half
+        const int q = warp & 3, h = warp >> 2;        // TMEM lane quarter, quarter of the work
         const int64_t chunks = a.bytes_per_input >> 4;
         const int k1 = 8 * q + (lane >> 2);           // epilogue 1: this thread's k1 (< 32)
 
@@ -315,9 +322,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
         auto decode = [&](int j) {
             const uint32_t* rw0 = reinterpret_cast<const uint32_t*>(sm + OFF_RAW + (j & 1) * RAW_BYTES);
             unsigned char* b1 = sm + OFF_B1;
-#pragma unroll
-            for (int r = 0; r < 2; r++) {
-                const int idx = tid + WORKERS * r;
+            {
+                const int idx = tid;                      // QS x 128 words, one per worker
                 const int g = idx >> 7, wd = idx & 127;
                 const int off = offs[(j & 1) * QS + g];
                 const uint32_t* rw = rw0 + g * RAWC * 4 + (off >> 4) + wd;
@@ -333,137 +339,31 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             }
         };
         uint32_t* stg = reinterpret_cast<uint32_t*>(sm + OFF_STG);
-        // one spectrum value of the segment (unit-relative `seg`) into the staging
-        auto stage = [&](int seg, int s, int c, float2 X, float2& B, const float2 D) {
-            if (PHASE) {
-                X = cmul(X, B);
-                B = cmul(B, D);
-            }
-            if (a.scale) X = cscale(X, __ldg(a.scale + (int64_t)s * FC + c));
-            stg[seg * STG_PITCH + c] = h2u(__floats2half2_rn(X.x, X.y));
-        };
-        auto phasor = [&](int s, int k, float cstart, float cstep, float2& B, float2& D) {
-            if (PHASE) {
-                const int64_t sk = (int64_t)s * K + k;
-                const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);
-                float sn, cs;
-                sincosf(ph0 + cstart * dph, &sn, &cs);
-                B = make_float2(cs, sn);
-                sincosf(cstep * dph, &sn, &cs);
-                D = make_float2(cs, sn);
-            } else {
-                B = D = make_float2(1.f, 0.f);
-            }
-        };
-
-        // ---- epilogue 1 of quad j: Y -> Z = Y W_2048^(n2 k1) -> A2 buffer j & 1 ----
-        auto epilogue1 = [&](int j) {
-            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
-            unsigned char* a2 = sm + OFF_A2 + b * A2_BYTES;
-            unsigned char* a2p = sm + OFF_A2P + (u & 1) * A2P_REGION;
-            const uint32_t d1 = tmem + COL_D1 + 128u * b;
-#pragma unroll
-            for (int gi = 0; gi < 2; gi++) {
-                const int g = 2 * h + gi;                 // segment in the quad
-                uint32_t r[16];
-                tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16) + 32u * g, r);
-                uint32_t r32[16];
-                if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16) + 32u * g, r32);
-                tc::tmem_ld_wait();
-                pin16(r);
-                const uint32_t row = 32 * g + k1;
-#pragma unroll
-                for (int m = 0; m < 4; m++) {
-                    const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
-                    const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
-                    const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
-                    const uint32_t kpos = 8 * m + 2 * (lane & 3);
-                    *reinterpret_cast<uint32_t*>(a2 + sw128(row, kpos)) = h2u(__floats2half2_rn(z0.x, z1.x));
-                    *reinterpret_cast<uint32_t*>(a2 + sw128(row, 32 + kpos)) = h2u(__floats2half2_rn(z0.y, z1.y));
-                }
-                if (q == 0) {
-                    // lanes 16..23 hold copies of the real k1 = 32 row: thread
-                    // (lane) takes column 8 m32 + 2 (lane % 4) + e32 of its copy
-                    pin16(r32);
-                    float y = 0.f;                         // r32[4 m32 + e32] without local memory
-#pragma unroll
-                    for (int i = 0; i < 16; i++)
-                        if (i == 4 * m32 + e32) y = __uint_as_float(r32[i]);
-                    const __half zr = __float2half_rn(y * tw32.x), zi = __float2half_rn(y * tw32.y);
-                    const uint32_t prow = QS * qd + g;     // segment of the unit
-                    *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = zr;
-                    *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = zi;
-                }
-            }
-        };
-        // ---- epilogue 2 of quad j: X -> phasor, scale -> FP16 staging ----
-        auto epilogue2 = [&](int j, int s, int kb) {
-            // lane quarter q = segment q of the quad, lane = k1; half h: k2 in [16 h, 16 h + 16)
-            const int b = j & 1, qd = j % QUADS;
-            const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
-            uint32_t re[16], im[16];
-            tc::tmem_ld_32x32b_x16(d2 + 16u * h, re);
-            tc::tmem_ld_32x32b_x16(d2 + 32u + 16u * h, im);
-            tc::tmem_ld_wait();
-            pin16(re);
-            pin16(im);
-            const int kk1 = lane;                           // k1 of this TMEM lane
-            const int seg = QS * qd + q, k = kb * US + seg;
-            float2 B, D;
-            if (h == 0) {
-                // c = k1 + 64 k2, k2 < 16
-                phasor(s, k, (float)kk1, 64.f, B, D);
-#pragma unroll
-                for (int i = 0; i < 16; i++)
-                    stage(seg, s, kk1 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
-            } else if (kk1 > 0) {
-                // c = 2048 - k1 - 64 k2 (k2 = 16 + i) holds conj(X[k1 + 64 k2])
-                phasor(s, k, (float)(FC - kk1), -64.f, B, D);
-#pragma unroll
-                for (int i = 0; i < 16; i++)
-                    stage(seg, s, FC - kk1 - 64 * i, make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])), B, D);
-            }
-        };
-        // ---- the unit's k1 = 32 channels (c = 32 + 64 k2), then its write-out ----
-        auto unit_end = [&](int u, int s, int kb) {
-            if (warp == 0) {
-                uint32_t re[16], im[16];
-                tc::tmem_ld_32x32b_x16(tmem + COL_D2P, re);
-                tc::tmem_ld_32x32b_x16(tmem + COL_D2P + 32u, im);
-                tc::tmem_ld_wait();
-                pin16(re);
-                pin16(im);
-                const int seg = lane, k = kb * US + seg;
-                float2 B, D;
-                phasor(s, k, 32.f, 64.f, B, D);
-#pragma unroll
-                for (int i = 0; i < 16; i++)
-                    stage(seg, s, 32 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])), B, D);
-            }
-            tc::fence_before();
-            tc::mbar_arrive(bar(B_EPI2P));
-            worker_bar();                                   // the unit's staging is complete
-            // (channel, 8-segment group) tasks, 4 lanes per channel
-            __half* out = reinterpret_cast<__half*>(a.out);
-            const int64_t row0 = (int64_t)s * args.nkb + kb;       // run index of channel 0
-            const int64_t crow = (int64_t)args.s_rows * args.nkb;   // runs between channels
-#pragma unroll 4
-            for (int r = 0; r < (FC * 4) / WORKERS; r++) {
-                const int task = r * WORKERS + tid;
-                const int c = task >> 2, g4 = task & 3;
-                uint32_t w[8];
-#pragma unroll
-                for (int i = 0; i < 8; i++) w[i] = stg[(8 * g4 + i) * STG_PITCH + c];
-                __half* run = out + ((int64_t)c * crow + row0) * 64;
-                *reinterpret_cast<uint4*>(run + 8 * g4) =
-                    make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
-                               __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
-                *reinterpret_cast<uint4*>(run + 32 + 8 * g4) =
-                    make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
-                               __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
-            }
-            worker_bar();                                   // staging free for the next unit
-        };
+        // (B, D) = exp(i (phase0 + cstart dphase)), exp(i cstep dphase) of segment k
+        // of input s: the delay model's phasor at the first channel a thread
+        // writes and its step to the next (the identity without a delay model)
+#define TC32_PHASOR(s_, k_, cstart, cstep)                                              \
+        float2 B = make_float2(1.f, 0.f), D = B;                                        \
+        if (PHASE) {                                                                    \
+            const int64_t sk = (int64_t)(s_) * K + (k_);                                \
+            const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);         \
+            float sn, cs;                                                               \
+            sincosf(ph0 + (cstart) * dph, &sn, &cs);                                    \
+            B = make_float2(cs, sn);                                                    \
+            sincosf((cstep) * dph, &sn, &cs);                                           \
+            D = make_float2(cs, sn);                                                    \
+        }
+        // one spectrum value X of channel c_ (unit-relative segment seg_) into the staging
+#define TC32_STAGE(seg_, s_, c_, X_)                                                    \
+        {                                                                               \
+            float2 X = (X_);                                                            \
+            if (PHASE) {                                                                \
+                X = cmul(X, B);                                                         \
+                B = cmul(B, D);                                                         \
+            }                                                                           \
+            if (scl) X = cscale(X, __ldg(scl + (c_)));                                  \
+            stg[(seg_) * STG_PITCH + (c_)] = h2u(__floats2half2_rn(X.x, X.y));          \
+        }
 
         bool ok = true;
         if (nquads > 0) {
@@ -481,7 +381,43 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 ok = tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
                 if (!worker_vote(ok)) { ok = false; break; }
                 tc::fence_after();
-                epilogue1(j);
+                // ---- epilogue 1: Y -> Z = Y W_2048^(n2 k1) -> A2 buffer j & 1; warp (q, h):
+                // TMEM lane quarter q (k1 = 8q..8q+7), segment h of the quad ----
+                {
+                    const int b = j & 1, qd = j % QUADS, u = j / QUADS, g = h;
+                    unsigned char* a2 = sm + OFF_A2 + b * A2_BYTES;
+                    const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * g;
+                    uint32_t r[16], r32[16];
+                    tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r);
+                    if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
+                    tc::tmem_ld_wait();
+                    pin16(r);
+                    const uint32_t row = 32 * g + k1;
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
+                        const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
+                        const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
+                        const uint32_t kpos = 8 * m + 2 * (lane & 3);
+                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, kpos)) = h2u(__floats2half2_rn(z0.x, z1.x));
+                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, 32 + kpos)) = h2u(__floats2half2_rn(z0.y, z1.y));
+                    }
+                    if (q == 0) {
+                        // lanes 16..23 hold copies of the real k1 = 32 row: thread
+                        // (lane) takes column 8 m32 + 2 (lane % 4) + e32 of its copy
+                        pin16(r32);
+                        // y = r32[4 m32 + e32] as selects on constant indices
+                        // (an indexed read would put r32 in local memory)
+                        const bool m1 = m32 & 1, m2 = m32 & 2;
+                        const uint32_t ya = m2 ? (m1 ? r32[12] : r32[8]) : (m1 ? r32[4] : r32[0]);
+                        const uint32_t yb = m2 ? (m1 ? r32[13] : r32[9]) : (m1 ? r32[5] : r32[1]);
+                        const float y = __uint_as_float(e32 ? yb : ya);
+                        unsigned char* a2p = sm + OFF_A2P + (u & 1) * A2P_REGION;
+                        const uint32_t prow = QS * qd + g;     // segment of the unit
+                        *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = __float2half_rn(y * tw32.x);
+                        *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = __float2half_rn(y * tw32.y);
+                    }
+                }
                 tc::fence_before();
                 tc::fence_proxy_async();
                 tc::mbar_arrive(bar(B_EPI1));
@@ -498,29 +434,103 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 if (j + 2 < nquads) fetch(j + 2);
             }
             if (j >= 1) {
-                const int jj = j - 1, u = jj / QUADS;
+                const int jj = j - 1, u = jj / QUADS, b = jj & 1, qd = jj % QUADS;
                 int s, kb;
                 unit_of(u, s, kb);
-                ok = tc::mbar_wait(bar(B_D2FULL0 + (jj & 1)), (uint32_t)(jj >> 1) & 1, &g_fst32_error, E_WORKER_WAIT,
+                const float* scl = a.scale ? a.scale + (int64_t)s * FC : nullptr;
+                ok = tc::mbar_wait(bar(B_D2FULL0 + b), (uint32_t)(jj >> 1) & 1, &g_fst32_error, E_WORKER_WAIT,
                                    WAIT_CYCLES);
                 if (!worker_vote(ok)) { ok = false; break; }
                 tc::fence_after();
-                epilogue2(jj, s, kb);
+                // ---- epilogue 2: X -> phasor, scale -> FP16 staging; warp (q, h): lane
+                // quarter q = segment q of the quad, lane = k1, k2 in [8 h, 8 h + 8) ----
+                {
+                    const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
+                    uint32_t re[8], im[8];
+                    tc::tmem_ld_32x32b_x8(d2 + 8u * h, re);
+                    tc::tmem_ld_32x32b_x8(d2 + 32u + 8u * h, im);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        asm volatile("" : "+r"(re[i]));
+                        asm volatile("" : "+r"(im[i]));
+                    }
+                    const int kk1 = lane;                       // k1 of this TMEM lane
+                    const int seg = QS * qd + q, k = kb * US + seg;
+                    if (h < 2) {
+                        // c = k1 + 64 k2, k2 = 8 h + i < 16
+                        const int c0 = kk1 + 512 * h;
+                        TC32_PHASOR(s, k, (float)c0, 64.f)
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            TC32_STAGE(seg, s, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
+                    } else if (kk1 > 0) {
+                        // c = 2048 - k1 - 64 k2 (k2 = 8 h + i >= 16) holds conj(X[k1 + 64 k2])
+                        const int c0 = FC - kk1 - 512 * (h - 2);
+                        TC32_PHASOR(s, k, (float)c0, -64.f)
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            TC32_STAGE(seg, s, c0 - 64 * i, make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])))
+                    }
+                }
                 tc::fence_before();
-                tc::mbar_arrive(bar(B_EPI2_0 + (jj & 1)));
-                if (jj % QUADS == QUADS - 1) {
+                tc::mbar_arrive(bar(B_EPI2_0 + b));
+                if (qd == QUADS - 1) {
                     ok = tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
                     if (!worker_vote(ok)) { ok = false; break; }
                     tc::fence_after();
-                    unit_end(u, s, kb);
+                    // ---- the unit's k1 = 32 channels (c = 32 + 64 k2, k2 < 16): warps
+                    // 0 and 4 (lane quarter 0: lane = segment of the unit) ----
+                    if (q == 0 && h < 2) {
+                        uint32_t re[8], im[8];
+                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 8u * h, re);
+                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 32u + 8u * h, im);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            asm volatile("" : "+r"(re[i]));
+                            asm volatile("" : "+r"(im[i]));
+                        }
+                        const int seg = lane, k = kb * US + seg, c0 = 32 + 512 * h;
+                        TC32_PHASOR(s, k, (float)c0, 64.f)
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            TC32_STAGE(seg, s, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
+                    }
+                    tc::fence_before();
+                    tc::mbar_arrive(bar(B_EPI2P));
+                    worker_bar();                               // the unit's staging is complete
+                    // ---- write-out: (channel, 8-segment group) tasks, 4 lanes per channel ----
+                    __half* out = reinterpret_cast<__half*>(a.out);
+                    const int64_t row0 = (int64_t)s * args.nkb + kb;       // run index of channel 0
+                    const int64_t crow = (int64_t)args.s_rows * args.nkb;   // runs between channels
+#pragma unroll 2
+                    for (int r = 0; r < (FC * 4) / WORKERS; r++) {
+                        const int task = r * WORKERS + tid;
+                        const int c = task >> 2, g4 = task & 3;
+                        const uint32_t* col = stg + 8 * g4 * STG_PITCH + c;
+                        uint32_t w[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) w[i] = col[i * STG_PITCH];
+                        __half* run = out + ((int64_t)c * crow + row0) * 64 + 8 * g4;
+                        *reinterpret_cast<uint4*>(run) =
+                            make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
+                                       __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
+                        *reinterpret_cast<uint4*>(run + 32) =
+                            make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
+                                       __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
+                    }
+                    worker_bar();                               // staging free for the next unit
                 }
             }
         }
+#undef TC32_PHASOR
+#undef TC32_STAGE
         cp_async_wait_all();
         tc::fence_before();
     }
     __syncthreads();
-    if (warp == 8) {
+    if (warp == MMA_WARP) {
         tc::fence_after();
         tc::tmem_dealloc(tmem, TMEM_COLS);
     }

@@ -122,6 +122,16 @@ __device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, uint32_t (&r)
         : "memory");
 }
 
+// 32 lanes x 32 bit, 8 columns: thread t <- lane t, register j <- column j.
+__device__ __forceinline__ void tmem_ld_32x32b_x8(uint32_t taddr, uint32_t (&r)[8])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
+}
+
 // 16 lanes x 256 bit, repeated 4x along the columns (32 columns): for
 // repetition m, thread t holds (lane t/4, columns 8m + 2(t%4) + {0,1}) in
 // r[4m], r[4m+1] and (lane 8 + t/4, same columns) in r[4m+2], r[4m+3].
