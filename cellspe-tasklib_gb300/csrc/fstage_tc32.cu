@@ -40,7 +40,9 @@
 // j+1 during epilogue 2 (A2 and D2 double-buffered, D1 double-buffered in
 // TMEM).  Every mbarrier wait is bounded
 // (~2 s): on timeout the threads record an error code, leave their loops
-// together (worker votes), drain the tensor pipe and free TMEM.
+// together (worker votes), drain the tensor pipe and free TMEM.  One worker
+// thread polls each barrier the workers wait on and the vote that follows
+// releases the others (no spinning warps); the workers arrive once per warp.
 #include "common.cuh"
 #include "kernels.h"
 #include "tcgen05.cuh"
@@ -130,6 +132,14 @@ CS_DEV bool worker_vote(bool ok)
     return r != 0;
 }
 
+// Worker arrival on a barrier that counts warps: every lane's earlier writes
+// (and its own fences) are ordered before lane 0's arrive by the warp sync.
+CS_DEV void warp_arrive(uint32_t bar)
+{
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) tc::mbar_arrive(bar);
+}
+
 // After tcgen05.wait::ld: ties the loaded registers to that point.
 CS_DEV void pin16(uint32_t (&r)[16])
 {
@@ -183,15 +193,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
         lut2[tid] = __floats2half2_rn(lv(tid & 3), lv(tid >> 2));
     }
     if (tid == 0) {
-        tc::mbar_init(bar(B_B1FULL), WORKERS);
+        tc::mbar_init(bar(B_B1FULL), WORKERS / 32);
         tc::mbar_init(bar(B_D1FULL), 1);
-        tc::mbar_init(bar(B_EPI1), WORKERS);
+        tc::mbar_init(bar(B_EPI1), WORKERS / 32);
         tc::mbar_init(bar(B_D2FULL0), 1);
         tc::mbar_init(bar(B_D2FULL0 + 1), 1);
-        tc::mbar_init(bar(B_EPI2_0), WORKERS);
-        tc::mbar_init(bar(B_EPI2_0 + 1), WORKERS);
+        tc::mbar_init(bar(B_EPI2_0), WORKERS / 32);
+        tc::mbar_init(bar(B_EPI2_0 + 1), WORKERS / 32);
         tc::mbar_init(bar(B_D2PFULL), 1);
-        tc::mbar_init(bar(B_EPI2P), WORKERS);
+        tc::mbar_init(bar(B_EPI2P), WORKERS / 32);
         tc::mbar_init(bar(B_DRAIN), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -285,6 +295,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 sincospi(-(double)((n2 * k1) & 2047) / 1024.0, &sn, &cs);
                 tw[m][e] = make_float2((float)cs, (float)sn);
             }
+        // epilogue 1 stores: A2 row 32 h + k1 (fixed per thread), K positions
+        // 8 m + 2 (lane % 4) (Re) and 32 + that (Im): swizzled byte offsets
+        uint32_t e1off[4][2];
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const uint32_t row = 32 * h + k1, kpos = 8 * m + 2 * (lane & 3);
+            e1off[m][0] = sw128(row, kpos);
+            e1off[m][1] = sw128(row, 32 + kpos);
+        }
         // the k1 = 32 row (quarter 0): this thread's (m, e) and W_64^(n2)
         const int m32 = (lane >> 2) & 3, e32 = lane >> 4;
         const int n2_32 = 8 * m32 + 2 * (lane & 3) + e32;
@@ -373,12 +392,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             worker_bar();
             decode(0);
             tc::fence_proxy_async();
-            tc::mbar_arrive(bar(B_B1FULL));
+            warp_arrive(bar(B_B1FULL));
         }
         // iteration j: epilogue 1 (j), decode (j+1), epilogue 2 (j-1)
         for (int j = 0; j <= nquads; j++) {
             if (j < nquads) {
-                ok = tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+                ok = tid != 0 || tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
                 if (!worker_vote(ok)) { ok = false; break; }
                 tc::fence_after();
                 // ---- epilogue 1: Y -> Z = Y W_2048^(n2 k1) -> A2 buffer j & 1; warp (q, h):
@@ -392,15 +411,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                     if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
                     tc::tmem_ld_wait();
                     pin16(r);
-                    const uint32_t row = 32 * g + k1;
 #pragma unroll
                     for (int m = 0; m < 4; m++) {
                         const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
                         const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
                         const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
-                        const uint32_t kpos = 8 * m + 2 * (lane & 3);
-                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, kpos)) = h2u(__floats2half2_rn(z0.x, z1.x));
-                        *reinterpret_cast<uint32_t*>(a2 + sw128(row, 32 + kpos)) = h2u(__floats2half2_rn(z0.y, z1.y));
+                        *reinterpret_cast<uint32_t*>(a2 + e1off[m][0]) = h2u(__floats2half2_rn(z0.x, z1.x));
+                        *reinterpret_cast<uint32_t*>(a2 + e1off[m][1]) = h2u(__floats2half2_rn(z0.y, z1.y));
                     }
                     if (q == 0) {
                         // lanes 16..23 hold copies of the real k1 = 32 row: thread
@@ -420,14 +437,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 }
                 tc::fence_before();
                 tc::fence_proxy_async();
-                tc::mbar_arrive(bar(B_EPI1));
+                warp_arrive(bar(B_EPI1));
                 // B1 is free: pass 1 of quad j has completed (D1FULL)
                 if (j + 1 < nquads) {
                     cp_async_wait_all();
                     worker_bar();                               // every thread's copies have landed
                     decode(j + 1);
                     tc::fence_proxy_async();
-                    tc::mbar_arrive(bar(B_B1FULL));
+                    warp_arrive(bar(B_B1FULL));
                 }
                 // raw buffer j & 1 (and its offsets) were read by decode(j),
                 // behind the worker barrier above
@@ -438,8 +455,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 int s, kb;
                 unit_of(u, s, kb);
                 const float* scl = a.scale ? a.scale + (int64_t)s * FC : nullptr;
-                ok = tc::mbar_wait(bar(B_D2FULL0 + b), (uint32_t)(jj >> 1) & 1, &g_fst32_error, E_WORKER_WAIT,
-                                   WAIT_CYCLES);
+                ok = tid != 0 || tc::mbar_wait(bar(B_D2FULL0 + b), (uint32_t)(jj >> 1) & 1, &g_fst32_error,
+                                               E_WORKER_WAIT, WAIT_CYCLES);
                 if (!worker_vote(ok)) { ok = false; break; }
                 tc::fence_after();
                 // ---- epilogue 2: X -> phasor, scale -> FP16 staging; warp (q, h): lane
@@ -474,9 +491,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                     }
                 }
                 tc::fence_before();
-                tc::mbar_arrive(bar(B_EPI2_0 + b));
+                warp_arrive(bar(B_EPI2_0 + b));
                 if (qd == QUADS - 1) {
-                    ok = tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+                    ok = tid != 0 || tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT,
+                                                   WAIT_CYCLES);
                     if (!worker_vote(ok)) { ok = false; break; }
                     tc::fence_after();
                     // ---- the unit's k1 = 32 channels (c = 32 + 64 k2, k2 < 16): warps
@@ -498,7 +516,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                             TC32_STAGE(seg, s, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
                     }
                     tc::fence_before();
-                    tc::mbar_arrive(bar(B_EPI2P));
+                    warp_arrive(bar(B_EPI2P));
                     worker_bar();                               // the unit's staging is complete
                     // ---- write-out: (channel, 8-segment group) tasks, 4 lanes per channel ----
                     __half* out = reinterpret_cast<__half*>(a.out);
