@@ -229,8 +229,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc(const __grid_consta
         if (lane == 0) {
             for (int j = 0; j < nunits; j++) {
                 if (!tc::mbar_wait(bar(B_REPACK), (uint32_t)j & 1, &g_fstc_error, E_STORE_WAIT, WAIT_CYCLES)) break;
-                const int64_t u = (int64_t)blockIdx.x + (int64_t)j * gridDim.x;
-                const int s = (int)(u / args.units_k), k0 = (int)(u % args.units_k) * G;
+                const uint32_t u = blockIdx.x + (uint32_t)j * gridDim.x;      // 32-bit: no FP64-assisted division
+                const int s = (int)(u / (uint32_t)args.units_k), k0 = (int)(u % (uint32_t)args.units_k) * G;
                 const uint32_t src = sbase + OFF_B1 + (uint32_t)(j & 1) * B1_BYTES;
 #pragma unroll 1
                 for (int b = 0; b < (FC * 2) / 256; b++) tma_store_3d(src + 4096u * b, &tmap_out, k0, s, 256 * b);
@@ -262,9 +262,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc(const __grid_consta
                 }
 
         auto unit_of = [&](int j, int& s, int& k0) {
-            const int64_t u = (int64_t)blockIdx.x + (int64_t)j * gridDim.x;
-            s = (int)(u / args.units_k);
-            k0 = (int)(u % args.units_k) * G;
+            const uint32_t u = blockIdx.x + (uint32_t)j * gridDim.x;
+            s = (int)(u / (uint32_t)args.units_k);
+            k0 = (int)(u % (uint32_t)args.units_k) * G;
         };
         // raw chunks of unit j -> raw buffer j & 1 (zero outside the input)
         auto fetch = [&](int j) {
@@ -526,6 +526,7 @@ bool cs_fstage_tc_supported(const CsFStageArgs& a)
 int cs_fx_fstage_tc(const CsFStageArgs& a, cudaStream_t st)
 {
     if (!cs_fstage_tc_supported(a)) return CS_ERR_UNSUPPORTED;
+    if ((int64_t)a.S * ((a.K + G - 1) / G) >= (int64_t)1 << 31) return CS_ERR_UNSUPPORTED;   // 32-bit unit indices
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
     const uint4* consts = tc_constants();

@@ -314,10 +314,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             tw32 = make_float2((float)cs, (float)sn);
         }
 
+        // unit u of this CTA -> (input, 32-segment block); 32-bit arithmetic
+        // (a 64-bit division is a long FP64-assisted sequence on the GPU)
         auto unit_of = [&](int u, int& s, int& kb) {
-            const int64_t uu = (int64_t)blockIdx.x + (int64_t)u * gridDim.x;
-            s = (int)(uu / args.units_k);
-            kb = (int)(uu % args.units_k);
+            const uint32_t uu = blockIdx.x + (uint32_t)u * gridDim.x;
+            const uint32_t si = uu / (uint32_t)args.units_k;
+            s = (int)si;
+            kb = (int)(uu - si * (uint32_t)args.units_k);
         };
         // raw chunks of quad j -> raw buffer j & 1 (zero outside the input)
         auto fetch = [&](int j) {
@@ -622,6 +625,7 @@ bool cs_fstage_tc32_supported(const CsFStageArgs& a)
 int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st)
 {
     if (!cs_fstage_tc32_supported(a)) return CS_ERR_UNSUPPORTED;
+    if ((int64_t)a.S * (a.K / US) >= (int64_t)1 << 31) return CS_ERR_UNSUPPORTED;   // unit indices are 32-bit
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
     const uint4* consts = tc32_constants();
