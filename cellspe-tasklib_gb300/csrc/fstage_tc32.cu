@@ -291,9 +291,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
 #pragma unroll
             for (int e = 0; e < 2; e++) {
                 const int n2 = 8 * m + 2 * (lane & 3) + e;
-                double sn, cs;
-                sincospi(-(double)((n2 * k1) & 2047) / 1024.0, &sn, &cs);
-                tw[m][e] = make_float2((float)cs, (float)sn);
+                float sn, cs;
+                sincospif(-(float)((n2 * k1) & 2047) / 1024.0f, &sn, &cs);
+                tw[m][e] = make_float2(cs, sn);
             }
         // epilogue 1 stores: A2 row 32 h + k1 (fixed per thread), K positions
         // 8 m + 2 (lane % 4) (Re) and 32 + that (Im): swizzled byte offsets
@@ -309,9 +309,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
         const int n2_32 = 8 * m32 + 2 * (lane & 3) + e32;
         float2 tw32;
         {
-            double sn, cs;
-            sincospi(-(double)n2_32 / 32.0, &sn, &cs);
-            tw32 = make_float2((float)cs, (float)sn);
+            float sn, cs;
+            sincospif(-(float)n2_32 / 32.0f, &sn, &cs);
+            tw32 = make_float2(cs, sn);
         }
 
         // unit u of this CTA -> (input, 32-segment block); 32-bit arithmetic
@@ -397,23 +397,52 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             tc::fence_proxy_async();
             warp_arrive(bar(B_B1FULL));
         }
-        // iteration j: epilogue 1 (j), decode (j+1), epilogue 2 (j-1)
+        // Iteration j: one wait (worker thread 0 polls D1 of quad j, D2 of
+        // quad j-1 and, at a unit's end, D2'; the vote releases the others,
+        // and every thread's raw-word copies have landed before it), the TMEM
+        // loads of both epilogues issued together, then epilogue 1 (j), the
+        // decode of quad j+1, the fetch of quad j+2 and epilogue 2 (j-1).
         for (int j = 0; j <= nquads; j++) {
-            if (j < nquads) {
-                ok = tid != 0 || tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
-                if (!worker_vote(ok)) { ok = false; break; }
-                tc::fence_after();
+            const bool do1 = j < nquads, do2 = j >= 1;
+            const int jj = j - 1;
+            const bool uend = do2 && (jj % QUADS == QUADS - 1);
+            cp_async_wait_all();
+            ok = true;
+            if (tid == 0) {
+                if (do1) ok = tc::mbar_wait(bar(B_D1FULL), (uint32_t)j & 1, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+                if (ok && do2)
+                    ok = tc::mbar_wait(bar(B_D2FULL0 + (jj & 1)), (uint32_t)(jj >> 1) & 1, &g_fst32_error,
+                                       E_WORKER_WAIT, WAIT_CYCLES);
+                if (ok && uend)
+                    ok = tc::mbar_wait(bar(B_D2PFULL), (uint32_t)(jj / QUADS) & 1, &g_fst32_error, E_WORKER_WAIT,
+                                       WAIT_CYCLES);
+            }
+            if (!worker_vote(ok)) { ok = false; break; }
+            tc::fence_after();
+            uint32_t r[16], r32[16], re[8], im[8];
+            if (do1) {
+                const uint32_t d1 = tmem + COL_D1 + 128u * (j & 1) + 32u * h;
+                tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r);
+                if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
+            }
+            if (do2) {
+                const uint32_t d2 = tmem + COL_D2 + 64u * (jj & 1) + ((uint32_t)(32 * q) << 16);
+                tc::tmem_ld_32x32b_x8(d2 + 8u * h, re);
+                tc::tmem_ld_32x32b_x8(d2 + 32u + 8u * h, im);
+            }
+            tc::tmem_ld_wait();
+            pin16(r);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                asm volatile("" : "+r"(re[i]));
+                asm volatile("" : "+r"(im[i]));
+            }
+            if (do1) {
                 // ---- epilogue 1: Y -> Z = Y W_2048^(n2 k1) -> A2 buffer j & 1; warp (q, h):
                 // TMEM lane quarter q (k1 = 8q..8q+7), segment h of the quad ----
                 {
                     const int b = j & 1, qd = j % QUADS, u = j / QUADS, g = h;
                     unsigned char* a2 = sm + OFF_A2 + b * A2_BYTES;
-                    const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * g;
-                    uint32_t r[16], r32[16];
-                    tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r);
-                    if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
-                    tc::tmem_ld_wait();
-                    pin16(r);
 #pragma unroll
                     for (int m = 0; m < 4; m++) {
                         const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
@@ -441,40 +470,24 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 tc::fence_before();
                 tc::fence_proxy_async();
                 warp_arrive(bar(B_EPI1));
-                // B1 is free: pass 1 of quad j has completed (D1FULL)
+                // B1 is free (pass 1 of quad j completed) and the raw words of
+                // quad j+1 are in shared memory (waited before the vote)
                 if (j + 1 < nquads) {
-                    cp_async_wait_all();
-                    worker_bar();                               // every thread's copies have landed
                     decode(j + 1);
                     tc::fence_proxy_async();
                     warp_arrive(bar(B_B1FULL));
                 }
-                // raw buffer j & 1 (and its offsets) were read by decode(j),
-                // behind the worker barrier above
+                // raw buffer j & 1 was read by decode(j) before this iteration's vote
                 if (j + 2 < nquads) fetch(j + 2);
             }
-            if (j >= 1) {
-                const int jj = j - 1, u = jj / QUADS, b = jj & 1, qd = jj % QUADS;
+            if (do2) {
+                const int u = jj / QUADS, b = jj & 1, qd = jj % QUADS;
                 int s, kb;
                 unit_of(u, s, kb);
                 const float* scl = a.scale ? a.scale + (int64_t)s * FC : nullptr;
-                ok = tid != 0 || tc::mbar_wait(bar(B_D2FULL0 + b), (uint32_t)(jj >> 1) & 1, &g_fst32_error,
-                                               E_WORKER_WAIT, WAIT_CYCLES);
-                if (!worker_vote(ok)) { ok = false; break; }
-                tc::fence_after();
                 // ---- epilogue 2: X -> phasor, scale -> FP16 staging; warp (q, h): lane
                 // quarter q = segment q of the quad, lane = k1, k2 in [8 h, 8 h + 8) ----
                 {
-                    const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
-                    uint32_t re[8], im[8];
-                    tc::tmem_ld_32x32b_x8(d2 + 8u * h, re);
-                    tc::tmem_ld_32x32b_x8(d2 + 32u + 8u * h, im);
-                    tc::tmem_ld_wait();
-#pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        asm volatile("" : "+r"(re[i]));
-                        asm volatile("" : "+r"(im[i]));
-                    }
                     const int kk1 = lane;                       // k1 of this TMEM lane
                     const int seg = QS * qd + q, k = kb * US + seg;
                     if (h < 2) {
@@ -495,11 +508,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 }
                 tc::fence_before();
                 warp_arrive(bar(B_EPI2_0 + b));
-                if (qd == QUADS - 1) {
-                    ok = tid != 0 || tc::mbar_wait(bar(B_D2PFULL), (uint32_t)u & 1, &g_fst32_error, E_WORKER_WAIT,
-                                                   WAIT_CYCLES);
-                    if (!worker_vote(ok)) { ok = false; break; }
-                    tc::fence_after();
+                if (uend) {
                     // ---- the unit's k1 = 32 channels (c = 32 + 64 k2, k2 < 16): warps
                     // 0 and 4 (lane quarter 0: lane = segment of the unit) ----
                     if (q == 0 && h < 2) {
