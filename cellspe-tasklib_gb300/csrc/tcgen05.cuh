@@ -37,14 +37,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
+// As mbar_try_wait, but the thread may be suspended in hardware for up to
+// `ns` nanoseconds while the phase is incomplete (it resumes as soon as the
+// phase completes), so a waiting thread issues no spin loop.
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint32_t bar, uint32_t parity, uint32_t ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait on phase `parity`: false (and `code` recorded in *err) after
-// `limit` cycles.
+// `limit` cycles.  Between checks of the bound the thread sleeps in
+// try_wait (at most 0.1 ms at a time) instead of spinning.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned* err, unsigned code,
                                           long long limit)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
+    while (!mbar_try_wait_suspend(bar, parity, 100000u)) {
         if (clock64() - t0 > limit) {
             atomicCAS(err, 0u, code);
             return false;
