@@ -141,7 +141,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc(const __grid_consta
                                                                 const __grid_constant__ CUtensorMap tmap_out)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    // offset from the shared array itself (not an integer round trip), so that
+    // the compiler keeps shared-space 32-bit addressing for every access
+    unsigned char* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
     const uint32_t sbase = tc::smem_u32(sm);
     const CsFStageArgs& a = args.f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -169,7 +169,9 @@ template <bool PHASE>
 __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_constant__ Tc32Args args)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    // offset from the shared array itself (not an integer round trip), so that
+    // the compiler keeps shared-space 32-bit addressing for every access
+    unsigned char* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
     const uint32_t sbase = tc::smem_u32(sm);
     const CsFStageArgs& a = args.f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -296,14 +298,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 tw[m][e] = make_float2(cs, sn);
             }
         // epilogue 1 stores: A2 row 32 h + k1 (fixed per thread), K positions
-        // 8 m + 2 (lane % 4) (Re) and 32 + that (Im): swizzled byte offsets
-        uint32_t e1off[4][2];
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-            const uint32_t row = 32 * h + k1, kpos = 8 * m + 2 * (lane & 3);
-            e1off[m][0] = sw128(row, kpos);
-            e1off[m][1] = sw128(row, 32 + kpos);
-        }
+        // 8 m + 2 (lane % 4) (Re) and 32 + that (Im).  Their swizzled byte
+        // offsets are sw128(row, 0) + 4 (lane % 4) with the 16-byte chunk index
+        // XORed by m (and by 4 more for Im): e1base ^ (m << 4) ^ (e << 6)
+        const uint32_t e1base = sw128(32 * h + k1, 2 * (lane & 3));
         // the k1 = 32 row (quarter 0): this thread's (m, e) and W_64^(n2)
         const int m32 = (lane >> 2) & 3, e32 = lane >> 4;
         const int n2_32 = 8 * m32 + 2 * (lane & 3) + e32;
@@ -419,12 +417,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
             }
             if (!worker_vote(ok)) { ok = false; break; }
             tc::fence_after();
-            uint32_t r[16], r32[16], re[8], im[8];
-            if (do1) {
-                const uint32_t d1 = tmem + COL_D1 + 128u * (j & 1) + 32u * h;
-                tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r);
-                if (q == 0) tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
-            }
+            uint32_t r[16], re[8], im[8];
+            const uint32_t d1 = tmem + COL_D1 + 128u * (j & 1) + 32u * h;
+            if (do1) tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r);
             if (do2) {
                 const uint32_t d2 = tmem + COL_D2 + 64u * (jj & 1) + ((uint32_t)(32 * q) << 16);
                 tc::tmem_ld_32x32b_x8(d2 + 8u * h, re);
@@ -448,12 +443,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                         const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
                         const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
                         const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
-                        *reinterpret_cast<uint32_t*>(a2 + e1off[m][0]) = h2u(__floats2half2_rn(z0.x, z1.x));
-                        *reinterpret_cast<uint32_t*>(a2 + e1off[m][1]) = h2u(__floats2half2_rn(z0.y, z1.y));
+                        *reinterpret_cast<uint32_t*>(a2 + (e1base ^ (m << 4))) = h2u(__floats2half2_rn(z0.x, z1.x));
+                        *reinterpret_cast<uint32_t*>(a2 + (e1base ^ (m << 4) ^ 64u)) = h2u(__floats2half2_rn(z0.y, z1.y));
                     }
                     if (q == 0) {
                         // lanes 16..23 hold copies of the real k1 = 32 row: thread
                         // (lane) takes column 8 m32 + 2 (lane % 4) + e32 of its copy
+                        // (loaded here, by the four warps of quarter 0 only, which
+                        // keeps it out of the other warps' register budget)
+                        uint32_t r32[16];
+                        tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
+                        tc::tmem_ld_wait();
                         pin16(r32);
                         // y = r32[4 m32 + e32] as selects on constant indices
                         // (an indexed read would put r32 in local memory)

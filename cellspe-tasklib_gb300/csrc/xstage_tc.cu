@@ -27,6 +27,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "tcgen05.cuh"
 #include "tma.h"
 
 #include <mutex>
@@ -48,113 +49,17 @@ constexpr unsigned ERR_FULL_WAIT = 1, ERR_EMPTY_WAIT = 2, ERR_ACC_WAIT = 3;
 
 __device__ unsigned g_tc_error;
 
-CS_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+using tc::smem_u32;
 
-CS_DEV void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-CS_DEV void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-CS_DEV bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait: false (and the error code recorded) after WAIT_CYCLES.
+// Bounded wait: false (and the error code recorded in g_tc_error) after WAIT_CYCLES.
 CS_DEV bool mbar_wait(uint32_t bar, uint32_t parity, unsigned code)
 {
-    if (mbar_try_wait(bar, parity)) return true;
-    long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicCAS(&g_tc_error, 0u, code);
-            return false;
-        }
-    }
-    return true;
+    return tc::mbar_wait(bar, parity, &g_tc_error, code, WAIT_CYCLES);
 }
-
-CS_DEV void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
-
-// k-blocked spectra: coordinates (k within the block, plane, block, row)
-CS_DEV void tma_load_4d(uint32_t dst, const CUtensorMap* tm, int x, int p, int kb, int row, uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-        "[%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(p), "r"(kb), "r"(row), "r"(bar)
-        : "memory");
-}
-
-CS_DEV void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-CS_DEV void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
 // K-major operand in shared memory with 64-byte swizzle: 8-row x 64-byte
 // atoms stacked along M/N every 512 bytes (stride byte offset).
-CS_DEV uint64_t sw64_desc(uint32_t saddr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);     // start address
-    d |= (uint64_t)1 << 16;                       // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(512 >> 4) << 32;              // stride byte offset
-    d |= (uint64_t)1 << 46;                       // descriptor version (tcgen05)
-    d |= (uint64_t)4 << 61;                       // layout: 64-byte swizzle
-    return d;
-}
-
-// kind::f16 instruction descriptor: D F32, A/B F16, K-major, M=128, N=n (16..256, multiple of 16).
-CS_DEV uint32_t make_idesc(bool neg_a, uint32_t n)
-{
-    return (1u << 4) | (0u << 7) | (0u << 10) | ((neg_a ? 1u : 0u) << 13) | ((n >> 3) << 17) |
-           ((uint32_t)(BM >> 4) << 24);
-}
-
-CS_DEV void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-
-CS_DEV void umma_commit(uint32_t bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                 : "memory");
-}
-
-CS_DEV void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
-{
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-}
-
-CS_DEV void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+CS_DEV uint64_t sw64_desc(uint32_t saddr) { return tc::smem_desc(saddr, 16, 512, tc::SW64); }
 
 struct TcArgs {
     int S, C, K;
@@ -174,7 +79,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                                                            const __grid_constant__ TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    // offset from the shared array itself (not an integer round trip), so that
+    // the compiler keeps shared-space 32-bit addressing for every access
+    unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     // S <= BM: a stage holds Ar and Ai only (the tile is diagonal, B = A)
     const uint32_t stage_bytes = a.small ? 2 * A_BYTES : STAGE_BYTES;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);   // full[S], empty[S], acc
@@ -200,22 +107,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, 1);
+            tc::mbar_init(full0 + 8 * s, 1);
+            tc::mbar_init(empty0 + 8 * s, 1);
         }
-        mbar_init(accb, 1);
+        tc::mbar_init(accb, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
     }
     if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(a.tmem_cols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc::tmem_alloc(smem_u32(tmem_slot), a.tmem_cols);
     }
-    tc_fence_before();
+    tc::fence_before();
     __syncthreads();
-    tc_fence_after();
+    tc::fence_after();
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
@@ -226,8 +130,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
             // k-blocked: rows (c, s) with the plane a coordinate of its own
             const int krowA = c * S + i0, krowB = c * S + j0;
             auto load = [&](uint32_t dst, int kc, int plane, int row2d, int rowk, uint32_t bar) {
-                if (a.kblock) tma_load_4d(dst, &tmap, 0, plane, kc, rowk, bar);
-                else tma_load_2d(dst, &tmap, kc * BK, row2d, bar);
+                if (a.kblock) tc::tma_load_4d(dst, &tmap, 0, plane, kc, rowk, bar);
+                else tc::tma_load_2d(dst, &tmap, kc * BK, row2d, bar);
             };
             int issued = 0;
             bool ok = true;
@@ -237,7 +141,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 if (!mbar_wait(empty0 + 8 * s, ph ^ 1, ERR_EMPTY_WAIT)) { ok = false; break; }
                 const uint32_t st = sbase + s * stage_bytes;
                 const uint32_t fb = full0 + 8 * s;
-                mbar_expect_tx(fb, stage_tx);
+                tc::mbar_expect_tx(fb, stage_tx);
                 load(st, kc, 0, rowA_re, krowA, fb);
                 load(st + A_BYTES, kc, 1, rowA_im, krowA, fb);
                 if (!a.small) {
@@ -257,13 +161,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            const uint32_t id_pos = make_idesc(false, n_eff), id_neg = make_idesc(true, n_eff);
+            const uint32_t id_pos = tc::idesc_f16(BM, n_eff, false, false, false), id_neg = tc::idesc_f16(BM, n_eff, true, false, false);
             const uint32_t d_re = tmem, d_im = tmem + a.tmem_cols / 2;
             bool ok = true;
             for (int kc = 0; kc < nk; kc++) {
                 const int s = kc % STAGES;
                 if (!mbar_wait(full0 + 8 * s, (kc / STAGES) & 1, ERR_FULL_WAIT)) { ok = false; break; }
-                tc_fence_after();
+                tc::fence_after();
                 const uint32_t st = sbase + s * stage_bytes;
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; kk++) {
@@ -272,16 +176,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                     const uint64_t br = a.small ? ar : sw64_desc(st + 2 * A_BYTES + off);
                     const uint64_t bi = a.small ? ai : sw64_desc(st + 2 * A_BYTES + B_BYTES + off);
                     const uint32_t acc = (kc | kk) ? 1u : 0u;
-                    umma_f16(d_re, ar, br, id_pos, acc);           // Re += Ar Br^T
-                    umma_f16(d_re, ai, bi, id_pos, 1u);            // Re += Ai Bi^T
-                    umma_f16(d_im, ai, br, id_pos, acc);           // Im += Ai Br^T
-                    umma_f16(d_im, ar, bi, id_neg, 1u);            // Im -= Ar Bi^T
+                    tc::mma_f16(d_re, ar, br, id_pos, acc);           // Re += Ar Br^T
+                    tc::mma_f16(d_re, ai, bi, id_pos, 1u);            // Re += Ai Bi^T
+                    tc::mma_f16(d_im, ai, br, id_pos, acc);           // Im += Ai Br^T
+                    tc::mma_f16(d_im, ar, bi, id_neg, 1u);            // Im -= Ar Bi^T
                 }
-                umma_commit(empty0 + 8 * s);                       // stage free once these MMAs finish
+                tc::commit(empty0 + 8 * s);                       // stage free once these MMAs finish
             }
             // Always commit: the barrier then completes only after every MMA
             // issued so far has finished, so TMEM is never freed under one.
-            umma_commit(accb);
+            tc::commit(accb);
             if (!ok) atomicCAS(&g_tc_error, 0u, ERR_FULL_WAIT);
         }
         __syncwarp();
@@ -294,7 +198,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
         ok = ok && (*reinterpret_cast<volatile unsigned*>(&g_tc_error) == 0u);
         __syncwarp();
         if (__all_sync(0xffffffffu, ok)) {
-            tc_fence_after();
+            tc::fence_after();
             // Stage each 32-row x 16-column block through shared memory (the
             // operand ring is free once the accumulators are final) so that a
             // store instruction writes two 128-byte runs of one output row.
@@ -304,9 +208,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
             const int ncb = (int)(n_eff / 16);
             for (int cb = 0; cb < ncb; cb++) {
                 uint32_t re[16], im[16];
-                tmem_ld16(lane_base + cb * 16, re);
-                tmem_ld16(lane_base + a.tmem_cols / 2 + cb * 16, im);
-                tmem_ld_wait();
+                tc::tmem_ld_32x32b_x16(lane_base + cb * 16, re);
+                tc::tmem_ld_32x32b_x16(lane_base + a.tmem_cols / 2 + cb * 16, im);
+                tc::tmem_ld_wait();
 #pragma unroll
                 for (int jj = 0; jj < 16; jj++) {
                     float f = si;
@@ -335,12 +239,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 __syncwarp();
             }
         }
-        tc_fence_before();
+        tc::fence_before();
     }
     __syncthreads();
     if (warp == 1) {
-        tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, a.tmem_cols);
     }
 }
 
