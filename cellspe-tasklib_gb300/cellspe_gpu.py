@@ -115,6 +115,28 @@ class VdifInfo(ctypes.Structure):
                 ("thread_id", ctypes.c_int), ("station_id", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
+class Addr64(ctypes.Union):
+    """addr64 (cellspe_control_blocks.h)."""
+    _fields_ = [("ull", ctypes.c_ulonglong), ("ui", ctypes.c_uint * 2), ("p", ctypes.c_void_p)]
+
+
+class ControlBlock(ctypes.Structure):
+    """control_block of the minicorrelator (cellspe_control_blocks.h): 256 bytes, 128-byte aligned."""
+    _fields_ = [("rawdata_src", Addr64), ("autocorrelation_out", Addr64), ("baselines_out", Addr64 * 15),
+                ("fmultipliers_src", Addr64), ("syncline", Addr64), ("spe_num", ctypes.c_int),
+                ("num_spes", ctypes.c_int), ("ffts_total", ctypes.c_uint), ("ffts_to_integrate", ctypes.c_uint),
+                ("spe_ls_listOnPPU", Addr64), ("spe_sig_listOnPPU", Addr64), ("_pad", ctypes.c_ubyte * 72)]
+
+
+class ControlBlockT(ctypes.Structure):
+    """control_block_t of the Cell spectrometer (cellspe_control_blocks.h): 128 bytes."""
+    _fields_ = [("rank", ctypes.c_uint), ("terminate_flag", ctypes.c_uint), ("fft_points", ctypes.c_uint),
+                ("fft_points_log2", ctypes.c_uint), ("overlap_factor", ctypes.c_uint),
+                ("integrate_ffts", ctypes.c_uint), ("samples_per_rawbyte", ctypes.c_uint), ("_pad0", ctypes.c_uint),
+                ("rawif_src", Addr64), ("rawif_bytecount", ctypes.c_uint), ("_pad1", ctypes.c_uint),
+                ("spectrum_dst", Addr64), ("_pad2", ctypes.c_ubyte * 72)]
+
+
 class XmacParams(ctypes.Structure):
     _fields_ = [("S", ctypes.c_int), ("C", ctypes.c_int), ("K", ctypes.c_int), ("accumulate", ctypes.c_int)]
 
@@ -226,6 +248,18 @@ def lib() -> ctypes.CDLL:
             "cellspe_mark5b_deframe": ([V, LL, I, LL, V, V, I, V], I),
             "cellspe_vdif_decode": ([V, LL, I, I, LL, V, I, V], I),
             "cellspe_vdif_deframe": ([V, LL, I, I, LL, V, V, I, V], I),
+            "cellspe_minicorrelator_run": ([V, I], I),
+            "cellspe_cell_spectrometer_task": ([ctypes.POINTER(V), V, V, V], I),
+            "cellspe_pcal_new": ([D, D, I, ctypes.c_ulonglong], V),
+            "cellspe_pcal_free": ([V], None),
+            "cellspe_pcal_kind": ([V], I),
+            "cellspe_pcal_length": ([V], I),
+            "cellspe_pcal_nbins": ([V], LL),
+            "cellspe_pcal_seconds": ([V], D),
+            "cellspe_pcal_clear": ([V], I),
+            "cellspe_pcal_adjust_sample_offset": ([V, ctypes.c_ulonglong], I),
+            "cellspe_pcal_extract": ([V, V, LL, I], I),
+            "cellspe_pcal_final": ([V, V], LL),
             "cellspe_service_create": ([V], V),
             "cellspe_service_submit": ([V, V, V, V, V, ctypes.POINTER(ctypes.c_longlong)], I),
             "cellspe_service_wait": ([V, ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)], I),
@@ -438,6 +472,81 @@ def mark5b_deframe(framed, nchan: int, frames: int = 0, payload=None, valid_mask
                                         _ptr(valid_mask)[0] if valid_mask is not None else None,
                                         _mem(framed, payload, valid_mask), ctypes.byref(info)))
     return info
+
+
+def minicorrelator_run(blocks) -> None:
+    """cellspe_minicorrelator_run on an array of 6 ControlBlock (host buffers)."""
+    arr = (ControlBlock * len(blocks))(*blocks)
+    _check(lib().cellspe_minicorrelator_run(ctypes.addressof(arr), len(blocks)))
+
+
+PCAL_TRIVIAL, PCAL_SHIFTING, PCAL_IMPLICIT_SHIFT = 0, 1, 2
+
+
+class Pcal:
+    """A PCal extractor (cellspe_pcal.h): PCal::getNew and its methods."""
+
+    def __init__(self, bandwidth_hz: float, spacing_hz: float, offset_hz: int, sampleoffset: int = 0):
+        self.h = lib().cellspe_pcal_new(bandwidth_hz, spacing_hz, int(offset_hz), int(sampleoffset))
+        if not self.h:
+            raise CellspeError(ERR_ARG, last_error())
+
+    kind = property(lambda self: lib().cellspe_pcal_kind(self.h))
+    length = property(lambda self: lib().cellspe_pcal_length(self.h))
+    nbins = property(lambda self: lib().cellspe_pcal_nbins(self.h))
+    seconds = property(lambda self: lib().cellspe_pcal_seconds(self.h))
+
+    def clear(self):
+        _check(lib().cellspe_pcal_clear(self.h))
+
+    def adjust_sample_offset(self, sampleoffset: int):
+        _check(lib().cellspe_pcal_adjust_sample_offset(self.h, int(sampleoffset)))
+
+    def extract(self, samples):
+        if _is_torch_cuda(samples):
+            _check(lib().cellspe_pcal_extract(self.h, samples.data_ptr(), samples.numel(), MEM_DEVICE))
+        else:
+            x = np.ascontiguousarray(samples, np.float32)
+            _check(lib().cellspe_pcal_extract(self.h, x.ctypes.data, x.size, MEM_HOST))
+
+    def final(self, out=None):
+        """(tones complex64 [length], samples integrated); tones the reference
+        leaves unwritten keep `out`'s values (zeros by default)."""
+        out = np.zeros(self.length, np.complex64) if out is None else out
+        n = lib().cellspe_pcal_final(self.h, out.ctypes.data)
+        if n < 0:
+            _check(-n)
+        return out, n
+
+    def close(self):
+        if self.h:
+            lib().cellspe_pcal_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CellSpectrometerTask:
+    """One Cell-spectrometer SPE context: run(cb) per task, close() sends terminate_flag."""
+
+    def __init__(self, levels4=None):
+        self.state = ctypes.c_void_p(None)
+        self.levels = None if levels4 is None else np.ascontiguousarray(levels4, np.float32)
+
+    def run(self, cb: ControlBlockT):
+        stats = (ctypes.c_uint * 3)()
+        lv = None if self.levels is None else self.levels.ctypes.data
+        _check(lib().cellspe_cell_spectrometer_task(ctypes.byref(self.state), ctypes.addressof(cb), lv, stats))
+        return list(stats)
+
+    def close(self):
+        cb = ControlBlockT()
+        cb.terminate_flag = 1
+        _check(lib().cellspe_cell_spectrometer_task(ctypes.byref(self.state), ctypes.addressof(cb), None, None))
 
 
 def spectrometer_noalloc(params: SpecParams, raw, power, pcal_bins=None, pcal_tones=None, stream: int = 0):

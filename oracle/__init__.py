@@ -439,3 +439,125 @@ def vis_errors(got, ref, autos, K: int):
                 cross_cov += int(a != b)
     return {"max_rel_amp": amp, "max_phase_deg": ph, "phase_cells": cells, "cross_products_above_floor": cross_cov,
             "products": n * (n + 1) // 2, "cross_products": n * (n - 1) // 2}
+
+
+# ---------------------------------------------------------------------------
+# Cell control blocks (restated from the SPE programs)
+# ---------------------------------------------------------------------------
+MC_PARTNER = (1, 3, 4)      # minicorrelator_spu.c:302-304: partners rank+1, rank+3, rank+4 (mod 6)
+
+
+def minicorrelator_slots_f64(raws, ffts_total: int, ffts_to_integrate: int):
+    """The minicorrelator SPE job (minicorrelator_spu.c:326-481, 835-866) as the
+    engine defines it: station s = raws[s] (ffts_total x 256 bytes of 2-bit
+    offset-binary samples), one 2048-sample segment per time period (two
+    1024-sample FFT buffers), blocks of ffts_to_integrate / 2 segments.
+    Returns (autos[s][b][1024], slots{slot: [b][1024]}) of FP64 complex sums,
+    slot s + 6 m < 15 holding X_s conj(X_o), o = (s + MC_PARTNER[m]) % 6."""
+    S, N = 6, 2048
+    K = ffts_total // 2
+    Kb = ffts_to_integrate // 2
+    blocks = ffts_total // ffts_to_integrate
+    raw = np.stack([np.asarray(r, np.uint8) for r in raws])
+    X = fx_spectra_f64(raw, S, N, K)                       # [S][K][1024]
+    X = X[:, : blocks * Kb].reshape(S, blocks, Kb, N // 2)
+    autos = np.einsum("sbkc,sbkc->sbc", X, np.conj(X))
+    slots = {}
+    for s in range(S):
+        for m, off in enumerate(MC_PARTNER):
+            slot = s + S * m
+            if slot < 15:
+                o = (s + off) % S
+                slots[slot] = np.einsum("bkc,bkc->bc", X[s], np.conj(X[o]))
+    return autos, slots
+
+
+def cell_spectrometer_f64(buffers, N: int, K: int, overlap: int, spr: int = 1, levels=None):
+    """The Cell spectrometer SPE task (spectrometer_spu.c:96-205) over a
+    sequence of raw buffers, one task each, as the engine defines it: FFT f
+    of a buffer starts at byte f*d, d = (N/spr)//overlap, for
+    f < min(len//d - 1, (len - N/spr)//d + 1); samples byte - 127.5 (spr 1)
+    or 2-bit LSB-first codes through `levels` (spr 4); window
+    sin^2(pi i/(N-1)) (calc_cos_window_function, :286-312); |X_k|^2 / K of
+    the N-point FFT summed over K FFTs, the running spectrum carried from one
+    task to the next; each finished spectrum as N {power, 0} pairs.
+    Returns one list of spectra ([N][2] float64 arrays) per task."""
+    w = np.sin(np.pi * np.arange(N) / (N - 1)) ** 2
+    rb = N // spr
+    d = rb // overlap
+    acc = np.zeros(N)
+    n = 0
+    out = []
+    lv = None if levels is None else np.asarray(levels, np.float64)
+    for buf in buffers:
+        buf = np.asarray(buf, np.uint8)
+        B = buf.size
+        nfft = min(B // d - 1 if B >= 2 * d else 0, (B - rb) // d + 1 if B >= rb else 0)
+        spectra = []
+        for f in range(nfft):
+            chunk = buf[f * d: f * d + rb]
+            if spr == 1:
+                x = chunk.astype(np.float64) - 127.5
+            else:
+                codes = (chunk[:, None] >> (2 * np.arange(4))[None, :]) & 3
+                x = lv[codes.reshape(-1)]
+            X = np.fft.fft(x * w)
+            acc += np.abs(X) ** 2 / K
+            n += 1
+            if n == K:
+                spectra.append(np.stack([acc, np.zeros(N)], axis=1))
+                acc = np.zeros(N)
+                n = 0
+        out.append(spectra)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# PCal library (spectrometer/src/IA-32/PhaseCal/PCal.cpp)
+# ---------------------------------------------------------------------------
+def pcal_config(bw: float, spacing: float, offset: int):
+    """PCal::getNew's choice (PCal.cpp:92-112) and each extractor's derived
+    sizes: (kind, nbins, rotlen, ntones, first, step); kind 0 Trivial,
+    1 Shifting, 2 ImplicitShift."""
+    from math import floor, gcd
+
+    fs = int(2 * bw)
+    sp = int(spacing)
+    Np = fs // gcd(sp, fs)
+    if offset == 0:
+        return 0, Np, 1, int(floor(bw / spacing)), 0, 1
+    No = fs // gcd(int(offset), fs)
+    ntones = int(floor((bw - offset) / spacing)) + 1
+    if No % Np == 0:
+        return 2, No, 1, ntones, int(floor(No * offset / fs)), int(floor(No * (spacing / fs)))
+    return 1, Np, No, ntones, 0, int(floor(Np * (spacing / fs)))
+
+
+def pcal_extract_f64(pieces, bw: float, spacing: float, offset: int, sampleoffset: int = 0):
+    """The PCal extractors' result in FP64 for a sequence of pieces, each
+    (samples, new_sampleoffset or None): sample n after an offset o lands in
+    bin (o + n) mod nbins (Trivial PCal.cpp:235-253, ImplicitShift :610-628),
+    mixed by exp(-2 pi i offset (o + n) / fs) first for Shifting (:421-462,
+    every sample counted); then the DFT of the bins divided by nbins and the
+    picked bins (:301-315, :477-507, :669-688).  Returns (tones, samplecount),
+    tones past the last bin < nbins omitted."""
+    kind, nbins, rotlen, ntones, first, step = pcal_config(bw, spacing, offset)
+    fs = 2 * bw
+    acc = np.zeros(nbins, np.complex128)
+    pos = sampleoffset
+    count = 0
+    for samples, new_off in pieces:
+        if new_off is not None:
+            pos = new_off
+        x = np.asarray(samples, np.float64)
+        n = pos + np.arange(x.size, dtype=np.int64)
+        if kind == 1:
+            r = (int(offset) * (n % int(fs))) % int(fs)
+            x = x * np.exp(-2j * np.pi * r / fs)
+        np.add.at(acc, n % nbins, x)
+        pos += x.size
+        count += x.size
+    bins = [first + t * step for t in range(ntones) if first + t * step < nbins]
+    b = np.arange(nbins)
+    tones = np.array([np.sum(acc * np.exp(-2j * np.pi * ((k * b) % nbins) / nbins)) / nbins for k in bins])
+    return tones, count

@@ -165,3 +165,44 @@ def test_cxx_linkage_aliases_link_and_run(tmp_path):
     syms = subprocess.run(["nm", "-D", "--defined-only", str(cellspe_gpu.LIB_PATH)], capture_output=True, text=True,
                           check=True).stdout
     assert "_Z17celldsp_startTaskiP14CellDSPTask_tt" in syms and "_Z18speAddProduct_32fcP4fc32S0_S0_i" in syms
+
+
+def test_control_block_layouts_match_reference(tmp_path):
+    """control_block (minicorrelator.h:107-119) and control_block_t
+    (cell_spectrometer.h:104-115): member offsets of the reference's
+    declarations on LP64 (addr64 is 8 bytes, the first member and the struct
+    128-byte aligned), from the C header and from the ctypes mirror."""
+    import cellspe_gpu as cg
+
+    src = tmp_path / "cb.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "cellspe_control_blocks.h"
+int main(void){
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(control_block), _Alignof(control_block),
+   offsetof(control_block, rawdata_src), offsetof(control_block, autocorrelation_out),
+   offsetof(control_block, baselines_out), offsetof(control_block, fmultipliers_src), offsetof(control_block, syncline),
+   offsetof(control_block, spe_num), offsetof(control_block, num_spes), offsetof(control_block, ffts_total),
+   offsetof(control_block, ffts_to_integrate), offsetof(control_block, spe_ls_listOnPPU),
+   offsetof(control_block, spe_sig_listOnPPU));
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(control_block_t), _Alignof(control_block_t),
+   offsetof(control_block_t, rank), offsetof(control_block_t, terminate_flag), offsetof(control_block_t, fft_points),
+   offsetof(control_block_t, fft_points_log2), offsetof(control_block_t, overlap_factor),
+   offsetof(control_block_t, integrate_ffts), offsetof(control_block_t, samples_per_rawbyte),
+   offsetof(control_block_t, rawif_src), offsetof(control_block_t, rawif_bytecount),
+   offsetof(control_block_t, spectrum_dst));
+ return 0; }''')
+    exe = tmp_path / "cb"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    lines = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines()
+    cb, cbt = (list(map(int, ln.split())) for ln in lines)
+    assert cb == [256, 128, 0, 8, 16, 136, 144, 152, 156, 160, 164, 168, 176]
+    assert cbt == [128, 128, 0, 4, 8, 12, 16, 20, 24, 32, 40, 48]
+    C, T = cg.ControlBlock, cg.ControlBlockT
+    assert [ctypes.sizeof(C), C.rawdata_src.offset, C.autocorrelation_out.offset, C.baselines_out.offset,
+            C.fmultipliers_src.offset, C.syncline.offset, C.spe_num.offset, C.num_spes.offset, C.ffts_total.offset,
+            C.ffts_to_integrate.offset, C.spe_ls_listOnPPU.offset, C.spe_sig_listOnPPU.offset] == [cb[0]] + cb[2:]
+    assert [ctypes.sizeof(T), T.rank.offset, T.terminate_flag.offset, T.fft_points.offset, T.fft_points_log2.offset,
+            T.overlap_factor.offset, T.integrate_ffts.offset, T.samples_per_rawbyte.offset, T.rawif_src.offset,
+            T.rawif_bytecount.offset, T.spectrum_dst.offset] == [cbt[0]] + cbt[2:]
