@@ -234,7 +234,20 @@ def run_configs(cg, torch, x_mode: int, with_cpu: bool, raw, vis_main):
                         "error": vis_error(torch, raw, vis, S, N, K, 16, 32, seed=K)}
     if x_mode == cg.X_TC_FP16:
         out["tc_vs_fp32_max_rel"] = rel_all(torch, vis_main, vis)
-    del vis
+    # -- the same job with the INT8 X stage (mma.sync IMMA; tcgen05 has no kind::i8 on sm_103a)
+    vis8 = torch.empty((C, P), dtype=torch.complex64, device="cuda")
+    p8 = cg.fx_params(S, N, K, T // 4, x_mode=cg.X_INT8, vis_order=cg.VIS_CHANNEL_MAJOR)
+    ms8 = _time_calls(torch, lambda: cg.fx_correlate(p8, raw, vis8), steps=3, warmup=1)
+    st8 = cg.stage_times()
+    x8_ops = 8.0 * C * P * K                                  # 4 real int8 MACs per complex MAC
+    out["int8_path"] = {"value": S * T / (ms8 * 1e-3) / 1e9, "unit": "Gsamples/s", "ms_per_step": ms8,
+                        "workload": "same job and input as the headline, x_mode = INT8 (per input/channel "
+                                    "max-abs int8 spectra, mma.sync m16n8k32 IMMA, int32 sums)",
+                        "stages_ms": {"f_stage_and_quantise": st8[1], "x_stage": st8[2]},
+                        "x_stage_tops": x8_ops / (st8[2] * 1e-3) / 1e12,
+                        "error": vis_error(torch, raw, vis8, S, N, K, 16, 32, seed=K),
+                        "int8_vs_fp32_max_rel": rel_all(torch, vis, vis8)}
+    del vis, vis8
 
     import synth
 

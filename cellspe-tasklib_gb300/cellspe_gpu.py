@@ -25,7 +25,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_NOMEM, ERR_CUDA, ERR_INJECTED = range(6)
 LEVELS_MARK5B, LEVELS_TWOBIT, LEVELS_OFFSET_BINARY, LEVELS_VDIF = 0, 1, 2, 3
 UNPACK_MSB_FIRST = 0x100
-X_FP32, X_TC_FP16 = 0, 1
+X_FP32, X_TC_FP16, X_INT8 = 0, 1, 2
 VIS_CHANNEL_MAJOR, VIS_BASELINE_MAJOR = 0, 1
 SPEC_INTERLEAVED, SPEC_PLANES, SPEC_MARK5B_FRAMED, SPEC_VDIF_FRAMED = 0, 1, 2, 3
 MARK5B_FRAME, MARK5B_PAYLOAD = 10016, 10000
@@ -235,6 +235,7 @@ def lib() -> ctypes.CDLL:
             "cellspe_xmac": ([V, I, I, I, V, I, I], I),
             "cellspe_vis_lags": ([V, V, LL, I, D, I], I),
             "cellspe_xmac_f16": ([V, I, I, I, V, I, I], I),
+            "cellspe_xmac_i8": ([V, V, I, I, I, V, I, I], I),
             "cellspe_fx_correlate": ([V, V, V, V], I),
             "cellspe_fx_workspace_bytes": ([V], LL),
             "cellspe_fx_correlate_async": ([V, V, V, V, V], I),
@@ -378,6 +379,12 @@ def xmac_f16(spectra_f16, S: int, C: int, K: int, vis, accumulate: bool = False)
     _check(lib().cellspe_xmac_f16(_ptr(spectra_f16)[0], S, C, K, _ptr(vis)[0], int(accumulate),
                                   _mem(spectra_f16, vis)))
     return vis
+
+
+def xmac_i8(planes, scale, S: int, C: int, K: int, vis, accumulate: bool = False):
+    """INT8 X stage on planes int8 [C][2][S][K] and scale float [S][C]."""
+    _check(lib().cellspe_xmac_i8(_ptr(planes)[0], _ptr(scale)[0], S, C, K, _ptr(vis)[0], int(accumulate),
+                                 _mem(planes, scale, vis)))
 
 
 def fx_params(S, N, K, bytes_per_input, x_mode=X_FP32, vis_order=VIS_CHANNEL_MAJOR,

@@ -116,6 +116,13 @@ int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis,
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
                    int scale_stride, int accumulate, cudaStream_t st,
                    int kblock = 0);   // inv_scale[s * scale_stride + c]
+// INT8 X stage (legacy mma.sync IMMA: tcgen05 has no kind::i8 on sm_103a),
+// int32 accumulate: planes int8 [C][2][S][kp] (K, kp % 32 == 0, K <= 65536),
+// V_ij scaled by scale[i*stride + c] scale[j*stride + c].
+int cs_xmac_i8(const int8_t* planes, int S, int C, int K, int kp, float2* vis, const float* scale, int scale_stride,
+                  int accumulate, cudaStream_t st);
+// FP32 spectra [C][S][kp] -> int8 planes [C][2][S][kp], per-row max-abs scale [S][C].
+int cs_quantise_i8(const float2* spectra, int S, int C, int K, int kp, int8_t* planes, float* scale, cudaStream_t st);
 // Error code of the last tensor-core X-stage launch (0 = ok; 1..3 = a
 // pipeline wait timed out).  Call after the launching stream has synchronised.
 int cs_xmac_tc_status(unsigned* code);

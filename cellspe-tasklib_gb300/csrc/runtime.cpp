@@ -411,6 +411,24 @@ int op_xmac_f16(Workspace& ws, bool host, const void* spectra, int S, int C, int
     return rc;
 }
 
+int op_xmac_i8(Workspace& ws, bool host, const void* planes, const float* scale, int S, int C, int K, void* vis,
+               int accumulate)
+{
+    if (!planes || !scale || !vis || S <= 0 || C <= 0 || K <= 0 || K % 16 || K > 65536)
+        return set_err(CELLSPE_ERR_ARG, "xmac_i8: bad arguments (K must be a multiple of 16, at most 65536)");
+    long long P = (long long)S * (S + 1) / 2;
+    Job j(ws, host);
+    const void* d_pl = j.in(planes, (size_t)C * 2 * S * K);
+    const void* d_sc = j.in(scale, (size_t)S * C * 4);
+    void* d_vis = j.out(vis, (size_t)C * P * 8, accumulate != 0);
+    if (!j.err) {
+        int rc = map_rc(cs_xmac_i8((const int8_t*)d_pl, S, C, K, K, (float2*)d_vis, (const float*)d_sc, C, accumulate,
+                                   ws.stream), "xmac_i8");
+        if (rc) j.err = rc;
+    }
+    return j.finish();
+}
+
 // Row pitch (elements) of the internal spectra between the F and X stages:
 // K + 64 for long rows.  Unpadded, the F stage's corner-turn writes land on
 // rows a power-of-two number of bytes apart (4 MiB at 512 inputs x 4096
@@ -427,11 +445,13 @@ long long fx_bytes(const cellspe_fx_params* p, bool with_poly)
     long long b = 0;
     if (host) b += align256(S * p->bytes_per_input);
     if (with_poly) b += align256(S * 32) + 3 * align256(S * K * 4);
-    b += align256(C * S * spectra_pitch(K) * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));
-    if (N >= 4096) b += align256(C * S * K * (p->x_mode == CELLSPE_X_FP32 ? 8 : 4));   // segment-major spectra
+    const bool f32 = p->x_mode != CELLSPE_X_TC_FP16;   // FP32 spectra (FP32 and INT8 X stages)
+    b += align256(C * S * spectra_pitch(K) * (f32 ? 8 : 4));
+    if (N >= 4096) b += align256(C * S * K * (f32 ? 8 : 4));   // segment-major spectra
+    if (p->x_mode == CELLSPE_X_INT8) b += align256(C * 2 * S * spectra_pitch(K)) + align256(S * C * 4);
     bool stage_vis = host || p->vis_order == CELLSPE_VIS_BASELINE_MAJOR || p->accumulate;
     if (stage_vis) b += 3 * align256(C * P * 8);
-    if (p->x_mode != CELLSPE_X_FP32) b += 2 * align256(S * C * 4);
+    if (p->x_mode == CELLSPE_X_TC_FP16) b += 2 * align256(S * C * 4);
     return b;
 }
 
@@ -445,8 +465,10 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         return set_err(CELLSPE_ERR_ARG, "fx: bytes_per_input must be a positive multiple of 16");
     if (!poly && (p->start_sample < 0 || p->start_sample + (long long)K * N > p->bytes_per_input * 4))
         return set_err(CELLSPE_ERR_ARG, "fx: segments run past the end of the input");
-    if (p->x_mode != CELLSPE_X_FP32 && p->x_mode != CELLSPE_X_TC_FP16)
+    if (p->x_mode != CELLSPE_X_FP32 && p->x_mode != CELLSPE_X_TC_FP16 && p->x_mode != CELLSPE_X_INT8)
         return set_err(CELLSPE_ERR_ARG, "fx: unknown x_mode");
+    if (p->x_mode == CELLSPE_X_INT8 && (K % 16 || K > 65536))
+        return set_err(CELLSPE_ERR_ARG, "fx: the INT8 X stage needs K a multiple of 16, at most 65536");
     if (poly && !(p->sample_rate_hz > 0)) return set_err(CELLSPE_ERR_ARG, "fx: delay model needs sample_rate_hz");
     float lut[4];
     if (!pick_levels(p->levels, p->custom_levels, lut)) return set_err(CELLSPE_ERR_ARG, "fx: unknown level table");
@@ -491,7 +513,7 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     fa.start_sample = p->start_sample;
     std::memcpy(fa.lut, lut, sizeof lut);
     fa.msb_first = (p->levels & CELLSPE_UNPACK_MSB_FIRST) ? 1 : 0;
-    fa.format = p->x_mode == CELLSPE_X_FP32 ? CS_SPECTRA_F32 : CS_SPECTRA_F16;
+    fa.format = p->x_mode == CELLSPE_X_TC_FP16 ? CS_SPECTRA_F16 : CS_SPECTRA_F32;
     if (poly) {
         const double* d_poly = (const double*)j.in(poly, (size_t)S * 4 * sizeof(double));
         CsDelayState ds;
@@ -505,7 +527,7 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         fa.shift = ds.shift; fa.phase0 = ds.phase0; fa.dphase = ds.dphase;
     }
     const float* d_inv_scale = nullptr;
-    if (p->x_mode != CELLSPE_X_FP32 && p->channel_scale) {
+    if (p->x_mode == CELLSPE_X_TC_FP16 && p->channel_scale) {
         // F stage multiplies channel c of input s by scale[s][c] before the
         // FP16 cast; the X-stage epilogue divides V_ij by scale_i * scale_j.
         fa.scale = (const float*)j.in(p->channel_scale, (size_t)S * C * 4);
@@ -554,6 +576,17 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
                         "spectra transpose");
         if (rc) j.err = rc;
     }
+    // INT8 X stage: FP32 spectra -> int8 planes [C][2][S][kp] and per-row scales
+    int8_t* i8_planes = nullptr;
+    float* i8_scale = nullptr;
+    if (p->x_mode == CELLSPE_X_INT8 && !j.err) {
+        i8_planes = (int8_t*)j.scratch((size_t)C * 2 * S * kp);
+        i8_scale = (float*)j.scratch((size_t)S * C * 4);
+        if (!j.err) {
+            int rc = map_rc(cs_quantise_i8((const float2*)fa.out, S, C, K, kp, i8_planes, i8_scale, ws.stream), "INT8 quantise");
+            if (rc) j.err = rc;
+        }
+    }
     if (sync) cudaEventRecord(ws.sev[2], ws.stream);
     // X stage into a channel-major buffer
     const bool direct = !host && p->vis_order == CELLSPE_VIS_CHANNEL_MAJOR && !p->accumulate;
@@ -570,6 +603,9 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         int rc;
         if (p->x_mode == CELLSPE_X_FP32)
             rc = cs_xmac_f32((const float2*)fa.out + c0 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P, 0, ws.stream);
+        else if (p->x_mode == CELLSPE_X_INT8)
+            rc = cs_xmac_i8(i8_planes + c0 * 2 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P, i8_scale + c0, C, 0,
+                            ws.stream);
         else
             rc = cs_xmac_tc_f16((const uint16_t*)fa.out + c0 * 2 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P,
                                 d_inv_scale ? d_inv_scale + c0 : nullptr, C, 0, ws.stream, fa.kblock);
@@ -619,7 +655,7 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     // after a failure the copy stream may still hold copies into the workspace
     if (nsc > 1 && j.err) cudaStreamSynchronize(ws.copy);
     int rc = j.finish(sync);
-    if (sync && !rc && p->x_mode != CELLSPE_X_FP32) {
+    if (sync && !rc && p->x_mode == CELLSPE_X_TC_FP16) {
         unsigned code = 0;
         unsigned code32 = 0;
         if (cs_fstage_tc_status(&code) != 0 || code != 0 || cs_fstage_tc32_status(&code32) != 0 || code32 != 0)
@@ -2149,6 +2185,13 @@ int cellspe_xmac_f16(const void* spectra_f16, int S, int C, int K, void* vis, in
 {
     DIRECT_PROLOGUE
     return op_xmac_f16(*ws, memory == CELLSPE_MEM_HOST, spectra_f16, S, C, K, vis, accumulate);
+}
+
+int cellspe_xmac_i8(const void* planes_i8, const float* scale, int S, int C, int K, void* vis, int accumulate,
+                    int memory)
+{
+    DIRECT_PROLOGUE
+    return op_xmac_i8(*ws, memory == CELLSPE_MEM_HOST, planes_i8, scale, S, C, K, vis, accumulate);
 }
 
 int cellspe_fx_correlate(const cellspe_fx_params* p, const void* raw, const double* delay_poly, void* vis)

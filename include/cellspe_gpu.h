@@ -44,6 +44,9 @@ extern "C" {
 /* X-stage arithmetic */
 #define CELLSPE_X_FP32     0   /* FP32 CUDA cores                                   */
 #define CELLSPE_X_TC_FP16  1   /* tcgen05 tensor cores, FP16 inputs, FP32 accumulate */
+#define CELLSPE_X_INT8     2   /* int8 spectra (per input and channel max-abs scale),
+                                  mma.sync IMMA, int32 accumulate; K % 16 == 0.
+                                  tcgen05 has no kind::i8 on sm_103a */
 
 /* Visibility layout */
 #define CELLSPE_VIS_CHANNEL_MAJOR   0  /* vis[C][P]  (X-engine order)            */
@@ -112,6 +115,13 @@ int cellspe_xmac(const void* spectra, int S, int C, int K, void* vis, int accumu
 /* Tensor-core X stage on FP16 spectra, layout half [C][2][S][K] (plane 0 Re,
  * plane 1 Im, K a multiple of 8) -> vis complex64 [C][P], FP32 accumulation. */
 int cellspe_xmac_f16(const void* spectra_f16, int S, int C, int K, void* vis, int accumulate, int memory);
+/* INT8 X stage: int8 spectra planes [C][2][S][K] (plane 0 Re, plane 1 Im,
+ * K a multiple of 16, at most 65536) with a dequantisation scale [S][C] ->
+ * vis complex64 [C][P], V_ij = scale[i][c] scale[j][c] sum_k q_i conj(q_j),
+ * the integer sums exact (int32) and scaled in FP32.  Warp-level mma.sync
+ * IMMA: tcgen05 has no kind::i8 on sm_103a. */
+int cellspe_xmac_i8(const void* planes_i8, const float* scale, int S, int C, int K, void* vis, int accumulate,
+                    int memory);
 /* Parameters of CELLDSP_TASK_XMAC (input vector 0). */
 typedef struct { int S, C, K, accumulate; } cellspe_xmac_params;
 

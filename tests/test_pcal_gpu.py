@@ -101,6 +101,6 @@ def test_pcal_finalise_clear_and_errors(cg):
     c, k = pc.final()
     assert k == 32000 and np.allclose(c, a, rtol=1e-6, atol=1e-7)
     with pytest.raises(cg.CellspeError):
-        cg.Pcal(16.5, 1e6, 0)                 # 2 x bandwidth not a whole number of Hz
+        cg.Pcal(16.25, 1e6, 0)                # 2 x bandwidth not a whole number of Hz
     with pytest.raises(cg.CellspeError):
         cg.Pcal(16e6, 0.0, 0)
