@@ -463,7 +463,7 @@ def main():
     # ---- end to end through the C ABI with host buffers --------------------
     raw_h = np.empty((S_run, T_run // 4), np.uint8)
     raw_h[:] = raw.cpu().numpy()
-    e2e_ms, e2e_value, e2e_sync = None, None, None
+    e2e_ms, e2e_value, e2e_sync, e2e_concurrent = None, None, None, None
     if not args.no_e2e:
         pin_raw = torch.from_numpy(raw_h).pin_memory()
         pin_vis = [torch.empty((C_run, P_run), dtype=torch.complex64).pin_memory() for _ in range(2)]
@@ -493,8 +493,13 @@ def main():
         svc = cg.Service(max_streams=2, priority_samples=-1)
         jobs = [cg.fx_params(S_run, N_run, K_run, T_run // 4, x_mode=x_mode, vis_order=cg.VIS_CHANNEL_MAJOR)
                 for _ in range(2)]
-        for w in range(2):                            # each worker sizes its workspace
-            svc.wait(svc.submit(jobs[w], raw_np, vis_np[w]))
+        # warm-up with two jobs in flight, so that both workers have sized
+        # their workspaces (jobs waited one at a time can all land on one
+        # worker, and the other's first allocation then falls in the timed loop)
+        for _ in range(max(2, args.warmup)):
+            warm = [svc.submit(jobs[w], raw_np, vis_np[w]) for w in range(2)]
+            for jid in warm:
+                svc.wait(jid)
         barrier()
         pending = []
         t_e2e = time.perf_counter()
@@ -507,6 +512,7 @@ def main():
         torch.cuda.synchronize()
         e2e_ms = replicas.max_over_ranks(1e3 * (time.perf_counter() - t_e2e) / args.e2e_steps, dist, device="cuda")
         e2e_value = replicas.aggregate_gsamples(world, S_run * T_run, e2e_ms)
+        e2e_concurrent = svc.stats()["max_running"]
         svc.close()
         del pin_vis, pin_raw
 
@@ -608,7 +614,7 @@ def main():
                     "d2h_bytes_per_step": int(C_run * P_run * 8), "ms_per_step": e2e_ms,
                     "mode": "host buffers through cellspe_service_* (two streams, two jobs in flight; "
                             "wall clock over e2e_steps jobs)",
-                    "sync": e2e_sync},
+                    "max_concurrent_jobs": e2e_concurrent, "sync": e2e_sync},
             "gpu_launches": int(launches),
             "roofline": roof,
             "error": error,
