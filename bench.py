@@ -119,52 +119,109 @@ def cpu_baseline(raw_host: np.ndarray, k_sample: int, nthreads: int):
     return S * k_sample * N / dt / 1e9, dt
 
 
-def run_serving(cg, torch, seconds: float, rate: float, x_mode: int, seed: int = 5):
-    """Batched streaming service: Poisson arrivals, uneven jobs (S, C, T) as in the
-    serving configuration, device-resident buffers; latency is submit -> done.
-    The service runs with its defaults: two streams, jobs under 2^24 samples on
-    a high-priority stream."""
-    rng = np.random.default_rng(seed)
+def _serving_jobs(rng, seconds: float, rate: float):
     s_choices, c_choices = [4, 8, 24, 64, 200], [256, 1024, 4096, 16384]
     t_arr, t = [], 0.0
     while True:
-        t += rng.exponential(1.0 / rate)
-        if t > seconds:
+        t += rng.exponential(1.0 / rate) if rate > 0 else 0.0
+        if t > seconds or (rate <= 0 and len(t_arr) >= int(seconds)):
             break
         t_arr.append(t)
-    jobs = [(int(rng.choice(s_choices)), int(rng.choice(c_choices)), 2 ** int(rng.integers(18, 25)),
-             float(rng.uniform(0.01, 0.2))) for _ in t_arr]
-    max_raw = max(S * T // 4 for S, _, T, _ in jobs)
-    g = torch.Generator(device="cuda").manual_seed(seed)
-    raw_pool = torch.randint(0, 256, (max_raw,), dtype=torch.uint8, device="cuda", generator=g)
+    jobs = [(int(rng.choice(s_choices)), int(rng.choice(c_choices)), 2 ** int(rng.integers(18, 25))) for _ in t_arr]
+    return jobs, t_arr
+
+
+def _serve(cg, torch, jobs, t_arr, x_mode, raw_pool, keep=()):
+    """Submit the jobs at their arrival times (all at once when t_arr is all 0),
+    at most 64 outstanding; returns latencies, makespan, stats and the kept outputs."""
     svc = cg.Service()
-    pending, lat, samples = [], [], 0
+    pending, lat, kept = [], [], {}
     t0 = time.perf_counter()
-    for (S, C, T, _), ta in zip(jobs, t_arr):
+    for n, ((S, C, T), ta) in enumerate(zip(jobs, t_arr)):
         now = time.perf_counter() - t0
         if ta > now:
             time.sleep(ta - now)
-        N = 2 * C
         raw = raw_pool[: S * T // 4].view(S, T // 4)
         vis = torch.empty((C, S * (S + 1) // 2), dtype=torch.complex64, device="cuda")
-        p = cg.fx_params(S, N, T // N, T // 4, x_mode=x_mode)
-        pending.append((svc.submit(p, raw, vis), vis))
-        samples += S * T
+        p = cg.fx_params(S, 2 * C, T // (2 * C), T // 4, x_mode=x_mode)
+        pending.append((svc.submit(p, raw, vis), vis, n))
         while len(pending) > 64:                      # bounded outstanding outputs
-            jid, _ = pending.pop(0)
+            jid, v, k = pending.pop(0)
             lat.append(svc.wait(jid))
-    for jid, _ in pending:
+            if k in keep:
+                kept[k] = v
+    for jid, v, k in pending:
         lat.append(svc.wait(jid))
+        if k in keep:
+            kept[k] = v
     makespan = time.perf_counter() - t0
     st = svc.stats()
     svc.close()
+    return lat, makespan, st, kept
+
+
+def run_serving(cg, torch, seconds: float, rate: float, x_mode: int, seed: int = 5, error_jobs: int = 16,
+                near_seconds: float = 10.0):
+    """Batched streaming service: Poisson arrivals, uneven jobs (S, C, T) as in the
+    serving configuration, device-resident buffers; latency is submit -> done.
+    The service runs with its defaults: two streams, jobs under 2^24 samples on
+    a high-priority stream.  Three runs of the same job mix:
+      * the Poisson window at `rate` jobs/s;
+      * capacity: 2000 jobs submitted at once (64 outstanding), served rate;
+      * near capacity: Poisson arrivals at 0.8 x the capacity job rate for
+        `near_seconds`;
+    and, for `error_jobs` seeded jobs of the first run, the tensor-core result
+    against the FP32 CUDA-core path (max over products of the relative L2
+    error over channels)."""
+    rng = np.random.default_rng(seed)
+    jobs, t_arr = _serving_jobs(rng, seconds, rate)
+    max_raw = 200 * (1 << 24) // 4                   # the mix's largest job (S = 200, T = 2^24)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    raw_pool = torch.randint(0, 256, (max_raw,), dtype=torch.uint8, device="cuda", generator=g)
+    # outputs of up to 256 MB are kept for the error check
+    small = [k for k, (S, C, T) in enumerate(jobs) if C * S * (S + 1) // 2 * 8 <= 256 << 20]
+    keep = set(np.random.default_rng(seed + 1).choice(small, size=min(error_jobs, len(small)), replace=False).tolist())
+    lat, makespan, st, kept = _serve(cg, torch, jobs, t_arr, x_mode, raw_pool, keep)
+    samples = sum(S * T for S, _, T in jobs)
+    res = {"jobs": len(jobs), "arrival_rate_per_s": rate, "window_s": seconds,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "offered_gsamples_s": samples / seconds / 1e9, "served_gsamples_s": samples / makespan / 1e9,
+           "max_concurrent_jobs": st["max_running"], "failed": st["failed"],
+           "p99_queue_ms": st["p99_queue_ms"], "streams": 2, "priority_samples": 1 << 24,
+           "job_mix": "S in {4,8,24,64,200}, C in {256,1024,4096,16384}, T = 2^U, U in [18,24]"}
+    if x_mode == cg.X_TC_FP16 and kept:
+        errs = []
+        for k, v in kept.items():
+            S, C, T = jobs[k]
+            ref = torch.empty_like(v)
+            raw = raw_pool[: S * T // 4].view(S, T // 4)
+            cg.fx_correlate(cg.fx_params(S, 2 * C, T // (2 * C), T // 4, x_mode=cg.X_FP32), raw, ref)
+            num = torch.linalg.vector_norm(v - ref, dim=0)
+            errs.append(float((num / torch.linalg.vector_norm(ref, dim=0)).max()))
+        res["tc_vs_fp32"] = {"jobs": len(errs), "max_rel": max(errs), "median_rel": float(np.median(errs)),
+                             "sample": "seeded jobs with outputs up to 256 MB; max over products of the "
+                                       "relative L2 error over channels"}
+    kept.clear()
+    # capacity: the same mix, all submitted at once
+    cj, _ = _serving_jobs(np.random.default_rng(seed + 2), 2000, 0.0)
+    clat, cspan, cst, _ = _serve(cg, torch, cj, [0.0] * len(cj), x_mode, raw_pool)
+    csamples = sum(S * T for S, _, T in cj)
+    cap_rate = len(cj) / cspan
+    res["capacity"] = {"jobs": len(cj), "served_gsamples_s": csamples / cspan / 1e9, "jobs_per_s": cap_rate,
+                       "failed": cst["failed"], "max_concurrent_jobs": cst["max_running"]}
+    if near_seconds > 0:
+        nrate = 0.8 * cap_rate
+        nj, nt = _serving_jobs(np.random.default_rng(seed + 3), near_seconds, nrate)
+        nlat, nspan, nst, _ = _serve(cg, torch, nj, nt, x_mode, raw_pool)
+        nsamples = sum(S * T for S, _, T in nj)
+        res["near_capacity"] = {"jobs": len(nj), "arrival_rate_per_s": nrate, "window_s": near_seconds,
+                                "offered_gsamples_s": nsamples / near_seconds / 1e9,
+                                "served_gsamples_s": nsamples / nspan / 1e9,
+                                "p50_ms": float(np.percentile(nlat, 50)), "p99_ms": float(np.percentile(nlat, 99)),
+                                "p99_queue_ms": nst["p99_queue_ms"], "failed": nst["failed"],
+                                "max_concurrent_jobs": nst["max_running"]}
     del raw_pool
-    return {"jobs": len(jobs), "arrival_rate_per_s": rate, "window_s": seconds,
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "offered_gsamples_s": samples / seconds / 1e9, "served_gsamples_s": samples / makespan / 1e9,
-            "max_concurrent_jobs": st["max_running"], "failed": st["failed"],
-            "p99_queue_ms": st["p99_queue_ms"], "streams": 2, "priority_samples": 1 << 24,
-            "job_mix": "S in {4,8,24,64,200}, C in {256,1024,4096,16384}, T = 2^U, U in [18,24]"}
+    return res
 
 
 def _time_calls(torch, fn, steps: int, warmup: int) -> float:
@@ -393,7 +450,7 @@ def main():
     ap.add_argument("--no-error", action="store_true", help="skip the FP64 accuracy check of the timed job")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the FP32-path, spectrometer and delay-tracked measurements")
-    ap.add_argument("--serve-seconds", type=float, default=4.0,
+    ap.add_argument("--serve-seconds", type=float, default=30.0,
                     help="length of the Poisson arrival window of the serving measurement (0 skips it)")
     ap.add_argument("--segments", type=int, default=K,
                     help="spectra per integration (smaller values make a profiling-sized case)")
