@@ -29,6 +29,7 @@
 #include "kernels.h"
 
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -204,6 +205,230 @@ __global__ void __launch_bounds__(SCfg<MC>::NT) k_spec_power(const __grid_consta
     }
 }
 
+// N = 32768 (P = 1) and 65536 (P = 2): the CTA's 16384-point complex FFT as
+// a warp four-step with decimation in frequency, so that every input read
+// (plane words, window pairs, twiddles) is coalesced across threads:
+//   n = 1024 n1 + m (n1 < 16, m < 1024),  k = k1 + 16 k2 (k1 < 16, k2 < 1024)
+//   W_MC^(n k) = W_16^(n1 k1) W_MC^(m k1) W_1024^(m k2).
+// Column phase: thread t takes columns m = t, t + 512: 16 windowed inputs
+// (P = 2: the parity fold of both halves), DFT-16 over n1, twiddle
+// W_MC^(m k1), stored to row k1 of a [16][1088] tile.  Row phase: warp k1
+// takes row k1: a 1024-point DFT in registers (32 points per lane: DFT-32,
+// twiddle, transpose through the row's own padded region, DFT-32) and stores
+// Y[k1][k2] back in natural k2 order.  Pair phase: each thread owns fixed
+// items (k1, k2) whose real-FFT partner lies in row 16 - k1 (P = 1 and p = 0)
+// or 15 - k1 (p = 1), splits them (r2c_pair) and adds |X|^2 into its own
+// shared-memory slots [slot][thread] (no two threads share a bin), which the
+// CTA writes as the chunk's partial spectrum.  512 threads, one CTA per SM.
+constexpr int SW_NT = 512, SW_MC = 16384, SW_ROWP = 1088, SW_SLOTS = 34;
+
+// tile column of index k2 (or m): two float2 of padding after every 32
+CS_DEV int sw_pad(int k2) { return k2 + 2 * (k2 >> 5); }
+
+template <int P, bool MASK>
+__global__ void __launch_bounds__(SW_NT, 1) k_spec_power_w(const __grid_constant__ CsSpecArgs a, const float2* __restrict__ tw,
+                                                           const float* __restrict__ win, int nchunk, int ch)
+{
+    constexpr int MC = SW_MC, M = MC * P, N = 2 * M;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* tile = reinterpret_cast<float2*>(smem);                       // [16][SW_ROWP]
+    float* slots = reinterpret_cast<float*>(tile + 16 * SW_ROWP);         // [SW_SLOTS][SW_NT]
+    uint32_t* rawsm = reinterpret_cast<uint32_t*>(slots + SW_SLOTS * SW_NT);   // the FFT's N / 16 plane words
+    __shared__ float2 lut16[16];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int chunk = blockIdx.x, row = blockIdx.y;
+    const int sub = row / a.nspec, spec = row % a.nspec;
+    const int p = (P == 2) ? (int)blockIdx.z : 0;
+    const int novl = a.overlap * a.ffts_per_spectrum - (a.overlap - 1);
+    const int hop = N / a.overlap;
+    const uint32_t* plane = reinterpret_cast<const uint32_t*>(a.planes + (int64_t)sub * a.bytes_per_sub);
+    // blanking mask only in the MASK form (framed recordings), so the plain
+    // form carries no per-sample mask code
+    const uint32_t* vmask = MASK ? a.valid_mask : nullptr;
+    const float2* win2 = reinterpret_cast<const float2*>(win);
+    if (tid < 16) lut16[tid] = make_float2(a.lut[tid & 3], a.lut[tid >> 2]);
+    for (int i = tid; i < SW_SLOTS * SW_NT; i += SW_NT) slots[i] = 0.f;
+
+    // pair items of this thread: (k1, k2) with partner (k1', k2')
+    //  P = 1 / p = 0: rows 1..7 (k2 = t, t + 512), row 8 (k2 = t), row 0 (k2 = t; t = 0 also k2 = 512)
+    //  p = 1:         rows 0..7 (k2 = t, t + 512)
+    const bool odd = P == 2 && p == 1;
+    // row-phase twiddles W_1024^(lane e), e < 8 (balanced recurrence), and
+    // W_1024^(8 lane), kept in shared memory [e][lane] for every warp
+    __shared__ float2 wps[9][32];
+    if (warp == 0) {
+        float2 wp[8];
+        float sn, cs;
+        sincospif(-(float)lane / 512.0f, &sn, &cs);
+        wp[0] = make_float2(1.f, 0.f);
+        wp[1] = make_float2(cs, sn);
+#pragma unroll
+        for (int e = 2; e < 8; e++) wp[e] = (e & 1) ? cmul(wp[e - 1], wp[1]) : cmul(wp[e / 2], wp[e / 2]);
+#pragma unroll
+        for (int e = 0; e < 8; e++) wps[e][lane] = wp[e];
+        wps[8][lane] = cmul(wp[4], wp[4]);
+    }
+    // per-thread constants: W_M^m and W_MC^m of the thread's two columns m = t, t + 512;
+    // the split twiddle W_N^k of item (k1, k2), k = P (k1 + 16 k2) + p, as
+    // ck[k1] = W_N^(P k1 + p) (shared, broadcast) times W_N^(16 P k2) of k2 = t, t + 512
+    __shared__ float2 ck[16];
+    if (tid < 16) ck[tid] = __ldg(tw + P * tid + p);
+    float2 tmc[2], umc[2], bk[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        const int m = tid + SW_NT * c;                   // column-phase columns and pair-phase k2
+        tmc[c] = (P == 2) ? __ldg(tw + 2 * m) : make_float2(1.f, 0.f);   // W_M^m
+        umc[c] = __ldg(tw + 2 * P * m);                  // W_MC^m
+        bk[c] = __ldg(tw + 16 * P * m);                  // W_N^(16 P k2)
+    }
+    const float2 bk512 = __ldg(tw + 16 * P * 512);       // k2 = 512 (thread 0's extra item)
+    __syncthreads();
+
+    const int j_begin = chunk * ch, j_end = min(novl, j_begin + ch);
+    // the plane words of FFT j go to shared memory by cp.async (hop is a
+    // multiple of 64 samples, so each FFT starts on a 16-byte boundary); the
+    // next FFT's are fetched while this one's row and pair phases run
+    auto fetch = [&](int jj) {
+        const int64_t st = (int64_t)spec * a.ffts_per_spectrum * N + (int64_t)jj * hop;
+        const char* src = reinterpret_cast<const char*>(plane + (st >> 4));
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(rawsm);
+        for (int i = tid; i < N / 64; i += SW_NT)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i), "l"(src + 16 * i) : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    if (j_begin < j_end) fetch(j_begin);
+    for (int j = j_begin; j < j_end; j++) {
+        const int64_t start = (int64_t)spec * a.ffts_per_spectrum * N + (int64_t)j * hop;   // a multiple of 64
+        const uint32_t* wsrc = rawsm;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();                                   // this FFT's words are in
+        // ---- column phase: columns m = t, t + 512 ----
+#pragma unroll 1
+        for (int c = 0; c < 2; c++) {
+            const int m = tid + SW_NT * c;
+            float2 v[16];
+            const float2 tm = c ? tmc[1] : tmc[0];                                     // W_M^m
+#pragma unroll
+            for (int n1 = 0; n1 < 16; n1++) {
+                const int n = 1024 * n1 + m;
+                const float2 x1 = sample_pair16(lut16, wsrc[n >> 3], (2 * n) & 15, vmask, start + 2 * n);
+                const float2 wa = __ldg(win2 + n);
+                const float2 z1 = make_float2(x1.x * wa.x, x1.y * wa.y);
+                if constexpr (P == 1) {
+                    v[n1] = z1;
+                } else {
+                    const int n2 = n + MC;
+                    const float2 x2 = sample_pair16(lut16, wsrc[n2 >> 3], (2 * n2) & 15, vmask, start + 2 * n2);
+                    // cosine^2: w(i + N/2) = 1 - w(i) (one table read for both halves)
+                    const float2 wb = (a.window == 2) ? make_float2(1.f - wa.x, 1.f - wa.y) : __ldg(win2 + n2);
+                    const float2 z2 = make_float2(x2.x * wb.x, x2.y * wb.y);
+                    // y_1[n] = (z[n] - z[n + MC]) W_M^n, W_M^(1024 n1 + m) = W_32^n1 W_M^m
+                    v[n1] = p ? cmul(csub(z1, z2), rot32(tm, n1)) : cadd(z1, z2);
+                }
+            }
+            Dft<16>::run(v);
+            // W_MC^(m k1): powers of u = W_MC^m by a balanced recurrence
+            const float2 u = c ? umc[1] : umc[0];
+            float2 wk[16];
+            wk[0] = make_float2(1.f, 0.f);
+            wk[1] = u;
+#pragma unroll
+            for (int e = 2; e < 16; e++) wk[e] = (e & 1) ? cmul(wk[e - 1], u) : cmul(wk[e / 2], wk[e / 2]);
+#pragma unroll
+            for (int k1 = 0; k1 < 16; k1++) tile[k1 * SW_ROWP + sw_pad(m)] = k1 ? cmul(v[k1], wk[k1]) : v[k1];
+        }
+        __syncthreads();                                   // the words are consumed: fetch the next FFT's
+        if (j + 1 < j_end) fetch(j + 1);
+        // ---- row phase: warp k1 ----
+        {
+            float2* rowp = tile + warp * SW_ROWP;
+            float2 x[32];
+#pragma unroll
+            for (int e = 0; e < 32; e++) x[e] = rowp[lane + 34 * e];          // m = lane + 32 e
+            Dft<32>::run(x);
+            float2 q = make_float2(1.f, 0.f);
+            const float2 w8 = wps[8][lane];
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    if (b == 0 && r == 0) continue;
+                    const float2 wr = wps[r][lane];
+                    x[8 * b + r] = cmul(x[8 * b + r], b ? cmul(q, wr) : wr);
+                }
+                q = b ? cmul(q, w8) : w8;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int e = 0; e < 32; e++) rowp[e * 33 + lane] = x[e];
+            __syncwarp();
+#pragma unroll
+            for (int e = 0; e < 32; e++) x[e] = rowp[lane * 33 + e];
+            Dft<32>::run(x);                                                    // x[e] = Y[warp][lane + 32 e]
+            __syncwarp();
+#pragma unroll
+            for (int e = 0; e < 32; e++) rowp[lane + 34 * e] = x[e];          // k2 = lane + 32 e
+        }
+        __syncthreads();
+        // ---- pair phase ----
+        int s = 0;
+        // SPECIAL: row 0 of the even forms, which holds k = 0 (DC and Nyquist
+        // from Z[0]) and k = M/2 (its own partner)
+        auto item = [&](int k1, int k2, float2 b, bool special) {
+            int k1b, k2b;
+            if (odd) k1b = 15 - k1, k2b = 1023 - k2;
+            else if (k1 == 0) k1b = 0, k2b = (1024 - k2) & 1023;
+            else k1b = 16 - k1, k2b = 1023 - k2;
+            const float2 za = tile[k1 * SW_ROWP + sw_pad(k2)], zb = tile[k1b * SW_ROWP + sw_pad(k2b)];
+            const int mp = k1 + 16 * k2;                   // index in the CTA's transform
+            const int k = P * mp + p;                      // bin of the full real FFT
+            float2 Xk, Xm;
+            r2c_pair(za, zb, cmul(ck[k1], b), Xk, Xm);          // W_N^k
+            if (special && k == 0) {
+                slots[s * SW_NT + tid] += Xk.x * Xk.x;
+                slots[(s + 1) * SW_NT + tid] += Xm.x * Xm.x;
+            } else {
+                slots[s * SW_NT + tid] += Xk.x * Xk.x + Xk.y * Xk.y;
+                if (!special || k != M / 2) slots[(s + 1) * SW_NT + tid] += Xm.x * Xm.x + Xm.y * Xm.y;
+            }
+            s += 2;
+        };
+        if (odd) {
+#pragma unroll
+            for (int k1 = 0; k1 < 8; k1++) item(k1, tid, bk[0], false), item(k1, tid + SW_NT, bk[1], false);
+        } else {
+#pragma unroll
+            for (int k1 = 1; k1 < 8; k1++) item(k1, tid, bk[0], false), item(k1, tid + SW_NT, bk[1], false);
+            item(8, tid, bk[0], false);
+            item(0, tid, bk[0], true);
+            if (tid == 0) item(0, 512, bk512, true);
+        }
+        __syncthreads();                                   // the tile is rewritten by the next FFT
+    }
+    // ---- the chunk's partial spectrum: the same items' bins ----
+    float* prow = a.partial + ((int64_t)row * nchunk + chunk) * (M + 1);
+    int s = 0;
+    auto put = [&](int k1, int k2) {
+        const int k = P * (k1 + 16 * k2) + p;
+        if (k == 0) {
+            prow[0] = slots[s * SW_NT + tid];
+            prow[M] = slots[(s + 1) * SW_NT + tid];
+        } else {
+            prow[k] = slots[s * SW_NT + tid];
+            if (k != M / 2) prow[M - k] = slots[(s + 1) * SW_NT + tid];
+        }
+        s += 2;
+    };
+    if (odd) {
+        for (int k1 = 0; k1 < 8; k1++) put(k1, tid), put(k1, tid + SW_NT);
+    } else {
+        for (int k1 = 1; k1 < 8; k1++) put(k1, tid), put(k1, tid + SW_NT);
+        put(8, tid);
+        put(0, tid);
+        if (tid == 0) put(0, 512);
+    }
+}
+
 __global__ void k_spec_reduce(const float* __restrict__ partial, float* __restrict__ power, int rows, int nchunk,
                               int nb, float scale)
 {
@@ -336,6 +561,17 @@ __global__ void k_pcal_reduce(const float2* __restrict__ partial, int rows, int 
 constexpr int PCAL_THREADS = 128;
 constexpr int PCAL_BLOCKS = 32;
 
+// CELLSPE_SPEC_CTA_FFT=1 selects the shared-memory radix-16 kernel for N =
+// 32768 and 65536 instead of the warp four-step (both compute the same sums).
+bool spec_cta_fft()
+{
+    static const bool v = [] {
+        const char* e = getenv("CELLSPE_SPEC_CTA_FFT");
+        return e && e[0] == '1';
+    }();
+    return v;
+}
+
 int spec_chunk(const CsSpecArgs& a) { return a.ffts_per_chunk > 0 ? a.ffts_per_chunk : SPEC_CH; }
 
 template <int MC, int P>
@@ -351,6 +587,22 @@ int launch_power(const CsSpecArgs& a, int nchunk, cudaStream_t st)
     CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(nchunk, a.nsub * a.nspec, P);
     kern<<<grid, C::NT, smem, st>>>(a, tw, win, nchunk, spec_chunk(a)), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}
+
+template <int P>
+int launch_power_w(const CsSpecArgs& a, int nchunk, cudaStream_t st)
+{
+    constexpr int N = 2 * SW_MC * P;
+    const float2* tw = a.tw_table ? a.tw_table : cs_twiddles(N);
+    const float* win = a.win_table ? a.win_table : window_table(a.window, N);
+    if (!tw || !win) return CS_ERR_ARG;
+    if ((N / a.overlap) % 64) return launch_power<SW_MC, P>(a, nchunk, st);   // FFT starts not 16-byte aligned
+    const size_t smem = (size_t)16 * SW_ROWP * sizeof(float2) + (size_t)SW_SLOTS * SW_NT * sizeof(float) + N / 16 * 4;
+    auto kern = a.valid_mask ? k_spec_power_w<P, true> : k_spec_power_w<P, false>;
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(nchunk, a.nsub * a.nspec, P);
+    kern<<<grid, SW_NT, smem, st>>>(a, tw, win, nchunk, spec_chunk(a)), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 
@@ -399,8 +651,8 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
         case 4096: rc = launch_power<2048, 1>(a, nchunk, st); break;
         case 8192: rc = launch_power<4096, 1>(a, nchunk, st); break;
         case 16384: rc = launch_power<8192, 1>(a, nchunk, st); break;
-        case 32768: rc = launch_power<16384, 1>(a, nchunk, st); break;
-        case 65536: rc = launch_power<16384, 2>(a, nchunk, st); break;
+        case 32768: rc = spec_cta_fft() ? launch_power<16384, 1>(a, nchunk, st) : launch_power_w<1>(a, nchunk, st); break;
+        case 65536: rc = spec_cta_fft() ? launch_power<16384, 2>(a, nchunk, st) : launch_power_w<2>(a, nchunk, st); break;
         default: return CS_ERR_UNSUPPORTED;
     }
     if (rc) return rc;

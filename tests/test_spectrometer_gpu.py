@@ -20,7 +20,10 @@ def _oracle(orc, words, nsub, N, overlap, window, K, tonebins=0, rotatorlen=0, o
 
 @pytest.mark.parametrize("nsub,N,overlap,window,K,nspec", [
     (16, 1024, 2, 2, 8, 2), (4, 4096, 1, 0, 4, 1), (1, 2048, 4, 1, 3, 2), (8, 32768, 2, 2, 2, 1),
-    (4, 65536, 2, 2, 3, 1)])
+    (4, 65536, 2, 2, 3, 1),
+    # the warp four-step kernel of N = 32768 / 65536 with every other window and overlap
+    (4, 65536, 1, 1, 2, 2), (4, 32768, 4, 3, 2, 1), (1, 65536, 4, 5, 2, 1), (1, 32768, 1, 0, 3, 2),
+    (1, 65536, 2, 4, 2, 1)])
 def test_spectrometer_vs_oracle(cg, orc, nsub, N, overlap, window, K, nspec):
     import synth
 
