@@ -150,7 +150,19 @@ struct Arena {
 // wait for the first one; output blocks stay large enough to fill the GPU.
 constexpr int PIPE_IN = 16, PIPE_OUT = 8;
 
+// Input-copy order shared by the workers of one service: a host-buffer job's
+// input copies start after the previous job's input copies have finished
+// (a device-side wait on `in_done`), so two jobs in flight do not copy and
+// compute in lockstep (each at half speed) but one's input moves while the
+// other computes.
+struct CopyChain {
+    std::mutex mu;
+    cudaEvent_t in_done = nullptr;
+    bool valid = false;
+};
+
 struct Workspace {
+    CopyChain* chain = nullptr;       // set by the service for its workers
     cudaStream_t stream = nullptr;
     cudaStream_t copy = nullptr;      // host <-> device copies overlapping the kernels
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -497,12 +509,20 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
         // the copy stream starts after everything queued before this job
         cudaEventRecord(ws.cev[PIPE_IN + PIPE_OUT], ws.stream);
         cudaStreamWaitEvent(ws.copy, ws.cev[PIPE_IN + PIPE_OUT], 0);
+        std::unique_lock<std::mutex> chain_lk;
+        if (ws.chain) {
+            chain_lk = std::unique_lock<std::mutex>(ws.chain->mu);
+            if (ws.chain->valid) cudaStreamWaitEvent(ws.copy, ws.chain->in_done, 0);
+        }
         for (int i = 0; i < nsc && !j.err; i++) {
             const long long s0 = (long long)S * i / nsc, s1 = (long long)S * (i + 1) / nsc;
             cudaError_t e = cudaMemcpyAsync((void*)(d_raw + s0 * bpi), (const uint8_t*)raw + s0 * bpi,
                                             (size_t)((s1 - s0) * bpi), cudaMemcpyHostToDevice, ws.copy);
             if (e == cudaSuccess) e = cudaEventRecord(ws.cev[i], ws.copy);
             if (e != cudaSuccess) j.err = cuda_fail(e, "host to device copy");
+        }
+        if (ws.chain && !j.err) {
+            ws.chain->valid = cudaEventRecord(ws.chain->in_done, ws.copy) == cudaSuccess;
         }
     }
     if (sync) cudaEventRecord(ws.sev[0], ws.stream);
@@ -1282,6 +1302,7 @@ struct SvcJob {
 }  // namespace
 
 struct cellspe_service {
+    CopyChain chain;                  // input-copy order of host-buffer jobs
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<SvcJob>> queue;
@@ -1302,6 +1323,7 @@ void service_worker(cellspe_service* sv)
 {
     Workspace ws;
     int init = ws.init();
+    ws.chain = &sv->chain;
     cs_fstage_allow_timing(false);       // no schedule timing inside a live job
     // small jobs go to a stream of the greatest priority: the block scheduler
     // then dispatches their thread blocks before the waiting blocks of large
@@ -2234,6 +2256,11 @@ cellspe_service* cellspe_service_create(const cellspe_service_config* cfg)
     auto* sv = new cellspe_service();
     long long b = (cfg && cfg->hbm_budget_bytes > 0) ? cfg->hbm_budget_bytes : (long long)(0.8 * (double)budget_bytes() / 0.9);
     sv->budget = b;
+    if (cudaEventCreateWithFlags(&sv->chain.in_done, cudaEventDisableTiming) != cudaSuccess) {
+        delete sv;
+        cuda_fail(cudaGetLastError(), "service setup");
+        return nullptr;
+    }
     int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 2;
     sv->priority_samples = !cfg || cfg->priority_samples == 0 ? (1LL << 24) : cfg->priority_samples;
     sv->large_samples = cfg ? cfg->large_samples : 0;
@@ -2317,6 +2344,7 @@ void cellspe_service_destroy(cellspe_service* sv)
     for (auto& t : sv->workers) t.join();
     for (auto& j : sv->queue)              // never started
         if (j->ready) cudaEventDestroy(j->ready), j->ready = nullptr;
+    if (sv->chain.in_done) cudaEventDestroy(sv->chain.in_done);
     delete sv;
 }
 
