@@ -302,6 +302,7 @@ def run_configs(cg, torch, x_mode: int, with_cpu: bool, raw, vis_main):
                                     "max-abs int8 spectra, mma.sync m16n8k32 IMMA, int32 sums)",
                         "stages_ms": {"f_stage_and_quantise": st8[1], "x_stage": st8[2]},
                         "x_stage_tops": x8_ops / (st8[2] * 1e-3) / 1e12,
+                        "imma_peak_tops": 151.0,     # register-only mma.sync s8 m16n8k32 loop on this GB300
                         "error": vis_error(torch, raw, vis8, S, N, K, 16, 32, seed=K),
                         "int8_vs_fp32_max_rel": rel_all(torch, vis, vis8)}
     del vis, vis8
