@@ -1335,6 +1335,7 @@ int launch_w1024(const CsFStageArgs& a, cudaStream_t st)
 }  // namespace
 
 void cs_fstage_allow_timing(bool allow) { t_w2048_timing_allowed = allow; }
+bool cs_fstage_timing_allowed() { return t_w2048_timing_allowed; }
 
 namespace {
 

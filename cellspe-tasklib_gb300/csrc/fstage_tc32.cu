@@ -165,7 +165,7 @@ struct Tc32Args {
     int s_rows;               // S_out
 };
 
-template <bool PHASE>
+template <bool PHASE, bool SCALE>
 __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_constant__ Tc32Args args)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 X = cmul(X, B);                                                         \
                 B = cmul(B, D);                                                         \
             }                                                                           \
-            if (scl) X = cscale(X, __ldg(scl + (c_)));                                  \
+            if (SCALE) X = cscale(X, __ldg(scl + (c_)));                                \
             stg[(seg_) * STG_PITCH + (c_)] = h2u(__floats2half2_rn(X.x, X.y));          \
         }
 
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
                 const int u = jj / QUADS, b = jj & 1, qd = jj % QUADS;
                 int s, kb;
                 unit_of(u, s, kb);
-                const float* scl = a.scale ? a.scale + (int64_t)s * FC : nullptr;
+                const float* scl = SCALE ? a.scale + (int64_t)s * FC : nullptr;
                 // ---- epilogue 2: X -> phasor, scale -> FP16 staging; warp (q, h): lane
                 // quarter q = segment q of the quad, lane = k1, k2 in [8 h, 8 h + 8) ----
                 {
@@ -656,13 +656,11 @@ int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st)
     t.nkb = (a.kp ? a.kp : a.K) / US;
     t.s_rows = a.S_out ? a.S_out : a.S;
     const int grid = (int)std::min<int64_t>(t.units, g_sms32);
-    if (a.phase0) {
-        CS_CUDA_TRY(cudaFuncSetAttribute(k_fx_fstage_tc32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        k_fx_fstage_tc32<true><<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
-    } else {
-        CS_CUDA_TRY(cudaFuncSetAttribute(k_fx_fstage_tc32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        k_fx_fstage_tc32<false><<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
-    }
+    // the delay phasor and the channel scale are compiled in only where used
+    auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32<true, true> : k_fx_fstage_tc32<true, false>)
+                         : (a.scale ? k_fx_fstage_tc32<false, true> : k_fx_fstage_tc32<false, false>);
+    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    kern<<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
 

@@ -76,6 +76,7 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
 // this thread's jobs (default true; the correlation service's workers turn it
 // off and use the last timed schedule).
 void cs_fstage_allow_timing(bool allow);
+bool cs_fstage_timing_allowed();   // this thread may time kernel choices (autotuners)
 // True when the F stage for these arguments writes FP16 spectra k-blocked:
 // __half [C][S_out][kp/32][2][32], i.e. for each (channel, input) and block of
 // 32 segments the 32 Re halves then the 32 Im halves (128 contiguous bytes, the

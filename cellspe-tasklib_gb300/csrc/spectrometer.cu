@@ -32,6 +32,7 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -303,6 +304,9 @@ __global__ void __launch_bounds__(SW_NT, 1) k_spec_power_w(const __grid_constant
         asm volatile("cp.async.wait_group 0;" ::: "memory");
         __syncthreads();                                   // this FFT's words are in
         // ---- column phase: columns m = t, t + 512 ----
+        // (the mask is applied only to windows that contain blanked samples)
+        auto column_phase = [&](auto masked) {
+        const uint32_t* vm = decltype(masked)::value ? vmask : nullptr;
 #pragma unroll 1
         for (int c = 0; c < 2; c++) {
             const int m = tid + SW_NT * c;
@@ -311,14 +315,14 @@ __global__ void __launch_bounds__(SW_NT, 1) k_spec_power_w(const __grid_constant
 #pragma unroll
             for (int n1 = 0; n1 < 16; n1++) {
                 const int n = 1024 * n1 + m;
-                const float2 x1 = sample_pair16(lut16, wsrc[n >> 3], (2 * n) & 15, vmask, start + 2 * n);
+                const float2 x1 = sample_pair16(lut16, wsrc[n >> 3], (2 * n) & 15, vm, start + 2 * n);
                 const float2 wa = __ldg(win2 + n);
                 const float2 z1 = make_float2(x1.x * wa.x, x1.y * wa.y);
                 if constexpr (P == 1) {
                     v[n1] = z1;
                 } else {
                     const int n2 = n + MC;
-                    const float2 x2 = sample_pair16(lut16, wsrc[n2 >> 3], (2 * n2) & 15, vmask, start + 2 * n2);
+                    const float2 x2 = sample_pair16(lut16, wsrc[n2 >> 3], (2 * n2) & 15, vm, start + 2 * n2);
                     // cosine^2: w(i + N/2) = 1 - w(i) (one table read for both halves)
                     const float2 wb = (a.window == 2) ? make_float2(1.f - wa.x, 1.f - wa.y) : __ldg(win2 + n2);
                     const float2 z2 = make_float2(x2.x * wb.x, x2.y * wb.y);
@@ -337,6 +341,17 @@ __global__ void __launch_bounds__(SW_NT, 1) k_spec_power_w(const __grid_constant
 #pragma unroll
             for (int k1 = 0; k1 < 16; k1++) tile[k1 * SW_ROWP + sw_pad(m)] = k1 ? cmul(v[k1], wk[k1]) : v[k1];
         }
+        };
+        bool blanked = false;
+        if constexpr (MASK) {
+            // any blanked sample in this window? (N / 32 mask words, a few per thread)
+            const uint32_t* mw = vmask + (start >> 5);
+            bool mine = false;
+            for (int i = tid; i < N / 32; i += SW_NT) mine |= __ldg(mw + i) != 0xffffffffu;
+            blanked = __syncthreads_or(mine) != 0;
+        }
+        if (blanked) column_phase(std::true_type{});
+        else column_phase(std::false_type{});
         __syncthreads();                                   // the words are consumed: fetch the next FFT's
         if (j + 1 < j_end) fetch(j + 1);
         // ---- row phase: warp k1 ----
@@ -562,7 +577,7 @@ constexpr int PCAL_THREADS = 128;
 constexpr int PCAL_BLOCKS = 32;
 
 // CELLSPE_SPEC_CTA_FFT=1 selects the shared-memory radix-16 kernel for N =
-// 32768 and 65536 instead of the warp four-step (both compute the same sums).
+// 32768 and 65536 instead of choosing between it and the warp four-step.
 bool spec_cta_fft()
 {
     static const bool v = [] {
@@ -604,6 +619,54 @@ int launch_power_w(const CsSpecArgs& a, int nchunk, cudaStream_t st)
     dim3 grid(nchunk, a.nsub * a.nspec, P);
     kern<<<grid, SW_NT, smem, st>>>(a, tw, win, nchunk, spec_chunk(a)), cs_count_launches(1);
     return (int)cudaGetLastError();
+}
+
+// N = 32768 / 65536: the warp four-step or the CTA radix-16 power kernel,
+// chosen per (device, N, overlap) by timing both once on the caller's own job
+// (both compute the same partial sums, so each runs once warm and once timed
+// and the chosen one runs for the result); outside stream capture and where
+// the calling thread allows timing (not inside service workers).  Until a
+// timed choice exists, and with CELLSPE_SPEC_CTA_FFT=1, fixed choices.
+std::mutex g_sp_tune_mu;
+std::map<std::tuple<int, int, int>, int> g_sp_choice;   // (device, N, overlap) -> 0 warp, 1 CTA
+
+template <int P>
+int launch_power_long(const CsSpecArgs& a, int nchunk, cudaStream_t st)
+{
+    if (spec_cta_fft()) return launch_power<SW_MC, P>(a, nchunk, st);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, a.N, a.overlap);
+    int choice = -1;
+    {
+        std::lock_guard<std::mutex> lk(g_sp_tune_mu);
+        auto it = g_sp_choice.find(key);
+        if (it != g_sp_choice.end()) choice = it->second;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const bool can_time = cs_fstage_timing_allowed() && cudaStreamIsCapturing(st, &cap) == cudaSuccess &&
+                          cap == cudaStreamCaptureStatusNone;
+    if (choice < 0 && can_time) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float t[2] = {1e30f, 1e30f};
+        if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+            for (int v = 0; v < 2; v++) {
+                auto run = [&] { return v ? launch_power<SW_MC, P>(a, nchunk, st) : launch_power_w<P>(a, nchunk, st); };
+                if (run() != 0) continue;
+                cudaEventRecord(e0, st);
+                const int rc = run();
+                cudaEventRecord(e1, st);
+                if (rc == 0 && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&t[v], e0, e1);
+            }
+        }
+        cudaGetLastError();
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        choice = t[1] < 0.98f * t[0] ? 1 : 0;
+        std::lock_guard<std::mutex> lk(g_sp_tune_mu);
+        g_sp_choice[key] = choice;
+    }
+    return choice == 1 ? launch_power<SW_MC, P>(a, nchunk, st) : launch_power_w<P>(a, nchunk, st);
 }
 
 int spec_nchunk(const CsSpecArgs& a)
@@ -651,8 +714,8 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
         case 4096: rc = launch_power<2048, 1>(a, nchunk, st); break;
         case 8192: rc = launch_power<4096, 1>(a, nchunk, st); break;
         case 16384: rc = launch_power<8192, 1>(a, nchunk, st); break;
-        case 32768: rc = spec_cta_fft() ? launch_power<16384, 1>(a, nchunk, st) : launch_power_w<1>(a, nchunk, st); break;
-        case 65536: rc = spec_cta_fft() ? launch_power<16384, 2>(a, nchunk, st) : launch_power_w<2>(a, nchunk, st); break;
+        case 32768: rc = launch_power_long<1>(a, nchunk, st); break;
+        case 65536: rc = launch_power_long<2>(a, nchunk, st); break;
         default: return CS_ERR_UNSUPPORTED;
     }
     if (rc) return rc;

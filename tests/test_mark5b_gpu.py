@@ -136,6 +136,35 @@ def test_spectrometer_on_framed_input_vs_oracle(cg, orc, nch, N, overlap, K, nsp
     assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < 1e-5
 
 
+@pytest.mark.parametrize("nch,N,K,fill", [(16, 65536, 4, (3, 4)), (4, 32768, 2, (2,))])
+def test_long_fft_framed_spectrometer_with_blanked_and_clean_windows(cg, orc, nch, N, K, fill):
+    """N = 32768 / 65536 run the warp four-step power kernel, which applies the
+    blanking mask only to windows that contain a blanked sample: fill in a
+    few frames gives both kinds of window in one call (16 channels, N = 65536:
+    only the first of 7 overlapped windows touches frames 3 and 4)."""
+    import synth
+
+    fs, tb, nspec, overlap = 32e6, 32, 1, 2
+    T = N * K * nspec
+    spf = 10000 // (nch // 4)
+    nf = -(-T // spf) + 1
+    words, _ = synth.mark5b_subbands(16, nf * spf, fs_hz=fs, seed=nch + N + 1, n_channels=N // 2, pcal_amp=0.3)
+    codes = np.stack([(words >> np.uint32(2 * c)) & np.uint32(3) for c in range(nch)], axis=1)
+    payload = synth.pack2bit(codes.reshape(-1))
+    pre = 77
+    fr = synth.mark5b_frames(payload, prefix=pre)
+    for f in fill:
+        synth.mark5b_fill(fr, f, 0, 10000, pre)
+    p = cg.spec_params(N, overlap, 2, K, nspec, nch, fr.size, layout=cg.SPEC_MARK5B_FRAMED, tonebins=tb,
+                       rotatorlen=tb, ntones=16, fs_hz=fs)
+    power = np.zeros((nch, nspec, N // 2 + 1), np.float32)
+    bins = np.zeros((nch, nspec, tb), np.complex64)
+    cg.spectrometer(p, fr, power, bins)
+    ref_p, ref_b = _spec_oracle(orc, fr, nch, N, overlap, K, nspec, tb, fs)
+    assert np.linalg.norm(power - ref_p) / np.linalg.norm(ref_p) < 1e-5
+    assert np.linalg.norm(bins - ref_b) / np.linalg.norm(ref_b) < 1e-5
+
+
 def test_framed_spectrometer_equals_payload_spectrometer_at_scale(cg):
     """Size-independent property: with no fill, framed input gives bit-identical
     spectra to the stripped payload through the interleaved layout (16 ch,
