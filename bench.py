@@ -131,10 +131,10 @@ def _serving_jobs(rng, seconds: float, rate: float):
     return jobs, t_arr
 
 
-def _serve(cg, torch, jobs, t_arr, x_mode, raw_pool, keep=()):
+def _serve(cg, torch, jobs, t_arr, x_mode, raw_pool, keep=(), batch_inputs=0):
     """Submit the jobs at their arrival times (all at once when t_arr is all 0),
     at most 64 outstanding; returns latencies, makespan, stats and the kept outputs."""
-    svc = cg.Service()
+    svc = cg.Service(batch_inputs=batch_inputs)
     pending, lat, kept = [], [], {}
     t0 = time.perf_counter()
     for n, ((S, C, T), ta) in enumerate(zip(jobs, t_arr)):
@@ -187,6 +187,7 @@ def run_serving(cg, torch, seconds: float, rate: float, x_mode: int, seed: int =
            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
            "offered_gsamples_s": samples / seconds / 1e9, "served_gsamples_s": samples / makespan / 1e9,
            "max_concurrent_jobs": st["max_running"], "failed": st["failed"],
+           "batched_jobs": st["batched_jobs"], "batched_launches": st["batched_launches"],
            "p99_queue_ms": st["p99_queue_ms"], "streams": 2, "priority_samples": 1 << 24,
            "job_mix": "S in {4,8,24,64,200}, C in {256,1024,4096,16384}, T = 2^U, U in [18,24]"}
     if x_mode == cg.X_TC_FP16 and kept:
@@ -208,18 +209,22 @@ def run_serving(cg, torch, seconds: float, rate: float, x_mode: int, seed: int =
     csamples = sum(S * T for S, _, T in cj)
     cap_rate = len(cj) / cspan
     res["capacity"] = {"jobs": len(cj), "served_gsamples_s": csamples / cspan / 1e9, "jobs_per_s": cap_rate,
-                       "failed": cst["failed"], "max_concurrent_jobs": cst["max_running"]}
+                       "failed": cst["failed"], "max_concurrent_jobs": cst["max_running"],
+                       "batched_jobs": cst["batched_jobs"], "batched_launches": cst["batched_launches"]}
     if near_seconds > 0:
         nrate = 0.8 * cap_rate
         nj, nt = _serving_jobs(np.random.default_rng(seed + 3), near_seconds, nrate)
-        nlat, nspan, nst, _ = _serve(cg, torch, nj, nt, x_mode, raw_pool)
         nsamples = sum(S * T for S, _, T in nj)
-        res["near_capacity"] = {"jobs": len(nj), "arrival_rate_per_s": nrate, "window_s": near_seconds,
-                                "offered_gsamples_s": nsamples / near_seconds / 1e9,
-                                "served_gsamples_s": nsamples / nspan / 1e9,
-                                "p50_ms": float(np.percentile(nlat, 50)), "p99_ms": float(np.percentile(nlat, 99)),
-                                "p99_queue_ms": nst["p99_queue_ms"], "failed": nst["failed"],
-                                "max_concurrent_jobs": nst["max_running"]}
+        # the same arrivals with the service's default batching and with batching off
+        for key, b in (("near_capacity", 0), ("near_capacity_unbatched", -1)):
+            nlat, nspan, nst, _ = _serve(cg, torch, nj, nt, x_mode, raw_pool, batch_inputs=b)
+            res[key] = {"jobs": len(nj), "arrival_rate_per_s": nrate, "window_s": near_seconds,
+                        "offered_gsamples_s": nsamples / near_seconds / 1e9,
+                        "served_gsamples_s": nsamples / nspan / 1e9,
+                        "p50_ms": float(np.percentile(nlat, 50)), "p99_ms": float(np.percentile(nlat, 99)),
+                        "p99_queue_ms": nst["p99_queue_ms"], "failed": nst["failed"],
+                        "max_concurrent_jobs": nst["max_running"], "batched_jobs": nst["batched_jobs"],
+                        "batched_launches": nst["batched_launches"]}
     del raw_pool
     return res
 

@@ -91,14 +91,15 @@ class SpecParams(ctypes.Structure):
 
 
 class ServiceConfig(ctypes.Structure):
-    _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_streams", ctypes.c_int), ("reserved", ctypes.c_int),
+    _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_streams", ctypes.c_int), ("batch_inputs", ctypes.c_int),
                 ("priority_samples", ctypes.c_longlong), ("large_samples", ctypes.c_longlong)]
 
 
 class ServiceStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong), ("queued", ctypes.c_longlong),
                 ("running", ctypes.c_int), ("max_running", ctypes.c_int), ("p50_ms", ctypes.c_double),
-                ("p99_ms", ctypes.c_double), ("p99_queue_ms", ctypes.c_double), ("budget_bytes", ctypes.c_longlong)]
+                ("p99_ms", ctypes.c_double), ("p99_queue_ms", ctypes.c_double), ("budget_bytes", ctypes.c_longlong),
+                ("batched_jobs", ctypes.c_longlong), ("batched_launches", ctypes.c_longlong)]
 
 
 class Mark5bInfo(ctypes.Structure):
@@ -570,8 +571,8 @@ class Service:
     """cellspe_service_*: continuous-batching correlation service."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_streams: int = 0, priority_samples: int = 0,
-                 large_samples: int = 0):
-        cfg = ServiceConfig(hbm_budget_bytes, max_streams, 0, priority_samples, large_samples)
+                 large_samples: int = 0, batch_inputs: int = 0):
+        cfg = ServiceConfig(hbm_budget_bytes, max_streams, batch_inputs, priority_samples, large_samples)
         self._h = lib().cellspe_service_create(ctypes.byref(cfg))
         if not self._h:
             raise CellspeError(ERR_CUDA, last_error())

@@ -127,6 +127,22 @@ int cs_quantise_i8(const float2* spectra, int S, int C, int K, int kp, int8_t* p
 // Error code of the last tensor-core X-stage launch (0 = ok; 1..3 = a
 // pipeline wait timed out).  Call after the launching stream has synchronised.
 int cs_xmac_tc_status(unsigned* code);
+// Batched service jobs: job b's inputs are rows off .. off + S - 1 of a stacked
+// job whose channel-major triangle is src [C][P_stacked]; its own triangle goes to
+// dst ([C][P] or, baseline_major, [P][C]).
+constexpr int CS_GATHER_MAX = 16;
+struct CsGatherJob {
+    int off, S;
+    float2* dst;
+    int baseline_major;
+};
+struct CsGatherArgs {
+    int n, C;
+    int64_t P_stacked;
+    const float2* src;
+    CsGatherJob job[CS_GATHER_MAX];
+};
+int cs_vis_gather(const CsGatherArgs& a, cudaStream_t st);
 // Baseline-major <-> channel-major triangle transpose ([C][P] -> [P][C]).
 int cs_vis_to_baseline_major(const float2* vis_cp, float2* vis_pc, int C, int64_t P, cudaStream_t st);
 

@@ -1311,6 +1311,8 @@ struct cellspe_service {
     std::vector<double> latency_ms, queue_ms;
     long long budget = 0, in_flight = 0, next_id = 1, completed = 0, failed = 0;
     long long priority_samples = 0;   // smaller jobs run on a high-priority stream (<= 0: none)
+    int batch_inputs = 0;             // > 0: small jobs of one shape share launches, up to this many inputs
+    long long batched_jobs = 0, batched_launches = 0;
     long long large_samples = 0;      // jobs this large run one at a time (<= 0: no limit)
     int large_running = 0;
     int running = 0, max_running = 0;
@@ -1318,6 +1320,74 @@ struct cellspe_service {
 };
 
 namespace {
+
+// A job that can share launches with others: device buffers, at most 16
+// inputs, tensor-core X stage, no delay model, scale, custom levels or
+// accumulation.  Jobs of one batch have the same shape.
+bool batchable(const SvcJob& q)
+{
+    const cellspe_fx_params& p = q.p;
+    return p.memory == CELLSPE_MEM_DEVICE && !q.poly && p.n_inputs <= 16 && p.x_mode == CELLSPE_X_TC_FP16 &&
+           !p.accumulate && !p.custom_levels && !p.channel_scale && !q.large;
+}
+
+bool same_shape(const SvcJob& a, const SvcJob& b)
+{
+    return a.p.fft_points == b.p.fft_points && a.p.n_segments == b.p.n_segments && a.p.levels == b.p.levels &&
+           a.p.bytes_per_input == b.p.bytes_per_input && a.p.start_sample == b.p.start_sample;
+}
+
+// One stacked job for the batch: the members' inputs back to back (device
+// copies), one FX correlation, then each member's triangle gathered out of
+// the stacked one.  Per-input F-stage results do not depend on the other
+// inputs, and the X stage sums each product over the same segments in the
+// same order, so a member's visibilities equal its solo run's.
+int run_batch(Workspace& ws, const std::vector<std::shared_ptr<SvcJob>>& batch)
+{
+    const cellspe_fx_params& p0 = batch[0]->p;
+    int S = 0;
+    for (auto& m : batch) S += m->p.n_inputs;
+    const long long bpi = p0.bytes_per_input, C = p0.fft_points / 2, P = (long long)S * (S + 1) / 2;
+    char* d_raw = nullptr;
+    float2* d_vis = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d_raw), (size_t)(S * bpi), ws.stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&d_vis), (size_t)(C * P * 8), ws.stream);
+    int rc = e == cudaSuccess ? 0 : cuda_fail(e, "batch buffers");
+    long long off = 0;
+    for (size_t b = 0; b < batch.size() && !rc; b++) {
+        const long long n = (long long)batch[b]->p.n_inputs * bpi;
+        e = cudaMemcpyAsync(d_raw + off * bpi, batch[b]->raw, (size_t)n, cudaMemcpyDeviceToDevice, ws.stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "batch input copy");
+        off += batch[b]->p.n_inputs;
+    }
+    if (!rc) {
+        cellspe_fx_params sp = p0;
+        sp.n_inputs = S;
+        sp.vis_order = CELLSPE_VIS_CHANNEL_MAJOR;
+        rc = op_fx(ws, &sp, d_raw, nullptr, d_vis, true);
+    }
+    if (!rc) {
+        CsGatherArgs g{};
+        g.n = (int)batch.size();
+        g.C = (int)C;
+        g.P_stacked = P;
+        g.src = d_vis;
+        int o = 0;
+        for (size_t b = 0; b < batch.size(); b++) {
+            g.job[b] = {o, batch[b]->p.n_inputs, static_cast<float2*>(batch[b]->vis),
+                        batch[b]->p.vis_order == CELLSPE_VIS_BASELINE_MAJOR ? 1 : 0};
+            o += batch[b]->p.n_inputs;
+        }
+        rc = map_rc(cs_vis_gather(g, ws.stream), "batch gather");
+        if (!rc) {
+            e = cudaStreamSynchronize(ws.stream);
+            if (e != cudaSuccess) rc = cuda_fail(e, "batch gather");
+        }
+    }
+    if (d_raw) cudaFreeAsync(d_raw, ws.stream);
+    if (d_vis) cudaFreeAsync(d_vis, ws.stream);
+    return rc;
+}
 
 void service_worker(cellspe_service* sv)
 {
@@ -1354,39 +1424,67 @@ void service_worker(cellspe_service* sv)
         if (sv->stop) break;
         std::shared_ptr<SvcJob> j = *at;
         sv->queue.erase(at);
+        // batching: queued jobs of the same shape join a small job (one F-stage
+        // and one X-stage launch for all of them)
+        std::vector<std::shared_ptr<SvcJob>> batch{j};
+        if (sv->batch_inputs > 0 && batchable(*j)) {
+            int total = j->p.n_inputs;
+            for (auto it = sv->queue.begin(); it != sv->queue.end() && (int)batch.size() < CS_GATHER_MAX;) {
+                const SvcJob& q = **it;
+                if (batchable(q) && same_shape(q, *j) && total + q.p.n_inputs <= sv->batch_inputs) {
+                    total += q.p.n_inputs;
+                    batch.push_back(*it);
+                    it = sv->queue.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+        }
+        long long footprint = 0;
+        for (auto& m : batch) footprint += m->footprint;
         if (j->large) sv->large_running++;
-        sv->in_flight += j->footprint;
+        sv->in_flight += footprint;
         sv->running++;
         sv->max_running = std::max(sv->max_running, sv->running);
+        if (batch.size() > 1) {
+            sv->batched_jobs += (long long)batch.size();
+            sv->batched_launches++;
+        }
         lk.unlock();
         sv->cv_work.notify_all();
-        j->t_start = std::chrono::steady_clock::now();
+        const auto t_start = std::chrono::steady_clock::now();
+        for (auto& m : batch) m->t_start = t_start;
         int rc = init;
         const long long samples = (long long)j->p.n_inputs * j->p.fft_points * j->p.n_segments;
         ws.stream = (hi && samples < sv->priority_samples) ? hi : lo;
-        if (!rc && j->ready) {
-            cudaError_t e = cudaStreamWaitEvent(ws.stream, j->ready, 0);
-            if (e != cudaSuccess) rc = cuda_fail(e, "service job ordering");
-        }
-        if (!rc) rc = op_fx(ws, &j->p, j->raw, j->poly, j->vis, true);
+        for (auto& m : batch)
+            if (!rc && m->ready) {
+                cudaError_t e = cudaStreamWaitEvent(ws.stream, m->ready, 0);
+                if (e != cudaSuccess) rc = cuda_fail(e, "service job ordering");
+            }
+        if (!rc) rc = batch.size() > 1 ? run_batch(ws, batch) : op_fx(ws, &j->p, j->raw, j->poly, j->vis, true);
         ws.stream = lo;
-        if (j->ready) {
-            cudaEventDestroy(j->ready);
-            j->ready = nullptr;
-        }
-        j->t_done = std::chrono::steady_clock::now();
+        const auto t_done = std::chrono::steady_clock::now();
+        const std::string err = rc ? t_err : std::string();
         lk.lock();
         if (j->large) sv->large_running--;
-        sv->in_flight -= j->footprint;
+        sv->in_flight -= footprint;
         sv->running--;
-        j->status = rc;
-        if (rc) j->error = t_err;
-        j->done = true;
-        if (rc) sv->failed++;
-        else {
-            sv->completed++;
-            sv->latency_ms.push_back(std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count());
-            sv->queue_ms.push_back(std::chrono::duration<double, std::milli>(j->t_start - j->t_submit).count());
+        for (auto& m : batch) {
+            if (m->ready) {
+                cudaEventDestroy(m->ready);
+                m->ready = nullptr;
+            }
+            m->t_done = t_done;
+            m->status = rc;
+            if (rc) m->error = err;
+            m->done = true;
+            if (rc) sv->failed++;
+            else {
+                sv->completed++;
+                sv->latency_ms.push_back(std::chrono::duration<double, std::milli>(m->t_done - m->t_submit).count());
+                sv->queue_ms.push_back(std::chrono::duration<double, std::milli>(m->t_start - m->t_submit).count());
+            }
         }
         sv->cv_done.notify_all();
         sv->cv_work.notify_all();
@@ -2264,6 +2362,8 @@ cellspe_service* cellspe_service_create(const cellspe_service_config* cfg)
     int n = (cfg && cfg->max_streams > 0) ? cfg->max_streams : 2;
     sv->priority_samples = !cfg || cfg->priority_samples == 0 ? (1LL << 24) : cfg->priority_samples;
     sv->large_samples = cfg ? cfg->large_samples : 0;
+    // batching is on by default (64 inputs); a negative batch_inputs turns it off
+    sv->batch_inputs = !cfg || cfg->batch_inputs == 0 ? 64 : std::max(0, std::min(cfg->batch_inputs, 128));
     for (int i = 0; i < n; i++) sv->workers.emplace_back(service_worker, sv);
     return sv;
 }
@@ -2330,6 +2430,8 @@ int cellspe_service_get_stats(cellspe_service* sv, cellspe_service_stats* out)
     out->p99_ms = percentile(sv->latency_ms, 0.99);
     out->p99_queue_ms = percentile(sv->queue_ms, 0.99);
     out->budget_bytes = sv->budget;
+    out->batched_jobs = sv->batched_jobs;
+    out->batched_launches = sv->batched_launches;
     return 0;
 }
 

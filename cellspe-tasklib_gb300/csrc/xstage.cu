@@ -177,3 +177,37 @@ int cs_vis_to_baseline_major(const float2* vis_cp, float2* vis_pc, int C, int64_
     k_vis_transpose<<<grid, dim3(32, 8), 0, st>>>(vis_cp, vis_pc, C, P), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Batched service jobs: several small jobs' inputs run as one stacked job;
+// each job's products are gathered from the stacked channel-major triangle.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void k_vis_gather(const __grid_constant__ CsGatherArgs a)
+{
+    const CsGatherJob& J = a.job[blockIdx.y];
+    const int64_t P = (int64_t)J.S * (J.S + 1) / 2, total = (int64_t)a.C * P;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c, p;
+        if (J.baseline_major) p = t / a.C, c = t - p * a.C;
+        else c = t / P, p = t - c * P;
+        // p = i (i + 1) / 2 + j, j <= i: i from the root, corrected by one step either way
+        int i = (int)((sqrtf(8.f * (float)p + 1.f) - 1.f) * 0.5f);
+        while ((int64_t)i * (i + 1) / 2 > p) i--;
+        while ((int64_t)(i + 1) * (i + 2) / 2 <= p) i++;
+        const int j = (int)(p - (int64_t)i * (i + 1) / 2);
+        const int64_t gi = J.off + i, gj = J.off + j;
+        const float2 v = a.src[c * a.P_stacked + gi * (gi + 1) / 2 + gj];
+        J.dst[J.baseline_major ? p * a.C + c : c * P + p] = v;
+    }
+}
+
+}  // namespace
+
+int cs_vis_gather(const CsGatherArgs& a, cudaStream_t st)
+{
+    if (!a.src || a.n <= 0 || a.n > CS_GATHER_MAX || a.C <= 0) return CS_ERR_ARG;
+    k_vis_gather<<<dim3(152, a.n), 256, 0, st>>>(a), cs_count_launches(1);
+    return (int)cudaGetLastError();
+}

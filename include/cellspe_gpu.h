@@ -177,13 +177,19 @@ int cellspe_release_workspace(void);
  * p99 latency).  Each large kernel fills the GPU on its own, so jobs that run
  * side by side all finish late: two streams keep the p99 latency near the
  * largest job's own run time while small jobs pass large ones.  Workers use the F-stage schedule that a direct call has timed (they
- * time none themselves).
+ * time none themselves).  Unless batch_inputs < 0, a worker that takes a small
+ * job (device buffers, at most 16 inputs, tensor-core X stage, no delay
+ * model, scale, custom levels or accumulation) also takes the queued jobs of
+ * the same shape (FFT size, segments, input length, start sample, levels)
+ * up to batch_inputs inputs in all, and runs them as one stacked job: one
+ * F-stage and one X-stage launch, each job's triangle then gathered into its
+ * own visibility buffer (the values equal each job's solo run).
  * Buffers must stay valid until cellspe_service_wait returns for the job. */
 typedef struct cellspe_service cellspe_service;
 typedef struct {
     long long hbm_budget_bytes;   /* 0: 80% of free device memory            */
     int       max_streams;        /* concurrent jobs (0: 2)                    */
-    int       reserved;
+    int       batch_inputs;       /* small jobs batched up to this many inputs (<= 128); 0: 64; < 0: off */
     long long priority_samples;   /* 0: 2^24; < 0: one priority for all jobs */
     long long large_samples;      /* <= 0: no limit (large jobs may overlap)  */
 } cellspe_service_config;
@@ -193,6 +199,8 @@ typedef struct {
     double    p50_ms, p99_ms;     /* submit -> done latency of completed jobs */
     double    p99_queue_ms;       /* submit -> start                          */
     long long budget_bytes;
+    long long batched_jobs;       /* jobs that ran in a shared launch          */
+    long long batched_launches;   /* stacked jobs those formed                 */
 } cellspe_service_stats;
 cellspe_service* cellspe_service_create(const cellspe_service_config* cfg);
 int  cellspe_service_submit(cellspe_service* s, const cellspe_fx_params* p, const void* raw,

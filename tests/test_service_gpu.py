@@ -135,3 +135,50 @@ def test_service_failed_job_reports_worker_error(cg):
     ref = np.zeros_like(out)
     cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1]), raw, ref)
     assert np.array_equal(out, ref) and st["failed"] == 1 and st["completed"] == 1
+
+
+@pytest.mark.parametrize("N,K", [(2048, 64), (1024, 32), (8192, 8)])
+def test_service_batches_small_jobs_bit_identical(cg, N, K):
+    """batch_inputs > 0: queued small device-buffer jobs of one shape run as one
+    stacked job (one F-stage and one X-stage launch) and each job's triangle is
+    gathered into its own buffer, channel- or baseline-major.  One worker and a
+    large job submitted first let the small ones queue up; every small job's
+    visibilities must equal its solo run bit for bit, and the service must have
+    formed at least one batch."""
+    import torch
+
+    import synth
+
+    sizes = [4, 8, 2, 16, 5, 12, 3, 8, 7]
+    small = []
+    for n, S in enumerate(sizes):
+        raw = synth.device_stations(S, N * K, 0.1, seed=300 + n)
+        order = cg.VIS_BASELINE_MAJOR if n % 3 == 2 else cg.VIS_CHANNEL_MAJOR
+        small.append((S, raw, order))
+    big_raw = synth.device_stations(200, 2048 * 1024, 0.02, seed=299)
+    solo = []
+    for S, raw, order in small:
+        C, P = N // 2, S * (S + 1) // 2
+        v = torch.empty((P, C) if order == cg.VIS_BASELINE_MAJOR else (C, P), dtype=torch.complex64, device="cuda")
+        cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=order), raw, v)
+        solo.append(v)
+    torch.cuda.synchronize()
+    svc = cg.Service(max_streams=1, batch_inputs=64)
+    try:
+        big = torch.empty((1024, 200 * 201 // 2), dtype=torch.complex64, device="cuda")
+        ids = [svc.submit(cg.fx_params(200, 2048, 1024, big_raw.shape[1], x_mode=cg.X_TC_FP16), big_raw, big)]
+        outs = []
+        for S, raw, order in small:
+            v = torch.full_like(solo[len(outs)], float("nan"))
+            outs.append(v)
+            ids.append(svc.submit(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, vis_order=order), raw, v))
+        for i in ids:
+            svc.wait(i)
+        st = svc.stats()
+    finally:
+        svc.close()
+    torch.cuda.synchronize()
+    for a, b in zip(outs, solo):
+        assert torch.equal(a.view(torch.float32), b.view(torch.float32))
+    assert st["failed"] == 0 and st["completed"] == len(ids)
+    assert st["batched_jobs"] >= 2 and st["batched_launches"] >= 1
