@@ -25,6 +25,24 @@ std::map<std::pair<int, int>, float2*> g_tw;   // (device, n) -> table
 long long cs_launch_count() { return g_launches.load(); }
 void cs_count_launches(int n) { g_launches += n; }
 
+// The attribute is per function and shared by every thread: two host threads
+// launching one kernel with different shared-memory sizes could lower it
+// under each other's launch.  It only ever grows here (per device), under a lock.
+cudaError_t cs_smem_at_least(const void* fn, int bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, int> cur;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    int& v = cur[{dev, fn}];
+    if (bytes <= v) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) v = bytes;
+    return e;
+}
+
 const float2* cs_twiddles(int n)
 {
     if (n <= 0 || (n & (n - 1))) return nullptr;
@@ -156,7 +174,7 @@ int launch_batch(const void* in, float2* out, int64_t batch, float scale, cudaSt
     if (!tw) return CS_ERR_ARG;
     size_t smem = (size_t)C::GROUPS * fpad_size(M) * sizeof(float2);
     auto kern = k_fft_batch<M, REAL, INV>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     int64_t blocks = (batch + C::GROUPS - 1) / C::GROUPS;
     kern<<<(unsigned)blocks, C::NT, smem, st>>>(in, out, batch, tw, scale), cs_count_launches(1);
     return (int)cudaGetLastError();

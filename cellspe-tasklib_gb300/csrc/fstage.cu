@@ -248,7 +248,7 @@ int launch_fstage(const CsFStageArgs& a, cudaStream_t st)
     if (!tw) return CS_ERR_ARG;
     size_t smem = fstage_smem<M, FMT, SEGMAJ>();
     auto kern = k_fx_fstage<M, FMT, PHASE, SEGMAJ>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     dim3 grid((a.K + G - 1) / G, a.S);
     kern<<<grid, Cfg::NT, smem, st>>>(a, tw), cs_count_launches(1);
     return (int)cudaGetLastError();
@@ -534,7 +534,7 @@ int launch_w2048_variant(const CsFStageArgs& a, const float2* tw, cudaStream_t s
 {
     size_t smem = w2048_smem<FMT, WARPS, G>();
     auto kern = k_fx_fstage_w2048<FMT, PHASE, WARPS, ROUNDS, G>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     dim3 grid((a.K + G * ROUNDS - 1) / (G * ROUNDS), a.S);
     kern<<<grid, 32 * WARPS, smem, st>>>(a, tw), cs_count_launches(1);
     return (int)cudaGetLastError();
@@ -892,7 +892,7 @@ int launch_wbig(const CsFStageArgs& a, cudaStream_t st)
     constexpr int SEGS = wbig_segs<M1, PHASE>();
     const size_t smem = wbig_smem<M1, PHASE>();
     auto kern = k_fx_fstage_wbig<M1, FMT, PHASE>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     kern<<<dim3((a.K + SEGS - 1) / SEGS, a.S), 32 * M1, smem, st>>>(a, tw), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
@@ -1118,7 +1118,7 @@ int launch_w512(const CsFStageArgs& a, cudaStream_t st)
 {
     const size_t smem = w512_smem<FMT>();
     auto kern = k_fx_fstage_w512<FMT, PHASE>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     kern<<<dim3((a.K + H_G - 1) / H_G, a.S), 256, smem, st>>>(a, nullptr), cs_count_launches(1);
     return (int)cudaGetLastError();
 }
@@ -1326,7 +1326,7 @@ int launch_w1024(const CsFStageArgs& a, cudaStream_t st)
 {
     const size_t smem = w1024_smem<FMT>();
     auto kern = k_fx_fstage_w1024<FMT, PHASE>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     constexpr int G = w1024_g<FMT>();
     kern<<<dim3((a.K + G - 1) / G, a.S), 256, smem, st>>>(a, nullptr), cs_count_launches(1);
     return (int)cudaGetLastError();

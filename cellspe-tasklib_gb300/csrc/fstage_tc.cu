@@ -564,10 +564,10 @@ int cs_fx_fstage_tc(const CsFStageArgs& a, cudaStream_t st)
     t.units = (int64_t)a.S * t.units_k;
     const int grid = (int)std::min<int64_t>(t.units, g_sms);
     if (a.phase0) {
-        CS_CUDA_TRY(cudaFuncSetAttribute(k_fx_fstage_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(k_fx_fstage_tc<true>), (int)(SMEM_BYTES)));
         k_fx_fstage_tc<true><<<grid, THREADS, SMEM_BYTES, st>>>(t, tm), cs_count_launches(1);
     } else {
-        CS_CUDA_TRY(cudaFuncSetAttribute(k_fx_fstage_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(k_fx_fstage_tc<false>), (int)(SMEM_BYTES)));
         k_fx_fstage_tc<false><<<grid, THREADS, SMEM_BYTES, st>>>(t, tm), cs_count_launches(1);
     }
     return (int)cudaGetLastError();

@@ -659,7 +659,7 @@ int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st)
     // the delay phasor and the channel scale are compiled in only where used
     auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32<true, true> : k_fx_fstage_tc32<true, false>)
                          : (a.scale ? k_fx_fstage_tc32<false, true> : k_fx_fstage_tc32<false, false>);
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)(SMEM_BYTES)));
     kern<<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
     return (int)cudaGetLastError();
 }

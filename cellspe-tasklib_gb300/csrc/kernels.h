@@ -26,6 +26,8 @@ int cs_cornerturn2bit(const void* raw, int64_t nsamp, int nchan, void* planes, c
 // Twiddle table exp(-2 pi i m / n), m in [0, n), FP64-computed, device copy.
 // Cached per (device, n); valid until cs_free_twiddles().
 const float2* cs_twiddles(int n);
+// Raise (never lower) a kernel's dynamic shared-memory limit to `bytes`.
+cudaError_t cs_smem_at_least(const void* fn, int bytes);
 void cs_free_twiddles();
 // Batched forward C2C FFT, n points (32..16384), interleaved complex.
 int cs_cfft_batch(const float2* in, float2* out, int n, int64_t batch, cudaStream_t st);

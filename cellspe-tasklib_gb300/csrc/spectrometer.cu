@@ -599,7 +599,7 @@ int launch_power(const CsSpecArgs& a, int nchunk, cudaStream_t st)
     if (!tw || !win) return CS_ERR_ARG;
     size_t smem = (size_t)C::GROUPS * fpad_size(MC) * sizeof(float2) + (size_t)C::GROUPS * (M / P + 1) * sizeof(float);
     auto kern = k_spec_power<MC, P>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     dim3 grid(nchunk, a.nsub * a.nspec, P);
     kern<<<grid, C::NT, smem, st>>>(a, tw, win, nchunk, spec_chunk(a)), cs_count_launches(1);
     return (int)cudaGetLastError();
@@ -615,7 +615,7 @@ int launch_power_w(const CsSpecArgs& a, int nchunk, cudaStream_t st)
     if ((N / a.overlap) % 64) return launch_power<SW_MC, P>(a, nchunk, st);   // FFT starts not 16-byte aligned
     const size_t smem = (size_t)16 * SW_ROWP * sizeof(float2) + (size_t)SW_SLOTS * SW_NT * sizeof(float) + N / 16 * 4;
     auto kern = a.valid_mask ? k_spec_power_w<P, true> : k_spec_power_w<P, false>;
-    CS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)smem));
     dim3 grid(nchunk, a.nsub * a.nspec, P);
     kern<<<grid, SW_NT, smem, st>>>(a, tw, win, nchunk, spec_chunk(a)), cs_count_launches(1);
     return (int)cudaGetLastError();
@@ -738,7 +738,7 @@ int cs_spectrometer(const CsSpecArgs& a, cudaStream_t st)
         int64_t samp_per_spec = (int64_t)a.ffts_per_spectrum * a.N;
         int nt = PCAL_THREADS;
         size_t smem = (size_t)T * nt * sizeof(float2);
-        CS_CUDA_TRY(cudaFuncSetAttribute(k_pcal_fold, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(k_pcal_fold), (int)smem));
         const int ns = a.pcal_sources > 0 ? a.pcal_sources : 1;
         k_pcal_fold<<<dim3(PCAL_BLOCKS, rows), nt, smem, st>>>(a.planes, a.bytes_per_sub, a.nspec, samp_per_spec, a.N,
                                                                a.overlap, novl, ns, a.pcal_source, T, L, rot, a.lut[0],

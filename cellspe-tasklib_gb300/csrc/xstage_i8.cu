@@ -240,7 +240,7 @@ int cs_xmac_i8(const int8_t* planes, int S, int C, int K, int kp, float2* vis, c
     if (!tiles) return CS_ERR_ARG;
     I8Args a{planes, S, C, K, kp, (int64_t)S * (S + 1) / 2, tiles, vis, scale, scale_stride > 0 ? scale_stride : C,
              accumulate};
-    CS_CUDA_TRY(cudaFuncSetAttribute(k_xmac_i8, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(k_xmac_i8), (int)(SMEM)));
     k_xmac_i8<<<dim3(ntiles, C), THREADS, SMEM, st>>>(a), cs_count_launches(1);
     return (int)cudaGetLastError();
 }

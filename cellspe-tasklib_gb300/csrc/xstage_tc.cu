@@ -343,7 +343,7 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
     TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, scale_stride > 0 ? scale_stride : C,
              accumulate, box_rows, small, cols, kblock ? 1 : 0};
     const size_t smem = (size_t)STAGES * (small ? 2 * A_BYTES : STAGE_BYTES) + 1024 + 256;
-    CS_CUDA_TRY(cudaFuncSetAttribute(k_xmac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(k_xmac_tc), (int)smem));
     dim3 grid(ntiles, C);
     k_xmac_tc<<<grid, TC_THREADS, smem, st>>>(tm, a), cs_count_launches(1);
     return (int)cudaGetLastError();

@@ -182,3 +182,33 @@ def test_service_batches_small_jobs_bit_identical(cg, N, K):
         assert torch.equal(a.view(torch.float32), b.view(torch.float32))
     assert st["failed"] == 0 and st["completed"] == len(ids)
     assert st["batched_jobs"] >= 2 and st["batched_launches"] >= 1
+
+
+def test_service_concurrent_small_and_large_x_tiles(cg):
+    """Two workers launch the tensor-core X stage with its single-tile form
+    (S <= 128, smaller shared memory) and its tiled form (S > 128) at the same
+    time: the kernel's shared-memory limit is only ever raised, so neither
+    launch can find it lowered by the other (which failed with 'too many
+    resources requested for launch' before)."""
+    import torch
+
+    import synth
+
+    N, K = 512, 64
+    raws = {S: synth.device_stations(S, N * K, 0.05, seed=S) for S in (24, 200)}
+    svc = cg.Service(max_streams=2, batch_inputs=-1)
+    try:
+        ids, outs = [], []
+        for n in range(24):
+            S = 24 if n % 2 else 200
+            v = torch.empty((N // 2, S * (S + 1) // 2), dtype=torch.complex64, device="cuda")
+            outs.append(v)
+            ids.append(svc.submit(cg.fx_params(S, N, K, raws[S].shape[1], x_mode=cg.X_TC_FP16), raws[S], v))
+        for i in ids:
+            svc.wait(i)
+        st = svc.stats()
+    finally:
+        svc.close()
+    assert st["failed"] == 0 and st["completed"] == 24
+    for a, b in zip(outs[2:], outs):
+        assert torch.equal(a, b)
