@@ -143,3 +143,19 @@ def test_cell_spectrometer_task_argument_checks(cg):
     assert "samples_per_rawbyte" in str(e.value)
     task.close()
     assert task.state.value is None
+
+
+def test_cell_spectrometer_task_short_and_empty_buffers(cg, orc):
+    """Buffers shorter than two hops give no FFT (the SPE's loop bound), an
+    empty buffer none either; the partial spectrum of earlier tasks carries over
+    untouched, and the spectrum destination is not written."""
+    N, K, overlap = 1024, 3, 2
+    rng = np.random.default_rng(21)
+    bufs = [rng.integers(0, 256, n, dtype=np.uint8) for n in (5000, 1023, 0, 600, 9000)]
+    outs, stats = _cell_tasks(cg, bufs, N, K, overlap, 1)
+    ref = orc.cell_spectrometer_f64(bufs, N, K, overlap, 1)
+    for t, (got, want, st) in enumerate(zip(outs, ref, stats)):
+        assert st[1] == len(want), (t, st)
+        if want:
+            assert _rel(got, np.stack(want)) < TOL
+    assert [s[2] for s in stats] == [8, 0, 0, 0, 16]      # floor(B / 512) - 1, none below two hops
