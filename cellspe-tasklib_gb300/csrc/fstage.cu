@@ -1401,7 +1401,7 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
     }
     if (a.kblock && cs_fstage_tc32_supported(a)) {
         const char* e = getenv("CELLSPE_FSTAGE_TC32");
-        if (e && e[0] == '1') return cs_fx_fstage_tc32(a, st);
+        if (e && (e[0] == '1' || e[0] == '2')) return cs_fx_fstage_tc32(a, st, e[0] == '2');
     }
     if (a.N == 2048 && !a.msb_first) {
         const bool ph = a.phase0 != nullptr;

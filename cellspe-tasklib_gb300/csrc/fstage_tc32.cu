@@ -81,14 +81,16 @@ constexpr int A2P_REGION = 32 * 128;
 constexpr int STG_PITCH = FC + 1;                     // words per staging row (one row per segment)
 constexpr int OFF_STG = OFF_A2P + 2 * A2P_REGION;     // staging: [US][STG_PITCH] half2 (Re, Im)
 constexpr int STG_BYTES = US * STG_PITCH * 4;
-constexpr int OFF_RAW = OFF_STG + STG_BYTES;          // 2 x QS x RAWC x 16
+constexpr int NRAW = 4;                               // raw buffers (the lockstep form uses two)
+constexpr int OFF_RAW = OFF_STG + STG_BYTES;          // NRAW x QS x RAWC x 16
 constexpr int RAW_BYTES = QS * RAWC * 16;
-constexpr int OFF_OFFS = OFF_RAW + 2 * RAW_BYTES;     // sample offsets: 2 x QS ints
-constexpr int OFF_LUT = OFF_OFFS + 32;                // 16 half2 pair levels
+constexpr int OFF_OFFS = OFF_RAW + NRAW * RAW_BYTES;  // sample offsets: NRAW x QS ints
+constexpr int OFF_LUT = OFF_OFFS + NRAW * QS * 4;     // 16 half2 pair levels
 constexpr int OFF_BAR = OFF_LUT + 64;                 // mbarriers
-constexpr int NBAR = 12;
+constexpr int NBAR = 16;
 constexpr int OFF_SLOT = OFF_BAR + 8 * NBAR;
-constexpr int SMEM_USED = OFF_SLOT + 16;
+constexpr int OFF_LUT4 = OFF_SLOT + 16;               // byte -> 4 FP16 levels (warp-specialised form)
+constexpr int SMEM_USED = OFF_LUT4 + 256 * 8;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;          // + alignment of the base to 1024 B
 constexpr uint32_t TMEM_COLS = 512;                   // D1: 0, 128; D2: 256, 320; D2': 384
 constexpr uint32_t COL_D1 = 0, COL_D2 = 256, COL_D2P = 384;
@@ -566,6 +568,429 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
     }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-specialised form (CELLSPE_FSTAGE_TC32=2): the same transform, buffers
+// and TMEM columns, but each phase has warps of its own and the phases hand
+// buffers to each other through mbarriers, so they run concurrently instead
+// of in step between CTA-wide barriers:
+//   warps 0-3   epilogue 1 (TMEM lane quarter = warp), all 4 segments of a quad
+//   warps 4-7   epilogue 2 (lane quarter = segment of the quad), the k1 = 32
+//               channels at a unit's end
+//   warps 8-11  raw fetch (cp.async, two quads ahead) and decode into B1
+//               (a byte of four 2-bit codes -> four FP16 levels per table read)
+//   warps 12-15 write-out of a unit's staging
+//   warp 16     TMEM owner and MMA issuer
+// A group's first thread polls each barrier (bounded wait) and a named-barrier
+// vote of the group releases the others; a failed wait ends that group's loop,
+// and every group's waits are bounded, so all reach the final barrier.
+// ---------------------------------------------------------------------------
+constexpr int WS_E1 = 0, WS_E2 = 4, WS_DEC = 8, WS_WO = 12, WS_MMA = 16;
+constexpr int WS_THREADS = 17 * 32;
+constexpr int WB_B1FULL = 0, WB_D1FULL = 1, WB_E1DONE = 3, WB_D2FULL = 5, WB_E2DONE = 7, WB_D2PFULL = 9,
+              WB_E2PDONE = 11, WB_STGFULL = 12, WB_STGFREE = 13, WB_DRAIN = 14;   // [2] where two follow
+static_assert(WB_DRAIN < NBAR, "barriers");
+static_assert(NRAW == 4, "the decode group's cp.async waits assume four raw buffers");
+static_assert(WS_E1 == 0 && WS_E2 == WS_E1 + 4, "epilogue-1 warps are 0..3 (TMEM lane quarter = warp)");
+// named barriers (id, threads) of the groups
+constexpr int NB_DEC = 1, NB_E1 = 2, NB_E2 = 3, NB_WO = 4;
+
+CS_DEV bool grp_vote(int id, int n, bool ok)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(ok ? 1u : 0u), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
+CS_DEV void grp_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+template <bool PHASE, bool SCALE>
+__global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid_constant__ Tc32Args args)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+    const uint32_t sbase = tc::smem_u32(sm);
+    const CsFStageArgs& a = args.f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x;
+    const uint32_t bar0 = sbase + OFF_BAR;
+    auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
+    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + OFF_SLOT);
+    int* offs = reinterpret_cast<int*>(sm + OFF_OFFS);
+    __half2* lut2 = reinterpret_cast<__half2*>(sm + OFF_LUT);
+    uint32_t* stg = reinterpret_cast<uint32_t*>(sm + OFF_STG);
+
+    for (int i = tid; i < CONST_BYTES / 16; i += WS_THREADS)
+        reinterpret_cast<uint4*>(sm)[i] = __ldg(args.consts + i);
+    for (int i = tid; i < 2 * A2P_REGION / 16; i += WS_THREADS)
+        reinterpret_cast<uint4*>(sm + OFF_A2P)[i] = make_uint4(0, 0, 0, 0);
+    uint2* lut4 = reinterpret_cast<uint2*>(sm + OFF_LUT4);
+    if (tid < 256) {
+        const float l0 = a.lut[0], l1 = a.lut[1], l2 = a.lut[2], l3 = a.lut[3];
+        auto lv = [&](int c) { return c == 0 ? l0 : c == 1 ? l1 : c == 2 ? l2 : l3; };
+        if (tid < 16) lut2[tid] = __floats2half2_rn(lv(tid & 3), lv(tid >> 2));
+        lut4[tid] = make_uint2(h2u(__floats2half2_rn(lv(tid & 3), lv((tid >> 2) & 3))),
+                               h2u(__floats2half2_rn(lv((tid >> 4) & 3), lv(tid >> 6))));
+    }
+    if (tid == 0) {
+        tc::mbar_init(bar(WB_B1FULL), 4);
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(bar(WB_D1FULL + b), 1);
+            tc::mbar_init(bar(WB_E1DONE + b), 4);
+            tc::mbar_init(bar(WB_D2FULL + b), 1);
+            tc::mbar_init(bar(WB_E2DONE + b), 4);
+            tc::mbar_init(bar(WB_D2PFULL + b), 1);
+        }
+        tc::mbar_init(bar(WB_E2PDONE), 4);
+        tc::mbar_init(bar(WB_STGFULL), 4);
+        tc::mbar_init(bar(WB_STGFREE), 4);
+        tc::mbar_init(bar(WB_DRAIN), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == WS_MMA) tc::tmem_alloc(tc::smem_u32(slot), TMEM_COLS);
+    tc::fence_proxy_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *slot;
+
+    const int64_t units = args.units;
+    const int nunits = (blockIdx.x < units) ? (int)((units - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    const int nquads = nunits * QUADS;
+    const int K = a.K;
+    auto unit_of = [&](int u, int& s, int& kb) {
+        const uint32_t uu = blockIdx.x + (uint32_t)u * gridDim.x;
+        const uint32_t si = uu / (uint32_t)args.units_k;
+        s = (int)si;
+        kb = (int)(uu - si * (uint32_t)args.units_k);
+    };
+    // group wait: the leader polls, the group's vote releases everyone
+    auto gwait = [&](int id, int n, bool leader, uint32_t b, uint32_t parity) -> bool {
+        bool ok = true;
+        if (leader) ok = tc::mbar_wait(b, parity, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
+        return grp_vote(id, n, ok);
+    };
+
+    if (warp == WS_MMA) {
+        // ------------------------------ MMA issuer ------------------------------
+        if (lane == 0) {
+            const uint32_t id1 = tc::idesc_f16(128, 128, false, false, true);
+            const uint32_t id2 = tc::idesc_f16(128, 64, false, false, false);
+            auto w = [&](int i, uint32_t ph) {
+                return tc::mbar_wait(bar(i), ph, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
+            };
+            for (int j = 0; j < nquads; j++) {
+                const int b = j & 1, u = j / QUADS;
+                if (!w(WB_B1FULL, (uint32_t)j & 1)) break;
+                tc::fence_after();
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t da = tc::smem_desc(sbase + OFF_A1 + 32u * kk, 16, 1024, tc::SW128);
+                    const uint64_t db = tc::smem_desc(sbase + OFF_B1 + 2048u * kk, 8192, 1024, tc::SW128);
+                    tc::mma_f16(tmem + COL_D1 + 128u * b, da, db, id1, kk ? 1u : 0u);
+                }
+                tc::commit(bar(WB_D1FULL + b));
+                if (j >= 2 && !w(WB_E2DONE + b, (uint32_t)((j - 2) >> 1) & 1)) break;   // D2[b] read
+                if (!w(WB_E1DONE + b, (uint32_t)(j >> 1) & 1)) break;                  // A2[b] written, D1[b] read
+                tc::fence_after();
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t da = tc::smem_desc(sbase + OFF_A2 + (uint32_t)b * A2_BYTES + 32u * kk, 16, 1024, tc::SW128);
+                    const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
+                    tc::mma_f16(tmem + COL_D2 + 64u * b, da, db, id2, kk ? 1u : 0u);
+                }
+                tc::commit(bar(WB_D2FULL + b));
+                if (j % QUADS == QUADS - 1) {
+                    if (u >= 1 && !w(WB_E2PDONE, (uint32_t)(u - 1) & 1)) break;       // D2' read
+                    tc::fence_after();
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint64_t da = tc::smem_desc(sbase + OFF_A2P + (uint32_t)(u & 1) * A2P_REGION + 32u * kk,
+                                                          16, 1024, tc::SW128);
+                        const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
+                        tc::mma_f16(tmem + COL_D2P, da, db, id2, kk ? 1u : 0u);
+                    }
+                    tc::commit(bar(WB_D2PFULL + (u & 1)));
+                }
+            }
+            tc::commit(bar(WB_DRAIN));
+            tc::mbar_wait(bar(WB_DRAIN), 0, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
+        }
+        __syncwarp();
+    } else if (warp < WS_E2) {
+        // ------------------------------ epilogue 1 ------------------------------
+        const int q = warp, gt = tid;                       // group thread 0..127
+        const bool leader = gt == 0;
+        const int k1 = 8 * q + (lane >> 2);
+        float2 tw[4][2];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int n2 = 8 * m + 2 * (lane & 3) + e;
+                float sn, cs;
+                sincospif(-(float)((n2 * k1) & 2047) / 1024.0f, &sn, &cs);
+                tw[m][e] = make_float2(cs, sn);
+            }
+        const uint32_t e1base = sw128(k1, 2 * (lane & 3));   // row 32 h + k1: + 4096 h
+        const int m32 = (lane >> 2) & 3, e32 = lane >> 4;
+        const int n2_32 = 8 * m32 + 2 * (lane & 3) + e32;
+        float2 tw32;
+        {
+            float sn, cs;
+            sincospif(-(float)n2_32 / 32.0f, &sn, &cs);
+            tw32 = make_float2(cs, sn);
+        }
+        for (int j = 0; j < nquads; j++) {
+            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
+            if (qd == 0 && u >= 2 && !gwait(NB_E1, 128, leader, bar(WB_D2PFULL + (u & 1)), (uint32_t)((u - 2) >> 1) & 1))
+                break;                                      // A2' region u & 1 read by pass 2' of unit u - 2
+            if (j >= 2 && !gwait(NB_E1, 128, leader, bar(WB_D2FULL + b), (uint32_t)((j - 2) >> 1) & 1)) break;
+            if (!gwait(NB_E1, 128, leader, bar(WB_D1FULL + b), (uint32_t)(j >> 1) & 1)) break;
+            tc::fence_after();
+            unsigned char* a2 = sm + OFF_A2 + b * A2_BYTES;
+            // two segments per TMEM wait
+            auto e1seg = [&](int h, uint32_t (&r)[16]) {
+                const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * h;
+                unsigned char* a2h = a2 + 4096 * h;
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    const float2 y0 = make_float2(__uint_as_float(r[4 * m]), __uint_as_float(r[4 * m + 2]));
+                    const float2 y1 = make_float2(__uint_as_float(r[4 * m + 1]), __uint_as_float(r[4 * m + 3]));
+                    const float2 z0 = cmul(y0, tw[m][0]), z1 = cmul(y1, tw[m][1]);
+                    *reinterpret_cast<uint32_t*>(a2h + (e1base ^ (m << 4))) = h2u(__floats2half2_rn(z0.x, z1.x));
+                    *reinterpret_cast<uint32_t*>(a2h + (e1base ^ (m << 4) ^ 64u)) = h2u(__floats2half2_rn(z0.y, z1.y));
+                }
+                if (q == 0) {
+                    uint32_t r32[16];
+                    tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
+                    tc::tmem_ld_wait();
+                    pin16(r32);
+                    const bool mb1 = m32 & 1, mb2 = m32 & 2;
+                    const uint32_t ya = mb2 ? (mb1 ? r32[12] : r32[8]) : (mb1 ? r32[4] : r32[0]);
+                    const uint32_t yb = mb2 ? (mb1 ? r32[13] : r32[9]) : (mb1 ? r32[5] : r32[1]);
+                    const float y = __uint_as_float(e32 ? yb : ya);
+                    unsigned char* a2p = sm + OFF_A2P + (u & 1) * A2P_REGION;
+                    const uint32_t prow = QS * qd + h;
+                    *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = __float2half_rn(y * tw32.x);
+                    *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = __float2half_rn(y * tw32.y);
+                }
+            };
+#pragma unroll 1
+            for (int h = 0; h < QS; h += 2) {
+                const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * h + ((uint32_t)(32 * q) << 16);
+                uint32_t r0[16], r1[16];
+                tc::tmem_ld_16x256b_x4(d1, r0);
+                tc::tmem_ld_16x256b_x4(d1 + 32u, r1);
+                tc::tmem_ld_wait();
+                pin16(r0);
+                pin16(r1);
+                e1seg(h, r0);
+                e1seg(h + 1, r1);
+            }
+            tc::fence_before();
+            tc::fence_proxy_async();
+            warp_arrive(bar(WB_E1DONE + b));
+        }
+    } else if (warp < WS_DEC) {
+        // ------------------------------ epilogue 2 ------------------------------
+        const int q = warp & 3, gt = tid - 32 * WS_E2;
+        const bool leader = gt == 0;
+        const int kk1 = lane;
+#define TC32_PHASOR(s_, k_, cstart, cstep)                                              \
+        float2 B = make_float2(1.f, 0.f), D = B;                                        \
+        if (PHASE) {                                                                    \
+            const int64_t sk = (int64_t)(s_) * K + (k_);                                \
+            const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);         \
+            float sn, cs;                                                               \
+            sincosf(ph0 + (cstart) * dph, &sn, &cs);                                    \
+            B = make_float2(cs, sn);                                                    \
+            sincosf((cstep) * dph, &sn, &cs);                                           \
+            D = make_float2(cs, sn);                                                    \
+        }
+#define TC32_STAGE(seg_, c_, X_)                                                        \
+        {                                                                               \
+            float2 X = (X_);                                                            \
+            if (PHASE) {                                                                \
+                X = cmul(X, B);                                                         \
+                B = cmul(B, D);                                                         \
+            }                                                                           \
+            if (SCALE) X = cscale(X, __ldg(scl + (c_)));                                \
+            stg[(seg_) * STG_PITCH + (c_)] = h2u(__floats2half2_rn(X.x, X.y));          \
+        }
+        for (int j = 0; j < nquads; j++) {
+            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
+            int s, kb;
+            unit_of(u, s, kb);
+            const float* scl = SCALE ? a.scale + (int64_t)s * FC : nullptr;
+            if (qd == 0 && u >= 1 && !gwait(NB_E2, 128, leader, bar(WB_STGFREE), (uint32_t)(u - 1) & 1)) break;
+            if (!gwait(NB_E2, 128, leader, bar(WB_D2FULL + b), (uint32_t)(j >> 1) & 1)) break;
+            tc::fence_after();
+            const int seg = QS * qd + q, k = kb * US + seg;
+            const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
+            // k2 blocks h = 0..3 in two pairs, one TMEM wait per pair
+            auto e2blk = [&](int h, const uint32_t (&re)[8], const uint32_t (&im)[8]) {
+                if (h < 2) {
+                    const int c0 = kk1 + 512 * h;
+                    TC32_PHASOR(s, k, (float)c0, 64.f)
+#pragma unroll
+                    for (int i = 0; i < 8; i++)
+                        TC32_STAGE(seg, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
+                } else if (kk1 > 0) {
+                    const int c0 = FC - kk1 - 512 * (h - 2);
+                    TC32_PHASOR(s, k, (float)c0, -64.f)
+#pragma unroll
+                    for (int i = 0; i < 8; i++)
+                        TC32_STAGE(seg, c0 - 64 * i, make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])))
+                }
+            };
+#pragma unroll 1
+            for (int h = 0; h < 4; h += 2) {
+                uint32_t re0[8], im0[8], re1[8], im1[8];
+                tc::tmem_ld_32x32b_x8(d2 + 8u * h, re0);
+                tc::tmem_ld_32x32b_x8(d2 + 32u + 8u * h, im0);
+                tc::tmem_ld_32x32b_x8(d2 + 8u * (h + 1), re1);
+                tc::tmem_ld_32x32b_x8(d2 + 32u + 8u * (h + 1), im1);
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    asm volatile("" : "+r"(re0[i]), "+r"(im0[i]), "+r"(re1[i]), "+r"(im1[i]));
+                }
+                e2blk(h, re0, im0);
+                e2blk(h + 1, re1, im1);
+            }
+            tc::fence_before();
+            warp_arrive(bar(WB_E2DONE + b));
+            if (qd == QUADS - 1) {
+                // the unit's k1 = 32 channels (c = 32 + 64 k2): warp 4 (lane quarter 0, lane = segment)
+                if (!gwait(NB_E2, 128, leader, bar(WB_D2PFULL + (u & 1)), (uint32_t)(u >> 1) & 1)) break;
+                tc::fence_after();
+                if (q == 0) {
+#pragma unroll 1
+                    for (int h = 0; h < 2; h++) {
+                        uint32_t re[8], im[8];
+                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 8u * h, re);
+                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 32u + 8u * h, im);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            asm volatile("" : "+r"(re[i]));
+                            asm volatile("" : "+r"(im[i]));
+                        }
+                        const int sg = lane, kq = kb * US + sg, c0 = 32 + 512 * h;
+                        TC32_PHASOR(s, kq, (float)c0, 64.f)
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            TC32_STAGE(sg, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
+                    }
+                }
+                tc::fence_before();
+                warp_arrive(bar(WB_E2PDONE));
+                warp_arrive(bar(WB_STGFULL));
+            }
+        }
+#undef TC32_PHASOR
+#undef TC32_STAGE
+    } else if (warp < WS_WO) {
+        // ------------------------------ fetch + decode ------------------------------
+        const int gt = tid - 32 * WS_DEC;                   // 0..127
+        const bool leader = gt == 0;
+        const int64_t chunks = a.bytes_per_input >> 4;
+        auto fetch = [&](int j) {
+            int s, kb;
+            unit_of(j / QUADS, s, kb);
+            const int kq = kb * US + (j % QUADS) * QS;
+            const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
+            const uint32_t dst0 = sbase + OFF_RAW + (uint32_t)(j & (NRAW - 1)) * RAW_BYTES;
+            for (int i = gt; i < QS * RAWC; i += 128) {
+                const int g = i / RAWC, c = i % RAWC, k = kq + g;
+                const int64_t start = a.start_sample + (int64_t)k * FN + (a.shift ? __ldg(a.shift + (int64_t)s * K + k) : 0);
+                const int64_t ci = (start >> 6) + c;
+                const bool ok = ci >= 0 && ci < chunks;
+                cp_async16(dst0 + 16u * i, ok ? base + 16 * ci : a.raw, ok);
+                if (c == 0) offs[(j & (NRAW - 1)) * QS + g] = (int)(start & 63);
+            }
+            cp_async_commit();
+        };
+        // raw words NRAW - 1 quads ahead (the DRAM latency is a sizeable part of a quad)
+        for (int f = 0; f < NRAW - 1 && f < nquads; f++) fetch(f);
+        for (int j = 0; j < nquads; j++) {
+            if (j + 2 < nquads) asm volatile("cp.async.wait_group 2;" ::: "memory");
+            else if (j + 1 < nquads) asm volatile("cp.async.wait_group 1;" ::: "memory");
+            else cp_async_wait_all();
+            // raw words of quad j in (group barrier), and B1 free (pass 1 of quad j - 1 done)
+            if (j == 0) grp_bar(NB_DEC, 128);
+            else if (!gwait(NB_DEC, 128, leader, bar(WB_D1FULL + ((j - 1) & 1)), (uint32_t)((j - 1) >> 1) & 1)) break;
+            const uint32_t* rw0 = reinterpret_cast<const uint32_t*>(sm + OFF_RAW + (j & (NRAW - 1)) * RAW_BYTES);
+            unsigned char* b1 = sm + OFF_B1;
+#pragma unroll
+            for (int r = 0; r < (QS * 128) / 128; r++) {          // segment r of the quad, word gt
+                const int g = r, wd = gt;
+                const int off = offs[(j & (NRAW - 1)) * QS + g];
+                const uint32_t* rw = rw0 + g * RAWC * 4 + (off >> 4) + wd;
+                const uint32_t bits = __funnelshift_r(rw[0], rw[1], 2 * (off & 15));
+                uint32_t hv[8];
+#pragma unroll
+                for (int p = 0; p < 4; p++) {
+                    const uint2 v = lut4[(bits >> (8 * p)) & 255u];
+                    hv[2 * p] = v.x;
+                    hv[2 * p + 1] = v.y;
+                }
+                const int n1 = wd >> 1;
+                const int chunk = 4 * (g & 1) + 2 * (wd & 1);
+                unsigned char* rowp = b1 + (g >> 1) * 8192 + n1 * 128;
+                *reinterpret_cast<uint4*>(rowp + (((chunk ^ n1) & 7) << 4)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+                *reinterpret_cast<uint4*>(rowp + ((((chunk + 1) ^ n1) & 7) << 4)) = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+            }
+            tc::fence_proxy_async();
+            warp_arrive(bar(WB_B1FULL));
+            grp_bar(NB_DEC, 128);                            // raw buffer j and its offsets are read
+            if (j + NRAW - 1 < nquads) fetch(j + NRAW - 1);
+        }
+        cp_async_wait_all();
+    } else if (warp < WS_MMA) {
+        // ------------------------------ write-out ------------------------------
+        const int gt = tid - 32 * WS_WO;                    // 0..127
+        const bool leader = gt == 0;
+        __half* out = reinterpret_cast<__half*>(a.out);
+        const int64_t crow = (int64_t)args.s_rows * args.nkb;
+        for (int u = 0; u < nunits; u++) {
+            int s, kb;
+            unit_of(u, s, kb);
+            if (!gwait(NB_WO, 128, leader, bar(WB_STGFULL), (uint32_t)u & 1)) break;
+            const int64_t row0 = (int64_t)s * args.nkb + kb;
+#pragma unroll 2
+            for (int r = 0; r < (FC * 4) / 128; r++) {
+                const int task = r * 128 + gt;
+                const int c = task >> 2, g4 = task & 3;
+                const uint32_t* col = stg + 8 * g4 * STG_PITCH + c;
+                uint32_t w[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) w[i] = col[i * STG_PITCH];
+                __half* run = out + ((int64_t)c * crow + row0) * 64 + 8 * g4;
+                *reinterpret_cast<uint4*>(run) =
+                    make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
+                               __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
+                *reinterpret_cast<uint4*>(run + 32) =
+                    make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
+                               __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
+            }
+            warp_arrive(bar(WB_STGFREE));
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == WS_MMA) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
 // A1 (DFT-64: per TMEM lane quarter q the Re rows 32q..32q+7 and Im rows
 // 32q+8..32q+15 of k1 = 8q..8q+7; rows 16..23 the real k1 = 32 row) and B2
 // (DFT-32 as a real 64 x 64 operand: rows k2 give Re X, rows 32 + k2 Im X) in
@@ -631,7 +1056,7 @@ bool cs_fstage_tc32_supported(const CsFStageArgs& a)
            kp % US == 0;
 }
 
-int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st)
+int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st, bool specialised)
 {
     if (!cs_fstage_tc32_supported(a)) return CS_ERR_UNSUPPORTED;
     if ((int64_t)a.S * (a.K / US) >= (int64_t)1 << 31) return CS_ERR_UNSUPPORTED;   // unit indices are 32-bit
@@ -656,11 +1081,19 @@ int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st)
     t.nkb = (a.kp ? a.kp : a.K) / US;
     t.s_rows = a.S_out ? a.S_out : a.S;
     const int grid = (int)std::min<int64_t>(t.units, g_sms32);
-    // the delay phasor and the channel scale are compiled in only where used
-    auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32<true, true> : k_fx_fstage_tc32<true, false>)
-                         : (a.scale ? k_fx_fstage_tc32<false, true> : k_fx_fstage_tc32<false, false>);
-    CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)(SMEM_BYTES)));
-    kern<<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
+    // the delay phasor and the channel scale are compiled in only where used;
+    // specialised: the warp-specialised form
+    if (specialised) {
+        auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32ws<true, true> : k_fx_fstage_tc32ws<true, false>)
+                             : (a.scale ? k_fx_fstage_tc32ws<false, true> : k_fx_fstage_tc32ws<false, false>);
+        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)(SMEM_BYTES)));
+        kern<<<grid, WS_THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
+    } else {
+        auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32<true, true> : k_fx_fstage_tc32<true, false>)
+                             : (a.scale ? k_fx_fstage_tc32<false, true> : k_fx_fstage_tc32<false, false>);
+        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)(SMEM_BYTES)));
+        kern<<<grid, THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
+    }
     return (int)cudaGetLastError();
 }
 

@@ -104,7 +104,7 @@ int cs_fstage_tc_status(unsigned* code);
 // symmetry halving the CUDA-core twiddle work.  cs_fx_fstage uses it for
 // those arguments unless CELLSPE_FSTAGE_TC32=0.
 bool cs_fstage_tc32_supported(const CsFStageArgs& a);
-int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st);
+int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st, bool specialised = false);
 int cs_fstage_tc32_status(unsigned* code);
 
 // xstage.cu -----------------------------------------------------------------

@@ -171,10 +171,11 @@ def test_fx_tc_fstage_2048_delay_model(cg, orc, fstage_engine):
     _tc_bars(orc, vis, X, pairs, K, cross_coverage=False)
 
 
-@pytest.fixture(params=["0", "1"], ids=["warp-fft", "tc32-fstage"])
+@pytest.fixture(params=["0", "1", "2"], ids=["warp-fft", "tc32-fstage", "tc32-specialised"])
 def fstage32(request, monkeypatch):
     """N = 2048 k-blocked FP16 spectra from the warp FFT or the 32-segment
-    tensor-core F stage (real-input symmetry, k1 = 32 row via pass 2')."""
+    tensor-core F stage (real-input symmetry, k1 = 32 row via pass 2'), in its
+    lockstep and its warp-specialised form."""
     monkeypatch.setenv("CELLSPE_FSTAGE_TC32", request.param)
     return request.param
 
