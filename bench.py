@@ -581,13 +581,15 @@ def main():
 
     # ---- roofline of the dominant kernel -----------------------------------
     # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) measured by
-    # ncu --set full on cases larger than L2 with the same per-unit work, scaled
-    # by the units one launch here processes: the warp-FFT F stage moved 4,375 B
-    # per input-segment (512 inputs x 512 segments, N = 2048, k-blocked FP16
-    # spectra); the tensor-core X stage read 2,049 B per (channel, segment) and
-    # wrote 1.02 MB of visibilities per channel (512 inputs x 1024 segments x
-    # 1024 channels).  None where no capture of that kernel exists.
-    F_TRAFFIC_PER_SEGMENT = 4375.0 if N_run == 2048 else None
+    # ncu on cases larger than L2 with the same per-unit work, scaled by the
+    # units one launch here processes: the warp-FFT F stage moved 4,375 B per
+    # input-segment (512 inputs x 512 segments, N = 2048, k-blocked FP16
+    # spectra, --set full); the warp-specialised tensor-core F stage 4,583 B
+    # (512 inputs x 4096 segments, one-pass dram__bytes_read/write capture);
+    # the tensor-core X stage read 2,049 B per (channel, segment) and wrote
+    # 1.02 MB of visibilities per channel (512 inputs x 1024 segments x 1024
+    # channels).  None where no capture of that kernel exists.
+    F_TRAFFIC_PER_SEGMENT = {"k_fx_fstage_w2048": 4375.0, "k_fx_fstage_tc32ws": 4583.0}
     X_TRAFFIC_PER_CHANNEL = 2049.0 * K_run + 1.0175e6
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
@@ -611,14 +613,23 @@ def main():
                     "traffic": X_TRAFFIC_PER_CHANNEL * C_run}
     else:
         pk = peaks["hbm_gbs"]
+        # the F-stage kernel the library picks for this job (fstage.cu's dispatch)
         tc_f = x_mode == cg.X_TC_FP16 and N_run == 2048 and os.environ.get("CELLSPE_FSTAGE_TC") == "1"
-        fk = "k_fx_fstage_tc" if tc_f else ("k_fx_fstage_w2048" if N_run == 2048 else
-                                            "k_fx_fstage_wbig" if N_run >= 4096 else "k_fx_fstage")
+        tc32 = os.environ.get("CELLSPE_FSTAGE_TC32", "2")[:1] or "2"
+        if x_mode == cg.X_TC_FP16 and N_run == 2048 and K_run % 32 == 0 and tc32 in "12":
+            fk = "k_fx_fstage_tc32ws" if tc32 == "2" else "k_fx_fstage_tc32"
+        elif tc_f:
+            fk = "k_fx_fstage_tc"
+        else:
+            fk = ("k_fx_fstage_w2048" if N_run == 2048 else "k_fx_fstage_wbig" if N_run >= 4096 else "k_fx_fstage")
+        per_seg = F_TRAFFIC_PER_SEGMENT.get(fk)
         roof = {"bound": "hbm", "kernel": fk, "achieved": stages["f_stage_gbs"], "peak": pk,
                 "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
-                "traffic": (F_TRAFFIC_PER_SEGMENT * S_run * K_run
-                            if F_TRAFFIC_PER_SEGMENT and fk == "k_fx_fstage_w2048" else None),
-                "note": "F stage is bound by instruction issue and the shared-memory pipe (ncu), not HBM"}
+                "traffic": per_seg * S_run * K_run if per_seg else None,
+                "note": ("F stage is bound by the LSU pipe (shared memory + global stores, 74% busy at 512 x 1024 "
+                         "segments) and at full size by DRAM write efficiency on the spectra's 32-byte sectors "
+                         "(ncu), not HBM bandwidth" if fk == "k_fx_fstage_tc32ws" else
+                         "F stage is bound by instruction issue and the shared-memory pipe (ncu), not HBM")}
 
     # ---- accuracy of the timed job (after the timed regions) ----------------
     # FP64 oracle on a seeded subset (16 inputs x 32 channels, full K) of this

@@ -81,16 +81,14 @@ constexpr int A2P_REGION = 32 * 128;
 constexpr int STG_PITCH = FC + 1;                     // words per staging row (one row per segment)
 constexpr int OFF_STG = OFF_A2P + 2 * A2P_REGION;     // staging: [US][STG_PITCH] half2 (Re, Im)
 constexpr int STG_BYTES = US * STG_PITCH * 4;
-constexpr int NRAW = 4;                               // raw buffers (the lockstep form uses two)
-constexpr int OFF_RAW = OFF_STG + STG_BYTES;          // NRAW x QS x RAWC x 16
+constexpr int OFF_RAW = OFF_STG + STG_BYTES;          // 2 x QS x RAWC x 16
 constexpr int RAW_BYTES = QS * RAWC * 16;
-constexpr int OFF_OFFS = OFF_RAW + NRAW * RAW_BYTES;  // sample offsets: NRAW x QS ints
-constexpr int OFF_LUT = OFF_OFFS + NRAW * QS * 4;     // 16 half2 pair levels
+constexpr int OFF_OFFS = OFF_RAW + 2 * RAW_BYTES;     // sample offsets: 2 x QS ints
+constexpr int OFF_LUT = OFF_OFFS + 2 * QS * 4;        // 16 half2 pair levels
 constexpr int OFF_BAR = OFF_LUT + 64;                 // mbarriers
-constexpr int NBAR = 16;
+constexpr int NBAR = 12;
 constexpr int OFF_SLOT = OFF_BAR + 8 * NBAR;
-constexpr int OFF_LUT4 = OFF_SLOT + 16;               // byte -> 4 FP16 levels (warp-specialised form)
-constexpr int SMEM_USED = OFF_LUT4 + 256 * 8;
+constexpr int SMEM_USED = OFF_SLOT + 16;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;          // + alignment of the base to 1024 B
 constexpr uint32_t TMEM_COLS = 512;                   // D1: 0, 128; D2: 256, 320; D2': 384
 constexpr uint32_t COL_D1 = 0, COL_D2 = 256, COL_D2P = 384;
@@ -569,27 +567,61 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
 }
 
 // ---------------------------------------------------------------------------
-// Warp-specialised form (CELLSPE_FSTAGE_TC32=2): the same transform, buffers
-// and TMEM columns, but each phase has warps of its own and the phases hand
-// buffers to each other through mbarriers, so they run concurrently instead
-// of in step between CTA-wide barriers:
+// Warp-specialised form (CELLSPE_FSTAGE_TC32=2): the same transform, but each
+// phase has warps of its own and the phases hand buffers to each other
+// through mbarriers, so they run concurrently instead of in step between
+// CTA-wide barriers:
 //   warps 0-3   epilogue 1 (TMEM lane quarter = warp), all 4 segments of a quad
-//   warps 4-7   epilogue 2 (lane quarter = segment of the quad), the k1 = 32
-//               channels at a unit's end
-//   warps 8-11  raw fetch (cp.async, two quads ahead) and decode into B1
-//               (a byte of four 2-bit codes -> four FP16 levels per table read)
-//   warps 12-15 write-out of a unit's staging
-//   warp 16     TMEM owner and MMA issuer
-// A group's first thread polls each barrier (bounded wait) and a named-barrier
-// vote of the group releases the others; a failed wait ends that group's loop,
-// and every group's waits are bounded, so all reach the final barrier.
+//   warps 4-7   epilogue 2 (lane quarter = segment of the quad) into the
+//               unit's staging, whose two 16-segment halves the write-out
+//               drains in turn; at a unit's end warp 4 writes the k1 = 32
+//               channels (lane = segment) to the spectra directly
+//   warps 8-11  decode into B1 (a nibble of two 2-bit codes -> two FP16
+//               levels per conflict-free table read)
+//   warps 12-15 write-out of a staging half: per channel and plane 16
+//               segments, two lanes' 16 bytes making one whole sector
+//   warp 16     TMEM owner and MMA issuer; pass 1 of quad j + 1 is issued
+//               before pass 2 of quad j, so epilogue 1 finds its next quad
+//               ready
+//   warp 17     raw fetch: bulk copies into NRAW buffers, up to NRAW quads
+//               ahead of the decode
+// A group's first thread polls the barriers (bounded waits) and a
+// named-barrier vote of the group releases the others; a failed wait ends
+// that group's loop, and every group's waits are bounded, so all reach the
+// final barrier.
 // ---------------------------------------------------------------------------
-constexpr int WS_E1 = 0, WS_E2 = 4, WS_DEC = 8, WS_WO = 12, WS_MMA = 16;
-constexpr int WS_THREADS = 17 * 32;
+constexpr int WS_E1 = 0, WS_E2 = 4, WS_DEC = 8, WS_WO = 12, WS_MMA = 16, WS_FETCH = 17;
+constexpr int WS_THREADS = 18 * 32;
+// shared memory of this form: constants, B1, A2 x 2, A2' x 2, the unit's
+// staging [US][WS_STG_PITCH] (pitch = 2 mod 32 words: the write-out's two
+// 8-segment groups of a channel fall 16 banks apart), raw x NRAW, offsets,
+// table, barriers
+constexpr int NRAW = 4;                               // raw buffers
+constexpr int WS_SH = US / 2;                         // segments per staging half
+constexpr int WS_STG_PITCH = FC + 2;
+constexpr int WS_OFF_B1 = CONST_BYTES;
+constexpr int WS_OFF_A2 = WS_OFF_B1 + B1_BYTES;
+constexpr int WS_OFF_A2P = WS_OFF_A2 + 2 * A2_BYTES;
+constexpr int WS_OFF_STG = WS_OFF_A2P + 2 * A2P_REGION;
+constexpr int WS_OFF_RAW = WS_OFF_STG + US * WS_STG_PITCH * 4;
+constexpr int WS_OFF_OFFS = WS_OFF_RAW + NRAW * RAW_BYTES;
+constexpr int WS_OFF_LUT = WS_OFF_OFFS + NRAW * QS * 4;
+constexpr int WS_OFF_BAR = WS_OFF_LUT + 64;
+constexpr int WS_NBAR = 26;
+constexpr int WS_OFF_SLOT = WS_OFF_BAR + 8 * WS_NBAR;
+constexpr int WS_SMEM_BYTES = WS_OFF_SLOT + 16 + 1024;   // + alignment of the base to 1024 B
+// barriers ([2]: by quad parity or staging half, [NRAW]: by raw buffer)
 constexpr int WB_B1FULL = 0, WB_D1FULL = 1, WB_E1DONE = 3, WB_D2FULL = 5, WB_E2DONE = 7, WB_D2PFULL = 9,
-              WB_E2PDONE = 11, WB_STGFULL = 12, WB_STGFREE = 13, WB_DRAIN = 14;   // [2] where two follow
-static_assert(WB_DRAIN < NBAR, "barriers");
-static_assert(NRAW == 4, "the decode group's cp.async waits assume four raw buffers");
+              WB_E2PDONE = 11, WB_STGFULL = 12, WB_STGFREE = 14, WB_DRAIN = 16, WB_RAWFULL = 17,
+              WB_RAWFREE = WB_RAWFULL + NRAW;
+static_assert(WB_RAWFREE + NRAW <= WS_NBAR, "barriers");
+static_assert(WS_SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(WS_OFF_B1 % 1024 == 0 && WS_OFF_A2 % 1024 == 0 && WS_OFF_A2P % 1024 == 0,
+              "swizzle atoms need 1024-B alignment");
+static_assert(WS_OFF_A2P + A2P_REGION + 16384 <= WS_OFF_RAW, "pass-2' windows inside shared memory");
+static_assert(WS_OFF_RAW % 16 == 0 && RAW_BYTES % 16 == 0 && WS_OFF_OFFS % 16 == 0, "raw buffers take bulk copies");
+static_assert((NRAW & (NRAW - 1)) == 0, "raw buffers are indexed by j & (NRAW - 1)");
+static_assert(WS_SH % QS == 0 && US == 2 * WS_SH, "a staging half holds whole quads");
 static_assert(WS_E1 == 0 && WS_E2 == WS_E1 + 4, "epilogue-1 warps are 0..3 (TMEM lane quarter = warp)");
 // named barriers (id, threads) of the groups
 constexpr int NB_DEC = 1, NB_E1 = 2, NB_E2 = 3, NB_WO = 4;
@@ -607,7 +639,6 @@ CS_DEV bool grp_vote(int id, int n, bool ok)
         : "memory");
     return r != 0;
 }
-CS_DEV void grp_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 
 template <bool PHASE, bool SCALE>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid_constant__ Tc32Args args)
@@ -618,24 +649,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
     const CsFStageArgs& a = args.f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tid = threadIdx.x;
-    const uint32_t bar0 = sbase + OFF_BAR;
+    const uint32_t bar0 = sbase + WS_OFF_BAR;
     auto bar = [&](int i) { return bar0 + 8u * (uint32_t)i; };
-    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + OFF_SLOT);
-    int* offs = reinterpret_cast<int*>(sm + OFF_OFFS);
-    __half2* lut2 = reinterpret_cast<__half2*>(sm + OFF_LUT);
-    uint32_t* stg = reinterpret_cast<uint32_t*>(sm + OFF_STG);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + WS_OFF_SLOT);
+    int* offs = reinterpret_cast<int*>(sm + WS_OFF_OFFS);
+    __half2* lut2 = reinterpret_cast<__half2*>(sm + WS_OFF_LUT);
+    uint32_t* stg = reinterpret_cast<uint32_t*>(sm + WS_OFF_STG);
 
     for (int i = tid; i < CONST_BYTES / 16; i += WS_THREADS)
         reinterpret_cast<uint4*>(sm)[i] = __ldg(args.consts + i);
     for (int i = tid; i < 2 * A2P_REGION / 16; i += WS_THREADS)
-        reinterpret_cast<uint4*>(sm + OFF_A2P)[i] = make_uint4(0, 0, 0, 0);
-    uint2* lut4 = reinterpret_cast<uint2*>(sm + OFF_LUT4);
-    if (tid < 256) {
+        reinterpret_cast<uint4*>(sm + WS_OFF_A2P)[i] = make_uint4(0, 0, 0, 0);
+    if (tid < 16) {
         const float l0 = a.lut[0], l1 = a.lut[1], l2 = a.lut[2], l3 = a.lut[3];
         auto lv = [&](int c) { return c == 0 ? l0 : c == 1 ? l1 : c == 2 ? l2 : l3; };
-        if (tid < 16) lut2[tid] = __floats2half2_rn(lv(tid & 3), lv(tid >> 2));
-        lut4[tid] = make_uint2(h2u(__floats2half2_rn(lv(tid & 3), lv((tid >> 2) & 3))),
-                               h2u(__floats2half2_rn(lv((tid >> 4) & 3), lv(tid >> 6))));
+        lut2[tid] = __floats2half2_rn(lv(tid & 3), lv(tid >> 2));
     }
     if (tid == 0) {
         tc::mbar_init(bar(WB_B1FULL), 4);
@@ -647,9 +675,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
             tc::mbar_init(bar(WB_D2PFULL + b), 1);
         }
         tc::mbar_init(bar(WB_E2PDONE), 4);
-        tc::mbar_init(bar(WB_STGFULL), 4);
-        tc::mbar_init(bar(WB_STGFREE), 4);
+        for (int t = 0; t < 2; t++) {
+            tc::mbar_init(bar(WB_STGFULL + t), 4);
+            tc::mbar_init(bar(WB_STGFREE + t), 4);
+        }
         tc::mbar_init(bar(WB_DRAIN), 1);
+        for (int r = 0; r < NRAW; r++) {
+            tc::mbar_init(bar(WB_RAWFULL + r), 1);
+            tc::mbar_init(bar(WB_RAWFREE + r), 4);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == WS_MMA) tc::tmem_alloc(tc::smem_u32(slot), TMEM_COLS);
@@ -669,12 +703,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
         s = (int)si;
         kb = (int)(uu - si * (uint32_t)args.units_k);
     };
-    // group wait: the leader polls, the group's vote releases everyone
-    auto gwait = [&](int id, int n, bool leader, uint32_t b, uint32_t parity) -> bool {
-        bool ok = true;
-        if (leader) ok = tc::mbar_wait(b, parity, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
-        return grp_vote(id, n, ok);
+    // a group leader's bounded wait (the group then votes on the outcome)
+    auto lwait = [&](int i, uint32_t parity) {
+        return tc::mbar_wait(bar(i), parity, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
     };
+    __half* out = reinterpret_cast<__half*>(a.out);
+    const int64_t crow = (int64_t)args.s_rows * args.nkb;   // spectra rows (input, k-block) per channel
 
     if (warp == WS_MMA) {
         // ------------------------------ MMA issuer ------------------------------
@@ -684,23 +718,34 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
             auto w = [&](int i, uint32_t ph) {
                 return tc::mbar_wait(bar(i), ph, &g_fst32_error, E_MMA_WAIT, WAIT_CYCLES);
             };
-            for (int j = 0; j < nquads; j++) {
-                const int b = j & 1, u = j / QUADS;
-                if (!w(WB_B1FULL, (uint32_t)j & 1)) break;
+            // pass 1 of quad j: B1 -> D1[j & 1].  D1[j & 1] was last read by
+            // epilogue 1 for quad j - 2, whose completion pass 2 of quad j - 2
+            // waited for before this is issued.
+            auto pass1 = [&](int j) -> bool {
+                const int b = j & 1;
+                if (!w(WB_B1FULL, (uint32_t)j & 1)) return false;
                 tc::fence_after();
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++) {
                     const uint64_t da = tc::smem_desc(sbase + OFF_A1 + 32u * kk, 16, 1024, tc::SW128);
-                    const uint64_t db = tc::smem_desc(sbase + OFF_B1 + 2048u * kk, 8192, 1024, tc::SW128);
+                    const uint64_t db =
+                        tc::smem_desc(sbase + WS_OFF_B1 + 2048u * kk, 8192, 1024, tc::SW128);
                     tc::mma_f16(tmem + COL_D1 + 128u * b, da, db, id1, kk ? 1u : 0u);
                 }
                 tc::commit(bar(WB_D1FULL + b));
+                return true;
+            };
+            bool ok = nquads == 0 || pass1(0);
+            for (int j = 0; ok && j < nquads; j++) {
+                const int b = j & 1, u = j / QUADS;
+                if (j + 1 < nquads && !pass1(j + 1)) break;
                 if (j >= 2 && !w(WB_E2DONE + b, (uint32_t)((j - 2) >> 1) & 1)) break;   // D2[b] read
                 if (!w(WB_E1DONE + b, (uint32_t)(j >> 1) & 1)) break;                  // A2[b] written, D1[b] read
                 tc::fence_after();
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++) {
-                    const uint64_t da = tc::smem_desc(sbase + OFF_A2 + (uint32_t)b * A2_BYTES + 32u * kk, 16, 1024, tc::SW128);
+                    const uint64_t da =
+                        tc::smem_desc(sbase + WS_OFF_A2 + (uint32_t)b * A2_BYTES + 32u * kk, 16, 1024, tc::SW128);
                     const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
                     tc::mma_f16(tmem + COL_D2 + 64u * b, da, db, id2, kk ? 1u : 0u);
                 }
@@ -710,8 +755,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                     tc::fence_after();
 #pragma unroll
                     for (int kk = 0; kk < 4; kk++) {
-                        const uint64_t da = tc::smem_desc(sbase + OFF_A2P + (uint32_t)(u & 1) * A2P_REGION + 32u * kk,
-                                                          16, 1024, tc::SW128);
+                        const uint64_t da = tc::smem_desc(
+                            sbase + WS_OFF_A2P + (uint32_t)(u & 1) * A2P_REGION + 32u * kk, 16, 1024, tc::SW128);
                         const uint64_t db = tc::smem_desc(sbase + OFF_B2 + 32u * kk, 16, 1024, tc::SW128);
                         tc::mma_f16(tmem + COL_D2P, da, db, id2, kk ? 1u : 0u);
                     }
@@ -748,15 +793,19 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
         }
         for (int j = 0; j < nquads; j++) {
             const int b = j & 1, qd = j % QUADS, u = j / QUADS;
-            if (qd == 0 && u >= 2 && !gwait(NB_E1, 128, leader, bar(WB_D2PFULL + (u & 1)), (uint32_t)((u - 2) >> 1) & 1))
-                break;                                      // A2' region u & 1 read by pass 2' of unit u - 2
-            if (j >= 2 && !gwait(NB_E1, 128, leader, bar(WB_D2FULL + b), (uint32_t)((j - 2) >> 1) & 1)) break;
-            if (!gwait(NB_E1, 128, leader, bar(WB_D1FULL + b), (uint32_t)(j >> 1) & 1)) break;
+            bool ok = true;
+            if (leader) {
+                // A2' region u & 1 read by pass 2' of unit u - 2; A2[b] read by
+                // pass 2 of quad j - 2; D1[b] of quad j written
+                if (qd == 0 && u >= 2) ok = lwait(WB_D2PFULL + (u & 1), (uint32_t)((u - 2) >> 1) & 1);
+                if (ok && j >= 2) ok = lwait(WB_D2FULL + b, (uint32_t)((j - 2) >> 1) & 1);
+                if (ok) ok = lwait(WB_D1FULL + b, (uint32_t)(j >> 1) & 1);
+            }
+            if (!grp_vote(NB_E1, 128, ok)) break;
             tc::fence_after();
-            unsigned char* a2 = sm + OFF_A2 + b * A2_BYTES;
-            // two segments per TMEM wait
-            auto e1seg = [&](int h, uint32_t (&r)[16]) {
-                const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * h;
+            unsigned char* a2 = sm + WS_OFF_A2 + b * A2_BYTES;
+            unsigned char* a2p = sm + WS_OFF_A2P + (u & 1) * A2P_REGION;
+            auto e1seg = [&](int h, const uint32_t (&r)[16]) {
                 unsigned char* a2h = a2 + 4096 * h;
 #pragma unroll
                 for (int m = 0; m < 4; m++) {
@@ -766,30 +815,41 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                     *reinterpret_cast<uint32_t*>(a2h + (e1base ^ (m << 4))) = h2u(__floats2half2_rn(z0.x, z1.x));
                     *reinterpret_cast<uint32_t*>(a2h + (e1base ^ (m << 4) ^ 64u)) = h2u(__floats2half2_rn(z0.y, z1.y));
                 }
-                if (q == 0) {
-                    uint32_t r32[16];
-                    tc::tmem_ld_16x256b_x4(d1 + (16u << 16), r32);
-                    tc::tmem_ld_wait();
-                    pin16(r32);
-                    const bool mb1 = m32 & 1, mb2 = m32 & 2;
-                    const uint32_t ya = mb2 ? (mb1 ? r32[12] : r32[8]) : (mb1 ? r32[4] : r32[0]);
-                    const uint32_t yb = mb2 ? (mb1 ? r32[13] : r32[9]) : (mb1 ? r32[5] : r32[1]);
-                    const float y = __uint_as_float(e32 ? yb : ya);
-                    unsigned char* a2p = sm + OFF_A2P + (u & 1) * A2P_REGION;
-                    const uint32_t prow = QS * qd + h;
-                    *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = __float2half_rn(y * tw32.x);
-                    *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = __float2half_rn(y * tw32.y);
-                }
             };
+            // the real k1 = 32 row (TMEM lanes 16..23 of quarter 0) of segment h
+            // -> row 4 qd + h of the unit's A2' region
+            auto e1row32 = [&](int h, const uint32_t (&r32)[16]) {
+                const bool mb1 = m32 & 1, mb2 = m32 & 2;
+                const uint32_t ya = mb2 ? (mb1 ? r32[12] : r32[8]) : (mb1 ? r32[4] : r32[0]);
+                const uint32_t yb = mb2 ? (mb1 ? r32[13] : r32[9]) : (mb1 ? r32[5] : r32[1]);
+                const float y = __uint_as_float(e32 ? yb : ya);
+                const uint32_t prow = QS * qd + h;
+                *reinterpret_cast<__half*>(a2p + sw128(prow, n2_32)) = __float2half_rn(y * tw32.x);
+                *reinterpret_cast<__half*>(a2p + sw128(prow, 32 + n2_32)) = __float2half_rn(y * tw32.y);
+            };
+            // two segments per TMEM wait
 #pragma unroll 1
             for (int h = 0; h < QS; h += 2) {
-                const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * h + ((uint32_t)(32 * q) << 16);
+                const uint32_t d1 = tmem + COL_D1 + 128u * b + 32u * h;
                 uint32_t r0[16], r1[16];
-                tc::tmem_ld_16x256b_x4(d1, r0);
-                tc::tmem_ld_16x256b_x4(d1 + 32u, r1);
-                tc::tmem_ld_wait();
-                pin16(r0);
-                pin16(r1);
+                tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r0);
+                tc::tmem_ld_16x256b_x4(d1 + 32u + ((uint32_t)(32 * q) << 16), r1);
+                if (q == 0) {
+                    uint32_t s0[16], s1[16];
+                    tc::tmem_ld_16x256b_x4(d1 + (16u << 16), s0);
+                    tc::tmem_ld_16x256b_x4(d1 + 32u + (16u << 16), s1);
+                    tc::tmem_ld_wait();
+                    pin16(r0);
+                    pin16(r1);
+                    pin16(s0);
+                    pin16(s1);
+                    e1row32(h, s0);
+                    e1row32(h + 1, s1);
+                } else {
+                    tc::tmem_ld_wait();
+                    pin16(r0);
+                    pin16(r1);
+                }
                 e1seg(h, r0);
                 e1seg(h + 1, r1);
             }
@@ -813,25 +873,27 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
             sincosf((cstep) * dph, &sn, &cs);                                           \
             D = make_float2(cs, sn);                                                    \
         }
-#define TC32_STAGE(seg_, c_, X_)                                                        \
-        {                                                                               \
-            float2 X = (X_);                                                            \
-            if (PHASE) {                                                                \
-                X = cmul(X, B);                                                         \
-                B = cmul(B, D);                                                         \
-            }                                                                           \
-            if (SCALE) X = cscale(X, __ldg(scl + (c_)));                                \
-            stg[(seg_) * STG_PITCH + (c_)] = h2u(__floats2half2_rn(X.x, X.y));          \
-        }
+#define TC32_APPLY(c_, X)                                                               \
+        if (PHASE) {                                                                    \
+            X = cmul(X, B);                                                             \
+            B = cmul(B, D);                                                             \
+        }                                                                               \
+        if (SCALE) X = cscale(X, __ldg(scl + (c_)));
         for (int j = 0; j < nquads; j++) {
-            const int b = j & 1, qd = j % QUADS, u = j / QUADS;
+            const int b = j & 1, qd = j % QUADS, u = j / QUADS, t = j / (WS_SH / QS), sh = t & 1;
             int s, kb;
             unit_of(u, s, kb);
             const float* scl = SCALE ? a.scale + (int64_t)s * FC : nullptr;
-            if (qd == 0 && u >= 1 && !gwait(NB_E2, 128, leader, bar(WB_STGFREE), (uint32_t)(u - 1) & 1)) break;
-            if (!gwait(NB_E2, 128, leader, bar(WB_D2FULL + b), (uint32_t)(j >> 1) & 1)) break;
+            bool ok = true;
+            if (leader) {
+                // staging half sh drained (for the unit before); D2[b] of quad j written
+                if (j % (WS_SH / QS) == 0 && t >= 2) ok = lwait(WB_STGFREE + sh, (uint32_t)((t >> 1) - 1) & 1);
+                if (ok) ok = lwait(WB_D2FULL + b, (uint32_t)(j >> 1) & 1);
+            }
+            if (!grp_vote(NB_E2, 128, ok)) break;
             tc::fence_after();
             const int seg = QS * qd + q, k = kb * US + seg;
+            uint32_t* srow = stg + seg * WS_STG_PITCH;
             const uint32_t d2 = tmem + COL_D2 + 64u * b + ((uint32_t)(32 * q) << 16);
             // k2 blocks h = 0..3 in two pairs, one TMEM wait per pair
             auto e2blk = [&](int h, const uint32_t (&re)[8], const uint32_t (&im)[8]) {
@@ -839,14 +901,20 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                     const int c0 = kk1 + 512 * h;
                     TC32_PHASOR(s, k, (float)c0, 64.f)
 #pragma unroll
-                    for (int i = 0; i < 8; i++)
-                        TC32_STAGE(seg, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
+                    for (int i = 0; i < 8; i++) {
+                        float2 X = make_float2(__uint_as_float(re[i]), __uint_as_float(im[i]));
+                        TC32_APPLY(c0 + 64 * i, X)
+                        srow[c0 + 64 * i] = h2u(__floats2half2_rn(X.x, X.y));
+                    }
                 } else if (kk1 > 0) {
                     const int c0 = FC - kk1 - 512 * (h - 2);
                     TC32_PHASOR(s, k, (float)c0, -64.f)
 #pragma unroll
-                    for (int i = 0; i < 8; i++)
-                        TC32_STAGE(seg, c0 - 64 * i, make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i])))
+                    for (int i = 0; i < 8; i++) {
+                        float2 X = make_float2(__uint_as_float(re[i]), -__uint_as_float(im[i]));
+                        TC32_APPLY(c0 - 64 * i, X)
+                        srow[c0 - 64 * i] = h2u(__floats2half2_rn(X.x, X.y));
+                    }
                 }
             };
 #pragma unroll 1
@@ -858,19 +926,24 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                 tc::tmem_ld_32x32b_x8(d2 + 32u + 8u * (h + 1), im1);
                 tc::tmem_ld_wait();
 #pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    asm volatile("" : "+r"(re0[i]), "+r"(im0[i]), "+r"(re1[i]), "+r"(im1[i]));
-                }
+                for (int i = 0; i < 8; i++) asm volatile("" : "+r"(re0[i]), "+r"(im0[i]), "+r"(re1[i]), "+r"(im1[i]));
                 e2blk(h, re0, im0);
                 e2blk(h + 1, re1, im1);
             }
             tc::fence_before();
             warp_arrive(bar(WB_E2DONE + b));
+            if (j % (WS_SH / QS) == WS_SH / QS - 1) warp_arrive(bar(WB_STGFULL + sh));
             if (qd == QUADS - 1) {
-                // the unit's k1 = 32 channels (c = 32 + 64 k2): warp 4 (lane quarter 0, lane = segment)
-                if (!gwait(NB_E2, 128, leader, bar(WB_D2PFULL + (u & 1)), (uint32_t)(u >> 1) & 1)) break;
+                // the unit's k1 = 32 channels c = 32 + 64 k2: warp 4 (lane quarter
+                // 0, lane = segment) writes them to the spectra directly, each
+                // store a channel's 32 segments of one plane (64 bytes)
+                ok = true;
+                if (leader) ok = lwait(WB_D2PFULL + (u & 1), (uint32_t)(u >> 1) & 1);
+                if (!grp_vote(NB_E2, 128, ok)) break;
                 tc::fence_after();
                 if (q == 0) {
+                    __half* o = out + ((int64_t)s * args.nkb + kb) * 64 + lane;
+                    const int kq = kb * US + lane;
 #pragma unroll 1
                     for (int h = 0; h < 2; h++) {
                         uint32_t re[8], im[8];
@@ -878,101 +951,113 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                         tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 32u + 8u * h, im);
                         tc::tmem_ld_wait();
 #pragma unroll
-                        for (int i = 0; i < 8; i++) {
-                            asm volatile("" : "+r"(re[i]));
-                            asm volatile("" : "+r"(im[i]));
-                        }
-                        const int sg = lane, kq = kb * US + sg, c0 = 32 + 512 * h;
+                        for (int i = 0; i < 8; i++) asm volatile("" : "+r"(re[i]), "+r"(im[i]));
+                        const int c0 = 32 + 512 * h;
                         TC32_PHASOR(s, kq, (float)c0, 64.f)
 #pragma unroll
-                        for (int i = 0; i < 8; i++)
-                            TC32_STAGE(sg, c0 + 64 * i, make_float2(__uint_as_float(re[i]), __uint_as_float(im[i])))
+                        for (int i = 0; i < 8; i++) {
+                            const int c = c0 + 64 * i;
+                            float2 X = make_float2(__uint_as_float(re[i]), __uint_as_float(im[i]));
+                            TC32_APPLY(c, X)
+                            __half* oc = o + (int64_t)c * crow * 64;
+                            oc[0] = __float2half_rn(X.x);
+                            oc[32] = __float2half_rn(X.y);
+                        }
                     }
                 }
                 tc::fence_before();
                 warp_arrive(bar(WB_E2PDONE));
-                warp_arrive(bar(WB_STGFULL));
             }
         }
 #undef TC32_PHASOR
-#undef TC32_STAGE
+#undef TC32_APPLY
     } else if (warp < WS_WO) {
-        // ------------------------------ fetch + decode ------------------------------
+        // ------------------------------ decode ------------------------------
         const int gt = tid - 32 * WS_DEC;                   // 0..127
         const bool leader = gt == 0;
-        const int64_t chunks = a.bytes_per_input >> 4;
-        auto fetch = [&](int j) {
-            int s, kb;
-            unit_of(j / QUADS, s, kb);
-            const int kq = kb * US + (j % QUADS) * QS;
-            const unsigned char* base = a.raw + (int64_t)s * a.bytes_per_input;
-            const uint32_t dst0 = sbase + OFF_RAW + (uint32_t)(j & (NRAW - 1)) * RAW_BYTES;
-            for (int i = gt; i < QS * RAWC; i += 128) {
-                const int g = i / RAWC, c = i % RAWC, k = kq + g;
-                const int64_t start = a.start_sample + (int64_t)k * FN + (a.shift ? __ldg(a.shift + (int64_t)s * K + k) : 0);
-                const int64_t ci = (start >> 6) + c;
-                const bool ok = ci >= 0 && ci < chunks;
-                cp_async16(dst0 + 16u * i, ok ? base + 16 * ci : a.raw, ok);
-                if (c == 0) offs[(j & (NRAW - 1)) * QS + g] = (int)(start & 63);
-            }
-            cp_async_commit();
-        };
-        // raw words NRAW - 1 quads ahead (the DRAM latency is a sizeable part of a quad)
-        for (int f = 0; f < NRAW - 1 && f < nquads; f++) fetch(f);
+        // Thread gt decodes raw word wd (16 samples: n1 = wd / 2, n2 = 16 (wd & 1)
+        // + 0..15).  The order puts eight consecutive lanes on eight rows n1 of
+        // one n2 half, so each quarter-warp's 16-byte B1 stores hit eight
+        // different swizzled chunks (no bank conflict).
+        const int wd = ((gt & 7) << 1) | ((gt >> 3) & 1) | (gt & ~15);
+        // the four levels as FP16 bytes 0-7 of {t1:t0}; code c is bytes 2c, 2c + 1
+        const uint32_t t0 = h2u(lut2[4]), t1 = h2u(lut2[14]);
         for (int j = 0; j < nquads; j++) {
-            if (j + 2 < nquads) asm volatile("cp.async.wait_group 2;" ::: "memory");
-            else if (j + 1 < nquads) asm volatile("cp.async.wait_group 1;" ::: "memory");
-            else cp_async_wait_all();
-            // raw words of quad j in (group barrier), and B1 free (pass 1 of quad j - 1 done)
-            if (j == 0) grp_bar(NB_DEC, 128);
-            else if (!gwait(NB_DEC, 128, leader, bar(WB_D1FULL + ((j - 1) & 1)), (uint32_t)((j - 1) >> 1) & 1)) break;
-            const uint32_t* rw0 = reinterpret_cast<const uint32_t*>(sm + OFF_RAW + (j & (NRAW - 1)) * RAW_BYTES);
-            unsigned char* b1 = sm + OFF_B1;
+            const int buf = j & (NRAW - 1);
+            // raw words of quad j landed, and B1 free (pass 1 of quad j - 1 done)
+            bool ok = true;
+            if (leader) {
+                ok = lwait(WB_RAWFULL + buf, (uint32_t)(j / NRAW) & 1);
+                if (ok && j > 0) ok = lwait(WB_D1FULL + ((j - 1) & 1), (uint32_t)((j - 1) >> 1) & 1);
+            }
+            if (!grp_vote(NB_DEC, 128, ok)) break;
+            const uint32_t* rw0 = reinterpret_cast<const uint32_t*>(sm + WS_OFF_RAW + buf * RAW_BYTES);
+            const int4 o4 = *reinterpret_cast<const int4*>(offs + buf * QS);
+            const int ov[QS] = {o4.x, o4.y, o4.z, o4.w};
+            // every load of the quad before any store (the B1 stores could
+            // otherwise alias them and serialise the segments)
+            uint32_t bits[QS];
 #pragma unroll
-            for (int r = 0; r < (QS * 128) / 128; r++) {          // segment r of the quad, word gt
-                const int g = r, wd = gt;
-                const int off = offs[(j & (NRAW - 1)) * QS + g];
-                const uint32_t* rw = rw0 + g * RAWC * 4 + (off >> 4) + wd;
-                const uint32_t bits = __funnelshift_r(rw[0], rw[1], 2 * (off & 15));
-                uint32_t hv[8];
+            for (int g = 0; g < QS; g++) {                  // segment g of the quad, word wd
+                const uint32_t* rw = rw0 + g * RAWC * 4 + (ov[g] >> 4) + wd;
+                bits[g] = __funnelshift_r(rw[0], rw[1], 2 * (ov[g] & 15));
+            }
+            // word w of the 8 output words holds samples 2w, 2w + 1 (codes a, b):
+            // a byte_perm of {t1:t0} with selector nibbles 2a, 2a + 1, 2b, 2b + 1
+            // = 0x1010 + 34 a + 8704 b.  Words w and w + 4 share one selector
+            // computation, one per 16-bit half (no carry: the sum stays below 2^15).
+            uint32_t hv[QS][8];
 #pragma unroll
-                for (int p = 0; p < 4; p++) {
-                    const uint2 v = lut4[(bits >> (8 * p)) & 255u];
-                    hv[2 * p] = v.x;
-                    hv[2 * p + 1] = v.y;
+            for (int g = 0; g < QS; g++)
+#pragma unroll
+                for (int w = 0; w < 4; w++) {
+                    const uint32_t pa = (bits[g] >> (4 * w)) & 0x00030003u;
+                    const uint32_t pb = (bits[g] >> (4 * w + 2)) & 0x00030003u;
+                    const uint32_t sel = pa * 34u + pb * 8704u + 0x10101010u;
+                    hv[g][w] = __byte_perm(t0, t1, sel);
+                    hv[g][w + 4] = __byte_perm(t0, t1, sel >> 16);
                 }
-                const int n1 = wd >> 1;
+            warp_arrive(bar(WB_RAWFREE + buf));            // this warp's reads of the buffer are done
+            unsigned char* b1 = sm + WS_OFF_B1;
+            const int n1 = wd >> 1;
+#pragma unroll
+            for (int g = 0; g < QS; g++) {
                 const int chunk = 4 * (g & 1) + 2 * (wd & 1);
                 unsigned char* rowp = b1 + (g >> 1) * 8192 + n1 * 128;
-                *reinterpret_cast<uint4*>(rowp + (((chunk ^ n1) & 7) << 4)) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-                *reinterpret_cast<uint4*>(rowp + ((((chunk + 1) ^ n1) & 7) << 4)) = make_uint4(hv[4], hv[5], hv[6], hv[7]);
+                *reinterpret_cast<uint4*>(rowp + (((chunk ^ n1) & 7) << 4)) =
+                    make_uint4(hv[g][0], hv[g][1], hv[g][2], hv[g][3]);
+                *reinterpret_cast<uint4*>(rowp + ((((chunk + 1) ^ n1) & 7) << 4)) =
+                    make_uint4(hv[g][4], hv[g][5], hv[g][6], hv[g][7]);
             }
             tc::fence_proxy_async();
             warp_arrive(bar(WB_B1FULL));
-            grp_bar(NB_DEC, 128);                            // raw buffer j and its offsets are read
-            if (j + NRAW - 1 < nquads) fetch(j + NRAW - 1);
         }
-        cp_async_wait_all();
     } else if (warp < WS_MMA) {
         // ------------------------------ write-out ------------------------------
+        // staging half t & 1 of unit t / 2: per channel the 16 segments' Re
+        // and Im halves; lanes 2i, 2i + 1 take segments 0-7 and 8-15 of one
+        // channel, so each plane's 32 bytes leave as one whole sector
         const int gt = tid - 32 * WS_WO;                    // 0..127
         const bool leader = gt == 0;
-        __half* out = reinterpret_cast<__half*>(a.out);
-        const int64_t crow = (int64_t)args.s_rows * args.nkb;
-        for (int u = 0; u < nunits; u++) {
+        const int nhalves = 2 * nunits;
+        for (int t = 0; t < nhalves; t++) {
+            const int sh = t & 1, u = t >> 1;
             int s, kb;
             unit_of(u, s, kb);
-            if (!gwait(NB_WO, 128, leader, bar(WB_STGFULL), (uint32_t)u & 1)) break;
-            const int64_t row0 = (int64_t)s * args.nkb + kb;
+            bool ok = true;
+            if (leader) ok = lwait(WB_STGFULL + sh, (uint32_t)(t >> 1) & 1);
+            if (!grp_vote(NB_WO, 128, ok)) break;
+            __half* o = out + ((int64_t)s * args.nkb + kb) * 64 + WS_SH * sh;
 #pragma unroll 2
-            for (int r = 0; r < (FC * 4) / 128; r++) {
+            for (int r = 0; r < 2 * FC / 128; r++) {
                 const int task = r * 128 + gt;
-                const int c = task >> 2, g4 = task & 3;
-                const uint32_t* col = stg + 8 * g4 * STG_PITCH + c;
+                const int c = task >> 1, g8 = task & 1;
+                if ((c & 63) == 32) continue;               // the k1 = 32 channels: written by epilogue 2
+                const uint32_t* col = stg + (WS_SH * sh + 8 * g8) * WS_STG_PITCH + c;
                 uint32_t w[8];
 #pragma unroll
-                for (int i = 0; i < 8; i++) w[i] = col[i * STG_PITCH];
-                __half* run = out + ((int64_t)c * crow + row0) * 64 + 8 * g4;
+                for (int i = 0; i < 8; i++) w[i] = col[i * WS_STG_PITCH];
+                __half* run = o + (int64_t)c * crow * 64 + 8 * g8;
                 *reinterpret_cast<uint4*>(run) =
                     make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
                                __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
@@ -980,8 +1065,55 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                     make_uint4(__byte_perm(w[0], w[1], 0x7632), __byte_perm(w[2], w[3], 0x7632),
                                __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
             }
-            warp_arrive(bar(WB_STGFREE));
+            warp_arrive(bar(WB_STGFREE + sh));
         }
+    } else if (warp == WS_FETCH) {
+        // ------------------------------ raw fetch ------------------------------
+        // Raw words of quad j into buffer j & (NRAW - 1): lane g < QS copies
+        // segment g's RAWC chunks with one bulk copy (the part inside the
+        // input; chunks outside it are zeroed, as the lockstep form's
+        // zero-filled cp.async leaves them) and the buffer's barrier completes
+        // when all bytes have landed.
+        const int64_t chunks = a.bytes_per_input >> 4;
+        int issued = 0;
+        for (int j = 0; j < nquads; j++) {
+            const int buf = j & (NRAW - 1);
+            bool ok = true;
+            if (lane == 0 && j >= NRAW) ok = lwait(WB_RAWFREE + buf, (uint32_t)(j / NRAW - 1) & 1);
+            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+            int s, kb;
+            unit_of(j / QUADS, s, kb);
+            const uint32_t rb = bar(WB_RAWFULL + buf);
+            int64_t ci0 = 0;
+            int lo = 0, hi = 0;
+            if (lane < QS) {
+                const int k = kb * US + (j % QUADS) * QS + lane;
+                const int64_t start = a.start_sample + (int64_t)k * FN + (a.shift ? __ldg(a.shift + (int64_t)s * K + k) : 0);
+                ci0 = start >> 6;
+                const int64_t l = -ci0 < 0 ? 0 : -ci0, h = chunks - ci0;
+                lo = (int)(l < RAWC ? l : RAWC);
+                hi = (int)(h < lo ? lo : h < RAWC ? h : RAWC);
+                offs[buf * QS + lane] = (int)(start & 63);
+                unsigned char* seg = sm + WS_OFF_RAW + buf * RAW_BYTES + lane * RAWC * 16;
+                for (int c = 0; c < lo; c++) *reinterpret_cast<uint4*>(seg + 16 * c) = make_uint4(0, 0, 0, 0);
+                for (int c = hi; c < RAWC; c++) *reinterpret_cast<uint4*>(seg + 16 * c) = make_uint4(0, 0, 0, 0);
+            }
+            uint32_t total = 16u * (uint32_t)(hi - lo);
+            total += __shfl_xor_sync(0xffffffffu, total, 1);
+            total += __shfl_xor_sync(0xffffffffu, total, 2);
+            __syncwarp();
+            if (lane == 0) tc::mbar_expect_tx(rb, total);   // the phase's one arrival
+            __syncwarp();
+            if (lane < QS && hi > lo)
+                tc::bulk_load(sbase + WS_OFF_RAW + buf * RAW_BYTES + (lane * RAWC + lo) * 16,
+                              a.raw + (int64_t)s * a.bytes_per_input + 16 * (ci0 + lo), 16u * (uint32_t)(hi - lo), rb);
+            issued = j + 1;
+        }
+        // copies still in flight (the latest phase of each buffer) land before the CTA ends
+        if (lane == 0)
+            for (int q = issued > NRAW ? issued - NRAW : 0; q < issued; q++)
+                lwait(WB_RAWFULL + (q & (NRAW - 1)), (uint32_t)(q / NRAW) & 1);
+        __syncwarp();
     }
     tc::fence_before();
     __syncthreads();
@@ -1086,8 +1218,8 @@ int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st, bool specialised)
     if (specialised) {
         auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32ws<true, true> : k_fx_fstage_tc32ws<true, false>)
                              : (a.scale ? k_fx_fstage_tc32ws<false, true> : k_fx_fstage_tc32ws<false, false>);
-        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)(SMEM_BYTES)));
-        kern<<<grid, WS_THREADS, SMEM_BYTES, st>>>(t), cs_count_launches(1);
+        CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(kern), (int)(WS_SMEM_BYTES)));
+        kern<<<grid, WS_THREADS, WS_SMEM_BYTES, st>>>(t), cs_count_launches(1);
     } else {
         auto kern = a.phase0 ? (a.scale ? k_fx_fstage_tc32<true, true> : k_fx_fstage_tc32<true, false>)
                              : (a.scale ? k_fx_fstage_tc32<false, true> : k_fx_fstage_tc32<false, false>);

@@ -101,8 +101,9 @@ int cs_fx_fstage_tc(const CsFStageArgs& a, cudaStream_t st);
 int cs_fstage_tc_status(unsigned* code);
 // fstage_tc32.cu: the N = 2048 tensor-core F stage with 32-segment units and
 // k-blocked FP16 output (kblock = 1, K and kp multiples of 32), real-input
-// symmetry halving the CUDA-core twiddle work.  cs_fx_fstage uses it for
-// those arguments unless CELLSPE_FSTAGE_TC32=0.
+// symmetry halving the CUDA-core twiddle work; `specialised` selects the
+// warp-specialised form.  cs_fx_fstage uses that form for those arguments
+// unless CELLSPE_FSTAGE_TC32 is 0 (the warp FFT) or 1 (the lockstep form).
 bool cs_fstage_tc32_supported(const CsFStageArgs& a);
 int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st, bool specialised = false);
 int cs_fstage_tc32_status(unsigned* code);
