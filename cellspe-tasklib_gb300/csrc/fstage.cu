@@ -1386,11 +1386,23 @@ bool cs_fstage_kblocked(const CsFStageArgs& a)
            kp % 32 == 0;
 }
 
+int cs_fstage_layout(const CsFStageArgs& a)
+{
+    if (!cs_fstage_kblocked(a)) return 0;
+    CsFStageArgs k = a;
+    k.kblock = 1;
+    if (!cs_fstage_tc32_supported(k)) return 1;
+    const char* e = getenv("CELLSPE_FSTAGE_TC32");
+    return e && (e[0] == '0' || e[0] == '1') ? 1 : 2;
+}
+
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
 {
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;
-    if (a.kblock && !cs_fstage_kblocked(a)) return CS_ERR_ARG;
+    if (a.kblock < 0 || a.kblock > 2 || (a.kblock && !cs_fstage_kblocked(a))) return CS_ERR_ARG;
+    // channel-grouped k-blocked spectra: only the warp-specialised form writes them
+    if (a.kblock == 2) return cs_fstage_tc32_supported(a) ? cs_fx_fstage_tc32(a, st, true) : CS_ERR_ARG;
     // The tensor-core F stage is opt-in (CELLSPE_FSTAGE_TC=1, read per call):
     // its 8-segment units give 16-byte output runs, and on 512 inputs x 4096
     // segments it measured 14.5 ms against 7.3 ms for the 16-segment warp
@@ -1399,14 +1411,12 @@ int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st)
         const char* e = getenv("CELLSPE_FSTAGE_TC");
         if (e && e[0] == '1') return cs_fx_fstage_tc(a, st);
     }
-    // N = 2048 k-blocked FP16 spectra: the warp-specialised tensor-core F
-    // stage (4.90 ms against 5.60 ms for the warp FFT below on 512 inputs x
-    // 4096 segments).  CELLSPE_FSTAGE_TC32 (read per call) selects another
-    // form: 0 the warp FFT, 1 the lockstep tensor-core form.
-    if (a.kblock && cs_fstage_tc32_supported(a)) {
+    // N = 2048 k-blocked FP16 spectra (layout 1): the lockstep tensor-core
+    // form when CELLSPE_FSTAGE_TC32=1 (read per call), else the warp FFT below.
+    // (The warp-specialised form, the default, writes layout 2 above.)
+    if (a.kblock == 1 && cs_fstage_tc32_supported(a)) {
         const char* e = getenv("CELLSPE_FSTAGE_TC32");
-        const char m = e && e[0] ? e[0] : '2';
-        if (m == '1' || m == '2') return cs_fx_fstage_tc32(a, st, m == '2');
+        if (e && e[0] == '1') return cs_fx_fstage_tc32(a, st, false);
     }
     if (a.N == 2048 && !a.msb_first) {
         const bool ph = a.phase0 != nullptr;

@@ -1,6 +1,9 @@
 // K-b/K-c on the tensor cores, 32-segment units: the FX F stage for N = 2048
-// with FP16 spectra written k-blocked (__half [C][S_out][kp/32][2][32], the
-// layout the tcgen05 X stage reads), for K and kp multiples of 32.
+// with FP16 spectra written k-blocked (128-byte runs of 32 Re then 32 Im
+// halves per channel, input and 32-segment block, which the tcgen05 X stage
+// reads), for K and kp multiples of 32: the lockstep form in layout 1
+// (__half [C][S_out][kp/32][2][32]), the warp-specialised form in the
+// channel-grouped layout 2 ([C/16][S_out][kp/32][16] runs; cs_fstage_layout).
 //
 // The real 2048-point DFT X[c] = sum_n x[n] W_2048^(n c), c < 1024, as a
 // four-step transform with both passes on the tensor cores (FP16 operands,
@@ -579,7 +582,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
 //   warps 8-11  decode into B1 (a nibble of two 2-bit codes -> two FP16
 //               levels per conflict-free table read)
 //   warps 12-15 write-out of a staging half: per channel and plane 16
-//               segments, two lanes' 16 bytes making one whole sector
+//               segments, two lanes' 16 bytes making one whole sector; in
+//               the channel-grouped layout a group's 16 channels of the
+//               unit lie in one 2 KB stretch, so the DRAM sees long runs
 //   warp 16     TMEM owner and MMA issuer; pass 1 of quad j + 1 is issued
 //               before pass 2 of quad j, so epilogue 1 finds its next quad
 //               ready
@@ -707,8 +712,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
     auto lwait = [&](int i, uint32_t parity) {
         return tc::mbar_wait(bar(i), parity, &g_fst32_error, E_WORKER_WAIT, WAIT_CYCLES);
     };
+    // channel-grouped k-blocked spectra: the 128-byte run of (channel c,
+    // input s, 32-segment block kb), in runs of 64 halves
     __half* out = reinterpret_cast<__half*>(a.out);
-    const int64_t crow = (int64_t)args.s_rows * args.nkb;   // spectra rows (input, k-block) per channel
+    auto grun = [&](int c, int s, int kb) -> int64_t {
+        return (((int64_t)(c >> 4) * args.s_rows + s) * args.nkb + kb) * 16 + (c & 15);
+    };
 
     if (warp == WS_MMA) {
         // ------------------------------ MMA issuer ------------------------------
@@ -942,7 +951,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                 if (!grp_vote(NB_E2, 128, ok)) break;
                 tc::fence_after();
                 if (q == 0) {
-                    __half* o = out + ((int64_t)s * args.nkb + kb) * 64 + lane;
+                    __half* o = out + lane;
                     const int kq = kb * US + lane;
 #pragma unroll 1
                     for (int h = 0; h < 2; h++) {
@@ -959,7 +968,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                             const int c = c0 + 64 * i;
                             float2 X = make_float2(__uint_as_float(re[i]), __uint_as_float(im[i]));
                             TC32_APPLY(c, X)
-                            __half* oc = o + (int64_t)c * crow * 64;
+                            __half* oc = o + grun(c, s, kb) * 64;
                             oc[0] = __float2half_rn(X.x);
                             oc[32] = __float2half_rn(X.y);
                         }
@@ -1047,7 +1056,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
             bool ok = true;
             if (leader) ok = lwait(WB_STGFULL + sh, (uint32_t)(t >> 1) & 1);
             if (!grp_vote(NB_WO, 128, ok)) break;
-            __half* o = out + ((int64_t)s * args.nkb + kb) * 64 + WS_SH * sh;
+            __half* o = out + WS_SH * sh;
 #pragma unroll 2
             for (int r = 0; r < 2 * FC / 128; r++) {
                 const int task = r * 128 + gt;
@@ -1057,7 +1066,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                 uint32_t w[8];
 #pragma unroll
                 for (int i = 0; i < 8; i++) w[i] = col[i * WS_STG_PITCH];
-                __half* run = o + (int64_t)c * crow * 64 + 8 * g8;
+                __half* run = o + grun(c, s, kb) * 64 + 8 * g8;
                 *reinterpret_cast<uint4*>(run) =
                     make_uint4(__byte_perm(w[0], w[1], 0x5410), __byte_perm(w[2], w[3], 0x5410),
                                __byte_perm(w[4], w[5], 0x5410), __byte_perm(w[6], w[7], 0x5410));
@@ -1191,6 +1200,8 @@ bool cs_fstage_tc32_supported(const CsFStageArgs& a)
 int cs_fx_fstage_tc32(const CsFStageArgs& a, cudaStream_t st, bool specialised)
 {
     if (!cs_fstage_tc32_supported(a)) return CS_ERR_UNSUPPORTED;
+    // the warp-specialised form writes the channel-grouped layout, the lockstep form layout 1
+    if (a.kblock != (specialised ? 2 : 1)) return CS_ERR_ARG;
     if ((int64_t)a.S * (a.K / US) >= (int64_t)1 << 31) return CS_ERR_UNSUPPORTED;   // unit indices are 32-bit
     if (!a.raw || !a.out || a.S <= 0 || a.K <= 0) return CS_ERR_ARG;
     if ((uintptr_t)a.raw % 16 || a.bytes_per_input % 16 || (uintptr_t)a.out % 16) return CS_ERR_ARG;

@@ -71,7 +71,8 @@ struct CsFStageArgs {
     int seg_major;              // 1: out is [S][K][C] (F32 float2, F16 half2 Re|Im), each
                                 // segment's spectrum contiguous; cs_spectra_transpose then
                                 // makes the channel-major layout (the generic kernels only)
-    int kblock;                 // F16 only, 1: k-blocked rows, see cs_fstage_kblocked
+    int kblock;                 // F16 only: 1 k-blocked rows, 2 channel-grouped k-blocked
+                                // rows; see cs_fstage_layout
 };
 int cs_fx_fstage(const CsFStageArgs& a, cudaStream_t st);
 // Per host thread: whether the 2048-point F stage may time its schedules on
@@ -86,6 +87,17 @@ bool cs_fstage_timing_allowed();   // this thread may time kernel choices (autot
 // multiples of 32; the X stage then reads the same layout (kblock = 1).  A
 // launch over a block of inputs writes at out + s0 * kp * 4 bytes.
 bool cs_fstage_kblocked(const CsFStageArgs& a);
+// The spectra layout the F stage writes for these arguments (its kblock):
+// 0 channel-major planes (or segment-major, see seg_major); 1 k-blocked as
+// above; 2 channel-grouped k-blocked: the same 128-byte (32 Re, 32 Im) runs,
+// ordered [C/16][S_out][kp/32][16]: run (c, s, b) at ((c / 16 * S_out + s) *
+// kp / 32 + b) * 16 + c % 16, so a 32-segment unit of one input writes each
+// group of 16 channels as one 2 KB stretch (the warp-specialised tensor-core
+// F stage, the default where it applies; CELLSPE_FSTAGE_TC32=0 or 1, read per
+// call, keeps layout 1).  A launch over a block of inputs writes at out +
+// s0 * kp * 64 bytes; a block of channels c0 (a multiple of 16) onwards
+// starts at c0 * S_out * kp * 4 bytes in both k-blocked layouts.
+int cs_fstage_layout(const CsFStageArgs& a);
 // Segment-major spectra [S][K][C] (tmp) -> the X stage's layout at out:
 // F32 float2 rows (c, s), F16 half rows (c, plane, s); row pitch kp, S_out
 // inputs per (c[, plane]) block (tmp and out already offset to the block).
@@ -115,8 +127,9 @@ int cs_xmac_f32(const float2* spectra, int S, int C, int K, int kp, float2* vis,
                 cudaStream_t st);
 // Tensor-core (tcgen05, FP16 in, FP32 accumulate) X stage:
 // spectra __half [C][2][S][kp] (K used; kp % 8 == 0), or k-blocked
-// [C][S][kp/32][2][32] with kblock = 1 (K, kp % 32 == 0) -> vis float2 [C][P];
-// inv_scale [S*C] or null.
+// [C][S][kp/32][2][32] with kblock = 1 (K, kp % 32 == 0), or channel-grouped
+// k-blocked with kblock = 2 (C % 16 == 0; see cs_fstage_layout) -> vis
+// float2 [C][P]; inv_scale [S*C] or null.
 int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis, const float* inv_scale,
                    int scale_stride, int accumulate, cudaStream_t st,
                    int kblock = 0);   // inv_scale[s * scale_stride + c]

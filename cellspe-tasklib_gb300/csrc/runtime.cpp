@@ -560,7 +560,9 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     }
     const int kp = (int)spectra_pitch(K);
     fa.kp = kp;
-    fa.kblock = cs_fstage_kblocked(fa) ? 1 : 0;        // FP16, N = 2048: 128-byte rows per 32 segments
+    // FP16, N = 2048: 128-byte runs per 32 segments, k-blocked (1) or
+    // channel-grouped k-blocked (2, the warp-specialised F stage)
+    fa.kblock = cs_fstage_layout(fa);
     fa.out = j.scratch((size_t)C * S * kp * (fa.format == CS_SPECTRA_F32 ? 8 : 4));
     if (sync) cudaEventRecord(ws.sev[1], ws.stream);
     // bytes of one spectra element: F32 rows [C][S][kp] of float2, F16 rows [C][2][S][kp] of half
@@ -579,8 +581,9 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
             fb.raw = d_raw + s0 * bpi;
             fb.S = (int)(s1 - s0);
             fb.S_out = S;
-            // input s0's row in every (c, plane) block, or its k-blocked rows in every channel
-            fb.out = (char*)fa.out + s0 * kp * el_bytes * (fa.kblock ? 2 : 1);
+            // input s0's row in every (c, plane) block, its k-blocked rows in every
+            // channel, or its runs in every channel group
+            fb.out = (char*)fa.out + s0 * kp * el_bytes * (fa.kblock == 2 ? 32 : fa.kblock ? 2 : 1);
             if (fa.shift) fb.shift = fa.shift + s0 * K;
             if (fa.phase0) fb.phase0 = fa.phase0 + s0 * K, fb.dphase = fa.dphase + s0 * K;
             if (fa.scale) fb.scale = fa.scale + s0 * C;
@@ -614,12 +617,16 @@ int op_fx(Workspace& ws, const cellspe_fx_params* p, const void* raw, const doub
     for (int b = 0; b < ncb && !j.err; b++) {
         // streamed output: a small first block (1/16 of the channels) starts the
         // copy out early; the rest in equal blocks
+        // (channel-grouped spectra: block bounds on whole groups of 16 channels)
         auto cbound = [&](int i) -> long long {
             if (ncb == 1) return i ? C : 0;
+            if (i == ncb) return C;
             const long long first = std::max(1LL, (long long)C / 16);
-            return i == 0 ? 0 : first + (long long)(C - first) * (i - 1) / (ncb - 1);
+            const long long c = i == 0 ? 0 : first + (long long)(C - first) * (i - 1) / (ncb - 1);
+            return fa.kblock == 2 ? c / 16 * 16 : c;
         };
         const long long c0 = cbound(b), c1 = cbound(b + 1), cn = c1 - c0;
+        if (cn <= 0) continue;
         int rc;
         if (p->x_mode == CELLSPE_X_FP32)
             rc = cs_xmac_f32((const float2*)fa.out + c0 * S * kp, S, (int)cn, K, kp, vis_cp + c0 * P, 0, ws.stream);

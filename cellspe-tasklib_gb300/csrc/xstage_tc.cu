@@ -72,7 +72,8 @@ struct TcArgs {
     int box_rows;               // rows per TMA box: BM, or S rounded up to 8 when S < BM
     int small;                  // S <= BM: one tile per channel whose B operand is its A operand
     uint32_t tmem_cols;         // TMEM columns: Re V in [0, cols/2), Im V in [cols/2, cols)
-    int kblock;                 // spectra k-blocked [C][S][kp/32][2][32] (4-D tensor map)
+    int kblock;                 // spectra k-blocked: 1 [C][S][kp/32][2][32] (4-D tensor map),
+                                // 2 channel-grouped [C/16][S][kp/32][16][2][32] (5-D)
 };
 
 __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant__ CUtensorMap tmap,
@@ -127,10 +128,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
         if (lane == 0) {
             const int rowA_re = (c * 2 + 0) * S + i0, rowA_im = (c * 2 + 1) * S + i0;
             const int rowB_re = (c * 2 + 0) * S + j0, rowB_im = (c * 2 + 1) * S + j0;
-            // k-blocked: rows (c, s) with the plane a coordinate of its own
-            const int krowA = c * S + i0, krowB = c * S + j0;
+            // k-blocked: rows (c, s) with the plane a coordinate of its own;
+            // channel-grouped: the input s a coordinate, the channel split
+            // into (c % 16, c / 16), the plane as x = 32 plane halves (64 B)
+            const int krowA = a.kblock == 2 ? i0 : c * S + i0, krowB = a.kblock == 2 ? j0 : c * S + j0;
             auto load = [&](uint32_t dst, int kc, int plane, int row2d, int rowk, uint32_t bar) {
-                if (a.kblock) tc::tma_load_4d(dst, &tmap, 0, plane, kc, rowk, bar);
+                if (a.kblock == 2) tc::tma_load_5d(dst, &tmap, 32 * plane, c & 15, kc, rowk, c >> 4, bar);
+                else if (a.kblock) tc::tma_load_4d(dst, &tmap, 0, plane, kc, rowk, bar);
                 else tc::tma_load_2d(dst, &tmap, kc * BK, row2d, bar);
             };
             int issued = 0;
@@ -295,7 +299,8 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
 {
     if (!spectra || !vis || S <= 0 || C <= 0 || K <= 0 || C > 65535 || kp < K) return CS_ERR_ARG;
     if (K % 8 != 0 || kp % 8 != 0 || (uintptr_t)spectra % 16) return CS_ERR_ARG;   // TMA: 16-byte pitch and base
-    if (kblock && (K % 32 != 0 || kp % 32 != 0)) return CS_ERR_ARG;
+    if (kblock < 0 || kblock > 2 || (kblock && (K % 32 != 0 || kp % 32 != 0)) || (kblock == 2 && C % 16 != 0))
+        return CS_ERR_ARG;
     CsEncodeTiledFn enc = cs_encode_tiled();
     if (!enc) return CS_ERR_UNSUPPORTED;
     int ntiles = 0;
@@ -311,6 +316,18 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
     CUresult r;
     if (!kblock) {
         r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(spectra), gdim, gstride, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    } else if (kblock == 2) {
+        // [C/16 groups][S inputs][K/32 used of kp/32 blocks][16 channels][64
+        // halves (Re 32, Im 32)]: a box of (32 halves, 1 channel, 1 block,
+        // box_rows inputs, 1 group) lands as the same [rows][32] tile; inputs
+        // past S read as zeros
+        cuuint64_t g5[5] = {64, 16, (cuuint64_t)K / 32, (cuuint64_t)S, (cuuint64_t)C / 16};
+        cuuint64_t s5[4] = {128, 2048, (cuuint64_t)kp / 32 * 2048, (cuuint64_t)S * (kp / 32) * 2048};
+        cuuint32_t b5[5] = {32, 1, 1, (cuuint32_t)box_rows, 1};
+        cuuint32_t e5[5] = {1, 1, 1, 1, 1};
+        r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(spectra), g5, s5, b5, e5,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     } else {
@@ -341,7 +358,7 @@ int cs_xmac_tc_f16(const void* spectra, int S, int C, int K, int kp, float2* vis
         while (cols < 2 * n_eff) cols *= 2;
     }
     TcArgs a{S, C, K, (int64_t)S * (S + 1) / 2, tiles, vis, inv_scale, scale_stride > 0 ? scale_stride : C,
-             accumulate, box_rows, small, cols, kblock ? 1 : 0};
+             accumulate, box_rows, small, cols, kblock};
     const size_t smem = (size_t)STAGES * (small ? 2 * A_BYTES : STAGE_BYTES) + 1024 + 256;
     CS_CUDA_TRY(cs_smem_at_least(reinterpret_cast<const void*>(k_xmac_tc), (int)smem));
     dim3 grid(ntiles, C);
