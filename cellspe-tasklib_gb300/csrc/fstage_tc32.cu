@@ -574,7 +574,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
 // phase has warps of its own and the phases hand buffers to each other
 // through mbarriers, so they run concurrently instead of in step between
 // CTA-wide barriers:
-//   warps 0-3   epilogue 1 (TMEM lane quarter = warp), all 4 segments of a quad
+//   warps 0-3   epilogue 1 (TMEM lane quarter = warp), all 4 segments of a
+//               quad, and each warp one segment's share of the k1 = 32 row
 //   warps 4-7   epilogue 2 (lane quarter = segment of the quad) into the
 //               unit's staging, whose two 16-segment halves the write-out
 //               drains in turn; at a unit's end warp 4 writes the k1 = 32
@@ -825,7 +826,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                     *reinterpret_cast<uint32_t*>(a2h + (e1base ^ (m << 4) ^ 64u)) = h2u(__floats2half2_rn(z0.y, z1.y));
                 }
             };
-            // the real k1 = 32 row (TMEM lanes 16..23 of quarter 0) of segment h
+            // the real k1 = 32 row (TMEM lanes 16..23 of this warp's quarter) of segment h
             // -> row 4 qd + h of the unit's A2' region
             auto e1row32 = [&](int h, const uint32_t (&r32)[16]) {
                 const bool mb1 = m32 & 1, mb2 = m32 & 2;
@@ -843,17 +844,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                 uint32_t r0[16], r1[16];
                 tc::tmem_ld_16x256b_x4(d1 + ((uint32_t)(32 * q) << 16), r0);
                 tc::tmem_ld_16x256b_x4(d1 + 32u + ((uint32_t)(32 * q) << 16), r1);
-                if (q == 0) {
-                    uint32_t s0[16], s1[16];
-                    tc::tmem_ld_16x256b_x4(d1 + (16u << 16), s0);
-                    tc::tmem_ld_16x256b_x4(d1 + 32u + (16u << 16), s1);
+                if ((q & ~1) == h) {
+                    // this warp's share of the k1 = 32 row: segment q, from the
+                    // copy of the row in its own lane quarter (rows 32 q + 16..23)
+                    uint32_t s0[16];
+                    tc::tmem_ld_16x256b_x4(d1 + 32u * (q & 1) + ((uint32_t)(32 * q + 16) << 16), s0);
                     tc::tmem_ld_wait();
                     pin16(r0);
                     pin16(r1);
                     pin16(s0);
-                    pin16(s1);
-                    e1row32(h, s0);
-                    e1row32(h + 1, s1);
+                    e1row32(q, s0);
                 } else {
                     tc::tmem_ld_wait();
                     pin16(r0);
@@ -1159,8 +1159,11 @@ const uint4* tc32_constants()
                 const int k1 = 8 * q + rr % 8;
                 const double th = 2.0 * M_PI * (double)((n1 * k1) % 64) / 64.0;
                 v = rr < 8 ? std::cos(th) : -std::sin(th);
-            } else if (q == 0 && rr < 24) {
-                v = (n1 & 1) ? -1.0 : 1.0;             // W_64^(32 n1)
+            } else if (rr < 24) {
+                // W_64^(32 n1): the real k1 = 32 row, in every lane quarter (the
+                // lockstep form reads quarter 0's; the warp-specialised form's
+                // epilogue-1 warp q reads quarter q's for segment q of a quad)
+                v = (n1 & 1) ? -1.0 : 1.0;
             }
             put(OFF_A1, r, n1, v);
         }
