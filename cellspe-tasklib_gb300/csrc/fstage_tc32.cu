@@ -578,14 +578,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_fx_fstage_tc32(const __grid_cons
 //               quad, and each warp one segment's share of the k1 = 32 row
 //   warps 4-7   epilogue 2 (lane quarter = segment of the quad) into the
 //               unit's staging, whose two 16-segment halves the write-out
-//               drains in turn; at a unit's end warp 4 writes the k1 = 32
-//               channels (lane = segment) to the spectra directly
-//   warps 8-11  decode into B1 (a nibble of two 2-bit codes -> two FP16
-//               levels per conflict-free table read)
+//               drains in turn
+//   warps 8-11  decode into B1 (a byte_perm of the four levels per pair of
+//               samples, no table in shared memory)
 //   warps 12-15 write-out of a staging half: per channel and plane 16
 //               segments, two lanes' 16 bytes making one whole sector; in
 //               the channel-grouped layout a group's 16 channels of the
-//               unit lie in one 2 KB stretch, so the DRAM sees long runs
+//               unit lie in one 2 KB stretch, so the DRAM sees long runs.
+//               After a unit's second half warp 12 (lane quarter 0, lane =
+//               segment) writes the unit's k1 = 32 channels from pass 2'
+//               straight to the spectra.
 //   warp 16     TMEM owner and MMA issuer; pass 1 of quad j + 1 is issued
 //               before pass 2 of quad j, so epilogue 1 finds its next quad
 //               ready
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
             tc::mbar_init(bar(WB_E2DONE + b), 4);
             tc::mbar_init(bar(WB_D2PFULL + b), 1);
         }
-        tc::mbar_init(bar(WB_E2PDONE), 4);
+        tc::mbar_init(bar(WB_E2PDONE), 1);
         for (int t = 0; t < 2; t++) {
             tc::mbar_init(bar(WB_STGFULL + t), 4);
             tc::mbar_init(bar(WB_STGFREE + t), 4);
@@ -720,6 +722,25 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
         return (((int64_t)(c >> 4) * args.s_rows + s) * args.nkb + kb) * 16 + (c & 15);
     };
 
+    // epilogue-2 helpers: the delay phasor of input s_, segment k_ from channel
+    // cstart in steps of cstep, and its product (and the channel scale) on X
+#define TC32_PHASOR(s_, k_, cstart, cstep)                                              \
+        float2 B = make_float2(1.f, 0.f), D = B;                                        \
+        if (PHASE) {                                                                    \
+            const int64_t sk = (int64_t)(s_) * K + (k_);                                \
+            const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);         \
+            float sn, cs;                                                               \
+            sincosf(ph0 + (cstart) * dph, &sn, &cs);                                    \
+            B = make_float2(cs, sn);                                                    \
+            sincosf((cstep) * dph, &sn, &cs);                                           \
+            D = make_float2(cs, sn);                                                    \
+        }
+#define TC32_APPLY(c_, X)                                                               \
+        if (PHASE) {                                                                    \
+            X = cmul(X, B);                                                             \
+            B = cmul(B, D);                                                             \
+        }                                                                               \
+        if (SCALE) X = cscale(X, __ldg(scl + (c_)));
     if (warp == WS_MMA) {
         // ------------------------------ MMA issuer ------------------------------
         if (lane == 0) {
@@ -871,23 +892,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
         const int q = warp & 3, gt = tid - 32 * WS_E2;
         const bool leader = gt == 0;
         const int kk1 = lane;
-#define TC32_PHASOR(s_, k_, cstart, cstep)                                              \
-        float2 B = make_float2(1.f, 0.f), D = B;                                        \
-        if (PHASE) {                                                                    \
-            const int64_t sk = (int64_t)(s_) * K + (k_);                                \
-            const float ph0 = __ldg(a.phase0 + sk), dph = __ldg(a.dphase + sk);         \
-            float sn, cs;                                                               \
-            sincosf(ph0 + (cstart) * dph, &sn, &cs);                                    \
-            B = make_float2(cs, sn);                                                    \
-            sincosf((cstep) * dph, &sn, &cs);                                           \
-            D = make_float2(cs, sn);                                                    \
-        }
-#define TC32_APPLY(c_, X)                                                               \
-        if (PHASE) {                                                                    \
-            X = cmul(X, B);                                                             \
-            B = cmul(B, D);                                                             \
-        }                                                                               \
-        if (SCALE) X = cscale(X, __ldg(scl + (c_)));
         for (int j = 0; j < nquads; j++) {
             const int b = j & 1, qd = j % QUADS, u = j / QUADS, t = j / (WS_SH / QS), sh = t & 1;
             int s, kb;
@@ -942,44 +946,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
             tc::fence_before();
             warp_arrive(bar(WB_E2DONE + b));
             if (j % (WS_SH / QS) == WS_SH / QS - 1) warp_arrive(bar(WB_STGFULL + sh));
-            if (qd == QUADS - 1) {
-                // the unit's k1 = 32 channels c = 32 + 64 k2: warp 4 (lane quarter
-                // 0, lane = segment) writes them to the spectra directly, each
-                // store a channel's 32 segments of one plane (64 bytes)
-                ok = true;
-                if (leader) ok = lwait(WB_D2PFULL + (u & 1), (uint32_t)(u >> 1) & 1);
-                if (!grp_vote(NB_E2, 128, ok)) break;
-                tc::fence_after();
-                if (q == 0) {
-                    __half* o = out + lane;
-                    const int kq = kb * US + lane;
-#pragma unroll 1
-                    for (int h = 0; h < 2; h++) {
-                        uint32_t re[8], im[8];
-                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 8u * h, re);
-                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 32u + 8u * h, im);
-                        tc::tmem_ld_wait();
-#pragma unroll
-                        for (int i = 0; i < 8; i++) asm volatile("" : "+r"(re[i]), "+r"(im[i]));
-                        const int c0 = 32 + 512 * h;
-                        TC32_PHASOR(s, kq, (float)c0, 64.f)
-#pragma unroll
-                        for (int i = 0; i < 8; i++) {
-                            const int c = c0 + 64 * i;
-                            float2 X = make_float2(__uint_as_float(re[i]), __uint_as_float(im[i]));
-                            TC32_APPLY(c, X)
-                            __half* oc = o + grun(c, s, kb) * 64;
-                            oc[0] = __float2half_rn(X.x);
-                            oc[32] = __float2half_rn(X.y);
-                        }
-                    }
-                }
-                tc::fence_before();
-                warp_arrive(bar(WB_E2PDONE));
-            }
         }
-#undef TC32_PHASOR
-#undef TC32_APPLY
     } else if (warp < WS_WO) {
         // ------------------------------ decode ------------------------------
         const int gt = tid - 32 * WS_DEC;                   // 0..127
@@ -1049,19 +1016,20 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
         const int gt = tid - 32 * WS_WO;                    // 0..127
         const bool leader = gt == 0;
         const int nhalves = 2 * nunits;
+        bool kfail = false;                                 // warp WS_WO: a pass-2' wait failed
         for (int t = 0; t < nhalves; t++) {
             const int sh = t & 1, u = t >> 1;
             int s, kb;
             unit_of(u, s, kb);
-            bool ok = true;
-            if (leader) ok = lwait(WB_STGFULL + sh, (uint32_t)(t >> 1) & 1);
+            bool ok = !kfail;
+            if (leader && ok) ok = lwait(WB_STGFULL + sh, (uint32_t)(t >> 1) & 1);
             if (!grp_vote(NB_WO, 128, ok)) break;
             __half* o = out + WS_SH * sh;
 #pragma unroll 2
             for (int r = 0; r < 2 * FC / 128; r++) {
                 const int task = r * 128 + gt;
                 const int c = task >> 1, g8 = task & 1;
-                if ((c & 63) == 32) continue;               // the k1 = 32 channels: written by epilogue 2
+                if ((c & 63) == 32) continue;               // the k1 = 32 channels: below
                 const uint32_t* col = stg + (WS_SH * sh + 8 * g8) * WS_STG_PITCH + c;
                 uint32_t w[8];
 #pragma unroll
@@ -1075,6 +1043,43 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                                __byte_perm(w[4], w[5], 0x7632), __byte_perm(w[6], w[7], 0x7632));
             }
             warp_arrive(bar(WB_STGFREE + sh));
+            if (sh == 1 && warp == WS_WO) {
+                // the unit's k1 = 32 channels c = 32 + 64 k2 from pass 2': this
+                // warp (lane quarter 0, lane = segment) writes them to the spectra
+                // directly, each store a channel's 32 segments of one plane (64 B)
+                bool okp = true;
+                if (lane == 0) okp = lwait(WB_D2PFULL + (u & 1), (uint32_t)(u >> 1) & 1);
+                if (!__shfl_sync(0xffffffffu, okp, 0)) {
+                    kfail = true;
+                } else {
+                    tc::fence_after();
+                    const float* scl = SCALE ? a.scale + (int64_t)s * FC : nullptr;
+                    __half* o = out + lane;
+                    const int kq = kb * US + lane;
+#pragma unroll 1
+                    for (int h = 0; h < 2; h++) {
+                        uint32_t re[8], im[8];
+                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 8u * h, re);
+                        tc::tmem_ld_32x32b_x8(tmem + COL_D2P + 32u + 8u * h, im);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int i = 0; i < 8; i++) asm volatile("" : "+r"(re[i]), "+r"(im[i]));
+                        const int c0 = 32 + 512 * h;
+                        TC32_PHASOR(s, kq, (float)c0, 64.f)
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            const int c = c0 + 64 * i;
+                            float2 X = make_float2(__uint_as_float(re[i]), __uint_as_float(im[i]));
+                            TC32_APPLY(c, X)
+                            __half* oc = o + grun(c, s, kb) * 64;
+                            oc[0] = __float2half_rn(X.x);
+                            oc[32] = __float2half_rn(X.y);
+                        }
+                    }
+                    tc::fence_before();
+                    warp_arrive(bar(WB_E2PDONE));
+                }
+            }
         }
     } else if (warp == WS_FETCH) {
         // ------------------------------ raw fetch ------------------------------
@@ -1124,6 +1129,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_fx_fstage_tc32ws(const __grid
                 lwait(WB_RAWFULL + (q & (NRAW - 1)), (uint32_t)(q / NRAW) & 1);
         __syncwarp();
     }
+#undef TC32_PHASOR
+#undef TC32_APPLY
     tc::fence_before();
     __syncthreads();
     if (warp == WS_MMA) {
