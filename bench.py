@@ -585,12 +585,12 @@ def main():
     # units one launch here processes: the warp-FFT F stage moved 4,375 B per
     # input-segment (512 inputs x 512 segments, N = 2048, k-blocked FP16
     # spectra, --set full); the warp-specialised tensor-core F stage 4,578 B
-    # and the tensor-core X stage 2,067 B per (channel, segment) read plus
+    # and the tensor-core X stage 2,074 B per (channel, segment) read plus
     # 1.025 MB of visibilities written per channel (512 inputs x 4096
     # segments, channel-grouped spectra, one-pass dram__bytes_read/write
     # capture).  None where no capture of that kernel exists.
     F_TRAFFIC_PER_SEGMENT = {"k_fx_fstage_w2048": 4375.0, "k_fx_fstage_tc32ws": 4578.0}
-    X_TRAFFIC_PER_CHANNEL = 2067.0 * K_run + 1.025e6
+    X_TRAFFIC_PER_CHANNEL = 2074.0 * K_run + 1.025e6
     peaks, peak_kind = _peaks()
     f_ms, x_ms = stage_ms[1], stage_ms[2]
     f_bytes = S_run * K_run * (N_run // 4 + C_run * (8 if x_mode == cg.X_FP32 else 4))     # raw in + spectra out
@@ -626,7 +626,7 @@ def main():
         roof = {"bound": "hbm", "kernel": fk, "achieved": stages["f_stage_gbs"], "peak": pk,
                 "unit": "GB/s", "frac": stages["f_stage_gbs"] / pk, "peak_source": f"{peak_kind} HBM copy",
                 "traffic": per_seg * S_run * K_run if per_seg else None,
-                "note": ("F stage is bound by the LSU data pipe (shared memory + spectra stores, 65% busy) and "
+                "note": ("F stage is bound by the LSU data pipe (shared memory + spectra stores, 67% busy) and "
                          "its epilogue warps (ncu), not HBM bandwidth; DRAM bytes equal the algorithmic ones"
                          if fk == "k_fx_fstage_tc32ws" else
                          "F stage is bound by instruction issue and the shared-memory pipe (ncu), not HBM")}
