@@ -100,10 +100,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     const int n_need = min(min(j0 + BN, i0 + BM), S) - j0;
     const uint32_t n_eff = (uint32_t)((n_need + 15) & ~15);
     const bool half_b = n_eff <= (uint32_t)BM;      // only the first 128 B rows are loaded
+    // a diagonal tile (i0 == j0) multiplies its rows by themselves: B is A, so
+    // its stages load A only (as every tile does when S <= BM)
+    const bool diag = a.small || i0 == j0;
     // S < 128: the boxes hold the S (rounded up to 8) rows that exist, so a
     // channel's planes are read once; the rows of the operand tiles past them
     // only feed accumulator rows and columns that are never stored
-    const uint32_t stage_tx = a.small ? 2u * (uint32_t)a.box_rows * BK * 2
+    const uint32_t stage_tx = diag ? 2u * (uint32_t)a.box_rows * BK * 2
                               : half_b ? 4u * (uint32_t)a.box_rows * BK * 2 : STAGE_BYTES;
 
     if (threadIdx.x == 0) {
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 tc::mbar_expect_tx(fb, stage_tx);
                 load(st, kc, 0, rowA_re, krowA, fb);
                 load(st + A_BYTES, kc, 1, rowA_im, krowA, fb);
-                if (!a.small) {
+                if (!diag) {
                     load(st + 2 * A_BYTES, kc, 0, rowB_re, krowB, fb);
                     load(st + 2 * A_BYTES + B_BYTES, kc, 1, rowB_im, krowB, fb);
                 }
@@ -177,8 +180,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                 for (int kk = 0; kk < BK / 16; kk++) {
                     const uint32_t off = kk * 32;                  // 16 FP16 along K
                     const uint64_t ar = sw64_desc(st + off), ai = sw64_desc(st + A_BYTES + off);
-                    const uint64_t br = a.small ? ar : sw64_desc(st + 2 * A_BYTES + off);
-                    const uint64_t bi = a.small ? ai : sw64_desc(st + 2 * A_BYTES + B_BYTES + off);
+                    const uint64_t br = diag ? ar : sw64_desc(st + 2 * A_BYTES + off);
+                    const uint64_t bi = diag ? ai : sw64_desc(st + 2 * A_BYTES + B_BYTES + off);
                     const uint32_t acc = (kc | kk) ? 1u : 0u;
                     tc::mma_f16(d_re, ar, br, id_pos, acc);           // Re += Ar Br^T
                     tc::mma_f16(d_re, ai, bi, id_pos, 1u);            // Re += Ai Bi^T
