@@ -41,6 +41,11 @@ constexpr int A_BYTES = BM * BK * 2;                // 8 KB
 constexpr int B_BYTES = BN * BK * 2;                // 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // Ar, Ai, Br, Bi = 32 KB
 constexpr int TC_THREADS = 192;
+// epilogue shared memory: four warps' 32 x 17 float2 staging blocks, then (on
+// a diagonal tile) M as [BM][MP] floats; both inside the operand ring
+constexpr int EPI_STG_BYTES = 4 * 32 * 17 * 8;
+constexpr int MP = BM + 1;
+static_assert(EPI_STG_BYTES + BM * MP * 4 <= STAGES * STAGE_BYTES, "epilogue M staging inside the ring");
 constexpr uint32_t TMEM_COLS = 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;     // ~2 s at 2 GHz
 
@@ -60,6 +65,23 @@ CS_DEV bool mbar_wait(uint32_t bar, uint32_t parity, unsigned code)
 // K-major operand in shared memory with 64-byte swizzle: 8-row x 64-byte
 // atoms stacked along M/N every 512 bytes (stride byte offset).
 CS_DEV uint64_t sw64_desc(uint32_t saddr) { return tc::smem_desc(saddr, 16, 512, tc::SW64); }
+
+// the four epilogue warps (2..5): named barrier 1 over their 128 threads, and
+// an AND vote on it that every one of them reaches
+CS_DEV void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+CS_DEV bool epi_vote(bool ok)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, 1, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(ok ? 1u : 0u)
+        : "memory");
+    return r != 0;
+}
 
 struct TcArgs {
     int S, C, K;
@@ -103,6 +125,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
     // a diagonal tile (i0 == j0) multiplies its rows by themselves: B is A, so
     // its stages load A only (as every tile does when S <= BM)
     const bool diag = a.small || i0 == j0;
+    // and, when its stages span the full ring, its imaginary part is M - M^T
+    // with M = Ai Ar^T: three MMAs per k-step instead of four, M staged through
+    // shared memory for the transpose in the epilogue
+    const bool mtr = diag && !a.small;
     // S < 128: the boxes hold the S (rounded up to 8) rows that exist, so a
     // channel's planes are read once; the rows of the operand tiles past them
     // only feed accumulator rows and columns that are never stored
@@ -185,8 +211,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
                     const uint32_t acc = (kc | kk) ? 1u : 0u;
                     tc::mma_f16(d_re, ar, br, id_pos, acc);           // Re += Ar Br^T
                     tc::mma_f16(d_re, ai, bi, id_pos, 1u);            // Re += Ai Bi^T
-                    tc::mma_f16(d_im, ai, br, id_pos, acc);           // Im += Ai Br^T
-                    tc::mma_f16(d_im, ar, bi, id_neg, 1u);            // Im -= Ar Bi^T
+                    tc::mma_f16(d_im, ai, br, id_pos, acc);           // Im += Ai Br^T  (M on a diagonal tile)
+                    if (!mtr) tc::mma_f16(d_im, ar, bi, id_neg, 1u);  // Im -= Ar Bi^T
                 }
                 tc::commit(empty0 + 8 * s);                       // stage free once these MMAs finish
             }
@@ -204,20 +230,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_xmac_tc(const __grid_constant
         bool ok = mbar_wait(accb, 0, ERR_ACC_WAIT);
         ok = ok && (*reinterpret_cast<volatile unsigned*>(&g_tc_error) == 0u);
         __syncwarp();
-        if (__all_sync(0xffffffffu, ok)) {
+        // M - M^T needs the other warps' rows: the four epilogue warps agree
+        // (one vote, so all of them or none reach the barrier below)
+        bool go = __all_sync(0xffffffffu, ok);
+        if (mtr) go = epi_vote(go);
+        if (go) {
             tc::fence_after();
             // Stage each 32-row x 16-column block through shared memory (the
             // operand ring is free once the accumulators are final) so that a
             // store instruction writes two 128-byte runs of one output row.
             float2* stg = reinterpret_cast<float2*>(smem) + (warp - 2) * 32 * 17;
+            // diagonal tile: M [BM][MP] after the four warps' staging blocks
+            float* msh = reinterpret_cast<float*>(smem + EPI_STG_BYTES);
             const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
             const float si = (a.inv_scale && i < S) ? __ldg(a.inv_scale + (int64_t)i * a.scale_stride + c) : 1.f;
             const int ncb = (int)(n_eff / 16);
+            if (mtr) {
+                for (int cb = 0; cb < ncb; cb++) {
+                    uint32_t mm[16];
+                    tc::tmem_ld_32x32b_x16(lane_base + a.tmem_cols / 2 + cb * 16, mm);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int jj = 0; jj < 16; jj++) msh[r * MP + cb * 16 + jj] = __uint_as_float(mm[jj]);
+                }
+                epi_bar();
+            }
             for (int cb = 0; cb < ncb; cb++) {
                 uint32_t re[16], im[16];
                 tc::tmem_ld_32x32b_x16(lane_base + cb * 16, re);
-                tc::tmem_ld_32x32b_x16(lane_base + a.tmem_cols / 2 + cb * 16, im);
+                if (!mtr) tc::tmem_ld_32x32b_x16(lane_base + a.tmem_cols / 2 + cb * 16, im);
                 tc::tmem_ld_wait();
+                if (mtr) {
+#pragma unroll
+                    for (int jj = 0; jj < 16; jj++) {
+                        const int jl = cb * 16 + jj;                   // column within the tile
+                        im[jj] = __float_as_uint(msh[r * MP + jl] - msh[jl * MP + r]);
+                    }
+                }
 #pragma unroll
                 for (int jj = 0; jj < 16; jj++) {
                     float f = si;
