@@ -12,7 +12,9 @@
 // is the instruction descriptor's negate-A bit, so no negated copy of the data
 // exists.  Operands are K-major (time innermost), loaded by TMA with 64-byte
 // swizzle into a 3-stage shared-memory ring (32 KB stages) guarded by
-// mbarriers.
+// mbarriers.  A diagonal tile (i0 = j0) loads its rows once and uses them as
+// both operands, and needs three MMAs per k-step: its Im columns accumulate
+// M = Xi Xr^T and the epilogue forms Im V = M - M^T through shared memory.
 //
 // Warp roles (6 warps): warp 0 = TMA producer, warp 1 = TMEM owner and MMA
 // issuer, warps 2..5 = epilogue (TMEM -> registers -> global; warp w reads
@@ -21,7 +23,8 @@
 // and returns, and the host reports the failure.
 //
 // Layout in:  __half spectra[C][2][S][K]  (plane 0 = Re, plane 1 = Im), or
-//             k-blocked [C][S][K/32][2][32] (4-D tensor map)
+//             k-blocked [C][S][K/32][2][32] (4-D tensor map), or channel-grouped
+//             k-blocked [C/16][S][K/32][16][2][32] (5-D tensor map)
 // Layout out: float2 vis[C][P], p = i(i+1)/2 + j, j <= i
 #include <cuda.h>
 
