@@ -38,14 +38,33 @@ def test_xmac_f16_exact_inputs(cg, S, C, K):
     assert np.abs(autos.imag).max() <= 1e-5 * np.abs(autos.real).max()
 
 
-def test_xmac_f16_accumulate(cg):
+@pytest.mark.parametrize("S", [40, 200])
+def test_xmac_f16_accumulate(cg, S):
+    """accumulate adds to the visibilities; S = 200 has diagonal tiles past the
+    single-tile size (Im = M - M^T staged in the epilogue) and an edge tile."""
     rng = np.random.default_rng(1)
-    S, C, K = 40, 2, 64
+    C, K = 2, 64
     spec = rng.standard_normal((C, 2, S, K)).astype(np.float16)
     vis = np.zeros((C, S * (S + 1) // 2), np.complex64)
     cg.xmac_f16(spec, S, C, K, vis)
     v2 = vis.copy()
     cg.xmac_f16(spec, S, C, K, v2, accumulate=True)
+    assert np.allclose(v2, 2 * vis, rtol=1e-6, atol=1e-4)
+
+
+def test_fx_tc_accumulate_channel_grouped(cg):
+    """FX with accumulate on the default N = 2048 tensor-core path (channel-grouped
+    spectra, diagonal tiles past 128 inputs): a second call adds the same
+    visibilities."""
+    import synth
+
+    S, N, K = 160, 2048, 64
+    raw = synth.stations_offset_binary(S, N * K, rho=0.2, seed=41)
+    P, C = S * (S + 1) // 2, N // 2
+    vis = np.zeros((C, P), np.complex64)
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16), raw, vis)
+    v2 = vis.copy()
+    cg.fx_correlate(cg.fx_params(S, N, K, raw.shape[1], x_mode=cg.X_TC_FP16, accumulate=True), raw, v2)
     assert np.allclose(v2, 2 * vis, rtol=1e-6, atol=1e-4)
 
 
